@@ -1,0 +1,64 @@
+// common.cuh — shared definitions for the fluidloom_gb300 CUDA library (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include <string>
+
+#include "fluidloom_gb300.h"
+
+#define FL_INVALID_INDEX 0xFFFFFFFFu
+#define FL_EMPTY_KEY 0xFFFFFFFFFFFFFFFFull
+
+// Per-context state.  One host thread drives a context; all work is ordered on
+// its stream.  Scratch is a growable device buffer (never shrunk) so steady
+// state launches allocate nothing.
+struct fl_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    uint32_t* dev_status = nullptr;     // device-side status words (see FL_DEVSTAT_*)
+    uint32_t* host_status = nullptr;    // pinned mirror
+    std::string last_error;
+};
+
+// Device status words written by kernels instead of trapping.
+enum {
+    FL_DEVSTAT_TIMEOUT = 0,     // a bounded spin gave up
+    FL_DEVSTAT_HASH_OVERFLOW = 1,
+    FL_DEVSTAT_LEVEL_JUMP = 2,  // a neighbour more than one level away
+    FL_DEVSTAT_BOUNDS = 3,      // an index failed a bounds check and the access was skipped
+    FL_DEVSTAT_WORDS = 8
+};
+
+int fl_set_error(fl_ctx* ctx, int code, const std::string& msg);
+int fl_check_cuda(fl_ctx* ctx, cudaError_t e, const char* what);
+// Ensure ctx->scratch holds at least `bytes` (256-byte aligned sub-buffers are carved by callers).
+int fl_scratch_reserve(fl_ctx* ctx, size_t bytes);
+// Read back and clear the device status words; returns FL_OK or the first error.
+int fl_collect_device_status(fl_ctx* ctx, const char* what);
+
+#define FL_TRY_CUDA(ctx, expr, what)                                  \
+    do {                                                              \
+        cudaError_t _e = (expr);                                      \
+        if (_e != cudaSuccess) return fl_check_cuda((ctx), _e, what); \
+    } while (0)
+
+#define FL_CHECK_LAUNCH(ctx, what) FL_TRY_CUDA(ctx, cudaGetLastError(), what)
+
+static inline size_t fl_align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+static inline unsigned fl_blocks(size_t n, unsigned threads, unsigned cap) {
+    size_t b = (n + threads - 1) / threads;
+    if (b == 0) b = 1;
+    if (b > cap) b = cap;
+    return (unsigned)b;
+}
+
+// Bounded spin budget for decoupled look-back (iterations of a polling loop).
+#define FL_SPIN_LIMIT (1u << 22)

@@ -1,0 +1,138 @@
+"""Loader for the CPU oracle (oracle/_build/liboracle.so) — tests only."""
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+P = ctypes.c_void_p
+_lib = None
+
+
+def ptr(a):
+    return a.ctypes.data_as(P) if a is not None else None
+
+
+class LbmCase(ctypes.Structure):
+    _fields_ = [("ext", ctypes.c_int32 * 3), ("bc", ctypes.c_int32 * 6), ("wall_u", ctypes.c_float * 3),
+                ("inlet_u", ctypes.c_float * 3), ("tau0", ctypes.c_float), ("max_level", ctypes.c_int32),
+                ("has_sphere", ctypes.c_int32), ("sphere_c", ctypes.c_float * 3), ("sphere_r", ctypes.c_float),
+                ("refine_frac", ctypes.c_float), ("coarsen_frac", ctypes.c_float), ("band", ctypes.c_float),
+                ("init_u", ctypes.c_float * 3)]
+
+
+class Mesh(ctypes.Structure):
+    _fields_ = [("x", P), ("y", P), ("z", P), ("level", P), ("state", P), ("flags", P), ("material", P),
+                ("case_id", P), ("n", ctypes.c_size_t)]
+
+
+class Domain(ctypes.Structure):
+    _fields_ = [("depth", ctypes.c_int), ("anchor_level", ctypes.c_int), ("max_level", ctypes.c_int),
+                ("ext", ctypes.c_int32 * 3), ("periodic", ctypes.c_int32 * 3)]
+
+
+class BalanceStats(ctypes.Structure):
+    _fields_ = [("converged", ctypes.c_int32), ("iterations", ctypes.c_uint32), ("violations", ctypes.c_uint32),
+                ("marked", ctypes.c_uint32), ("per_iter_violations", ctypes.c_uint32 * 64),
+                ("per_iter_marked", ctypes.c_uint32 * 64)]
+
+
+class AdaptCfg(ctypes.Structure):
+    _fields_ = [("max_level", ctypes.c_int), ("min_level", ctypes.c_int), ("balance_mode", ctypes.c_int),
+                ("max_balance_iterations", ctypes.c_int), ("enforce_balance", ctypes.c_int),
+                ("averaging_rule", ctypes.c_int)]
+
+
+class AdaptStats(ctypes.Structure):
+    _fields_ = [("num_split", ctypes.c_uint32), ("num_children", ctypes.c_uint32), ("num_groups", ctypes.c_uint32),
+                ("num_merged", ctypes.c_uint32), ("num_survivors", ctypes.c_uint32), ("num_out", ctypes.c_uint32),
+                ("balance", BalanceStats)]
+
+
+def load():
+    global _lib
+    if _lib is None:
+        from oracle.build import build
+        path = build()
+        L = ctypes.CDLL(path)
+        L.or_hilbert_encode1.restype = ctypes.c_uint64
+        L.or_hilbert_encode1.argtypes = [ctypes.c_int32] * 3 + [ctypes.c_uint8]
+        L.or_hilbert_encode.argtypes = [P, P, P, ctypes.c_uint8, P, P, ctypes.c_size_t]
+        L.or_hilbert_decode.argtypes = [P, ctypes.c_uint8, P, P, P, ctypes.c_size_t]
+        L.or_morton8_encode.argtypes = [P, P, P, P, ctypes.c_size_t]
+        L.or_cell_keys.argtypes = [P, P, P, P, P, ctypes.c_int, ctypes.c_int, P, ctypes.c_size_t]
+        L.or_sort_pairs_u64_u32.argtypes = [P, P, ctypes.c_size_t]
+        L.or_scan_exclusive_u32.restype = ctypes.c_uint32
+        L.or_scan_exclusive_u32.argtypes = [P, P, ctypes.c_size_t]
+        L.or_compact_and_permute.restype = ctypes.c_size_t
+        L.or_compact_and_permute.argtypes = [P, P, ctypes.c_size_t, P]
+        L.or_apply_permutation.argtypes = [P, P, ctypes.c_size_t, ctypes.c_size_t, P]
+        L.or_hash_capacity.restype = ctypes.c_uint64
+        L.or_hash_capacity.argtypes = [ctypes.c_size_t]
+        L.or_hash_build.restype = ctypes.c_int
+        L.or_hash_build.argtypes = [P, P, ctypes.c_size_t, ctypes.c_uint64, P, P]
+        L.or_hash_query.argtypes = [P, P, ctypes.c_uint64, P, P, ctypes.c_size_t]
+        L.or_neighbours.argtypes = [ctypes.POINTER(Mesh), ctypes.POINTER(Domain), ctypes.c_int, P]
+        L.or_balance.restype = ctypes.c_int
+        L.or_balance.argtypes = [ctypes.POINTER(Mesh), ctypes.POINTER(Domain), ctypes.c_int, ctypes.c_int,
+                                 ctypes.c_int, ctypes.POINTER(BalanceStats)]
+        L.or_adapt.restype = ctypes.c_size_t
+        L.or_adapt.argtypes = [ctypes.POINTER(Mesh), ctypes.POINTER(Domain), ctypes.POINTER(AdaptCfg), P,
+                               ctypes.c_uint32, ctypes.c_int] + [P] * 12 + [ctypes.POINTER(AdaptStats)]
+        L.or_interp_trilinear.argtypes = [ctypes.POINTER(Mesh), ctypes.POINTER(Domain), P, ctypes.c_uint32,
+                                          P, P, P, P, ctypes.c_size_t, P]
+        L.or_restrict_groups.argtypes = [P, ctypes.c_uint32, P, ctypes.c_size_t, ctypes.c_int, P]
+        L.or_pool_new.restype = P
+        L.or_pool_new.argtypes = [ctypes.POINTER(LbmCase), ctypes.c_int]
+        L.or_pool_free.argtypes = [P]
+        L.or_pool_steps.argtypes = [P, ctypes.c_int, ctypes.c_int]
+        L.or_pool_regrid.argtypes = [P]
+        L.or_pool_flags.argtypes = [P, P, P]
+        L.or_pool_size.restype = ctypes.c_size_t
+        L.or_pool_size.argtypes = [P]
+        L.or_pool_bricks.argtypes = [P, P, P, P, P, P]
+        L.or_pool_nbr.argtypes = [P, P]
+        L.or_pool_populations.argtypes = [P, P]
+        L.or_pool_conservation.argtypes = [P, P]
+        L.or_pool_fluid_lups.restype = ctypes.c_uint64
+        L.or_pool_fluid_lups.argtypes = [P]
+        _lib = L
+    return _lib
+
+
+# ---- numpy conveniences -------------------------------------------------
+def hilbert_encode(x, y, z, level):
+    L = load()
+    x, y, z = (np.ascontiguousarray(a, np.int32) for a in (x, y, z))
+    k = np.empty(len(x), np.uint64)
+    L.or_hilbert_encode(ptr(x), ptr(y), ptr(z), level, ptr(k), None, len(x))
+    return k
+
+
+def hilbert_decode(k, level):
+    L = load()
+    k = np.ascontiguousarray(k, np.uint64)
+    x, y, z = (np.empty(len(k), np.int32) for _ in range(3))
+    L.or_hilbert_decode(ptr(k), level, ptr(x), ptr(y), ptr(z), len(k))
+    return x, y, z
+
+
+def morton8(x, y, z):
+    L = load()
+    x, y, z = (np.ascontiguousarray(a, np.int32) for a in (x, y, z))
+    k = np.empty(len(x), np.uint64)
+    L.or_morton8_encode(ptr(x), ptr(y), ptr(z), ptr(k), len(x))
+    return k
+
+
+def cell_keys(x, y, z, level, case_id, depth, anchor_level):
+    L = load()
+    x, y, z = (np.ascontiguousarray(a, np.int32) for a in (x, y, z))
+    level = np.ascontiguousarray(level, np.uint8)
+    cs = None if case_id is None else np.ascontiguousarray(case_id, np.uint16)
+    k = np.empty(len(x), np.uint64)
+    L.or_cell_keys(ptr(x), ptr(y), ptr(z), ptr(level), ptr(cs), depth, anchor_level, ptr(k), len(x))
+    return k
