@@ -1,0 +1,664 @@
+// amr.cu — octree regrid on the GPU: 2:1 balance, split, merge and the
+// rebuild into key order, fully device-resident.
+//
+// Replaces AdaptationEngine::adapt (src/adaptation/AdaptationEngine.cpp:37-102),
+// BalanceEnforcer::enforce (src/adaptation/BalanceEnforcer.cpp:145-263),
+// SplitEngine::split (src/adaptation/SplitEngine.cpp:95-267),
+// MergeEngine::merge (src/adaptation/MergeEngine.cpp:140-334) and the GPU
+// rebuild (AdaptationEngine.cpp:417-656).  The reference moves every
+// intermediate result through the host (about a dozen blocking transfers per
+// call); here the only host reads are the balance counters (one per
+// iteration) and the output cell count.  Semantics (the oracle's):
+//  * balance FACE6 = the reference kernels (shadow levels, six face probes at
+//    anchor-1 / anchor+size, found at the cell whose shadow level matches,
+//    violation if found level > shadow + 1, at most max_balance_iterations);
+//    FULL26 = every leaf probes its 26 neighbours at its own size and forces
+//    a leaf two or more target levels coarser to refine, to a fixed point;
+//  * split: flag > 0, FLUID, level < max (split_cells.cl:31-33), children
+//    (p << 1) | bit with bit 0 = x, 1 = y, 2 = z (split_cells.cl:87-93);
+//  * merge: first siblings (all coordinates even) with flag -1, FLUID, whose
+//    eight siblings are leaves with flag -1, FLUID at the same level
+//    (merge_cells.cl:11-106), above min_level, numbered by first-sibling index;
+//    in FULL26 mode also no touching leaf outside the group may end above it;
+//  * rebuild: survivors + children (fields copied from the parent) + parents
+//    (children 0..7 summed in order, x0.125 for the arithmetic rule), sorted by
+//    the cell key, flags reset to 0 (the CPU rebuild, AdaptationEngine.cpp:104-276).
+#include "common.cuh"
+#include "amr.cuh"
+#include "hash.cuh"
+#include "keys.cuh"
+#include "scan.cuh"
+
+#include <vector>
+
+namespace {
+
+constexpr int kT = 256;
+
+struct KeyTables {
+    uint8_t t1[96];
+    uint16_t t3[12 * 512];
+};
+
+__device__ __forceinline__ bool fold3(int64_t* p, const fl_domain_dev::Case& d, int A) {
+    for (int a = 0; a < 3; ++a) {
+        int64_t ext = (int64_t)d.ext[a] << A;
+        if (p[a] < 0 || p[a] >= ext) {
+            if (!d.periodic[a]) return false;
+            p[a] = ((p[a] % ext) + ext) % ext;
+        }
+    }
+    return true;
+}
+
+__global__ void k_shadow(fl_mesh_dev m, int mode, uint8_t* __restrict__ shadow) {
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride)
+        shadow[i] = (uint8_t)(m.level[i] + ((mode == 1 && m.flags[i] > 0) ? 1 : 0));
+}
+
+__global__ void k_shadow_update(fl_mesh_dev m, uint8_t* __restrict__ shadow) {
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride)
+        shadow[i] = (uint8_t)(m.level[i] + (m.flags[i] > 0 ? 1 : 0));
+}
+
+// detect_balance_violations (balance_enforce.cl:57-147), exact lookups.
+__global__ void __launch_bounds__(kT) k_detect_face6(fl_mesh_dev m, fl_domain_dev dom, const uint64_t* __restrict__ tk,
+                                                     const uint32_t* __restrict__ tv, int lg,
+                                                     const uint8_t* __restrict__ shadow, uint8_t* __restrict__ viol,
+                                                     uint32_t* __restrict__ count) {
+    __shared__ KeyTables T;
+    fl_keys_fill_tables(T.t1, T.t3, false);
+    __syncthreads();
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    uint32_t local = 0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
+        viol[i] = 0;
+        if (m.state[i] != 0) continue;
+        uint16_t cs = m.case_id ? m.case_id[i] : 0;
+        const fl_domain_dev::Case& d = dom.c[m.case_id ? cs : 0];
+        int sl = shadow[i];
+        int sh = dom.anchor_level - m.level[i];
+        int64_t anc[3] = {(int64_t)m.x[i] << sh, (int64_t)m.y[i] << sh, (int64_t)m.z[i] << sh};
+        int ex = dom.anchor_level - sl;
+        int64_t ss = ex > 0 ? ((int64_t)1 << ex) : 1;
+        for (int f = 0; f < 6; ++f) {
+            int64_t p[3] = {anc[0], anc[1], anc[2]};
+            p[f >> 1] += (f & 1) ? ss : -1;
+            if (!fold3(p, d, dom.anchor_level)) continue;
+            uint32_t r = fl_locate(T.t1, T.t3, tk, tv, lg, shadow, dom, cs, m.case_id != nullptr, p, sl, nullptr);
+            if (r == FL_INVALID_INDEX) continue;
+            if ((int)shadow[r] > sl + 1) { viol[i] = 1; ++local; break; }
+        }
+    }
+    if (local) atomicAdd(count, local);
+}
+
+__global__ void __launch_bounds__(kT) k_detect_full26(fl_mesh_dev m, fl_domain_dev dom, const uint64_t* __restrict__ tk,
+                                                      const uint32_t* __restrict__ tv, int lg,
+                                                      const uint8_t* __restrict__ shadow, uint8_t* __restrict__ viol,
+                                                      uint32_t* __restrict__ count) {
+    __shared__ KeyTables T;
+    fl_keys_fill_tables(T.t1, T.t3, false);
+    __syncthreads();
+    size_t total = m.n * 26;
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    uint32_t local = 0;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
+        size_t i = t / 26;
+        int k = (int)(t - i * 26);
+        uint16_t cs = m.case_id ? m.case_id[i] : 0;
+        const fl_domain_dev::Case& d = dom.c[m.case_id ? cs : 0];
+        int lvl = m.level[i];
+        int sh = dom.anchor_level - lvl;
+        int64_t anc[3] = {(int64_t)m.x[i] << sh, (int64_t)m.y[i] << sh, (int64_t)m.z[i] << sh};
+        int64_t size = (int64_t)1 << sh;
+        int kk = k < 13 ? k : k + 1;
+        int dv[3] = {kk % 3 - 1, (kk / 3) % 3 - 1, kk / 9 - 1};
+        int64_t p[3];
+        for (int a = 0; a < 3; ++a) p[a] = dv[a] < 0 ? anc[a] - 1 : (dv[a] > 0 ? anc[a] + size : anc[a]);
+        if (!fold3(p, d, dom.anchor_level)) continue;
+        uint32_t r = fl_locate(T.t1, T.t3, tk, tv, lg, m.level, dom, cs, m.case_id != nullptr, p, lvl, nullptr);
+        if (r == FL_INVALID_INDEX) continue;
+        if ((int)shadow[i] >= (int)shadow[r] + 2) { viol[r] = 1; ++local; }
+    }
+    if (local) atomicAdd(count, local);
+}
+
+// mark_cascading_refinement (balance_enforce.cl:150-172).
+__global__ void k_mark(fl_mesh_dev m, int32_t* __restrict__ flags, const uint8_t* __restrict__ viol, int max_level,
+                       uint32_t* __restrict__ count) {
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    uint32_t local = 0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
+        if (!viol[i] || m.state[i] != 0 || m.level[i] >= max_level) continue;
+        if (flags[i] <= 0) { flags[i] = 1; ++local; }
+    }
+    if (local) atomicAdd(count, local);
+}
+
+__global__ void k_clear_u8(uint8_t* p, size_t n) {
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) p[i] = 0;
+}
+
+// Sibling lookup for a first sibling; returns false if the octet is not mergeable.
+__device__ bool find_group(const KeyTables& T, const fl_mesh_dev& m, const fl_domain_dev& dom,
+                           const uint64_t* tk, const uint32_t* tv, int lg, size_t i, int min_level, uint32_t* mem) {
+    if (m.flags[i] != -1 || m.state[i] != 0) return false;
+    if ((m.x[i] & 1) || (m.y[i] & 1) || (m.z[i] & 1)) return false;
+    int l = m.level[i];
+    if (l <= min_level) return false;
+    uint16_t cs = m.case_id ? m.case_id[i] : 0;
+    int sh = dom.anchor_level - l;
+    for (int c = 0; c < 8; ++c) {
+        int64_t sx = m.x[i] | (c & 1), sy = m.y[i] | ((c >> 1) & 1), sz = m.z[i] | ((c >> 2) & 1);
+        uint64_t key = fl_anchor_key(T.t1, T.t3, dom.depth, cs, m.case_id != nullptr, sx << sh, sy << sh, sz << sh);
+        uint32_t j = fl_hash_lookup(tk, tv, lg, key);
+        if (j == FL_INVALID_INDEX) return false;
+        if (m.level[j] != l || m.flags[j] != -1 || m.state[j] != 0) return false;
+        mem[c] = j;
+    }
+    return true;
+}
+
+__device__ bool group_balanced(const KeyTables& T, const fl_mesh_dev& m, const fl_domain_dev& dom,
+                               const uint64_t* tk, const uint32_t* tv, int lg, const uint8_t* shadow,
+                               const uint32_t* mem) {
+    uint16_t cs = m.case_id ? m.case_id[mem[0]] : 0;
+    const fl_domain_dev::Case& d = dom.c[m.case_id ? cs : 0];
+    int l = m.level[mem[0]];
+    for (int c = 0; c < 8; ++c) {
+        size_t j = mem[c];
+        int sh = dom.anchor_level - l;
+        int64_t anc[3] = {(int64_t)m.x[j] << sh, (int64_t)m.y[j] << sh, (int64_t)m.z[j] << sh};
+        int64_t size = (int64_t)1 << sh;
+        for (int k = 0; k < 26; ++k) {
+            int kk = k < 13 ? k : k + 1;
+            int dv[3] = {kk % 3 - 1, (kk / 3) % 3 - 1, kk / 9 - 1};
+            int64_t p[3];
+            for (int a = 0; a < 3; ++a) p[a] = dv[a] < 0 ? anc[a] - 1 : (dv[a] > 0 ? anc[a] + size : anc[a]);
+            if (!fold3(p, d, dom.anchor_level)) continue;
+            uint32_t r = fl_locate(T.t1, T.t3, tk, tv, lg, m.level, dom, cs, m.case_id != nullptr, p, l, nullptr);
+            if (r == FL_INVALID_INDEX) continue;
+            bool inside = false;
+            for (int q = 0; q < 8; ++q) inside |= (mem[q] == r);
+            if (!inside && (int)shadow[r] > l) return false;
+        }
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(kT) k_leaders(fl_mesh_dev m, fl_domain_dev dom, const uint64_t* __restrict__ tk,
+                                                const uint32_t* __restrict__ tv, int lg, int min_level, int check26,
+                                                const uint8_t* __restrict__ shadow, uint32_t* __restrict__ is_leader) {
+    __shared__ KeyTables T;
+    fl_keys_fill_tables(T.t1, T.t3, false);
+    __syncthreads();
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
+        uint32_t mem[8];
+        bool ok = find_group(T, m, dom, tk, tv, lg, i, min_level, mem);
+        if (ok && check26) ok = group_balanced(T, m, dom, tk, tv, lg, shadow, mem);
+        is_leader[i] = ok ? 1u : 0u;
+    }
+}
+
+__global__ void __launch_bounds__(kT) k_members(fl_mesh_dev m, fl_domain_dev dom, const uint64_t* __restrict__ tk,
+                                                const uint32_t* __restrict__ tv, int lg, int min_level,
+                                                const uint32_t* __restrict__ is_leader,
+                                                const uint32_t* __restrict__ gid, uint32_t* __restrict__ members,
+                                                uint32_t* __restrict__ group_of) {
+    __shared__ KeyTables T;
+    fl_keys_fill_tables(T.t1, T.t3, false);
+    __syncthreads();
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
+        if (!is_leader[i]) continue;
+        uint32_t mem[8];
+        find_group(T, m, dom, tk, tv, lg, i, min_level, mem);
+        uint32_t g = gid[i];
+        for (int c = 0; c < 8; ++c) {
+            members[(size_t)g * 8 + c] = mem[c];
+            group_of[mem[c]] = g;
+        }
+    }
+}
+
+// Output count per old cell.
+__global__ void k_counts(fl_mesh_dev m, int max_level, const uint32_t* __restrict__ is_leader,
+                         const uint32_t* __restrict__ group_of, uint32_t* __restrict__ cnt) {
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
+        bool split = m.flags[i] > 0 && m.state[i] == 0 && m.level[i] < max_level;
+        uint32_t c;
+        if (split) c = 8;
+        else if (group_of[i] != FL_INVALID_INDEX) c = is_leader[i] ? 1u : 0u;
+        else c = 1;
+        cnt[i] = c;
+    }
+}
+
+// Intermediate items in old-index order + their keys.
+__global__ void __launch_bounds__(kT) k_emit(fl_mesh_dev m, fl_domain_dev dom, int max_level,
+                                             const uint32_t* __restrict__ off, const uint32_t* __restrict__ is_leader,
+                                             const uint32_t* __restrict__ group_of, fl_items it) {
+    __shared__ KeyTables T;
+    fl_keys_fill_tables(T.t1, T.t3, false);
+    __syncthreads();
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
+        uint16_t cs = m.case_id ? m.case_id[i] : 0;
+        bool split = m.flags[i] > 0 && m.state[i] == 0 && m.level[i] < max_level;
+        uint32_t o = off[i];
+        auto put = [&](uint32_t j, int32_t x, int32_t y, int32_t z, uint8_t l, uint32_t src, uint8_t kind) {
+            it.x[j] = x; it.y[j] = y; it.z[j] = z; it.level[j] = l;
+            it.state[j] = m.state[i]; it.material[j] = m.material[i];
+            if (it.case_id) it.case_id[j] = cs;
+            it.src[j] = src; it.kind[j] = kind;
+            int sh = dom.anchor_level - l;
+            it.key[j] = fl_anchor_key(T.t1, T.t3, dom.depth, cs, m.case_id != nullptr, (int64_t)x << sh,
+                                      (int64_t)y << sh, (int64_t)z << sh);
+            it.pos[j] = j;
+        };
+        if (split) {
+            for (int c = 0; c < 8; ++c)
+                put(o + c, (m.x[i] << 1) | (c & 1), (m.y[i] << 1) | ((c >> 1) & 1), (m.z[i] << 1) | ((c >> 2) & 1),
+                    (uint8_t)(m.level[i] + 1), (uint32_t)i, (uint8_t)c);
+        } else if (group_of[i] != FL_INVALID_INDEX) {
+            if (is_leader[i])
+                put(o, m.x[i] >> 1, m.y[i] >> 1, m.z[i] >> 1, (uint8_t)(m.level[i] - 1), group_of[i], 9);
+        } else {
+            put(o, m.x[i], m.y[i], m.z[i], m.level[i], (uint32_t)i, 8);
+        }
+    }
+}
+
+// Final gather in key order; fields AoS (C per cell) with the reference's
+// prolongation (copy) and restriction (ordered sum, x0.125 for rule 0).
+__global__ void k_gather(fl_items it, const uint32_t* __restrict__ perm, size_t M, fl_mesh_out out,
+                         const float* __restrict__ fin, float* __restrict__ fout, uint32_t C, int rule,
+                         const uint32_t* __restrict__ members, uint32_t* __restrict__ osrc, uint8_t* __restrict__ okind) {
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < M; j += stride) {
+        uint32_t p = perm[j];
+        out.x[j] = it.x[p]; out.y[j] = it.y[p]; out.z[j] = it.z[p];
+        out.level[j] = it.level[p]; out.state[j] = it.state[p]; out.material[j] = it.material[p];
+        out.flags[j] = 0;
+        if (out.case_id) out.case_id[j] = it.case_id[p];
+        uint32_t src = it.src[p];
+        uint8_t kind = it.kind[p];
+        if (osrc) osrc[j] = src;
+        if (okind) okind[j] = kind;
+        if (fin && C) {
+            float* o = fout + j * C;
+            if (kind <= 8) {
+                const float* s = fin + (size_t)src * C;
+                for (uint32_t c = 0; c < C; ++c) o[c] = s[c];
+            } else {
+                const uint32_t* mem = members + (size_t)src * 8;
+                for (uint32_t c = 0; c < C; ++c) {
+                    float s = 0.0f;
+                    for (int q = 0; q < 8; ++q) s = __fadd_rn(s, fin[(size_t)mem[q] * C + c]);
+                    o[c] = rule == 1 ? s : __fmul_rn(s, 0.125f);
+                }
+            }
+        }
+    }
+}
+
+// Scratch carving helper.
+struct Carver {
+    char* p;
+    template <typename T>
+    T* take(size_t n) {
+        T* r = (T*)p;
+        p += fl_align256(n * sizeof(T));
+        return r;
+    }
+};
+
+}  // namespace
+
+fl_domain_dev fl_domain_from_config(fl_ctx* ctx, const fl_adapt_config* cfg, void* dev_case_slot) {
+    fl_domain_dev d;
+    d.depth = cfg->key_depth ? cfg->key_depth : 21;
+    d.anchor_level = cfg->anchor_level ? cfg->anchor_level : 21;
+    d.max_level = d.anchor_level;
+    fl_domain_dev::Case h;
+    for (int a = 0; a < 3; ++a) {
+        h.ext[a] = cfg->ext[a] > 0 ? cfg->ext[a] : 1;
+        h.periodic[a] = cfg->periodic[a];
+    }
+    cudaMemcpyAsync(dev_case_slot, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->stream);
+    d.c = (const fl_domain_dev::Case*)dev_case_slot;
+    return d;
+}
+
+size_t fl_adapt_scratch_bytes(size_t n, uint64_t cap) {
+    size_t M = n * 8 + 8;
+    size_t b = 0;
+    b += fl_align256(n * 8);                 // old keys
+    b += fl_align256(n * 4);                 // iota
+    b += fl_align256(cap * 8) + 2 * fl_align256(cap * 4);  // table + win
+    b += 2 * fl_align256(n);                 // shadow, viol
+    b += 4 * fl_align256(n * 4);             // leader, gid, group_of, cnt/off
+    b += fl_align256(n * 4);                 // members (n/8 groups * 8)
+    b += fl_align256(64);                    // counters
+    b += fl_align256(M * 4) * 5 + fl_align256(M) * 3 + fl_align256(M * 2) + fl_align256(M * 8) * 1;  // items
+    b += fl_scan_scratch_bytes(n) + fl_sort_scratch_bytes(M, 8) + 4096;
+    return b;
+}
+
+// Balance over a mesh with an already-built table (shared by fl_balance_enforce and fl_adapt).
+int fl_balance_run(fl_ctx* ctx, fl_mesh_dev md, int32_t* flags, const fl_domain_dev& dom, const uint64_t* tk,
+                   const uint32_t* tv, uint64_t cap, int mode, int max_level, int max_iters, uint8_t* shadow,
+                   uint8_t* viol, uint32_t* counters, fl_balance_result* res) {
+    fl_balance_result r{};
+    if (md.n == 0) { r.converged = 1; if (res) *res = r; return FL_OK; }
+    unsigned nb = fl_blocks(md.n, kT, ctx->num_sms * 8);
+    int lg = fl_hash_lg(cap);
+    k_shadow<<<nb, kT, 0, ctx->stream>>>(md, mode, shadow);
+    FL_CHECK_LAUNCH(ctx, "k_shadow");
+    int cap_it = mode == 0 ? max_iters : 4096;
+    uint32_t it = 0;
+    uint32_t h[2];
+    for (; it < (uint32_t)cap_it; ++it) {
+        FL_TRY_CUDA(ctx, cudaMemsetAsync(counters, 0, 8, ctx->stream), "balance counters");
+        if (mode == 0) {
+            k_detect_face6<<<nb, kT, 0, ctx->stream>>>(md, dom, tk, tv, lg, shadow, viol, counters);
+        } else {
+            k_clear_u8<<<nb, kT, 0, ctx->stream>>>(viol, md.n);
+            k_detect_full26<<<fl_blocks(md.n * 26, kT, ctx->num_sms * 8), kT, 0, ctx->stream>>>(md, dom, tk, tv, lg,
+                                                                                              shadow, viol, counters);
+        }
+        FL_CHECK_LAUNCH(ctx, "k_detect");
+        k_mark<<<nb, kT, 0, ctx->stream>>>(md, flags, viol, max_level, counters + 1);
+        FL_CHECK_LAUNCH(ctx, "k_mark");
+        FL_TRY_CUDA(ctx, cudaMemcpyAsync(h, counters, 8, cudaMemcpyDeviceToHost, ctx->stream), "balance read");
+        FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "balance sync");
+        r.total_violations_detected += h[0];
+        if (h[0] == 0) { r.converged = 1; r.iterations = it + 1; break; }
+        // k_mark ran after detection regardless; with zero violations it marks nothing
+        r.total_cells_marked_for_balance += h[1];
+        if (h[1] == 0) { r.converged = 0; r.iterations = it + 1; break; }
+        k_shadow_update<<<nb, kT, 0, ctx->stream>>>(md, shadow);
+        FL_CHECK_LAUNCH(ctx, "k_shadow_update");
+    }
+    if (it == (uint32_t)cap_it) { r.converged = 0; r.iterations = it; }
+    if (res) *res = r;
+    return FL_OK;
+}
+
+// Scratch layout of one regrid (carved identically by both phases).
+struct AdaptWork {
+    uint64_t cap;
+    uint64_t* keys; uint64_t* tk; uint32_t* tv; uint32_t* win;
+    uint8_t* shadow; uint8_t* viol;
+    uint32_t* leader; uint32_t* gid; uint32_t* group_of; uint32_t* cnt; uint32_t* members; uint32_t* counters;
+    fl_items it;
+    void* scan_scratch; void* sort_scratch;
+};
+
+static AdaptWork carve_adapt(void* scratch, size_t n, bool with_case) {
+    AdaptWork w;
+    w.cap = fl_table_capacity(n);
+    Carver cv{(char*)scratch};
+    w.keys = cv.take<uint64_t>(n);
+    w.tk = cv.take<uint64_t>(w.cap);
+    w.tv = cv.take<uint32_t>(w.cap);
+    w.win = cv.take<uint32_t>(w.cap);
+    w.shadow = cv.take<uint8_t>(n);
+    w.viol = cv.take<uint8_t>(n);
+    w.leader = cv.take<uint32_t>(n);
+    w.gid = cv.take<uint32_t>(n);
+    w.group_of = cv.take<uint32_t>(n);
+    w.cnt = cv.take<uint32_t>(n);
+    w.members = cv.take<uint32_t>(n + 8);
+    w.counters = cv.take<uint32_t>(16);
+    size_t Mcap = n * 8 + 8;
+    w.it.x = cv.take<int32_t>(Mcap); w.it.y = cv.take<int32_t>(Mcap); w.it.z = cv.take<int32_t>(Mcap);
+    w.it.src = cv.take<uint32_t>(Mcap); w.it.pos = cv.take<uint32_t>(Mcap);
+    w.it.level = cv.take<uint8_t>(Mcap); w.it.state = cv.take<uint8_t>(Mcap); w.it.kind = cv.take<uint8_t>(Mcap);
+    w.it.case_id = with_case ? cv.take<uint16_t>(Mcap) : nullptr;
+    w.it.material = cv.take<uint32_t>(Mcap);
+    w.it.key = cv.take<uint64_t>(Mcap);
+    w.scan_scratch = cv.take<char>(fl_scan_scratch_bytes(n));
+    w.sort_scratch = cv.p;
+    return w;
+}
+
+__global__ void k_count_kinds(fl_mesh_dev m, int max_level, const uint32_t* __restrict__ group_of,
+                              uint32_t* __restrict__ counters) {
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    uint32_t ns = 0, nv = 0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
+        bool split = m.flags[i] > 0 && m.state[i] == 0 && m.level[i] < max_level;
+        if (split) ++ns;
+        else if (group_of[i] == FL_INVALID_INDEX) ++nv;
+    }
+    if (ns) atomicAdd(counters + 4, ns);
+    if (nv) atomicAdd(counters + 5, nv);
+}
+
+// Phase 1: balance, classify, emit the unsorted new cell list; returns its size.
+int fl_adapt_prepare(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, const fl_domain_dev& dom,
+                     bool run_balance, void* scratch, size_t* M_out, fl_adapt_stats* st) {
+    size_t n = mesh->num_cells;
+    fl_adapt_stats s{};
+    *M_out = 0;
+    if (n == 0) { if (st) *st = s; return FL_OK; }
+    AdaptWork w = carve_adapt(scratch, n, mesh->case_id != nullptr);
+    fl_mesh_dev md{mesh->x, mesh->y, mesh->z, mesh->level, mesh->state, mesh->flags, mesh->material,
+                   mesh->case_id, n};
+    int rc = fl_launch_cell_keys(ctx, mesh->x, mesh->y, mesh->z, mesh->level, mesh->case_id, dom.depth,
+                                 dom.anchor_level, w.keys, n);
+    if (rc) return rc;
+    rc = fl_hash_build_with(ctx, w.tk, w.tv, w.cap, w.keys, nullptr, n, w.win);  // value = input index
+    if (rc) return rc;
+    FL_TRY_CUDA(ctx, cudaMemsetAsync(w.counters, 0, 64, ctx->stream), "adapt counters");
+    if (run_balance) {
+        rc = fl_balance_run(ctx, md, mesh->flags, dom, w.tk, w.tv, w.cap, cfg->balance_mode, cfg->max_refinement_level,
+                            (int)cfg->max_balance_iterations, w.shadow, w.viol, w.counters + 8, &s.balance);
+        if (rc) return rc;
+    }
+    unsigned nb = fl_blocks(n, kT, ctx->num_sms * 8);
+    int lg = fl_hash_lg(w.cap);
+    k_shadow_update<<<nb, kT, 0, ctx->stream>>>(md, w.shadow);
+    FL_CHECK_LAUNCH(ctx, "k_shadow_update");
+    int check26 = cfg->enforce_2_1_balance && cfg->balance_mode == 1;
+    k_leaders<<<nb, kT, 0, ctx->stream>>>(md, dom, w.tk, w.tv, lg, cfg->min_refinement_level, check26, w.shadow,
+                                          w.leader);
+    FL_CHECK_LAUNCH(ctx, "k_leaders");
+    rc = fl_scan_u32_with(ctx, w.leader, w.gid, n, w.counters + 2, w.scan_scratch);
+    if (rc) return rc;
+    rc = fl_launch_fill_u32(ctx, w.group_of, FL_INVALID_INDEX, n);
+    if (rc) return rc;
+    k_members<<<nb, kT, 0, ctx->stream>>>(md, dom, w.tk, w.tv, lg, cfg->min_refinement_level, w.leader, w.gid,
+                                          w.members, w.group_of);
+    FL_CHECK_LAUNCH(ctx, "k_members");
+    k_counts<<<nb, kT, 0, ctx->stream>>>(md, cfg->max_refinement_level, w.leader, w.group_of, w.cnt);
+    FL_CHECK_LAUNCH(ctx, "k_counts");
+    k_count_kinds<<<nb, kT, 0, ctx->stream>>>(md, cfg->max_refinement_level, w.group_of, w.counters);
+    FL_CHECK_LAUNCH(ctx, "k_count_kinds");
+    rc = fl_scan_u32_with(ctx, w.cnt, w.cnt, n, w.counters + 3, w.scan_scratch);
+    if (rc) return rc;
+    k_emit<<<nb, kT, 0, ctx->stream>>>(md, dom, cfg->max_refinement_level, w.cnt, w.leader, w.group_of, w.it);
+    FL_CHECK_LAUNCH(ctx, "k_emit");
+    uint32_t hc[6] = {0, 0, 0, 0, 0, 0};
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(hc, w.counters, 24, cudaMemcpyDeviceToHost, ctx->stream), "adapt counts");
+    rc = fl_collect_device_status(ctx, "fl_adapt");
+    if (rc) return rc;
+    s.num_groups = hc[2];
+    s.num_merged = hc[2] * 8;
+    s.num_split = hc[4];
+    s.num_children = hc[4] * 8;
+    s.num_survivors = hc[5];
+    s.num_cells_out = hc[3];
+    *M_out = hc[3];
+    if (st) *st = s;
+    return FL_OK;
+}
+
+// Phase 2: sort the emitted list by key and gather into `out` (capacity >= M).
+int fl_adapt_finish(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, const fl_domain_dev& dom,
+                    void* scratch, size_t M, const float* fields, uint32_t C, fl_mesh* out, float* out_fields,
+                    uint32_t* osrc, uint8_t* okind, uint32_t* omembers, uint32_t num_groups) {
+    size_t n = mesh->num_cells;
+    if (n == 0 || M == 0) return FL_OK;
+    AdaptWork w = carve_adapt(scratch, n, mesh->case_id != nullptr);
+    int end_bit = 3 * dom.depth + (mesh->case_id ? 12 : 0);
+    if (end_bit > 64) end_bit = 64;
+    int rc = fl_sort_pairs_with(ctx, w.it.key, w.it.pos, M, 0, end_bit, w.sort_scratch);
+    if (rc) return rc;
+    fl_mesh_out o{out->x, out->y, out->z, out->level, out->state, out->flags, out->material,
+                  mesh->case_id ? out->case_id : nullptr};
+    k_gather<<<fl_blocks(M, kT, ctx->num_sms * 8), kT, 0, ctx->stream>>>(w.it, w.it.pos, M, o, fields, out_fields, C,
+                                                                         cfg->averaging_rule, w.members, osrc, okind);
+    FL_CHECK_LAUNCH(ctx, "k_gather");
+    if (omembers && num_groups)
+        FL_TRY_CUDA(ctx, cudaMemcpyAsync(omembers, w.members, (size_t)num_groups * 32, cudaMemcpyDeviceToDevice,
+                                         ctx->stream), "members copy");
+    return FL_OK;
+}
+
+extern "C" {
+
+int fl_mesh_alloc(fl_ctx* ctx, size_t capacity, int with_case_id, fl_mesh* m) {
+    if (!ctx || !m) return FL_E_INVALID_ARG;
+    *m = fl_mesh{};
+    if (capacity == 0) capacity = 1;
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&m->x, capacity * 4, ctx->stream), "mesh alloc");
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&m->y, capacity * 4, ctx->stream), "mesh alloc");
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&m->z, capacity * 4, ctx->stream), "mesh alloc");
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&m->level, capacity, ctx->stream), "mesh alloc");
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&m->state, capacity, ctx->stream), "mesh alloc");
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&m->flags, capacity * 4, ctx->stream), "mesh alloc");
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&m->material, capacity * 4, ctx->stream), "mesh alloc");
+    if (with_case_id) FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&m->case_id, capacity * 2, ctx->stream), "mesh alloc");
+    m->capacity = capacity;
+    m->num_cells = 0;
+    return FL_OK;
+}
+
+int fl_mesh_free(fl_ctx* ctx, fl_mesh* m) {
+    if (!ctx || !m) return FL_E_INVALID_ARG;
+    void* ps[8] = {m->x, m->y, m->z, m->level, m->state, m->flags, m->material, m->case_id};
+    for (void* p : ps)
+        if (p) cudaFreeAsync(p, ctx->stream);
+    *m = fl_mesh{};
+    FL_TRY_CUDA(ctx, cudaGetLastError(), "mesh free");
+    return FL_OK;
+}
+
+int fl_balance_enforce(fl_ctx* ctx, fl_mesh* mesh, const fl_adapt_config* cfg, fl_balance_result* res) {
+    if (!ctx || !mesh || !cfg) return FL_E_INVALID_ARG;
+    size_t n = mesh->num_cells;
+    if (res) *res = fl_balance_result{};
+    if (n == 0) { if (res) res->converged = 1; return FL_OK; }
+    uint64_t cap = fl_table_capacity(n);
+    size_t need = fl_align256(n * 8) + fl_align256(cap * 8) + 2 * fl_align256(cap * 4) + 2 * fl_align256(n) + 512 + 256;
+    int rc = fl_scratch_reserve(ctx, need);
+    if (rc) return rc;
+    Carver cv{(char*)ctx->scratch};
+    void* dcase = cv.take<char>(256);
+    uint64_t* keys = cv.take<uint64_t>(n);
+    uint64_t* tk = cv.take<uint64_t>(cap);
+    uint32_t* tv = cv.take<uint32_t>(cap);
+    uint32_t* win = cv.take<uint32_t>(cap);
+    uint8_t* shadow = cv.take<uint8_t>(n);
+    uint8_t* viol = cv.take<uint8_t>(n);
+    uint32_t* counters = cv.take<uint32_t>(16);
+    fl_domain_dev dom = fl_domain_from_config(ctx, cfg, dcase);
+    rc = fl_launch_cell_keys(ctx, mesh->x, mesh->y, mesh->z, mesh->level, mesh->case_id, dom.depth, dom.anchor_level,
+                             keys, n);
+    if (rc) return rc;
+    rc = fl_hash_build_with(ctx, tk, tv, cap, keys, nullptr, n, win);
+    if (rc) return rc;
+    fl_mesh_dev md{mesh->x, mesh->y, mesh->z, mesh->level, mesh->state, mesh->flags, mesh->material, mesh->case_id, n};
+    fl_balance_result r;
+    rc = fl_balance_run(ctx, md, mesh->flags, dom, tk, tv, cap, cfg->balance_mode, cfg->max_refinement_level,
+                        (int)cfg->max_balance_iterations, shadow, viol, counters, &r);
+    if (rc) return rc;
+    rc = fl_collect_device_status(ctx, "fl_balance_enforce");
+    if (rc) return rc;
+    if (res) *res = r;
+    return r.converged ? FL_OK : FL_E_BALANCE_NOT_CONVERGED;
+}
+
+int fl_neighbour_rebuild(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, int subslots, uint32_t* nbr) {
+    if (!ctx || !mesh || !cfg || !nbr || (subslots != 1 && subslots != 4)) return FL_E_INVALID_ARG;
+    size_t n = mesh->num_cells;
+    if (n == 0) return FL_OK;
+    uint64_t cap = fl_table_capacity(n);
+    int rc = fl_scratch_reserve(ctx, 256 + fl_align256(n * 8) + fl_align256(cap * 8) + 2 * fl_align256(cap * 4) + 256);
+    if (rc) return rc;
+    Carver cv{(char*)ctx->scratch};
+    void* dcase = cv.take<char>(256);
+    uint64_t* keys = cv.take<uint64_t>(n);
+    uint64_t* tk = cv.take<uint64_t>(cap);
+    uint32_t* tv = cv.take<uint32_t>(cap);
+    uint32_t* win = cv.take<uint32_t>(cap);
+    fl_domain_dev dom = fl_domain_from_config(ctx, cfg, dcase);
+    dom.max_level = cfg->max_refinement_level;
+    rc = fl_launch_cell_keys(ctx, mesh->x, mesh->y, mesh->z, mesh->level, mesh->case_id, dom.depth, dom.anchor_level,
+                             keys, n);
+    if (rc) return rc;
+    rc = fl_hash_build_with(ctx, tk, tv, cap, keys, nullptr, n, win);
+    if (rc) return rc;
+    fl_mesh_dev md{mesh->x, mesh->y, mesh->z, mesh->level, mesh->state, mesh->flags, mesh->material, mesh->case_id, n};
+    rc = fl_neighbours_with(ctx, md, dom, tk, tv, cap, subslots, nbr);
+    if (rc) return rc;
+    return fl_collect_device_status(ctx, "fl_neighbour_rebuild");
+}
+
+int fl_adapt(fl_ctx* ctx, fl_mesh* mesh, const fl_adapt_config* cfg, float** fields, uint32_t C,
+             fl_adapt_stats* stats) {
+    if (!ctx || !mesh || !cfg) return FL_E_INVALID_ARG;
+    if (C && (!fields || !*fields)) return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_adapt: components without fields");
+    if (cfg->max_refinement_level > 21 || cfg->min_refinement_level > cfg->max_refinement_level)
+        return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_adapt: bad level limits (AdaptationConfig::validate)");
+    size_t n = mesh->num_cells;
+    if (stats) *stats = fl_adapt_stats{};
+    if (n == 0) return FL_OK;
+    int rc = fl_scratch_reserve(ctx, fl_adapt_scratch_bytes(n, fl_table_capacity(n)) + 512);
+    if (rc) return rc;
+    void* dcase = ctx->scratch;
+    void* scratch = (char*)ctx->scratch + 512;
+    fl_domain_dev dom = fl_domain_from_config(ctx, cfg, dcase);
+    dom.max_level = cfg->max_refinement_level > 0 ? cfg->max_refinement_level : dom.anchor_level;
+    size_t M = 0;
+    fl_adapt_stats s{};
+    rc = fl_adapt_prepare(ctx, mesh, cfg, dom, cfg->enforce_2_1_balance != 0, scratch, &M, &s);
+    if (rc) return rc;
+    // no change: keep the buffers (AdaptationEngine.cpp:72-77), flags still reset below
+    size_t cap_out = mesh->capacity;
+    if (M > cap_out) {  // growth rule of AdaptationEngine.cpp:473-478
+        double g = cfg->buffer_growth_factor > 1.0 ? cfg->buffer_growth_factor : 1.5;
+        size_t a = (size_t)((double)M * g), b = M + 1024;
+        cap_out = a > b ? a : b;
+    }
+    fl_mesh out{};
+    rc = fl_mesh_alloc(ctx, cap_out, mesh->case_id != nullptr, &out);
+    if (rc) return rc;
+    float* nf = nullptr;
+    if (C) FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&nf, cap_out * C * 4, ctx->stream), "fields alloc");
+    rc = fl_adapt_finish(ctx, mesh, cfg, dom, scratch, M, C ? *fields : nullptr, C, &out, nf, nullptr, nullptr,
+                         nullptr, s.num_groups);
+    if (rc) return rc;
+    fl_mesh old = *mesh;
+    fl_mesh_free(ctx, &old);
+    if (C) {
+        cudaFreeAsync(*fields, ctx->stream);
+        *fields = nf;
+    }
+    out.num_cells = M;
+    out.capacity = cap_out;
+    *mesh = out;
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "fl_adapt");
+    if (stats) *stats = s;
+    return (s.balance.converged || !cfg->enforce_2_1_balance) ? FL_OK : FL_E_BALANCE_NOT_CONVERGED;
+}
+
+}  // extern "C"

@@ -1,0 +1,92 @@
+// hash.cuh — device hash lookup, mesh/domain views and point location.
+#pragma once
+#include "common.cuh"
+#include "keys.cuh"
+
+// Device view of a mesh (native-level coordinates, one entry per leaf).
+struct fl_mesh_dev {
+    const int32_t* x;
+    const int32_t* y;
+    const int32_t* z;
+    const uint8_t* level;
+    const uint8_t* state;
+    const int32_t* flags;
+    const uint32_t* material;
+    const uint16_t* case_id;  // may be null: one case
+    size_t n;
+};
+
+// Key/anchor geometry plus per-case extent (level-0 cells) and periodicity.
+struct fl_domain_dev {
+    int depth;         // key levels: hilbert::encode(anchor, depth)
+    int anchor_level;  // anchor = native << (anchor_level - level)
+    int max_level;     // deepest level a probe may land on
+    struct Case {
+        int32_t ext[3];
+        int32_t periodic[3];
+    };
+    const Case* c;     // device array indexed by case id ([0] when the mesh has none)
+};
+
+static __device__ __forceinline__ uint64_t fl_hash_slot(uint64_t key, int lg) {
+    uint64_t h = key * 0x9e3779b97f4a7c15ull;
+    return lg ? (h >> (64 - lg)) : 0ull;
+}
+
+// hash_query (kernels/hashmap/hash_query.cl:22-56) with the slot rule above.
+static __device__ __forceinline__ uint32_t fl_hash_lookup(const uint64_t* __restrict__ tk,
+                                                          const uint32_t* __restrict__ tv, int lg, uint64_t key) {
+    if (key == FL_EMPTY_KEY) return FL_INVALID_INDEX;
+    const uint64_t mask = (1ull << lg) - 1;
+    uint64_t s = fl_hash_slot(key, lg);
+    for (int p = 0; p < 256; ++p) {
+        uint64_t k = __ldg((const unsigned long long*)(tk + s));
+        if (k == key) return __ldg(tv + s);
+        if (k == FL_EMPTY_KEY) return FL_INVALID_INDEX;
+        s = (s + 1) & mask;
+    }
+    return FL_INVALID_INDEX;
+}
+
+static __device__ __forceinline__ uint64_t fl_anchor_key(const uint8_t* t1, const uint16_t* t3, int depth,
+                                                         uint16_t cs, bool has_case, int64_t ax, int64_t ay,
+                                                         int64_t az) {
+    uint64_t k = fl_hilbert_encode_dev(t1, t3, (uint32_t)ax, (uint32_t)ay, (uint32_t)az, depth);
+    if (has_case) k |= (uint64_t)cs << (3 * depth);
+    return k;
+}
+
+// Point location: the leaf whose `lv` equals l and whose anchor equals p with
+// the low (A - l) bits cleared.  Levels are probed outward from `start`; in a
+// valid leaf set at most one level matches, so the order does not change the
+// answer, only the number of lookups.
+static __device__ __forceinline__ uint32_t fl_locate(const uint8_t* t1, const uint16_t* t3,
+                                                     const uint64_t* __restrict__ tk, const uint32_t* __restrict__ tv,
+                                                     int lg, const uint8_t* __restrict__ lv, const fl_domain_dev& dom,
+                                                     uint16_t cs, bool has_case, const int64_t* p, int start,
+                                                     const uint8_t* unused) {
+    (void)unused;
+    int maxl = dom.max_level;
+    if (start > maxl) start = maxl;
+    if (start < 0) start = 0;
+    for (int step = 0; step <= 2 * maxl + 1; ++step) {
+        int off = (step + 1) >> 1;
+        int l = (step & 1) ? start - off : start + off;
+        if (step == 0) l = start;
+        if (l < 0 || l > maxl) continue;
+        int sh = dom.anchor_level - l;
+        int64_t mask = ~(((int64_t)1 << sh) - 1);
+        uint64_t key = fl_anchor_key(t1, t3, dom.depth, cs, has_case, p[0] & mask, p[1] & mask, p[2] & mask);
+        uint32_t idx = fl_hash_lookup(tk, tv, lg, key);
+        if (idx != FL_INVALID_INDEX && lv[idx] == l) return idx;
+    }
+    return FL_INVALID_INDEX;
+}
+
+int fl_hash_lg(uint64_t cap);
+uint64_t fl_table_capacity(size_t n);
+// Clear + build; `win` is cap uint32 of scratch.
+int fl_hash_build_with(fl_ctx* ctx, uint64_t* tk, uint32_t* tv, uint64_t cap, const uint64_t* keys,
+                       const uint32_t* vals, size_t n, uint32_t* win);
+int fl_neighbours_with(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom, const uint64_t* tk,
+                       const uint32_t* tv, uint64_t cap, int subslots, uint32_t* nbr);

@@ -80,6 +80,101 @@ uint64_t fl_hilbert_get_parent(uint64_t key, uint8_t level);
 uint64_t fl_hilbert_get_child(uint64_t key, uint8_t level, uint8_t quadrant);
 int fl_hilbert_is_valid(uint64_t key, uint8_t level);
 
+/* ---- scan / sort / compaction */
+/* Exclusive scan of uint32 (single pass, decoupled look-back), any n < 2^32.
+ * Replaces AdaptationEngine::exclusiveScan (src/adaptation/AdaptationEngine.cpp:360-415).
+ * total (device pointer, may be NULL) receives the sum.  in == out is allowed. */
+int fl_scan_exclusive_u32(fl_ctx* ctx, const uint32_t* in, uint32_t* out, size_t n, uint32_t* total);
+/* Stable ascending LSD radix sort of (key, value) pairs in place on bits [begin_bit, end_bit).
+ * Replaces RadixSort::sortByKey (include/fluidloom/core/hashmap/RadixSort.h:33-35). */
+int fl_sort_pairs_u64_u32(fl_ctx* ctx, uint64_t* keys, uint32_t* vals, size_t n, int begin_bit, int end_bit);
+/* CompactionEngine::compactAndPermute (include/fluidloom/core/hashmap/CompactionEngine.h:43-46):
+ * keep state != 0 && key != EMPTY, sort kept keys, perm[old] = new (FL_INVALID if dropped).
+ * sorted_keys / sorted_ids need n entries; *num_valid is written (the call synchronizes). */
+int fl_compact_and_permute(fl_ctx* ctx, const uint64_t* keys, const uint32_t* state, size_t n, uint32_t* perm,
+                           uint64_t* sorted_keys, uint32_t* sorted_ids, size_t* num_valid);
+/* CompactionEngine::applyPermutationToFields (CompactionEngine.h:54-59): dst[perm[i]] = src[i]. */
+int fl_apply_permutation(fl_ctx* ctx, const void* src, void* dst, size_t elem_size, size_t old_n,
+                         const uint32_t* perm);
+
+/* ---- hash table (HashTableManager, include/fluidloom/core/hashmap/HashTableManager.h:34-56;
+ *      kernels/hashmap/hash_build.cl, hash_query.cl) */
+/* [host] HashTableManager::computeCapacity (HashTableManager.cpp:47-57). */
+uint64_t fl_hash_compute_capacity(size_t n);
+/* Clear and build: table_keys[capacity], table_vals[capacity]; vals may be NULL (value = input index).
+ * A repeated key keeps the value of its last occurrence.  Synchronizes; FL_E_HASH_OVERFLOW if a
+ * key found no slot within the probe limit. */
+int fl_hash_build(fl_ctx* ctx, uint64_t* table_keys, uint32_t* table_vals, uint64_t capacity, const uint64_t* keys,
+                  const uint32_t* vals, size_t n);
+/* out[i] = value of queries[i] or FL_INVALID. */
+int fl_hash_query(fl_ctx* ctx, const uint64_t* table_keys, const uint32_t* table_vals, uint64_t capacity,
+                  const uint64_t* queries, uint32_t* out, size_t n);
+
+/* ---- AMR mesh and regrid */
+/* Device columns of a leaf set, native-level coordinates (CellDescriptor.h:32-104 split into SoA,
+ * as AdaptationEngine::adapt takes them, AdaptationEngine.h:56-65). */
+typedef struct fl_mesh {
+    int32_t* x;
+    int32_t* y;
+    int32_t* z;
+    uint8_t* level;
+    uint8_t* state;      /* CellState: 0 FLUID, 1 SOLID, ... (CellDescriptor.h:107-114) */
+    int32_t* flags;      /* refine flags: > 0 split, -1 merge, 0 keep */
+    uint32_t* material;
+    uint16_t* case_id;   /* NULL for a single case */
+    size_t num_cells;
+    size_t capacity;
+} fl_mesh;
+
+/* AdaptationConfig (include/fluidloom/adaptation/AdaptationTypes.h:117-157) plus key geometry. */
+typedef struct fl_adapt_config {
+    uint8_t max_refinement_level;   /* <= 21 */
+    uint8_t min_refinement_level;
+    uint32_t max_balance_iterations;
+    int32_t enforce_2_1_balance;
+    int32_t balance_mode;           /* 0 FACE6 (reference semantics), 1 FULL26 to a fixed point */
+    int32_t averaging_rule;         /* 0 arithmetic, 1 volume weighted */
+    double buffer_growth_factor;
+    int32_t key_depth;              /* 0 -> 21 */
+    int32_t anchor_level;           /* 0 -> 21: anchor = native << (anchor_level - level) */
+    int32_t ext[3];                 /* level-0 extent in cells (0 -> 1) */
+    int32_t periodic[3];
+} fl_adapt_config;
+
+/* BalanceResult (AdaptationTypes.h:94-109). */
+typedef struct fl_balance_result {
+    int32_t converged;
+    uint32_t iterations;
+    uint32_t total_violations_detected;
+    uint32_t total_cells_marked_for_balance;
+} fl_balance_result;
+
+/* SplitResult / MergeResult counts (AdaptationTypes.h:27-87). */
+typedef struct fl_adapt_stats {
+    uint32_t num_split;
+    uint32_t num_children;
+    uint32_t num_groups;
+    uint32_t num_merged;
+    uint32_t num_survivors;
+    size_t num_cells_out;
+    fl_balance_result balance;
+} fl_adapt_stats;
+
+int fl_mesh_alloc(fl_ctx* ctx, size_t capacity, int with_case_id, fl_mesh* mesh);
+int fl_mesh_free(fl_ctx* ctx, fl_mesh* mesh);
+/* BalanceEnforcer::enforce (include/fluidloom/adaptation/BalanceEnforcer.h:48-53): updates flags.
+ * Returns FL_E_BALANCE_NOT_CONVERGED (warning) when it stops without converging. */
+int fl_balance_enforce(fl_ctx* ctx, fl_mesh* mesh, const fl_adapt_config* cfg, fl_balance_result* res);
+/* AdaptationEngine::adapt (AdaptationEngine.h:56-65): balance, split, merge, rebuild in key order.
+ * The mesh columns (and *fields, AoS with C floats per cell) are replaced by new allocations when
+ * the cell set changes capacity, as the reference releases and replaces its cl_mem handles. */
+int fl_adapt(fl_ctx* ctx, fl_mesh* mesh, const fl_adapt_config* cfg, float** fields, uint32_t C,
+             fl_adapt_stats* stats);
+/* Neighbour table: nbr[(i*26 + k)*subslots + s] = leaf containing the probe point of direction k
+ * (dz outer, dy, dx inner, centre skipped) at sub-slot s, FL_INVALID outside the domain
+ * (point-location rule of src/adaptation/kernels/balance_enforce.cl:107-143).  subslots 1 or 4. */
+int fl_neighbour_rebuild(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, int subslots, uint32_t* nbr);
+
 #ifdef __cplusplus
 }
 #endif

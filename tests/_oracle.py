@@ -136,3 +136,90 @@ def cell_keys(x, y, z, level, case_id, depth, anchor_level):
     k = np.empty(len(x), np.uint64)
     L.or_cell_keys(ptr(x), ptr(y), ptr(z), ptr(level), ptr(cs), depth, anchor_level, ptr(k), len(x))
     return k
+
+
+# ---- mesh helpers ---------------------------------------------------------
+def mesh_struct(cols):
+    """ctypes or_mesh over numpy columns (kept alive by the returned tuple)."""
+    keep = {k: np.ascontiguousarray(v) for k, v in cols.items()}
+    m = Mesh()
+    for k in ("x", "y", "z", "level", "state", "flags", "material"):
+        setattr(m, k, keep[k].ctypes.data_as(P))
+    m.case_id = keep["case_id"].ctypes.data_as(P) if "case_id" in keep else None
+    m.n = len(keep["x"])
+    return m, keep
+
+
+def domain(depth=21, anchor=21, max_level=21, ext=(1, 1, 1), periodic=(0, 0, 0)):
+    d = Domain()
+    d.depth, d.anchor_level, d.max_level = depth, anchor, max_level
+    d.ext[:] = list(ext)
+    d.periodic[:] = list(periodic)
+    return d
+
+
+def uniform_mesh(level, ext=(1, 1, 1)):
+    n = [e << level for e in ext]
+    g = np.stack(np.meshgrid(np.arange(n[0]), np.arange(n[1]), np.arange(n[2]), indexing="ij"), -1).reshape(-1, 3)
+    N = len(g)
+    return {"x": g[:, 0].astype(np.int32), "y": g[:, 1].astype(np.int32), "z": g[:, 2].astype(np.int32),
+            "level": np.full(N, level, np.uint8), "state": np.zeros(N, np.uint8), "flags": np.zeros(N, np.int32),
+            "material": np.zeros(N, np.uint32)}
+
+
+def adapt(cols, cfg_kw, dom, fields=None, C=0):
+    """Run the oracle regrid; returns (new columns, stats, new fields, src, kind, members)."""
+    L = load()
+    cols = {k: np.array(v) for k, v in cols.items()}
+    m, keep = mesh_struct(cols)
+    n = m.n
+    cap = 8 * n + 8
+    out = {"x": np.zeros(cap, np.int32), "y": np.zeros(cap, np.int32), "z": np.zeros(cap, np.int32),
+           "level": np.zeros(cap, np.uint8), "state": np.zeros(cap, np.uint8), "flags": np.zeros(cap, np.int32),
+           "material": np.zeros(cap, np.uint32), "case_id": np.zeros(cap, np.uint16)}
+    src = np.zeros(cap, np.uint32)
+    kind = np.zeros(cap, np.uint8)
+    members = np.zeros(cap, np.uint32)
+    of = np.zeros(cap * max(C, 1), np.float32)
+    cfg = AdaptCfg(**cfg_kw)
+    st = AdaptStats()
+    f = np.ascontiguousarray(fields, np.float32) if fields is not None else None
+    M = L.or_adapt(ctypes.byref(m), ctypes.byref(dom), ctypes.byref(cfg), ptr(f), C, 0,
+                   ptr(out["x"]), ptr(out["y"]), ptr(out["z"]), ptr(out["level"]), ptr(out["state"]),
+                   ptr(out["flags"]), ptr(out["material"]), ptr(out["case_id"]) if "case_id" in cols else None,
+                   ptr(of) if C else None, ptr(src), ptr(kind), ptr(members), ctypes.byref(st))
+    res = {k: v[:M] for k, v in out.items() if k != "case_id" or "case_id" in cols}
+    # flags after balance (the oracle updates the input columns in place)
+    return res, st, (of[:M * C].reshape(M, C) if C else None), src[:M], kind[:M], members[:st.num_groups * 8], keep
+
+
+def balance(cols, dom, mode, max_level, iters=10):
+    L = load()
+    cols = {k: np.array(v) for k, v in cols.items()}
+    m, keep = mesh_struct(cols)
+    st = BalanceStats()
+    L.or_balance(ctypes.byref(m), ctypes.byref(dom), mode, max_level, iters, ctypes.byref(st))
+    return keep["flags"].copy(), st
+
+
+def neighbours(cols, dom, subslots):
+    L = load()
+    m, keep = mesh_struct(cols)
+    nbr = np.zeros(m.n * 26 * subslots, np.uint32)
+    L.or_neighbours(ctypes.byref(m), ctypes.byref(dom), subslots, ptr(nbr))
+    return nbr
+
+
+def random_octree(seed, ext=(2, 2, 2), rounds=3, max_level=6, frac=0.3, balanced=True):
+    """A random leaf set built by repeated oracle regrids with random refine flags."""
+    rng = np.random.default_rng(seed)
+    cols = uniform_mesh(0, ext)
+    dom = domain(ext=ext, max_level=max_level)
+    for r in range(rounds):
+        n = len(cols["x"])
+        cols["flags"] = np.where(rng.random(n) < frac, 1, 0).astype(np.int32)
+        cols, st, *_ = adapt(cols, dict(max_level=max_level, min_level=0, balance_mode=1 if balanced else 0,
+                                        max_balance_iterations=10, enforce_balance=1 if balanced else 0,
+                                        averaging_rule=0), dom)
+        cols = {k: v.copy() for k, v in cols.items()}
+    return cols
