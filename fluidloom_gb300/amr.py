@@ -24,8 +24,11 @@ class AdaptConfig(ctypes.Structure):
                 ("anchor_level", ctypes.c_int32), ("ext", ctypes.c_int32 * 3), ("periodic", ctypes.c_int32 * 3)]
 
     @classmethod
-    def make(cls, max_level=8, min_level=0, balance_mode=0, enforce=True, iters=10, rule=0, depth=21, anchor=21,
+    def make(cls, max_level=8, min_level=0, balance_mode=0, enforce=True, iters=10, rule=0, depth=21, anchor=None,
              ext=(1, 1, 1), periodic=(0, 0, 0), growth=1.5):
+        if anchor is None:  # deepest anchor level with ext << anchor inside the depth-bit key space
+            e = max(ext)
+            anchor = depth - (int(e - 1).bit_length() if e > 1 else 0)
         c = cls()
         c.max_refinement_level = max_level
         c.min_refinement_level = min_level

@@ -321,6 +321,17 @@ struct Carver {
 
 }  // namespace
 
+bool fl_domain_config_valid(const fl_adapt_config* cfg) {
+    int D = cfg->key_depth ? cfg->key_depth : 21;
+    int A = cfg->anchor_level ? cfg->anchor_level : 21;
+    if (D < 1 || D > 21 || A < 0 || A > D || cfg->max_refinement_level > A) return false;
+    for (int a = 0; a < 3; ++a) {
+        int64_t e = cfg->ext[a] > 0 ? cfg->ext[a] : 1;
+        if ((e << A) > ((int64_t)1 << D)) return false;
+    }
+    return true;
+}
+
 fl_domain_dev fl_domain_from_config(fl_ctx* ctx, const fl_adapt_config* cfg, void* dev_case_slot) {
     fl_domain_dev d;
     d.depth = cfg->key_depth ? cfg->key_depth : 21;
@@ -554,6 +565,8 @@ int fl_mesh_free(fl_ctx* ctx, fl_mesh* m) {
 
 int fl_balance_enforce(fl_ctx* ctx, fl_mesh* mesh, const fl_adapt_config* cfg, fl_balance_result* res) {
     if (!ctx || !mesh || !cfg) return FL_E_INVALID_ARG;
+    if (!fl_domain_config_valid(cfg))
+        return fl_set_error(ctx, FL_E_INVALID_ARG, "key geometry: need anchor_level <= key_depth <= 21, max level <= anchor_level, ext << anchor_level <= 2^key_depth");
     size_t n = mesh->num_cells;
     if (res) *res = fl_balance_result{};
     if (n == 0) { if (res) res->converged = 1; return FL_OK; }
@@ -589,6 +602,8 @@ int fl_balance_enforce(fl_ctx* ctx, fl_mesh* mesh, const fl_adapt_config* cfg, f
 
 int fl_neighbour_rebuild(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, int subslots, uint32_t* nbr) {
     if (!ctx || !mesh || !cfg || !nbr || (subslots != 1 && subslots != 4)) return FL_E_INVALID_ARG;
+    if (!fl_domain_config_valid(cfg))
+        return fl_set_error(ctx, FL_E_INVALID_ARG, "key geometry: need anchor_level <= key_depth <= 21, max level <= anchor_level, ext << anchor_level <= 2^key_depth");
     size_t n = mesh->num_cells;
     if (n == 0) return FL_OK;
     uint64_t cap = fl_table_capacity(n);
@@ -619,6 +634,8 @@ int fl_adapt(fl_ctx* ctx, fl_mesh* mesh, const fl_adapt_config* cfg, float** fie
     if (C && (!fields || !*fields)) return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_adapt: components without fields");
     if (cfg->max_refinement_level > 21 || cfg->min_refinement_level > cfg->max_refinement_level)
         return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_adapt: bad level limits (AdaptationConfig::validate)");
+    if (!fl_domain_config_valid(cfg))
+        return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_adapt: key geometry needs ext << anchor_level <= 2^key_depth");
     size_t n = mesh->num_cells;
     if (stats) *stats = fl_adapt_stats{};
     if (n == 0) return FL_OK;

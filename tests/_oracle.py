@@ -150,7 +150,16 @@ def mesh_struct(cols):
     return m, keep
 
 
-def domain(depth=21, anchor=21, max_level=21, ext=(1, 1, 1), periodic=(0, 0, 0)):
+def anchor_for(ext, depth=21):
+    """Deepest anchor level that keeps ext << A within the depth-bit key space."""
+    e = max(ext)
+    return depth - int(np.ceil(np.log2(e))) if e > 1 else depth
+
+
+def domain(depth=21, anchor=None, max_level=21, ext=(1, 1, 1), periodic=(0, 0, 0)):
+    if anchor is None:
+        anchor = anchor_for(ext, depth)
+    max_level = min(max_level, anchor)
     d = Domain()
     d.depth, d.anchor_level, d.max_level = depth, anchor, max_level
     d.ext[:] = list(ext)
