@@ -1,0 +1,1041 @@
+// lbm.cu — D3Q19 BGK collide-stream over an octree of 8^3-site bricks, the
+// brick pool that owns it (cases, populations, neighbour table, per-level
+// brick lists), regrid with population remap, refinement flags and the FP64
+// conservation sums.
+//
+// The reference has no lattice-Boltzmann code: its lbm_* kernels are
+// generated empty (src/parsing/SimulationBuilder.cpp:394-400) and D3Q19 is
+// only lattice metadata (include/fluidloom/parsing/LatticeDescriptor.h:15-44).
+// The method is therefore the literature's, as the CPU oracle restates it:
+// BGK equilibrium (Qian, d'Humieres & Lallemand 1992), half-way bounce-back
+// with the moving-wall term 6 w_q rho0 (c_q . u_w) (Ladd 1994), equilibrium
+// velocity inlet and zero-gradient outlet (Kruger et al. 2017), acoustic
+// scaling across levels with tau_l = 2^l (tau_0 - 1/2) + 1/2 and level l
+// sub-cycled 2^l times per level-0 step (Dupuis & Chopard 2003).  The
+// coarse/fine coupling uses the reference's own prolongation (copy,
+// split_cells.cl:110-132) and restriction (mean of 8, merge_cells.cl:123-159,
+// FieldAveragingRules.h:31-41) per population, with the coarse side linearly
+// interpolated in time for the second fine sub-step.
+//
+// Layout in HBM: populations are structure-of-arrays, f[q][brick][site] with
+// site = x + 8y + 64z inside the brick, so a warp reading one population of
+// 32 consecutive sites touches one 128-byte line.  Three population buffers
+// are kept: A and B (per-level parity) and a spare that receives the remap
+// at each regrid.  This unit is compiled with -fmad=false so its FP32 results
+// are the IEEE sequence of operations written here, identical to the CPU
+// restatement it is tested against.
+#include "common.cuh"
+#include "amr.cuh"
+#include "hash.cuh"
+#include "keys.cuh"
+#include "scan.cuh"
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+namespace {
+
+constexpr int Q = 19;
+constexpr uint64_t kCXp = 0x1548889549ull;  // (c_x + 1) in 2 bits per population
+constexpr uint64_t kCYp = 0x895609495ull;
+constexpr uint64_t kCZp = 0x20a0954955ull;
+__host__ __device__ constexpr int CXq(int q) { return (int)((kCXp >> (2 * q)) & 3u) - 1; }
+__host__ __device__ constexpr int CYq(int q) { return (int)((kCYp >> (2 * q)) & 3u) - 1; }
+__host__ __device__ constexpr int CZq(int q) { return (int)((kCZp >> (2 * q)) & 3u) - 1; }
+__host__ __device__ constexpr int OPPq(int q) { return q == 0 ? 0 : ((q & 1) ? q + 1 : q - 1); }
+__device__ __forceinline__ float Wq(int q) {
+    return q == 0 ? (1.0f / 3.0f) : (q < 7 ? (1.0f / 18.0f) : (1.0f / 36.0f));
+}
+
+constexpr uint32_t kSlow = 0xFFFFFFFEu;
+
+}  // namespace
+
+// Per-case constants on the device.
+struct LbmCaseDev {
+    int32_t ext[3];
+    int32_t periodic[3];
+    int32_t bc[6];
+    float wall_u[3], inlet_u[3], init_u[3];
+    float omega[20];
+    int32_t max_level, has_sphere;
+    float sc[3], sr, refine_frac, coarsen_frac, band;
+};
+
+namespace {
+
+__device__ __forceinline__ float cdot(int q, float ux, float uy, float uz) {
+    float a = (float)CXq(q) * ux;
+    float b = (float)CYq(q) * uy;
+    float c = (float)CZq(q) * uz;
+    float s = a + b;
+    return s + c;
+}
+
+__device__ __forceinline__ float base_of(float ux, float uy, float uz) {
+    float usq = ux * ux;
+    usq = usq + uy * uy;
+    usq = usq + uz * uz;
+    float t = 1.5f * usq;
+    return 1.0f - t;
+}
+
+__device__ __forceinline__ float feq1(int q, float rho, float ux, float uy, float uz, float base) {
+    float cu = cdot(q, ux, uy, uz);
+    float t = 4.5f * cu;
+    t = 3.0f + t;
+    t = cu * t;
+    t = base + t;
+    float wr = Wq(q) * rho;
+    return wr * t;
+}
+
+__device__ __forceinline__ void moments(const float* f, float& rho, float& jx, float& jy, float& jz) {
+    float r = f[0];
+#pragma unroll
+    for (int q = 1; q < Q; ++q) r = r + f[q];
+    float a = f[1] - f[2];
+    a = a + (f[7] - f[8]); a = a + (f[9] - f[10]); a = a + (f[11] - f[12]); a = a + (f[13] - f[14]);
+    float b = f[3] - f[4];
+    b = b + (f[7] - f[8]); b = b + (f[10] - f[9]); b = b + (f[15] - f[16]); b = b + (f[17] - f[18]);
+    float c = f[5] - f[6];
+    c = c + (f[11] - f[12]); c = c + (f[14] - f[13]); c = c + (f[15] - f[16]); c = c + (f[18] - f[17]);
+    rho = r; jx = a; jy = b; jz = c;
+}
+
+__device__ __forceinline__ bool solid_at(const LbmCaseDev& c, int64_t sx, int64_t sy, int64_t sz, int l) {
+    if (!c.has_sphere) return false;
+    float inv = 1.0f / (float)(1 << l);
+    float px = ((float)sx + 0.5f) * inv, py = ((float)sy + 0.5f) * inv, pz = ((float)sz + 0.5f) * inv;
+    float dx = px - c.sc[0], dy = py - c.sc[1], dz = pz - c.sc[2];
+    float d2 = dx * dx;
+    d2 = d2 + dy * dy;
+    d2 = d2 + dz * dz;
+    float r2 = c.sr * c.sr;
+    return d2 < r2;
+}
+
+struct StepArgs {
+    const uint32_t* list;
+    uint32_t count;
+    int level, sub;
+    const float* R;      // own level, time t (post-collision)
+    float* W;            // own level, t + dt
+    const float* Cold;   // coarser level at the start of its step
+    const float* Cnew;   // coarser level after its step
+    const float* Fine;   // finer level, current
+    size_t cap;          // bricks per population plane
+    const int32_t* bx; const int32_t* by; const int32_t* bz;
+    const uint8_t* blevel; const uint16_t* bcase;
+    const uint32_t* nbr;  // [n][26][4]
+    const LbmCaseDev* cases;
+    uint32_t* dev_status;
+};
+
+__device__ __forceinline__ size_t fidx(size_t cap, int q, size_t b, int s) { return ((size_t)q * cap + b) * 512 + s; }
+
+// Pull of population q for a site whose source leaves the brick through a
+// non-same-level face/edge/corner, or the domain (oracle: or_lbm.cpp pull()).
+__device__ float pull_slow(const StepArgs& a, const LbmCaseDev& c, uint32_t b, int q, int l, const int64_t* G,
+                           int s_local) {
+    int64_t S[3] = {G[0] - CXq(q), G[1] - CYq(q), G[2] - CZq(q)};
+    int64_t N[3];
+    for (int ax = 0; ax < 3; ++ax) N[ax] = ((int64_t)c.ext[ax] * 8) << l;
+    int out_face[3] = {-1, -1, -1};
+    bool out = false;
+    for (int ax = 0; ax < 3; ++ax) {
+        if (c.periodic[ax]) continue;
+        if (S[ax] < 0) { out_face[ax] = 2 * ax; out = true; }
+        else if (S[ax] >= N[ax]) { out_face[ax] = 2 * ax + 1; out = true; }
+    }
+    if (out) {
+        bool inlet = false, outlet = false;
+        int moving = -1;
+        for (int ax = 0; ax < 3; ++ax) {
+            if (out_face[ax] < 0) continue;
+            int bt = c.bc[out_face[ax]];
+            if (bt == 3) inlet = true;
+            else if (bt == 4) outlet = true;
+            else if (bt == 2 && moving < 0) moving = out_face[ax];
+        }
+        if (inlet) {
+            float base = base_of(c.inlet_u[0], c.inlet_u[1], c.inlet_u[2]);
+            return feq1(q, 1.0f, c.inlet_u[0], c.inlet_u[1], c.inlet_u[2], base);
+        }
+        if (outlet) return a.R[fidx(a.cap, q, b, s_local)];
+        float v = a.R[fidx(a.cap, OPPq(q), b, s_local)];
+        if (moving >= 0) {
+            float cu = cdot(q, c.wall_u[0], c.wall_u[1], c.wall_u[2]);
+            float t = 6.0f * Wq(q);
+            t = t * cu;
+            v = v + t;
+        }
+        return v;
+    }
+    int64_t Sw[3];
+    for (int ax = 0; ax < 3; ++ax) Sw[ax] = c.periodic[ax] ? ((S[ax] % N[ax]) + N[ax]) % N[ax] : S[ax];
+    if (solid_at(c, Sw[0], Sw[1], Sw[2], l)) return a.R[fidx(a.cap, OPPq(q), b, s_local)];
+    int64_t Lc[3] = {S[0] - (int64_t)a.bx[b] * 8, S[1] - (int64_t)a.by[b] * 8, S[2] - (int64_t)a.bz[b] * 8};
+    if (Lc[0] >= 0 && Lc[0] < 8 && Lc[1] >= 0 && Lc[1] < 8 && Lc[2] >= 0 && Lc[2] < 8)
+        return a.R[fidx(a.cap, q, b, (int)(Lc[0] + 8 * Lc[1] + 64 * Lc[2]))];
+    int d[3], sub_slot = 0, bit = 0;
+    for (int ax = 0; ax < 3; ++ax) {
+        d[ax] = Lc[ax] < 0 ? -1 : (Lc[ax] >= 8 ? 1 : 0);
+        if (d[ax] == 0) { if (Lc[ax] >= 4) sub_slot |= 1 << bit; ++bit; }
+    }
+    int kk = (d[2] + 1) * 9 + (d[1] + 1) * 3 + (d[0] + 1);
+    int k = kk < 13 ? kk : kk - 1;
+    uint32_t nb = a.nbr[((size_t)b * 26 + k) * 4 + sub_slot];
+    if (nb == FL_INVALID_INDEX) return a.R[fidx(a.cap, OPPq(q), b, s_local)];
+    int ln = a.blevel[nb];
+    if (ln == l) {
+        int64_t lx = Sw[0] - (int64_t)a.bx[nb] * 8, ly = Sw[1] - (int64_t)a.by[nb] * 8, lz = Sw[2] - (int64_t)a.bz[nb] * 8;
+        return a.R[fidx(a.cap, q, nb, (int)(lx + 8 * ly + 64 * lz))];
+    }
+    if (ln == l - 1) {
+        int64_t lx = (Sw[0] >> 1) - (int64_t)a.bx[nb] * 8, ly = (Sw[1] >> 1) - (int64_t)a.by[nb] * 8,
+                lz = (Sw[2] >> 1) - (int64_t)a.bz[nb] * 8;
+        if (lx < 0 || lx > 7 || ly < 0 || ly > 7 || lz < 0 || lz > 7) {
+            atomicAdd(a.dev_status + FL_DEVSTAT_BOUNDS, 1u);
+            return a.R[fidx(a.cap, OPPq(q), b, s_local)];
+        }
+        size_t i = fidx(a.cap, q, nb, (int)(lx + 8 * ly + 64 * lz));
+        if (a.sub == 0) return a.Cold[i];
+        float t = a.Cold[i] + a.Cnew[i];
+        return t * 0.5f;
+    }
+    if (ln == l + 1) {
+        float sum = 0.0f;
+#pragma unroll
+        for (int kq = 0; kq < 8; ++kq) {
+            int64_t lx = 2 * Sw[0] + (kq & 1) - (int64_t)a.bx[nb] * 8;
+            int64_t ly = 2 * Sw[1] + ((kq >> 1) & 1) - (int64_t)a.by[nb] * 8;
+            int64_t lz = 2 * Sw[2] + ((kq >> 2) & 1) - (int64_t)a.bz[nb] * 8;
+            if (lx < 0 || lx > 7 || ly < 0 || ly > 7 || lz < 0 || lz > 7) {
+                atomicAdd(a.dev_status + FL_DEVSTAT_BOUNDS, 1u);
+                return a.R[fidx(a.cap, OPPq(q), b, s_local)];
+            }
+            sum = sum + a.Fine[fidx(a.cap, q, nb, (int)(lx + 8 * ly + 64 * lz))];
+        }
+        return sum * 0.125f;
+    }
+    atomicAdd(a.dev_status + FL_DEVSTAT_LEVEL_JUMP, 1u);
+    return a.R[fidx(a.cap, OPPq(q), b, s_local)];
+}
+
+// One CTA per brick (persistent over the level's list), 256 threads, two
+// sites per thread.  The 27-entry table holds this brick (centre) and its
+// same-level neighbours; any other relation takes pull_slow.
+__global__ void __launch_bounds__(256, 3) k_collide_stream(StepArgs a) {
+    __shared__ uint32_t s_nb[27];
+    __shared__ int s_near;
+    const int l = a.level;
+    for (uint32_t w = blockIdx.x; w < a.count; w += gridDim.x) {
+        const uint32_t b = a.list[w];
+        const uint16_t cs = a.bcase[b];
+        const LbmCaseDev& c = a.cases[cs];
+        if (threadIdx.x < 27) {
+            int d = threadIdx.x;
+            uint32_t e = b;
+            if (d != 13) {
+                int k = d < 13 ? d : d - 1;
+                uint32_t nb = a.nbr[((size_t)b * 26 + k) * 4];
+                e = (nb != FL_INVALID_INDEX && a.blevel[nb] == l) ? nb : kSlow;
+            }
+            s_nb[d] = e;
+        }
+        if (threadIdx.x == 32) {
+            // could a site of this brick or a source one site outside it be solid?
+            int near = 0;
+            if (c.has_sphere) {
+                float inv = 1.0f / (float)(1 << l);
+                int32_t o[3] = {a.bx[b] * 8, a.by[b] * 8, a.bz[b] * 8};
+                float dm = 0.0f;
+                for (int ax = 0; ax < 3; ++ax) {
+                    float lo = (float)(o[ax] - 1) * inv, hi = (float)(o[ax] + 9) * inv;
+                    float cc = c.sc[ax];
+                    float cl = cc < lo ? lo : (cc > hi ? hi : cc);
+                    dm += (cc - cl) * (cc - cl);
+                    if (c.periodic[ax] && (o[ax] == 0 || o[ax] + 8 >= ((c.ext[ax] * 8) << l))) near = 1;
+                }
+                float rr = c.sr + 2.0f * inv;
+                if (dm <= rr * rr) near = 1;
+            }
+            s_near = near;
+        }
+        __syncthreads();
+        const float omega = c.omega[l];
+        const int near = s_near;
+        const int64_t o0 = (int64_t)a.bx[b] * 8, o1 = (int64_t)a.by[b] * 8, o2 = (int64_t)a.bz[b] * 8;
+        for (int s = threadIdx.x; s < 512; s += 256) {
+            const int i = s & 7, j = (s >> 3) & 7, kz = s >> 6;
+            const int64_t G[3] = {o0 + i, o1 + j, o2 + kz};
+            if (near && solid_at(c, G[0], G[1], G[2], l)) {
+#pragma unroll
+                for (int q = 0; q < Q; ++q) a.W[fidx(a.cap, q, b, s)] = Wq(q);
+                continue;
+            }
+            float f[Q];
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                const int sx = i - CXq(q), sy = j - CYq(q), sz = kz - CZq(q);
+                const int d = ((sz >> 3) + 1) * 9 + ((sy >> 3) + 1) * 3 + ((sx >> 3) + 1);
+                const uint32_t e = s_nb[d];
+                if (e != kSlow) {
+                    bool bb = false;
+                    if (near) {
+                        int64_t Sw[3] = {G[0] - CXq(q), G[1] - CYq(q), G[2] - CZq(q)};
+                        for (int ax = 0; ax < 3; ++ax) {
+                            int64_t Nn = ((int64_t)c.ext[ax] * 8) << l;
+                            if (c.periodic[ax]) Sw[ax] = ((Sw[ax] % Nn) + Nn) % Nn;
+                        }
+                        bb = solid_at(c, Sw[0], Sw[1], Sw[2], l);
+                    }
+                    f[q] = bb ? a.R[fidx(a.cap, OPPq(q), b, s)]
+                              : a.R[fidx(a.cap, q, e, (sx & 7) + 8 * (sy & 7) + 64 * (sz & 7))];
+                } else {
+                    f[q] = pull_slow(a, c, b, q, l, G, s);
+                }
+            }
+            float rho, jx, jy, jz;
+            moments(f, rho, jx, jy, jz);
+            float inv = 1.0f / rho;
+            float ux = jx * inv, uy = jy * inv, uz = jz * inv;
+            float base = base_of(ux, uy, uz);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                float fe = feq1(q, rho, ux, uy, uz, base);
+                float dd = fe - f[q];
+                dd = omega * dd;
+                a.W[fidx(a.cap, q, b, s)] = f[q] + dd;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_init_populations(float* f, size_t cap, size_t n, const uint16_t* bcase, const LbmCaseDev* cases) {
+    size_t total = n * 512;
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
+        size_t b = t >> 9;
+        int s = (int)(t & 511);
+        const LbmCaseDev& c = cases[bcase[b]];
+        float base = base_of(c.init_u[0], c.init_u[1], c.init_u[2]);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) f[fidx(cap, q, b, s)] = feq1(q, 1.0f, c.init_u[0], c.init_u[1], c.init_u[2], base);
+    }
+}
+
+struct PoolView {
+    const int32_t* bx; const int32_t* by; const int32_t* bz; const uint8_t* blevel; const uint16_t* bcase;
+    const float* f0; const float* f1;  // A and B
+    size_t cap;
+    int parity[16];
+    const LbmCaseDev* cases;
+};
+
+__device__ __forceinline__ const float* cur_buf(const PoolView& p, int l) { return p.parity[l] ? p.f1 : p.f0; }
+
+// Per-brick max |curl u| (physical scale 2^level), central differences inside
+// the brick, one-sided at its faces; 0 in solid sites (oracle: brick_vorticity).
+__global__ void __launch_bounds__(512) k_vorticity(PoolView p, size_t n, float* __restrict__ wmax,
+                                                   unsigned* __restrict__ case_max) {
+    __shared__ float U[3][512];
+    __shared__ float red[16];
+    for (size_t b = blockIdx.x; b < n; b += gridDim.x) {
+        const int s = threadIdx.x;
+        const int l = p.blevel[b];
+        const LbmCaseDev& c = p.cases[p.bcase[b]];
+        const float* F = cur_buf(p, l);
+        int64_t G[3] = {(int64_t)p.bx[b] * 8 + (s & 7), (int64_t)p.by[b] * 8 + ((s >> 3) & 7),
+                        (int64_t)p.bz[b] * 8 + (s >> 6)};
+        if (solid_at(c, G[0], G[1], G[2], l)) {
+            U[0][s] = U[1][s] = U[2][s] = 0.0f;
+        } else {
+            float f[Q];
+#pragma unroll
+            for (int q = 0; q < Q; ++q) f[q] = F[fidx(p.cap, q, b, s)];
+            float rho, jx, jy, jz;
+            moments(f, rho, jx, jy, jz);
+            float inv = 1.0f / rho;
+            U[0][s] = jx * inv; U[1][s] = jy * inv; U[2][s] = jz * inv;
+        }
+        __syncthreads();
+        const int co[3] = {s & 7, (s >> 3) & 7, s >> 6};
+        auto dd = [&](int comp, int axis) {
+            int stride = axis == 0 ? 1 : (axis == 1 ? 8 : 64);
+            if (co[axis] == 0) return U[comp][s + stride] - U[comp][s];
+            if (co[axis] == 7) return U[comp][s] - U[comp][s - stride];
+            float t = U[comp][s + stride] - U[comp][s - stride];
+            return t * 0.5f;
+        };
+        float wx = dd(2, 1) - dd(1, 2);
+        float wy = dd(0, 2) - dd(2, 0);
+        float wz = dd(1, 0) - dd(0, 1);
+        float w2 = wx * wx;
+        w2 = w2 + wy * wy;
+        w2 = w2 + wz * wz;
+        float mag = sqrtf(w2) * (float)(1 << l);
+        for (int o = 16; o > 0; o >>= 1) mag = fmaxf(mag, __shfl_xor_sync(0xFFFFFFFFu, mag, o));
+        if ((s & 31) == 0) red[s >> 5] = mag;
+        __syncthreads();
+        if (s < 32) {
+            float m = s < 16 ? red[s] : 0.0f;
+            for (int o = 8; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+            if (s == 0) {
+                wmax[b] = m;
+                atomicMax(case_max + p.bcase[b], __float_as_uint(m));  // non-negative floats order as uints
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__device__ bool in_band(const LbmCaseDev& c, int32_t bx, int32_t by, int32_t bz, int l) {
+    if (!c.has_sphere) return false;
+    float inv = 1.0f / (float)(1 << l);
+    int32_t nat[3] = {bx, by, bz};
+    float dmin = 0.0f, dmax = 0.0f;
+    for (int ax = 0; ax < 3; ++ax) {
+        float lo = (float)(nat[ax] * 8) * inv;
+        float hi = (float)(nat[ax] * 8 + 8) * inv;
+        float cc = c.sc[ax];
+        float cl = cc < lo ? lo : (cc > hi ? hi : cc);
+        float e = cc - cl;
+        dmin = dmin + e * e;
+        float f1 = fabsf(cc - lo), f2 = fabsf(cc - hi);
+        float fm = f1 > f2 ? f1 : f2;
+        dmax = dmax + fm * fm;
+    }
+    float ro = c.sr + c.band;
+    float ri = c.sr - c.band;
+    if (ri < 0.0f) ri = 0.0f;
+    return dmin <= ro * ro && dmax >= ri * ri;
+}
+
+// Brick refine/coarsen flags (oracle: compute_flags): band bricks refine to
+// the case's max level; otherwise refine above refine_frac * case max |omega|,
+// coarsen below coarsen_frac * case max.
+__global__ void k_flags(PoolView p, size_t n, const float* __restrict__ wmax, const unsigned* __restrict__ case_max,
+                        int use_vorticity, int32_t* __restrict__ flags) {
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x; b < n; b += stride) {
+        const LbmCaseDev& c = p.cases[p.bcase[b]];
+        int l = p.blevel[b];
+        bool band = in_band(c, p.bx[b], p.by[b], p.bz[b], l);
+        float wm = use_vorticity ? wmax[b] : 0.0f;
+        float cm = use_vorticity ? __uint_as_float(case_max[p.bcase[b]]) : 0.0f;
+        int32_t fl = 0;
+        if (band) fl = l < c.max_level ? 1 : 0;
+        else if (cm > 0.0f && wm > c.refine_frac * cm && l < c.max_level) fl = 1;
+        else if (wm < c.coarsen_frac * cm && l > 0) fl = -1;
+        flags[b] = fl;
+    }
+}
+
+// Population remap after a regrid (oracle: regrid()).
+__global__ void k_remap(PoolView p, size_t M, const uint32_t* __restrict__ osrc, const uint8_t* __restrict__ okind,
+                        const uint32_t* __restrict__ members, float* __restrict__ out, size_t out_cap) {
+    size_t total = M * 512;
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
+        size_t j = t >> 9;
+        int s = (int)(t & 511);
+        int I = s & 7, J = (s >> 3) & 7, K = s >> 6;
+        int kind = okind[j];
+        uint32_t src = osrc[j];
+        if (kind == 8) {
+            const float* F = cur_buf(p, p.blevel[src]);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) out[fidx(out_cap, q, j, s)] = F[fidx(p.cap, q, src, s)];
+        } else if (kind < 8) {
+            const float* F = cur_buf(p, p.blevel[src]);
+            int ps = (4 * (kind & 1) + I / 2) + 8 * (4 * ((kind >> 1) & 1) + J / 2) + 64 * (4 * ((kind >> 2) & 1) + K / 2);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) out[fidx(out_cap, q, j, s)] = F[fidx(p.cap, q, src, ps)];
+        } else {
+            int oc = (I >> 2) | ((J >> 2) << 1) | ((K >> 2) << 2);
+            uint32_t cb = members[(size_t)src * 8 + oc];
+            const float* F = cur_buf(p, p.blevel[cb]);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                float sum = 0.0f;
+                for (int tt = 0; tt < 8; ++tt) {
+                    int fs = (2 * (I & 3) + (tt & 1)) + 8 * (2 * (J & 3) + ((tt >> 1) & 1)) + 64 * (2 * (K & 3) + ((tt >> 2) & 1));
+                    sum = sum + F[fidx(p.cap, q, cb, fs)];
+                }
+                out[fidx(out_cap, q, j, s)] = sum * 0.125f;
+            }
+        }
+    }
+}
+
+// Per-brick FP64 partial sums of rho, j (fluid sites, volume 8^-level) and the
+// fluid-site count.
+__global__ void __launch_bounds__(512) k_brick_sums(PoolView p, size_t n, double* __restrict__ part,
+                                                    uint32_t* __restrict__ fluid) {
+    __shared__ double red[4][16];
+    __shared__ uint32_t redc[16];
+    for (size_t b = blockIdx.x; b < n; b += gridDim.x) {
+        const int s = threadIdx.x;
+        const int l = p.blevel[b];
+        const LbmCaseDev& c = p.cases[p.bcase[b]];
+        const float* F = cur_buf(p, l);
+        int64_t G[3] = {(int64_t)p.bx[b] * 8 + (s & 7), (int64_t)p.by[b] * 8 + ((s >> 3) & 7),
+                        (int64_t)p.bz[b] * 8 + (s >> 6)};
+        double v[4] = {0, 0, 0, 0};
+        uint32_t cnt = 0;
+        if (!solid_at(c, G[0], G[1], G[2], l)) {
+            float f[Q];
+#pragma unroll
+            for (int q = 0; q < Q; ++q) f[q] = F[fidx(p.cap, q, b, s)];
+            float rho, jx, jy, jz;
+            moments(f, rho, jx, jy, jz);
+            v[0] = rho; v[1] = jx; v[2] = jy; v[3] = jz;
+            cnt = 1;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            for (int k = 0; k < 4; ++k) v[k] += __shfl_xor_sync(0xFFFFFFFFu, v[k], o);
+            cnt += __shfl_xor_sync(0xFFFFFFFFu, cnt, o);
+        }
+        if ((s & 31) == 0) {
+            for (int k = 0; k < 4; ++k) red[k][s >> 5] = v[k];
+            redc[s >> 5] = cnt;
+        }
+        __syncthreads();
+        if (s < 4) {
+            double t = 0.0;
+            for (int w = 0; w < 16; ++w) t += red[s][w];
+            part[b * 4 + s] = t / (double)(1ull << (3 * l));
+        }
+        if (s == 4) {
+            uint32_t t = 0;
+            for (int w = 0; w < 16; ++w) t += redc[w];
+            fluid[b] = t;
+        }
+        __syncthreads();
+    }
+}
+
+// Per case, sum the brick partials in brick order (cases occupy contiguous
+// brick ranges because bricks are sorted by case then key).
+__global__ void k_case_sums(const double* __restrict__ part, const uint32_t* __restrict__ case_begin, int ncases,
+                            double* __restrict__ out) {
+    int cs = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cs >= ncases) return;
+    double acc[4] = {0, 0, 0, 0};
+    for (uint32_t b = case_begin[cs]; b < case_begin[cs + 1]; ++b)
+        for (int k = 0; k < 4; ++k) acc[k] += part[(size_t)b * 4 + k];
+    for (int k = 0; k < 4; ++k) out[cs * 4 + k] = acc[k];
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ pool
+struct fl_pool {
+    std::vector<fl_lbm_case> cases;
+    std::vector<LbmCaseDev> hcases;
+    LbmCaseDev* d_cases = nullptr;
+    fl_domain_dev::Case* d_dom = nullptr;
+    fl_mesh mesh{};
+    size_t cap = 0;
+    uint32_t* nbr = nullptr;
+    float* f[3] = {nullptr, nullptr, nullptr};
+    int parity[16] = {0};
+    int maxL = 0;
+    uint32_t* list = nullptr;
+    std::vector<uint32_t> lvl_off;  // maxL + 2 entries
+    std::vector<uint32_t> case_begin;
+    uint32_t* d_case_begin = nullptr;
+    float* wmax = nullptr;
+    unsigned* case_max = nullptr;
+    double* part = nullptr;
+    double* cons = nullptr;
+    uint32_t* fluid = nullptr;
+    uint64_t lups = 0;
+    int graphs = 1;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one level-0 step, per level-0 parity
+    void* adapt_scratch = nullptr;
+    size_t adapt_scratch_bytes = 0;
+    int grid_mult = 3;
+};
+
+namespace {
+
+void to_dev_case(const fl_lbm_case& c, LbmCaseDev& d) {
+    std::memset(&d, 0, sizeof(d));
+    for (int a = 0; a < 3; ++a) {
+        d.ext[a] = c.ext[a];
+        d.periodic[a] = c.bc[2 * a] == 0;
+        d.wall_u[a] = c.wall_u[a];
+        d.inlet_u[a] = c.inlet_u[a];
+        d.init_u[a] = c.init_u[a];
+        d.sc[a] = c.sphere_c[a];
+    }
+    for (int k = 0; k < 6; ++k) d.bc[k] = c.bc[k];
+    for (int l = 0; l < 20; ++l) {
+        float t = c.tau0 - 0.5f;
+        t = (float)(1 << l) * t;
+        t = t + 0.5f;
+        d.omega[l] = 1.0f / t;
+    }
+    d.max_level = c.max_level;
+    d.has_sphere = c.has_sphere;
+    d.sr = c.sphere_r;
+    d.refine_frac = c.refine_frac;
+    d.coarsen_frac = c.coarsen_frac;
+    d.band = c.band;
+}
+
+fl_domain_dev pool_domain(fl_pool* P) {
+    fl_domain_dev d;
+    d.depth = 17;
+    d.anchor_level = 13;
+    d.max_level = 13;
+    d.c = P->d_dom;
+    return d;
+}
+
+PoolView view(fl_pool* P) {
+    PoolView v;
+    v.bx = P->mesh.x; v.by = P->mesh.y; v.bz = P->mesh.z; v.blevel = P->mesh.level; v.bcase = P->mesh.case_id;
+    v.f0 = P->f[0]; v.f1 = P->f[1];
+    v.cap = P->cap;
+    for (int l = 0; l < 16; ++l) v.parity[l] = P->parity[l];
+    v.cases = P->d_cases;
+    return v;
+}
+
+int pool_reserve_bricks(fl_ctx* ctx, fl_pool* P, size_t need) {
+    // grows nbr / flags scratch / partials; population buffers are handled by the regrid
+    if (need <= P->cap) return FL_OK;
+    return FL_E_CAPACITY;
+}
+
+int alloc_brick_arrays(fl_ctx* ctx, fl_pool* P, size_t cap) {
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->nbr, cap * 26 * 4 * 4, ctx->stream), "pool nbr");
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->list, cap * 4, ctx->stream), "pool list");
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->wmax, cap * 4, ctx->stream), "pool wmax");
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->part, cap * 32, ctx->stream), "pool partials");
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->fluid, cap * 4, ctx->stream), "pool fluid");
+    return FL_OK;
+}
+
+void free_brick_arrays(fl_ctx* ctx, fl_pool* P) {
+    void* ps[5] = {P->nbr, P->list, P->wmax, P->part, P->fluid};
+    for (void* p : ps)
+        if (p) cudaFreeAsync(p, ctx->stream);
+    P->nbr = nullptr; P->list = nullptr; P->wmax = nullptr; P->part = nullptr; P->fluid = nullptr;
+}
+
+void drop_graph(fl_pool* P) {
+    for (int k = 0; k < 2; ++k) {
+        if (P->graph[k]) cudaGraphExecDestroy(P->graph[k]);
+        P->graph[k] = nullptr;
+    }
+}
+
+// Neighbour table, per-level lists, case ranges and fluid count for the current mesh.
+int pool_topology(fl_ctx* ctx, fl_pool* P) {
+    size_t n = P->mesh.num_cells;
+    uint64_t cap = fl_table_capacity(n);
+    size_t need = fl_align256(n * 8) + fl_align256(cap * 8) + 2 * fl_align256(cap * 4) + 256;
+    int rc = fl_scratch_reserve(ctx, need);
+    if (rc) return rc;
+    char* p = (char*)ctx->scratch;
+    uint64_t* keys = (uint64_t*)p; p += fl_align256(n * 8);
+    uint64_t* tk = (uint64_t*)p; p += fl_align256(cap * 8);
+    uint32_t* tv = (uint32_t*)p; p += fl_align256(cap * 4);
+    uint32_t* win = (uint32_t*)p;
+    fl_domain_dev dom = pool_domain(P);
+    rc = fl_launch_cell_keys(ctx, P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.level, P->mesh.case_id, dom.depth,
+                             dom.anchor_level, keys, n);
+    if (rc) return rc;
+    rc = fl_hash_build_with(ctx, tk, tv, cap, keys, nullptr, n, win);
+    if (rc) return rc;
+    fl_mesh_dev md{P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.level, P->mesh.state, P->mesh.flags, P->mesh.material,
+                   P->mesh.case_id, n};
+    rc = fl_neighbours_with(ctx, md, dom, tk, tv, cap, 4, P->nbr);
+    if (rc) return rc;
+    // host-side lists (levels and case ids are small: one byte + two bytes per brick)
+    std::vector<uint8_t> lv(n);
+    std::vector<uint16_t> cs(n);
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(lv.data(), P->mesh.level, n, cudaMemcpyDeviceToHost, ctx->stream), "levels");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(cs.data(), P->mesh.case_id, n * 2, cudaMemcpyDeviceToHost, ctx->stream), "cases");
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "topology sync");
+    P->lvl_off.assign(P->maxL + 2, 0);
+    for (size_t i = 0; i < n; ++i) {
+        if (lv[i] > P->maxL) return fl_set_error(ctx, FL_E_INVALID_ARG, "brick level above the pool maximum");
+        P->lvl_off[lv[i] + 1]++;
+    }
+    for (int l = 0; l <= P->maxL; ++l) P->lvl_off[l + 1] += P->lvl_off[l];
+    std::vector<uint32_t> list(n), fill(P->lvl_off.begin(), P->lvl_off.end() - 1);
+    for (size_t i = 0; i < n; ++i) list[fill[lv[i]]++] = (uint32_t)i;
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->list, list.data(), n * 4, cudaMemcpyHostToDevice, ctx->stream), "list");
+    P->case_begin.assign(P->cases.size() + 1, 0);
+    for (size_t i = 0; i < n; ++i) P->case_begin[cs[i] + 1]++;
+    for (size_t c = 0; c < P->cases.size(); ++c) P->case_begin[c + 1] += P->case_begin[c];
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->d_case_begin, P->case_begin.data(), P->case_begin.size() * 4,
+                                     cudaMemcpyHostToDevice, ctx->stream), "case ranges");
+    // fluid sites per brick -> LUPs per level-0 step
+    k_brick_sums<<<fl_blocks(n, 1, ctx->num_sms * 8), 512, 0, ctx->stream>>>(view(P), n, P->part, P->fluid);
+    FL_CHECK_LAUNCH(ctx, "k_brick_sums");
+    std::vector<uint32_t> fl(n);
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(fl.data(), P->fluid, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "fluid");
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "topology sync");
+    P->lups = 0;
+    for (size_t i = 0; i < n; ++i) P->lups += (uint64_t)fl[i] << lv[i];
+    drop_graph(P);
+    return fl_collect_device_status(ctx, "pool topology");
+}
+
+int pool_init_populations(fl_ctx* ctx, fl_pool* P) {
+    size_t n = P->mesh.num_cells;
+    k_init_populations<<<fl_blocks(n * 512, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(
+        P->f[0], P->cap, n, P->mesh.case_id, P->d_cases);
+    FL_CHECK_LAUNCH(ctx, "k_init_populations");
+    for (int l = 0; l < 16; ++l) P->parity[l] = 0;
+    drop_graph(P);
+    return FL_OK;
+}
+
+// use_vorticity: 0 band only, 1 band + vorticity, -1 all flags 0 (the regrid then only sorts)
+int pool_flags(fl_ctx* ctx, fl_pool* P, int use_vorticity) {
+    size_t n = P->mesh.num_cells;
+    if (use_vorticity < 0) {
+        FL_TRY_CUDA(ctx, cudaMemsetAsync(P->mesh.flags, 0, n * 4, ctx->stream), "flags clear");
+        return FL_OK;
+    }
+    PoolView v = view(P);
+    FL_TRY_CUDA(ctx, cudaMemsetAsync(P->case_max, 0, P->cases.size() * 4, ctx->stream), "case max");
+    if (use_vorticity) {
+        k_vorticity<<<fl_blocks(n, 1, ctx->num_sms * 8), 512, 0, ctx->stream>>>(v, n, P->wmax, P->case_max);
+        FL_CHECK_LAUNCH(ctx, "k_vorticity");
+    }
+    k_flags<<<fl_blocks(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(v, n, P->wmax, P->case_max, use_vorticity,
+                                                                          P->mesh.flags);
+    FL_CHECK_LAUNCH(ctx, "k_flags");
+    return FL_OK;
+}
+
+// One regrid: flags, adapt (FULL26), population remap into the spare buffer.
+int pool_regrid(fl_ctx* ctx, fl_pool* P, int use_vorticity, fl_adapt_stats* st) {
+    int rc = pool_flags(ctx, P, use_vorticity);
+    if (rc) return rc;
+    size_t n = P->mesh.num_cells;
+    fl_adapt_config cfg{};
+    cfg.max_refinement_level = (uint8_t)P->maxL;
+    cfg.min_refinement_level = 0;
+    cfg.max_balance_iterations = 10;
+    cfg.enforce_2_1_balance = 1;
+    cfg.balance_mode = 1;
+    cfg.averaging_rule = 0;
+    fl_domain_dev dom = pool_domain(P);
+    size_t sb = fl_adapt_scratch_bytes(n, fl_table_capacity(n));
+    if (sb > P->adapt_scratch_bytes) {
+        if (P->adapt_scratch) cudaFreeAsync(P->adapt_scratch, ctx->stream);
+        P->adapt_scratch_bytes = sb + sb / 4;
+        FL_TRY_CUDA(ctx, cudaMallocAsync(&P->adapt_scratch, P->adapt_scratch_bytes, ctx->stream), "adapt scratch");
+    }
+    size_t M = 0;
+    fl_adapt_stats s{};
+    rc = fl_adapt_prepare(ctx, &P->mesh, &cfg, dom, true, P->adapt_scratch, &M, &s);
+    if (rc) return rc;
+    size_t new_cap = P->cap;
+    if (M > P->cap) new_cap = std::max((size_t)(M * 1.5), M + 64);
+    fl_mesh out{};
+    rc = fl_mesh_alloc(ctx, new_cap, 1, &out);
+    if (rc) return rc;
+    uint32_t *osrc = nullptr, *members = nullptr;
+    uint8_t* okind = nullptr;
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&osrc, (M + 1) * 4, ctx->stream), "remap src");
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&okind, M + 1, ctx->stream), "remap kind");
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&members, (size_t)s.num_groups * 32 + 32, ctx->stream), "members");
+    rc = fl_adapt_finish(ctx, &P->mesh, &cfg, dom, P->adapt_scratch, M, nullptr, 0, &out, nullptr, osrc, okind, members,
+                         s.num_groups);
+    if (rc) return rc;
+    float* target = P->f[2];
+    bool grew = new_cap != P->cap;
+    if (grew) FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&target, new_cap * 512 * Q * 4, ctx->stream), "populations");
+    k_remap<<<fl_blocks(M * 512, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(view(P), M, osrc, okind, members,
+                                                                                target, new_cap);
+    FL_CHECK_LAUNCH(ctx, "k_remap");
+    cudaFreeAsync(osrc, ctx->stream);
+    cudaFreeAsync(okind, ctx->stream);
+    cudaFreeAsync(members, ctx->stream);
+    fl_mesh old = P->mesh;
+    fl_mesh_free(ctx, &old);
+    out.num_cells = M;
+    out.capacity = new_cap;
+    P->mesh = out;
+    if (grew) {
+        for (int k = 0; k < 3; ++k) cudaFreeAsync(P->f[k], ctx->stream);
+        P->f[0] = target;
+        FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->f[1], new_cap * 512 * Q * 4, ctx->stream), "populations");
+        FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->f[2], new_cap * 512 * Q * 4, ctx->stream), "populations");
+        free_brick_arrays(ctx, P);
+        rc = alloc_brick_arrays(ctx, P, new_cap);
+        if (rc) return rc;
+        P->cap = new_cap;
+    } else {
+        // spare <- remapped; old A/B become free
+        float* old0 = P->f[0];
+        P->f[0] = target;
+        P->f[2] = old0;
+    }
+    for (int l = 0; l < 16; ++l) P->parity[l] = 0;
+    rc = pool_topology(ctx, P);
+    if (st) *st = s;
+    return rc;
+}
+
+void launch_level(fl_ctx* ctx, fl_pool* P, int l, int sub) {
+    uint32_t off = P->lvl_off[l], cnt = P->lvl_off[l + 1] - P->lvl_off[l];
+    if (cnt) {
+        StepArgs a;
+        a.list = P->list + off;
+        a.count = cnt;
+        a.level = l;
+        a.sub = sub;
+        a.R = P->f[P->parity[l]];
+        a.W = P->f[1 - P->parity[l]];
+        a.Cold = l > 0 ? P->f[1 - P->parity[l - 1]] : nullptr;
+        a.Cnew = l > 0 ? P->f[P->parity[l - 1]] : nullptr;
+        a.Fine = l < 15 ? P->f[P->parity[l + 1]] : nullptr;
+        a.cap = P->cap;
+        a.bx = P->mesh.x; a.by = P->mesh.y; a.bz = P->mesh.z; a.blevel = P->mesh.level; a.bcase = P->mesh.case_id;
+        a.nbr = P->nbr;
+        a.cases = P->d_cases;
+        a.dev_status = ctx->dev_status;
+        unsigned grid = std::min<unsigned>(cnt, (unsigned)ctx->num_sms * P->grid_mult);
+        k_collide_stream<<<grid, 256, 0, ctx->stream>>>(a);
+    }
+    P->parity[l] ^= 1;
+}
+
+void step_level(fl_ctx* ctx, fl_pool* P, int l, int sub) {
+    launch_level(ctx, P, l, sub);
+    if (l < P->maxL) {
+        step_level(ctx, P, l + 1, 0);
+        step_level(ctx, P, l + 1, 1);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int fl_pool_create(fl_ctx* ctx, const fl_lbm_case* cases, int ncases, fl_pool** out) {
+    if (!ctx || !cases || ncases <= 0 || ncases > 4096 || !out) return FL_E_INVALID_ARG;
+    *out = nullptr;
+    fl_pool* P = new fl_pool();
+    P->cases.assign(cases, cases + ncases);
+    P->hcases.resize(ncases);
+    std::vector<fl_domain_dev::Case> dom(ncases);
+    size_t n0 = 0;
+    for (int i = 0; i < ncases; ++i) {
+        const fl_lbm_case& c = cases[i];
+        for (int a = 0; a < 3; ++a)
+            if (c.ext[a] < 1 || c.ext[a] > 16) { delete P; return fl_set_error(ctx, FL_E_INVALID_ARG, "case extent must be 1..16 bricks per axis"); }
+        if (c.max_level < 0 || c.max_level > 13 || c.tau0 <= 0.5f) {
+            delete P;
+            return fl_set_error(ctx, FL_E_INVALID_ARG, "case max_level must be 0..13 and tau0 > 0.5");
+        }
+        to_dev_case(c, P->hcases[i]);
+        for (int a = 0; a < 3; ++a) { dom[i].ext[a] = c.ext[a]; dom[i].periodic[a] = c.bc[2 * a] == 0; }
+        P->maxL = std::max(P->maxL, (int)c.max_level);
+        n0 += (size_t)c.ext[0] * c.ext[1] * c.ext[2];
+    }
+    int rc = FL_OK;
+    auto fail = [&](int r) { fl_pool_destroy(ctx, P); return r; };
+    if (cudaMalloc(&P->d_cases, ncases * sizeof(LbmCaseDev)) != cudaSuccess) return fail(FL_E_OOM);
+    if (cudaMalloc(&P->d_dom, ncases * sizeof(fl_domain_dev::Case)) != cudaSuccess) return fail(FL_E_OOM);
+    if (cudaMalloc(&P->d_case_begin, (ncases + 1) * 4) != cudaSuccess) return fail(FL_E_OOM);
+    if (cudaMalloc(&P->case_max, ncases * 4) != cudaSuccess) return fail(FL_E_OOM);
+    if (cudaMalloc(&P->cons, ncases * 32) != cudaSuccess) return fail(FL_E_OOM);
+    cudaMemcpy(P->d_cases, P->hcases.data(), ncases * sizeof(LbmCaseDev), cudaMemcpyHostToDevice);
+    cudaMemcpy(P->d_dom, dom.data(), ncases * sizeof(fl_domain_dev::Case), cudaMemcpyHostToDevice);
+    // level-0 bricks, unsorted
+    std::vector<int32_t> x, y, z;
+    std::vector<uint16_t> cs;
+    for (int i = 0; i < ncases; ++i)
+        for (int32_t k = 0; k < cases[i].ext[2]; ++k)
+            for (int32_t j = 0; j < cases[i].ext[1]; ++j)
+                for (int32_t a = 0; a < cases[i].ext[0]; ++a) {
+                    x.push_back(a); y.push_back(j); z.push_back(k); cs.push_back((uint16_t)i);
+                }
+    P->cap = std::max<size_t>(n0 * 2, 64);
+    rc = fl_mesh_alloc(ctx, P->cap, 1, &P->mesh);
+    if (rc) return fail(rc);
+    cudaMemcpyAsync(P->mesh.x, x.data(), n0 * 4, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(P->mesh.y, y.data(), n0 * 4, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(P->mesh.z, z.data(), n0 * 4, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(P->mesh.case_id, cs.data(), n0 * 2, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemsetAsync(P->mesh.level, 0, n0, ctx->stream);
+    cudaMemsetAsync(P->mesh.state, 0, n0, ctx->stream);
+    cudaMemsetAsync(P->mesh.flags, 0, n0 * 4, ctx->stream);
+    cudaMemsetAsync(P->mesh.material, 0, n0 * 4, ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    P->mesh.num_cells = n0;
+    for (int k = 0; k < 3; ++k)
+        if (cudaMallocAsync((void**)&P->f[k], P->cap * 512 * Q * 4, ctx->stream) != cudaSuccess) return fail(FL_E_OOM);
+    rc = alloc_brick_arrays(ctx, P, P->cap);
+    if (rc) return fail(rc);
+    // an adapt with all flags 0 only sorts: bricks into key order
+    rc = pool_init_populations(ctx, P);
+    if (rc) return fail(rc);
+    rc = pool_regrid(ctx, P, -1, nullptr);
+    if (rc) return fail(rc);
+    for (int r = 0; r < P->maxL; ++r) {
+        rc = pool_regrid(ctx, P, 0, nullptr);
+        if (rc) return fail(rc);
+    }
+    rc = pool_init_populations(ctx, P);
+    if (rc) return fail(rc);
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "pool create");
+    *out = P;
+    return FL_OK;
+}
+
+int fl_pool_destroy(fl_ctx* ctx, fl_pool* P) {
+    if (!ctx || !P) return FL_E_INVALID_ARG;
+    cudaStreamSynchronize(ctx->stream);
+    drop_graph(P);
+    free_brick_arrays(ctx, P);
+    for (int k = 0; k < 3; ++k)
+        if (P->f[k]) cudaFreeAsync(P->f[k], ctx->stream);
+    if (P->mesh.x) fl_mesh_free(ctx, &P->mesh);
+    if (P->adapt_scratch) cudaFreeAsync(P->adapt_scratch, ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    if (P->d_cases) cudaFree(P->d_cases);
+    if (P->d_dom) cudaFree(P->d_dom);
+    if (P->d_case_begin) cudaFree(P->d_case_begin);
+    if (P->case_max) cudaFree(P->case_max);
+    if (P->cons) cudaFree(P->cons);
+    delete P;
+    return FL_OK;
+}
+
+int fl_pool_step(fl_ctx* ctx, fl_pool* P, int nsteps) {
+    if (!ctx || !P || nsteps < 0) return FL_E_INVALID_ARG;
+    for (int i = 0; i < nsteps; ++i) {
+        if (!P->graphs) {
+            step_level(ctx, P, 0, 0);
+            FL_CHECK_LAUNCH(ctx, "k_collide_stream");
+            continue;
+        }
+        // One level-0 step changes only level 0's parity (level l >= 1 runs an
+        // even number of sub-steps), so two captured graphs, one per level-0
+        // parity, replay every step until the topology changes.
+        int p0 = P->parity[0];
+        if (!P->graph[p0]) {
+            int saved[16];
+            std::memcpy(saved, P->parity, sizeof(saved));
+            cudaGraph_t g;
+            FL_TRY_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "capture begin");
+            step_level(ctx, P, 0, 0);
+            cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+            std::memcpy(P->parity, saved, sizeof(saved));
+            FL_TRY_CUDA(ctx, e, "capture end");
+            e = cudaGraphInstantiate(&P->graph[p0], g, 0);
+            cudaGraphDestroy(g);
+            FL_TRY_CUDA(ctx, e, "graph instantiate");
+        }
+        FL_TRY_CUDA(ctx, cudaGraphLaunch(P->graph[p0], ctx->stream), "graph launch");
+        P->parity[0] ^= 1;
+    }
+    return FL_OK;
+}
+
+int fl_pool_regrid(fl_ctx* ctx, fl_pool* P, fl_adapt_stats* st) {
+    if (!ctx || !P) return FL_E_INVALID_ARG;
+    int rc = pool_regrid(ctx, P, 1, st);
+    if (rc) return rc;
+    return fl_collect_device_status(ctx, "fl_pool_regrid");
+}
+
+int fl_pool_info_get(fl_ctx* ctx, fl_pool* P, fl_pool_info* info) {
+    if (!ctx || !P || !info) return FL_E_INVALID_ARG;
+    std::memset(info, 0, sizeof(*info));
+    info->num_bricks = P->mesh.num_cells;
+    info->capacity = P->cap;
+    info->num_cases = (int32_t)P->cases.size();
+    info->max_level = P->maxL;
+    for (int l = 0; l <= P->maxL && l < 16; ++l) info->bricks_per_level[l] = P->lvl_off[l + 1] - P->lvl_off[l];
+    info->fluid_lups_per_step = P->lups;
+    info->population_bytes = (uint64_t)P->cap * 512 * Q * 4 * 3;
+    return FL_OK;
+}
+
+int fl_pool_download(fl_ctx* ctx, fl_pool* P, int32_t* x, int32_t* y, int32_t* z, uint8_t* level, uint16_t* case_id,
+                     float* f) {
+    if (!ctx || !P) return FL_E_INVALID_ARG;
+    size_t n = P->mesh.num_cells;
+    if (x) FL_TRY_CUDA(ctx, cudaMemcpyAsync(x, P->mesh.x, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "dl");
+    if (y) FL_TRY_CUDA(ctx, cudaMemcpyAsync(y, P->mesh.y, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "dl");
+    if (z) FL_TRY_CUDA(ctx, cudaMemcpyAsync(z, P->mesh.z, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "dl");
+    if (level) FL_TRY_CUDA(ctx, cudaMemcpyAsync(level, P->mesh.level, n, cudaMemcpyDeviceToHost, ctx->stream), "dl");
+    if (case_id) FL_TRY_CUDA(ctx, cudaMemcpyAsync(case_id, P->mesh.case_id, n * 2, cudaMemcpyDeviceToHost, ctx->stream), "dl");
+    if (f) {
+        std::vector<uint8_t> lv(n);
+        FL_TRY_CUDA(ctx, cudaMemcpyAsync(lv.data(), P->mesh.level, n, cudaMemcpyDeviceToHost, ctx->stream), "dl");
+        FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "dl");
+        // bricks of one level are contiguous runs only by chance; copy per brick run of equal parity
+        for (int q = 0; q < Q; ++q) {
+            size_t b = 0;
+            while (b < n) {
+                int par = P->parity[lv[b]];
+                size_t e = b + 1;
+                while (e < n && P->parity[lv[e]] == par) ++e;
+                FL_TRY_CUDA(ctx, cudaMemcpyAsync(f + ((size_t)q * n + b) * 512, P->f[par] + ((size_t)q * P->cap + b) * 512,
+                                                 (e - b) * 512 * 4, cudaMemcpyDeviceToHost, ctx->stream), "dl f");
+                b = e;
+            }
+        }
+    }
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "download");
+    return FL_OK;
+}
+
+int fl_pool_nbr(fl_ctx* ctx, fl_pool* P, uint32_t* nbr) {
+    if (!ctx || !P || !nbr) return FL_E_INVALID_ARG;
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(nbr, P->nbr, P->mesh.num_cells * 26 * 4 * 4, cudaMemcpyDeviceToHost, ctx->stream), "nbr");
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "nbr");
+    return FL_OK;
+}
+
+int fl_pool_flags(fl_ctx* ctx, fl_pool* P, int32_t* flags, float* wmax) {
+    if (!ctx || !P) return FL_E_INVALID_ARG;
+    int rc = pool_flags(ctx, P, 1);
+    if (rc) return rc;
+    size_t n = P->mesh.num_cells;
+    if (flags) FL_TRY_CUDA(ctx, cudaMemcpyAsync(flags, P->mesh.flags, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "flags");
+    if (wmax) FL_TRY_CUDA(ctx, cudaMemcpyAsync(wmax, P->wmax, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "wmax");
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "flags");
+    return FL_OK;
+}
+
+int fl_pool_conservation(fl_ctx* ctx, fl_pool* P, double* out) {
+    if (!ctx || !P || !out) return FL_E_INVALID_ARG;
+    size_t n = P->mesh.num_cells;
+    k_brick_sums<<<fl_blocks(n, 1, ctx->num_sms * 8), 512, 0, ctx->stream>>>(view(P), n, P->part, P->fluid);
+    FL_CHECK_LAUNCH(ctx, "k_brick_sums");
+    int nc = (int)P->cases.size();
+    k_case_sums<<<(nc + 127) / 128, 128, 0, ctx->stream>>>(P->part, P->d_case_begin, nc, P->cons);
+    FL_CHECK_LAUNCH(ctx, "k_case_sums");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(out, P->cons, nc * 32, cudaMemcpyDeviceToHost, ctx->stream), "conservation");
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "conservation");
+    return fl_collect_device_status(ctx, "fl_pool_conservation");
+}
+
+int fl_pool_set_options(fl_ctx* ctx, fl_pool* P, int use_graphs, int grid_mult) {
+    if (!ctx || !P) return FL_E_INVALID_ARG;
+    P->graphs = use_graphs;
+    if (grid_mult > 0) P->grid_mult = grid_mult;
+    drop_graph(P);
+    return FL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,127 @@
+"""Python view of the brick-pool part of the C ABI (fl_lbm_case, fl_pool_*)."""
+import ctypes
+
+import numpy as np
+
+from .amr import AdaptStats
+
+P = ctypes.c_void_p
+Q = 19
+
+
+class LbmCase(ctypes.Structure):
+    _fields_ = [("ext", ctypes.c_int32 * 3), ("bc", ctypes.c_int32 * 6), ("wall_u", ctypes.c_float * 3),
+                ("inlet_u", ctypes.c_float * 3), ("tau0", ctypes.c_float), ("max_level", ctypes.c_int32),
+                ("has_sphere", ctypes.c_int32), ("sphere_c", ctypes.c_float * 3), ("sphere_r", ctypes.c_float),
+                ("refine_frac", ctypes.c_float), ("coarsen_frac", ctypes.c_float), ("band", ctypes.c_float),
+                ("init_u", ctypes.c_float * 3)]
+
+
+class PoolInfo(ctypes.Structure):
+    _fields_ = [("num_bricks", ctypes.c_size_t), ("capacity", ctypes.c_size_t), ("num_cases", ctypes.c_int32),
+                ("max_level", ctypes.c_int32), ("bricks_per_level", ctypes.c_uint32 * 16),
+                ("fluid_lups_per_step", ctypes.c_uint64), ("population_bytes", ctypes.c_uint64)]
+
+
+WALL, MOVING, INLET, OUTLET, PERIODIC = 1, 2, 3, 4, 0
+
+
+def cavity(edge_sites=32, max_level=2, u_lid=0.05, tau=0.56):
+    """Lid-driven cavity: walls, lid moving +x on the top z face."""
+    c = LbmCase()
+    e = edge_sites // 8
+    c.ext[:] = [e, e, e]
+    c.bc[:] = [WALL, WALL, WALL, WALL, WALL, MOVING]
+    c.wall_u[:] = [u_lid, 0.0, 0.0]
+    c.tau0 = tau
+    c.max_level = max_level
+    c.refine_frac, c.coarsen_frac = 0.5, 0.1
+    return c
+
+
+def sphere_channel(nx=128, ny=64, nz=64, max_level=3, radius=8.0, centre=(32.0, 32.0, 32.0), u_in=0.04,
+                   tau=0.56, band=6.0):
+    """Flow past a sphere: equilibrium inlet at x=0, zero-gradient outlet, periodic y/z."""
+    c = LbmCase()
+    c.ext[:] = [nx // 8, ny // 8, nz // 8]
+    c.bc[:] = [INLET, OUTLET, PERIODIC, PERIODIC, PERIODIC, PERIODIC]
+    c.inlet_u[:] = [u_in, 0.0, 0.0]
+    c.init_u[:] = [u_in, 0.0, 0.0]
+    c.tau0 = tau
+    c.max_level = max_level
+    c.has_sphere = 1
+    c.sphere_c[:] = list(centre)
+    c.sphere_r = radius
+    c.band = band
+    c.refine_frac, c.coarsen_frac = 0.5, 0.1
+    return c
+
+
+class Pool:
+    """A set of independent cases advanced together (fl_pool)."""
+
+    def __init__(self, ctx, cases):
+        self.ctx = ctx
+        arr = (LbmCase * len(cases))(*cases)
+        self.ncases = len(cases)
+        h = ctypes.c_void_p()
+        ctx.call("fl_pool_create", arr, len(cases), ctypes.byref(h))
+        self.h = h
+
+    def step(self, n=1):
+        self.ctx.call("fl_pool_step", self.h, n)
+
+    def regrid(self):
+        st = AdaptStats()
+        self.ctx.call("fl_pool_regrid", self.h, ctypes.byref(st))
+        return st
+
+    def info(self):
+        i = PoolInfo()
+        self.ctx.call("fl_pool_info_get", self.h, ctypes.byref(i))
+        return i
+
+    def set_options(self, graphs=1, grid_mult=0):
+        self.ctx.call("fl_pool_set_options", self.h, graphs, grid_mult)
+
+    def bricks(self):
+        n = self.info().num_bricks
+        x, y, z = (np.empty(n, np.int32) for _ in range(3))
+        lv, cs = np.empty(n, np.uint8), np.empty(n, np.uint16)
+        self.ctx.call("fl_pool_download", self.h, *[a.ctypes.data_as(P) for a in (x, y, z, lv, cs)], None)
+        return {"x": x, "y": y, "z": z, "level": lv, "case_id": cs}
+
+    def populations(self):
+        n = self.info().num_bricks
+        f = np.empty((Q, n, 512), np.float32)
+        self.ctx.call("fl_pool_download", self.h, None, None, None, None, None, f.ctypes.data_as(P))
+        return f
+
+    def nbr(self):
+        n = self.info().num_bricks
+        a = np.empty(n * 26 * 4, np.uint32)
+        self.ctx.call("fl_pool_nbr", self.h, a.ctypes.data_as(P))
+        return a
+
+    def flags(self):
+        n = self.info().num_bricks
+        fl, wm = np.empty(n, np.int32), np.empty(n, np.float32)
+        self.ctx.call("fl_pool_flags", self.h, fl.ctypes.data_as(P), wm.ctypes.data_as(P))
+        return fl, wm
+
+    def conservation(self):
+        out = np.empty((self.ncases, 4), np.float64)
+        self.ctx.call("fl_pool_conservation", self.h, out.ctypes.data_as(P))
+        return out
+
+    def close(self):
+        if self.h:
+            self.ctx.call("fl_pool_destroy", self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            if self.h and self.ctx.handle:
+                self.ctx.lib.fl_pool_destroy(self.ctx.handle, self.h)
+        except Exception:
+            pass

@@ -175,6 +175,60 @@ int fl_adapt(fl_ctx* ctx, fl_mesh* mesh, const fl_adapt_config* cfg, float** fie
  * (point-location rule of src/adaptation/kernels/balance_enforce.cl:107-143).  subslots 1 or 4. */
 int fl_neighbour_rebuild(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, int subslots, uint32_t* nbr);
 
+/* ---- D3Q19 BGK collide-stream over an octree of 8^3-site bricks.
+ * The reference emits empty lbm_* kernels (src/parsing/SimulationBuilder.cpp:394-400) behind
+ * KernelNode (include/fluidloom/runtime/nodes/KernelNode.h:46-72) and stores fields through
+ * SOAFieldManager (include/fluidloom/core/fields/SOAFieldManager.h:26-51); a pool owns the
+ * leaves of one or more independent cases (a "cell" of the AMR API is one brick here), their
+ * 19-component FP32 populations in SoA layout, the neighbour table and the per-level lists. */
+typedef struct fl_lbm_case {
+    int32_t ext[3];        /* level-0 bricks per axis (1..16); a brick is 8^3 sites */
+    int32_t bc[6];         /* faces -x,+x,-y,+y,-z,+z: 0 periodic, 1 wall, 2 moving wall, 3 inlet, 4 outlet */
+    float wall_u[3];       /* moving-wall velocity */
+    float inlet_u[3];      /* inlet velocity */
+    float tau0;            /* relaxation time at level 0 */
+    int32_t max_level;     /* 0..13 */
+    int32_t has_sphere;
+    float sphere_c[3];     /* centre, level-0 site units */
+    float sphere_r;        /* radius, level-0 site units */
+    float refine_frac;     /* refine a brick whose max |vorticity| exceeds this fraction of the case max */
+    float coarsen_frac;    /* coarsen below this fraction */
+    float band;            /* bricks within this distance of the sphere surface refine to max_level */
+    float init_u[3];       /* initial velocity (density 1) */
+} fl_lbm_case;
+
+typedef struct fl_pool fl_pool;
+
+typedef struct fl_pool_info {
+    size_t num_bricks;
+    size_t capacity;
+    int32_t num_cases;
+    int32_t max_level;
+    uint32_t bricks_per_level[16];
+    uint64_t fluid_lups_per_step;   /* fluid site updates per level-0 step: sum of 2^level */
+    uint64_t population_bytes;
+} fl_pool_info;
+
+/* Build the cases: level-0 bricks, max_level rounds of sphere-band refinement, equilibrium start. */
+int fl_pool_create(fl_ctx* ctx, const fl_lbm_case* cases, int ncases, fl_pool** out);
+int fl_pool_destroy(fl_ctx* ctx, fl_pool* pool);
+/* Advance every case by nsteps level-0 steps (levels sub-cycled), asynchronously. */
+int fl_pool_step(fl_ctx* ctx, fl_pool* pool, int nsteps);
+/* Regrid all cases: vorticity/band flags, FULL26 adapt, population remap, neighbour rebuild
+ * (the AdaptMeshNode::execute path, src/runtime/nodes/AdaptMeshNode.cpp:9-64). */
+int fl_pool_regrid(fl_ctx* ctx, fl_pool* pool, fl_adapt_stats* stats);
+int fl_pool_info_get(fl_ctx* ctx, fl_pool* pool, fl_pool_info* info);
+/* Host copies of the bricks and (f != NULL) the current populations as [19][n][512]. */
+int fl_pool_download(fl_ctx* ctx, fl_pool* pool, int32_t* x, int32_t* y, int32_t* z, uint8_t* level,
+                     uint16_t* case_id, float* f);
+int fl_pool_nbr(fl_ctx* ctx, fl_pool* pool, uint32_t* nbr);
+/* Refinement flags and per-brick max |vorticity| of the current state (host outputs). */
+int fl_pool_flags(fl_ctx* ctx, fl_pool* pool, int32_t* flags, float* wmax);
+/* Per case: fluid mass and momentum (FP64, sites weighted by 8^-level) -> out[ncases][4] (host). */
+int fl_pool_conservation(fl_ctx* ctx, fl_pool* pool, double* out);
+/* use_graphs: replay captured CUDA graphs per level-0 step; grid_mult: CTAs per SM (0 keeps). */
+int fl_pool_set_options(fl_ctx* ctx, fl_pool* pool, int use_graphs, int grid_mult);
+
 #ifdef __cplusplus
 }
 #endif

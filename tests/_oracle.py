@@ -232,3 +232,62 @@ def random_octree(seed, ext=(2, 2, 2), rounds=3, max_level=6, frac=0.3, balanced
                                         averaging_rule=0), dom)
         cols = {k: v.copy() for k, v in cols.items()}
     return cols
+
+
+# ---- brick pool ------------------------------------------------------------
+class OraclePool:
+    def __init__(self, cases):
+        L = load()
+        arr = (LbmCase * len(cases))()
+        for i, c in enumerate(cases):
+            ctypes.memmove(ctypes.byref(arr[i]), ctypes.byref(c), ctypes.sizeof(LbmCase))
+        self.ncases = len(cases)
+        self.h = L.or_pool_new(arr, len(cases))
+
+    def n(self):
+        return load().or_pool_size(self.h)
+
+    def step(self, k, threads=0):
+        import os
+        load().or_pool_steps(self.h, k, threads or (os.cpu_count() or 1))
+
+    def regrid(self):
+        load().or_pool_regrid(self.h)
+
+    def bricks(self):
+        n = self.n()
+        x, y, z = (np.empty(n, np.int32) for _ in range(3))
+        lv, cs = np.empty(n, np.uint8), np.empty(n, np.uint16)
+        load().or_pool_bricks(self.h, ptr(x), ptr(y), ptr(z), ptr(lv), ptr(cs))
+        return {"x": x, "y": y, "z": z, "level": lv, "case_id": cs}
+
+    def populations(self):
+        n = self.n()
+        f = np.empty((19, n, 512), np.float32)
+        load().or_pool_populations(self.h, ptr(f))
+        return f
+
+    def nbr(self):
+        a = np.empty(self.n() * 26 * 4, np.uint32)
+        load().or_pool_nbr(self.h, ptr(a))
+        return a
+
+    def flags(self):
+        n = self.n()
+        fl, wm = np.empty(n, np.int32), np.empty(n, np.float32)
+        load().or_pool_flags(self.h, ptr(fl), ptr(wm))
+        return fl, wm
+
+    def conservation(self):
+        out = np.empty((self.ncases, 4), np.float64)
+        load().or_pool_conservation(self.h, ptr(out))
+        return out
+
+    def lups(self):
+        return load().or_pool_fluid_lups(self.h)
+
+    def __del__(self):
+        try:
+            load().or_pool_free(self.h)
+        except Exception:
+            pass
