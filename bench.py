@@ -1,0 +1,396 @@
+"""bench.py — AMR lattice-Boltzmann throughput on one GB300 (flow past a sphere).
+
+Workload (the headline configuration): D3Q19 BGK, FP32 SoA populations in
+8^3-site bricks, base grid 128x64x64 sites (16x8x8 level-0 bricks), 3
+refinement levels, sphere of radius 8 base sites at (32,32,32) with half-way
+bounce-back, equilibrium inlet u=0.04 at x=0, zero-gradient outlet, periodic
+y/z, tau_0 = 0.56; bricks within 6 base sites of the sphere surface refined to
+level 3 (balanced 2:1 over faces, edges and corners); regrid every 25 steps
+from vorticity (refine > 0.5 max, coarsen < 0.1 max) plus the band.  A step is
+one level-0 time step (level l sub-cycled 2^l times).  Synthetic, seeded
+inputs: the reference publishes no dataset or benchmark numbers.
+
+value = fluid lattice updates per second over all ranks (MLUPS), populations
+resident in HBM.  e2e = the same through the public C ABI from pinned host
+memory: the full population state uploaded at the start and downloaded at the
+end of the timed region, per-step inlet/wall velocities host->device and the
+per-step FP64 mass/momentum read back.  Also reported: regrid ms per cycle on
+this workload and the 16.7M-leaf regrid microbenchmark (flags, 2:1 balance,
+split/merge, 63-bit key sort, compaction, neighbour rebuild).
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_LUP = 152  # 19 FP32 reads + 19 FP32 writes per fluid site update
+REGRID_EVERY = 25
+METRIC = "AMR-LBM MLUPS (D3Q19, flow past a sphere)"
+UNIT = "MLUPS"
+
+
+def sphere_case(scale=1):
+    from fluidloom_gb300 import lbm
+    return lbm.sphere_channel(128 // scale, 64 // scale, 64 // scale, 3, radius=8.0 / scale,
+                              centre=(32.0 / scale,) * 3, u_in=0.04, tau=0.56, band=6.0 / scale)
+
+
+def workload_config(extra=None):
+    c = {"workload": "flow past a sphere, D3Q19 BGK FP32, 128x64x64 base, 3 levels, r=8, u=0.04, tau0=0.56",
+         "base_grid": [128, 64, 64], "levels": 3, "brick": "8^3 sites", "regrid_every": REGRID_EVERY,
+         "l2": "inputs larger than L2 (populations > 129 MB), no flush", "graphs": True}
+    if extra:
+        c.update(extra)
+    return c
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return float(json.load(open(p))["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the collide-stream from the committed ncu summary, scaled per fluid site."""
+    p = os.path.join(ROOT, "profiles", "collide_stream_traffic.json")
+    if not os.path.exists(p):
+        return None
+    try:
+        d = json.load(open(p))
+        return float(d["dram_bytes_per_fluid_site"])
+    except Exception:
+        return None
+
+
+# ---------------------------------------------------------------- GPU arm
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return ws, rank, local, dist
+
+
+def dist_max(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_sum(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def timer(ctx):
+    import ctypes
+    ctx.call("fl_ctx_timer_start")
+
+    def stop():
+        ms = ctypes.c_float()
+        ctx.call("fl_ctx_timer_stop", ctypes.byref(ms))
+        return ms.value
+    return stop
+
+
+def regrid_microbench(ctx, seed=1):
+    """16.7M-leaf regrid: blob flags, FULL26 balance to a fixed point, split/merge,
+    key sort, rebuild; neighbour table; and a 16.7M 63-bit key sort alone."""
+    import ctypes
+    from fluidloom_gb300 import DeviceArray
+    from fluidloom_gb300.amr import AdaptConfig, AdaptStats, Mesh
+    L = 8
+    n1 = 1 << L
+    idx = np.arange(n1 ** 3, dtype=np.int64)
+    cols = {"x": (idx % n1).astype(np.int32), "y": ((idx // n1) % n1).astype(np.int32),
+            "z": (idx // (n1 * n1)).astype(np.int32), "level": np.full(len(idx), L, np.uint8)}
+    rng = np.random.default_rng(seed)
+    c = rng.random((64, 3))
+    s = rng.uniform(0.02, 0.1, 64)
+    blobs = np.ascontiguousarray(np.concatenate([c, (1 / (2 * s * s))[:, None], np.ones((64, 1))], 1), np.float32)
+    m = Mesh(ctx, cols)
+    cfg = AdaptConfig.make(max_level=9, min_level=0, balance_mode=1)
+    out = {}
+    stop = timer(ctx)
+    ctx.call("fl_flags_from_blobs", ctypes.byref(m.m), blobs.ctypes.data_as(ctypes.c_void_p), 64,
+             ctypes.c_float(0.05), ctypes.c_float(0.5), 9)
+    out["flags_ms"] = stop()
+    st = AdaptStats()
+    fp = ctypes.c_void_p(0)
+    stop = timer(ctx)
+    ctx.call("fl_adapt", ctypes.byref(m.m), ctypes.byref(cfg), ctypes.byref(fp), 0, ctypes.byref(st))
+    out["adapt_ms"] = stop()
+    n = m.n
+    nbr = DeviceArray(ctx, (n * 26,), np.uint32)
+    stop = timer(ctx)
+    ctx.call("fl_neighbour_rebuild", ctypes.byref(m.m), ctypes.byref(cfg), 1, nbr.ptr)
+    out["neighbour_ms"] = stop()
+    nbr.free()
+    keys = DeviceArray(ctx, (n,), np.uint64)
+    ids = DeviceArray(ctx, (n,), np.uint32)
+    ctx.call("fl_cell_keys", m.m.x, m.m.y, m.m.z, m.m.level, None, 21, 21, keys.ptr, n)
+    ctx.call("fl_hilbert_encode", m.m.x, m.m.y, m.m.z, 21, keys.ptr, ids.ptr, n)
+    ctx.sync()
+    stop = timer(ctx)
+    ctx.call("fl_sort_pairs_u64_u32", keys.ptr, ids.ptr, n, 0, 63)
+    out["sort_ms"] = stop()
+    out.update({"leaves_in": int(len(idx)), "leaves_out": int(n), "split": st.num_split, "merged_groups": st.num_groups,
+                "balance_iterations": st.balance.iterations, "balance_marked": st.balance.total_cells_marked_for_balance,
+                "sorted_keys_per_s": n / (out["sort_ms"] * 1e-3),
+                "regrid_ms": out["flags_ms"] + out["adapt_ms"] + out["neighbour_ms"]})
+    m.free()
+    return out
+
+
+def cpu_sample(steps, threads=None):
+    """The oracle (CPU port) on a half-resolution sample of the workload: 64x32x32 base, 3 levels, r=4."""
+    from tests import _oracle as O
+    case = sphere_case(scale=2)
+    p = O.OraclePool([case])
+    lups = p.lups()
+    threads = threads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    p.step(steps, threads)
+    dt = time.perf_counter() - t0
+    return lups * steps / dt / 1e6, threads, lups
+
+
+def run_gpu(args):
+    import ctypes
+    from fluidloom_gb300 import build as fbuild
+    fbuild.build()
+    import fluidloom_gb300 as fl
+    from fluidloom_gb300.lbm import Pool
+    ws, rank, local, dist = dist_setup()
+    ctx = fl.Context(local)
+    pool = Pool(ctx, [sphere_case()])
+    info = pool.info()
+    bricks0 = info.num_bricks
+    lups0 = info.fluid_lups_per_step
+    for _ in range(args.warmup):
+        pool.step(1)
+    ctx.sync()
+    barrier(dist)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    total_lups = 0
+    regrids = 0
+    regrid_ms = []
+    launches = 0
+    stop = timer(ctx)
+    for k in range(args.steps):
+        step_no = args.warmup + k + 1
+        inf = pool.info()
+        total_lups += inf.fluid_lups_per_step
+        launches += sum(1 << l for l in range(inf.max_level + 1) if inf.bricks_per_level[l])
+        pool.step(1)
+        if step_no % REGRID_EVERY == 0:
+            pool.regrid()
+            regrids += 1
+    ms = stop()
+    clk = clocks.stop()
+    barrier(dist)
+    ms_max = dist_max(dist, ms)
+    lups_all = dist_sum(dist, float(total_lups))
+    value = lups_all / (ms_max * 1e-3) / 1e6
+    # regrid ms per cycle on this workload (one more regrid, timed alone)
+    stop = timer(ctx)
+    st = pool.regrid()
+    regrid_ms.append(stop())
+    # roofline: per-launch CUDA events around every collide-stream launch
+    kms, nla, sites = pool.profile_steps(max(2, min(args.steps, 6)))
+    peak, peak_kind = measured_peak()
+    achieved = BYTES_PER_LUP * sites / (kms * 1e-3) / 1e9
+    tr = ncu_traffic()
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": (round(tr * sites / nla) if tr else None),
+                "kernel": "k_collide_stream", "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                "algorithmic_bytes_per_launch": round(BYTES_PER_LUP * sites / nla), "launches_profiled": nla,
+                "avg_launch_ms": round(kms / nla, 4)}
+    # e2e through the C ABI with pinned host buffers
+    inf = pool.info()
+    n = inf.num_bricks
+    fbytes = 19 * n * 512 * 4
+    hp = ctypes.c_void_p()
+    ctx.call("fl_host_alloc_pinned", ctypes.c_size_t(fbytes), ctypes.byref(hp))
+    hf = np.ctypeslib.as_array(ctypes.cast(hp, ctypes.POINTER(ctypes.c_float)), shape=(19, n, 512))
+    ctx.call("fl_pool_download", pool.h, None, None, None, None, None, hp)
+    vp = ctypes.c_void_p()
+    ctx.call("fl_host_alloc_pinned", ctypes.c_size_t(64), ctypes.byref(vp))
+    vel = np.ctypeslib.as_array(ctypes.cast(vp, ctypes.POINTER(ctypes.c_float)), shape=(2, 3))
+    vel[:] = 0.0
+    vel[1, 0] = 0.04
+    cons = np.empty((1, 4), np.float64)
+    e2e_lups = 0
+    pool.step(1)  # graph capture for the uploaded state happens in the loop below
+    ctx.sync()
+    barrier(dist)
+    t0 = time.perf_counter()
+    stop = timer(ctx)
+    ctx.call("fl_pool_upload", pool.h, hp)
+    for k in range(args.steps):
+        ctx.call("fl_pool_set_velocities", pool.h, vp, ctypes.c_void_p(vp.value + 12))
+        e2e_lups += inf.fluid_lups_per_step
+        pool.step(1)
+        ctx.call("fl_pool_conservation", pool.h, cons.ctypes.data_as(ctypes.c_void_p))
+    ctx.call("fl_pool_download", pool.h, None, None, None, None, None, hp)
+    e2e_ms = stop()
+    e2e_wall = time.perf_counter() - t0
+    e2e_ms = max(e2e_ms, e2e_wall * 1e3)
+    e2e_ms = dist_max(dist, e2e_ms)
+    e2e_value = dist_sum(dist, float(e2e_lups)) / (e2e_ms * 1e-3) / 1e6
+    h2d = (fbytes + args.steps * 24) / args.steps
+    d2h = (fbytes + args.steps * 32) / args.steps
+    ctx.call("fl_host_free_pinned", hp)
+    ctx.call("fl_host_free_pinned", vp)
+    micro = None
+    if rank == 0 and not args.no_microbench:
+        pool.close()
+        micro = regrid_microbench(ctx)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        v, th, sl = cpu_sample(1)
+        cpu = {"value": round(v, 2), "unit": UNIT, "cores": th, "kind": "port",
+               "sample": "CPU oracle (OpenMP, all host threads) on the same case at half resolution per axis "
+                         "(64x32x32 base, 3 levels, r=4; %d fluid updates per step), 1 level-0 step" % sl}
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": workload_config({"bricks": int(bricks0), "fluid_lups_per_step": int(lups0),
+                                           "parallelism": "replicas" if ws > 1 else "single"}),
+                "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                        "d2h_bytes_per_step": int(d2h)},
+                "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
+                "regrid_ms_per_cycle": round(statistics.mean(regrid_ms), 3), "regrids_in_timed_region": regrids,
+                "regrid_microbench": micro}
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from tests import _oracle as O
+    case = sphere_case(scale=2)
+    p = O.OraclePool([case])
+    lups = p.lups()
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        p.step(1, threads)
+    t0 = time.perf_counter()
+    p.step(args.steps, threads)
+    dt = time.perf_counter() - t0
+    value = lups * args.steps / dt / 1e6
+    sample = ("CPU restatement of the path (oracle/, OpenMP over all host threads; the reference has no "
+              "lattice-Boltzmann code and its OpenCL kernels cannot run on this host) on the workload at half "
+              "resolution per axis (64x32x32 base, 3 levels, r=4), %d fluid updates per step" % lups)
+    line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": workload_config({"sample_scale": 0.5}),
+            "cpu_baseline": {"value": round(value, 2), "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 2), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=25)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--no-microbench", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -25,6 +25,7 @@ struct fl_ctx {
     uint32_t* dev_status = nullptr;     // device-side status words (see FL_DEVSTAT_*)
     uint32_t* host_status = nullptr;    // pinned mirror
     std::string last_error;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // fl_ctx_timer_start / stop
 };
 
 // Device status words written by kernels instead of trapping.

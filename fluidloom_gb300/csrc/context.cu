@@ -106,6 +106,8 @@ int fl_ctx_destroy(fl_ctx* ctx) {
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->dev_status) cudaFree(ctx->dev_status);
     if (ctx->host_status) cudaFreeHost(ctx->host_status);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return FL_OK;
@@ -166,6 +168,38 @@ int fl_memcpy_d2h(fl_ctx* ctx, void* dst, const void* src, size_t bytes) {
     if (!bytes) return FL_OK;
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream), "fl_memcpy_d2h");
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "fl_memcpy_d2h sync");
+    return FL_OK;
+}
+
+int fl_host_alloc_pinned(fl_ctx* ctx, size_t bytes, void** out) {
+    if (!ctx || !out) return FL_E_INVALID_ARG;
+    *out = nullptr;
+    if (!bytes) return FL_OK;
+    FL_TRY_CUDA(ctx, cudaMallocHost(out, bytes), "fl_host_alloc_pinned");
+    return FL_OK;
+}
+
+int fl_host_free_pinned(fl_ctx* ctx, void* p) {
+    if (!ctx) return FL_E_INVALID_ARG;
+    if (p) FL_TRY_CUDA(ctx, cudaFreeHost(p), "fl_host_free_pinned");
+    return FL_OK;
+}
+
+int fl_ctx_timer_start(fl_ctx* ctx) {
+    if (!ctx) return FL_E_INVALID_ARG;
+    if (!ctx->ev0) {
+        FL_TRY_CUDA(ctx, cudaEventCreate(&ctx->ev0), "event");
+        FL_TRY_CUDA(ctx, cudaEventCreate(&ctx->ev1), "event");
+    }
+    FL_TRY_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream), "event record");
+    return FL_OK;
+}
+
+int fl_ctx_timer_stop(fl_ctx* ctx, float* ms) {
+    if (!ctx || !ms || !ctx->ev0) return FL_E_INVALID_ARG;
+    FL_TRY_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream), "event record");
+    FL_TRY_CUDA(ctx, cudaEventSynchronize(ctx->ev1), "event sync");
+    FL_TRY_CUDA(ctx, cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1), "event elapsed");
     return FL_OK;
 }
 

@@ -31,6 +31,7 @@
 #include "scan.cuh"
 
 #include <algorithm>
+#include <cstddef>
 #include <cstring>
 #include <vector>
 
@@ -531,7 +532,75 @@ __global__ void k_case_sums(const double* __restrict__ part, const uint32_t* __r
     for (int k = 0; k < 4; ++k) out[cs * 4 + k] = acc[k];
 }
 
+// exp(x) for x <= 0 from the mathematics: x = n ln2 + r with |r| <= ln2/2
+// (Cody & Waite 1980 two-constant reduction), e^r by its Taylor series to r^7,
+// then an exact scaling by 2^n.  Written operation by operation (this unit has
+// no FMA contraction) so the CPU restatement gives the same bits.
+__device__ __forceinline__ float fl_exp_neg(float x) {
+    if (x < -87.0f) return 0.0f;
+    float t = x * 1.44269504f;
+    t = t + 0.5f;
+    float n = floorf(t);
+    float r = x - n * 0.693145752f;
+    r = r - n * 1.42860677e-06f;
+    float p = 1.0f / 5040.0f;
+    p = p * r; p = p + 1.0f / 720.0f;
+    p = p * r; p = p + 1.0f / 120.0f;
+    p = p * r; p = p + 1.0f / 24.0f;
+    p = p * r; p = p + 1.0f / 6.0f;
+    p = p * r; p = p + 0.5f;
+    p = p * r; p = p + 1.0f;
+    p = p * r; p = p + 1.0f;
+    return ldexpf(p, (int)n);
+}
+
+// Synthetic refine/coarsen flags: the sum of Gaussian blobs at each cell's
+// centre (unit cube, native coords at `level`, anchor level A), refine above
+// `hi`, coarsen below `lo` (the regrid microbenchmark's flag source).
+__global__ void k_blob_flags(fl_mesh_dev m, const float* __restrict__ blobs, int nblobs, int anchor_level, float lo,
+                             float hi, int max_level, int32_t* __restrict__ flags) {
+    extern __shared__ float sb[];
+    for (int i = threadIdx.x; i < nblobs * 5; i += blockDim.x) sb[i] = blobs[i];
+    __syncthreads();
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
+        int l = m.level[i];
+        float inv = 1.0f / (float)(1 << l);
+        float px = ((float)m.x[i] + 0.5f) * inv, py = ((float)m.y[i] + 0.5f) * inv, pz = ((float)m.z[i] + 0.5f) * inv;
+        float v = 0.0f;
+        for (int k = 0; k < nblobs; ++k) {
+            const float* B = sb + 5 * k;  // cx, cy, cz, 1/(2 sigma^2), amplitude
+            float dx = px - B[0], dy = py - B[1], dz = pz - B[2];
+            float d2 = dx * dx;
+            d2 = d2 + dy * dy;
+            d2 = d2 + dz * dz;
+            float e = fl_exp_neg(-(d2 * B[3]));
+            v = v + B[4] * e;
+        }
+        int32_t f = 0;
+        if (v > hi && l < max_level) f = 1;
+        else if (v < lo) f = -1;
+        flags[i] = f;
+    }
+}
+
 }  // namespace
+
+extern "C" int fl_flags_from_blobs(fl_ctx* ctx, fl_mesh* mesh, const float* blobs_host, int nblobs, float lo, float hi,
+                                   int max_level) {
+    if (!ctx || !mesh || (nblobs && !blobs_host) || nblobs < 0 || nblobs > 1024) return FL_E_INVALID_ARG;
+    if (mesh->num_cells == 0) return FL_OK;
+    int rc = fl_scratch_reserve(ctx, (size_t)nblobs * 20 + 256);
+    if (rc) return rc;
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->scratch, blobs_host, (size_t)nblobs * 20, cudaMemcpyHostToDevice, ctx->stream),
+                "blobs");
+    fl_mesh_dev md{mesh->x, mesh->y, mesh->z, mesh->level, mesh->state, mesh->flags, mesh->material, mesh->case_id,
+                   mesh->num_cells};
+    k_blob_flags<<<fl_blocks(mesh->num_cells, 256, ctx->num_sms * 8), 256, (size_t)nblobs * 20, ctx->stream>>>(
+        md, (const float*)ctx->scratch, nblobs, 0, lo, hi, max_level, mesh->flags);
+    FL_CHECK_LAUNCH(ctx, "k_blob_flags");
+    return FL_OK;
+}
 
 // ------------------------------------------------------------------ pool
 struct fl_pool {
@@ -555,6 +624,7 @@ struct fl_pool {
     double* cons = nullptr;
     uint32_t* fluid = nullptr;
     uint64_t lups = 0;
+    uint64_t fluid_per_level[16] = {0};
     int graphs = 1;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one level-0 step, per level-0 parity
     void* adapt_scratch = nullptr;
@@ -686,7 +756,11 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(fl.data(), P->fluid, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "fluid");
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "topology sync");
     P->lups = 0;
-    for (size_t i = 0; i < n; ++i) P->lups += (uint64_t)fl[i] << lv[i];
+    for (int l = 0; l < 16; ++l) P->fluid_per_level[l] = 0;
+    for (size_t i = 0; i < n; ++i) {
+        P->lups += (uint64_t)fl[i] << lv[i];
+        P->fluid_per_level[lv[i]] += fl[i];
+    }
     drop_graph(P);
     return fl_collect_device_status(ctx, "pool topology");
 }
@@ -791,9 +865,20 @@ int pool_regrid(fl_ctx* ctx, fl_pool* P, int use_vorticity, fl_adapt_stats* st) 
     return rc;
 }
 
-void launch_level(fl_ctx* ctx, fl_pool* P, int l, int sub) {
+struct LaunchTimer {
+    std::vector<cudaEvent_t> ev;  // start/stop pairs
+    std::vector<uint64_t> sites;  // fluid sites processed by each launch
+};
+
+void launch_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm = nullptr) {
     uint32_t off = P->lvl_off[l], cnt = P->lvl_off[l + 1] - P->lvl_off[l];
     if (cnt) {
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if (tm) {
+            cudaEventCreate(&e0);
+            cudaEventCreate(&e1);
+            cudaEventRecord(e0, ctx->stream);
+        }
         StepArgs a;
         a.list = P->list + off;
         a.count = cnt;
@@ -811,15 +896,21 @@ void launch_level(fl_ctx* ctx, fl_pool* P, int l, int sub) {
         a.dev_status = ctx->dev_status;
         unsigned grid = std::min<unsigned>(cnt, (unsigned)ctx->num_sms * P->grid_mult);
         k_collide_stream<<<grid, 256, 0, ctx->stream>>>(a);
+        if (tm) {
+            cudaEventRecord(e1, ctx->stream);
+            tm->ev.push_back(e0);
+            tm->ev.push_back(e1);
+            tm->sites.push_back(P->fluid_per_level[l]);
+        }
     }
     P->parity[l] ^= 1;
 }
 
-void step_level(fl_ctx* ctx, fl_pool* P, int l, int sub) {
-    launch_level(ctx, P, l, sub);
+void step_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm = nullptr) {
+    launch_level(ctx, P, l, sub, tm);
     if (l < P->maxL) {
-        step_level(ctx, P, l + 1, 0);
-        step_level(ctx, P, l + 1, 1);
+        step_level(ctx, P, l + 1, 0, tm);
+        step_level(ctx, P, l + 1, 1, tm);
     }
 }
 
@@ -965,6 +1056,7 @@ int fl_pool_info_get(fl_ctx* ctx, fl_pool* P, fl_pool_info* info) {
     info->max_level = P->maxL;
     for (int l = 0; l <= P->maxL && l < 16; ++l) info->bricks_per_level[l] = P->lvl_off[l + 1] - P->lvl_off[l];
     info->fluid_lups_per_step = P->lups;
+    for (int l = 0; l < 16; ++l) info->fluid_sites_per_level[l] = P->fluid_per_level[l];
     info->population_bytes = (uint64_t)P->cap * 512 * Q * 4 * 3;
     return FL_OK;
 }
@@ -1028,6 +1120,56 @@ int fl_pool_conservation(fl_ctx* ctx, fl_pool* P, double* out) {
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(out, P->cons, nc * 32, cudaMemcpyDeviceToHost, ctx->stream), "conservation");
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "conservation");
     return fl_collect_device_status(ctx, "fl_pool_conservation");
+}
+
+int fl_pool_profile_steps(fl_ctx* ctx, fl_pool* P, int nsteps, double* kernel_ms, uint32_t* launches,
+                          uint64_t* fluid_sites) {
+    if (!ctx || !P || nsteps < 0) return FL_E_INVALID_ARG;
+    LaunchTimer tm;
+    for (int i = 0; i < nsteps; ++i) step_level(ctx, P, 0, 0, &tm);
+    FL_CHECK_LAUNCH(ctx, "k_collide_stream");
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "profile sync");
+    double ms = 0.0;
+    uint64_t sites = 0;
+    for (size_t k = 0; k < tm.ev.size(); k += 2) {
+        float t = 0.0f;
+        cudaEventElapsedTime(&t, tm.ev[k], tm.ev[k + 1]);
+        ms += t;
+        cudaEventDestroy(tm.ev[k]);
+        cudaEventDestroy(tm.ev[k + 1]);
+    }
+    for (uint64_t x : tm.sites) sites += x;
+    if (kernel_ms) *kernel_ms = ms;
+    if (launches) *launches = (uint32_t)(tm.ev.size() / 2);
+    if (fluid_sites) *fluid_sites = sites;
+    drop_graph(P);
+    return fl_collect_device_status(ctx, "fl_pool_profile_steps");
+}
+
+int fl_pool_upload(fl_ctx* ctx, fl_pool* P, const float* f) {
+    if (!ctx || !P || !f) return FL_E_INVALID_ARG;
+    size_t n = P->mesh.num_cells;
+    for (int q = 0; q < Q; ++q)
+        FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->f[0] + (size_t)q * P->cap * 512, f + (size_t)q * n * 512, n * 512 * 4,
+                                         cudaMemcpyHostToDevice, ctx->stream), "upload");
+    for (int l = 0; l < 16; ++l) P->parity[l] = 0;
+    drop_graph(P);
+    return FL_OK;
+}
+
+int fl_pool_set_velocities(fl_ctx* ctx, fl_pool* P, const float* wall_u, const float* inlet_u) {
+    if (!ctx || !P) return FL_E_INVALID_ARG;
+    // per case 3 floats each; a host->device copy ordered on the stream, read by the next step
+    for (size_t c = 0; c < P->cases.size(); ++c) {
+        char* base = (char*)P->d_cases + c * sizeof(LbmCaseDev);
+        if (wall_u)
+            FL_TRY_CUDA(ctx, cudaMemcpyAsync(base + offsetof(LbmCaseDev, wall_u), wall_u + 3 * c, 12,
+                                             cudaMemcpyHostToDevice, ctx->stream), "velocities");
+        if (inlet_u)
+            FL_TRY_CUDA(ctx, cudaMemcpyAsync(base + offsetof(LbmCaseDev, inlet_u), inlet_u + 3 * c, 12,
+                                             cudaMemcpyHostToDevice, ctx->stream), "velocities");
+    }
+    return FL_OK;
 }
 
 int fl_pool_set_options(fl_ctx* ctx, fl_pool* P, int use_graphs, int grid_mult) {

@@ -20,7 +20,8 @@ class LbmCase(ctypes.Structure):
 class PoolInfo(ctypes.Structure):
     _fields_ = [("num_bricks", ctypes.c_size_t), ("capacity", ctypes.c_size_t), ("num_cases", ctypes.c_int32),
                 ("max_level", ctypes.c_int32), ("bricks_per_level", ctypes.c_uint32 * 16),
-                ("fluid_lups_per_step", ctypes.c_uint64), ("population_bytes", ctypes.c_uint64)]
+                ("fluid_lups_per_step", ctypes.c_uint64), ("population_bytes", ctypes.c_uint64),
+                ("fluid_sites_per_level", ctypes.c_uint64 * 16)]
 
 
 WALL, MOVING, INLET, OUTLET, PERIODIC = 1, 2, 3, 4, 0
@@ -113,6 +114,21 @@ class Pool:
         out = np.empty((self.ncases, 4), np.float64)
         self.ctx.call("fl_pool_conservation", self.h, out.ctypes.data_as(P))
         return out
+
+    def profile_steps(self, n):
+        ms, la, st = ctypes.c_double(), ctypes.c_uint32(), ctypes.c_uint64()
+        self.ctx.call("fl_pool_profile_steps", self.h, n, ctypes.byref(ms), ctypes.byref(la), ctypes.byref(st))
+        return ms.value, la.value, st.value
+
+    def upload(self, f):
+        f = np.ascontiguousarray(f, np.float32)
+        self.ctx.call("fl_pool_upload", self.h, f.ctypes.data_as(P))
+
+    def set_velocities(self, wall_u=None, inlet_u=None):
+        w = None if wall_u is None else np.ascontiguousarray(wall_u, np.float32)
+        i = None if inlet_u is None else np.ascontiguousarray(inlet_u, np.float32)
+        self.ctx.call("fl_pool_set_velocities", self.h, w.ctypes.data_as(P) if w is not None else None,
+                      i.ctypes.data_as(P) if i is not None else None)
 
     def close(self):
         if self.h:

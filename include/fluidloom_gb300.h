@@ -57,6 +57,12 @@ int fl_device_free(fl_ctx* ctx, void* ptr);
 int fl_memcpy_h2d(fl_ctx* ctx, void* dst, const void* src, size_t bytes);   /* synchronous */
 int fl_memcpy_d2h(fl_ctx* ctx, void* dst, const void* src, size_t bytes);   /* synchronous */
 int fl_memset_d(fl_ctx* ctx, void* dst, int value, size_t bytes);           /* async */
+/* Page-locked host memory for asynchronous copies. */
+int fl_host_alloc_pinned(fl_ctx* ctx, size_t bytes, void** out);
+int fl_host_free_pinned(fl_ctx* ctx, void* ptr);
+/* CUDA-event timer on the context stream: start records, stop records, waits and returns ms. */
+int fl_ctx_timer_start(fl_ctx* ctx);
+int fl_ctx_timer_stop(fl_ctx* ctx, float* ms);
 
 /* ---- keys */
 /* hilbert::encode over n cells (include/fluidloom/core/hilbert/HilbertCodec.h:29;
@@ -175,6 +181,12 @@ int fl_adapt(fl_ctx* ctx, fl_mesh* mesh, const fl_adapt_config* cfg, float** fie
  * (point-location rule of src/adaptation/kernels/balance_enforce.cl:107-143).  subslots 1 or 4. */
 int fl_neighbour_rebuild(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, int subslots, uint32_t* nbr);
 
+/* Refine/coarsen flags from a sum of Gaussian blobs over the unit cube (the flag source of the
+ * regrid microbenchmark; the reference's flags come from DSL loops, benchmarks/lid_driven_cavity.fl:37-45).
+ * blobs: nblobs x {cx, cy, cz, 1/(2 sigma^2), amplitude} (host); flag 1 above hi (below max_level),
+ * -1 below lo, else 0.  Cell centres are (native + 0.5) / 2^level (single level-0 cell). */
+int fl_flags_from_blobs(fl_ctx* ctx, fl_mesh* mesh, const float* blobs, int nblobs, float lo, float hi, int max_level);
+
 /* ---- D3Q19 BGK collide-stream over an octree of 8^3-site bricks.
  * The reference emits empty lbm_* kernels (src/parsing/SimulationBuilder.cpp:394-400) behind
  * KernelNode (include/fluidloom/runtime/nodes/KernelNode.h:46-72) and stores fields through
@@ -207,6 +219,7 @@ typedef struct fl_pool_info {
     uint32_t bricks_per_level[16];
     uint64_t fluid_lups_per_step;   /* fluid site updates per level-0 step: sum of 2^level */
     uint64_t population_bytes;
+    uint64_t fluid_sites_per_level[16];
 } fl_pool_info;
 
 /* Build the cases: level-0 bricks, max_level rounds of sphere-band refinement, equilibrium start. */
@@ -226,6 +239,15 @@ int fl_pool_nbr(fl_ctx* ctx, fl_pool* pool, uint32_t* nbr);
 int fl_pool_flags(fl_ctx* ctx, fl_pool* pool, int32_t* flags, float* wmax);
 /* Per case: fluid mass and momentum (FP64, sites weighted by 8^-level) -> out[ncases][4] (host). */
 int fl_pool_conservation(fl_ctx* ctx, fl_pool* pool, double* out);
+/* Advance nsteps with a CUDA event pair around every collide-stream launch (no graphs); returns
+ * the summed kernel time, the launch count and the fluid sites those launches updated. */
+int fl_pool_profile_steps(fl_ctx* ctx, fl_pool* pool, int nsteps, double* kernel_ms, uint32_t* launches,
+                          uint64_t* fluid_sites);
+/* Replace the populations with a host array [19][n][512] (the layout fl_pool_download gives). */
+int fl_pool_upload(fl_ctx* ctx, fl_pool* pool, const float* f);
+/* Per-case moving-wall and inlet velocities ([ncases][3] host arrays, either may be NULL),
+ * copied on the stream and used from the next step on. */
+int fl_pool_set_velocities(fl_ctx* ctx, fl_pool* pool, const float* wall_u, const float* inlet_u);
 /* use_graphs: replay captured CUDA graphs per level-0 step; grid_mult: CTAs per SM (0 keeps). */
 int fl_pool_set_options(fl_ctx* ctx, fl_pool* pool, int use_graphs, int grid_mult);
 

@@ -426,7 +426,56 @@ void init_populations(Pool& P) {
 
 }  // namespace
 
+// exp(x) for x <= 0: Cody & Waite (1980) reduction x = n ln2 + r with ln2
+// split into a 16-bit head (0.693145751953125, so n*head is exact) and a tail,
+// Taylor series of e^r to r^7, exact scaling by 2^n.  Operation by operation,
+// as the CUDA flag kernel computes it.
+static float exp_neg(float x) {
+    if (x < -87.0f) return 0.0f;
+    float t = x * 1.44269504f;
+    t = t + 0.5f;
+    float n = std::floor(t);
+    float r = x - n * 0.693145752f;
+    r = r - n * 1.42860677e-06f;
+    float p = 1.0f / 5040.0f;
+    p = p * r; p = p + 1.0f / 720.0f;
+    p = p * r; p = p + 1.0f / 120.0f;
+    p = p * r; p = p + 1.0f / 24.0f;
+    p = p * r; p = p + 1.0f / 6.0f;
+    p = p * r; p = p + 0.5f;
+    p = p * r; p = p + 1.0f;
+    p = p * r; p = p + 1.0f;
+    return std::ldexp(p, (int)n);
+}
+
 extern "C" {
+
+// Flags from a sum of Gaussian blobs {cx, cy, cz, 1/(2 sigma^2), amplitude}
+// at cell centres (native + 0.5) / 2^level: 1 above hi (below max level),
+// -1 below lo.
+void or_blob_flags(const int32_t* x, const int32_t* y, const int32_t* z, const uint8_t* level, size_t n,
+                   const float* blobs, int nblobs, float lo, float hi, int max_level, int32_t* flags) {
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < (long long)n; ++i) {
+        int l = level[i];
+        float inv = 1.0f / (float)(1 << l);
+        float px = ((float)x[i] + 0.5f) * inv, py = ((float)y[i] + 0.5f) * inv, pz = ((float)z[i] + 0.5f) * inv;
+        float v = 0.0f;
+        for (int k = 0; k < nblobs; ++k) {
+            const float* B = blobs + 5 * k;
+            float dx = px - B[0], dy = py - B[1], dz = pz - B[2];
+            float d2 = dx * dx;
+            d2 = d2 + dy * dy;
+            d2 = d2 + dz * dz;
+            float e = exp_neg(-(d2 * B[3]));
+            v = v + B[4] * e;
+        }
+        int32_t f = 0;
+        if (v > hi && l < max_level) f = 1;
+        else if (v < lo) f = -1;
+        flags[i] = f;
+    }
+}
 
 // Build a pool: per case, level-0 bricks covering ext, then max_level rounds of
 // band-only refinement (adapt with FULL26 balance), then equilibrium

@@ -102,6 +102,9 @@ typedef struct or_lbm_case {
     float init_u[3];
 } or_lbm_case;
 
+void or_blob_flags(const int32_t* x, const int32_t* y, const int32_t* z, const uint8_t* level, size_t n,
+                   const float* blobs, int nblobs, float lo, float hi, int max_level, int32_t* flags);
+
 /* Opaque pool of cases (or_lbm.cpp). */
 void* or_pool_new(const or_lbm_case* cases, int ncases);
 void or_pool_free(void* h);

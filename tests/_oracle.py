@@ -85,6 +85,8 @@ def load():
         L.or_interp_trilinear.argtypes = [ctypes.POINTER(Mesh), ctypes.POINTER(Domain), P, ctypes.c_uint32,
                                           P, P, P, P, ctypes.c_size_t, P]
         L.or_restrict_groups.argtypes = [P, ctypes.c_uint32, P, ctypes.c_size_t, ctypes.c_int, P]
+        L.or_blob_flags.argtypes = [P, P, P, P, ctypes.c_size_t, P, ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                    ctypes.c_int, P]
         L.or_pool_new.restype = P
         L.or_pool_new.argtypes = [ctypes.POINTER(LbmCase), ctypes.c_int]
         L.or_pool_free.argtypes = [P]
@@ -291,3 +293,21 @@ class OraclePool:
             load().or_pool_free(self.h)
         except Exception:
             pass
+
+
+def gaussian_blobs(seed, n=64, sigma=(0.02, 0.1)):
+    """Seeded blob table {cx, cy, cz, 1/(2 sigma^2), amplitude} (the regrid microbenchmark's field)."""
+    rng = np.random.default_rng(seed)
+    c = rng.random((n, 3))
+    s = rng.uniform(sigma[0], sigma[1], n)
+    return np.concatenate([c, (1.0 / (2 * s * s))[:, None], np.ones((n, 1))], 1).astype(np.float32)
+
+
+def blob_flags(cols, blobs, lo, hi, max_level):
+    L = load()
+    n = len(cols["x"])
+    out = np.empty(n, np.int32)
+    keep = [np.ascontiguousarray(cols[k]) for k in ("x", "y", "z", "level")]
+    b = np.ascontiguousarray(blobs, np.float32)
+    L.or_blob_flags(*[ptr(a) for a in keep], n, ptr(b), len(b), lo, hi, max_level, ptr(out))
+    return out

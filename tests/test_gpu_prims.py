@@ -131,7 +131,8 @@ def test_apply_permutation(ctx):
     for dt in (np.uint8, np.float32, np.float64):
         src = rng.random(n).astype(dt) if dt != np.uint8 else rng.integers(0, 255, n).astype(np.uint8)
         ds, dd = D(ctx, src), D(ctx, np.zeros(n, dt))
-        ctx.call("fl_apply_permutation", ds.ptr, dd.ptr, np.dtype(dt).itemsize, n, D(ctx, perm).ptr)
+        dp = D(ctx, perm)  # keep every device buffer referenced until the call returns
+        ctx.call("fl_apply_permutation", ds.ptr, dd.ptr, np.dtype(dt).itemsize, n, dp.ptr)
         want = np.zeros(n, dt)
         O.load().or_apply_permutation(O.ptr(src), O.ptr(want), np.dtype(dt).itemsize, n, O.ptr(perm))
         np.testing.assert_array_equal(dd.to_host(), want)
@@ -149,12 +150,14 @@ def test_hash_build_query(ctx, n):
         keys[5] = keys[3]  # duplicate: the last occurrence wins
     vals = rng.integers(0, 2**31, n).astype(np.uint32)
     tk, tv = E(ctx, (cap,), np.uint64), E(ctx, (cap,), np.uint32)
-    ctx.call("fl_hash_build", tk.ptr, tv.ptr, ctypes.c_uint64(cap), D(ctx, keys).ptr if n else None,
-             D(ctx, vals).ptr if n else None, n)
+    dk = D(ctx, keys) if n else None  # keep every device buffer referenced until the call returns
+    dv = D(ctx, vals) if n else None
+    ctx.call("fl_hash_build", tk.ptr, tv.ptr, ctypes.c_uint64(cap), dk.ptr if n else None, dv.ptr if n else None, n)
     q = np.concatenate([keys, rng.integers(0, 2**63, 1000, dtype=np.uint64),
                         np.array([0xFFFFFFFFFFFFFFFF], np.uint64)])
     out = E(ctx, (len(q),), np.uint32)
-    ctx.call("fl_hash_query", tk.ptr, tv.ptr, ctypes.c_uint64(cap), D(ctx, q).ptr, out.ptr, len(q))
+    dq = D(ctx, q)
+    ctx.call("fl_hash_query", tk.ptr, tv.ptr, ctypes.c_uint64(cap), dq.ptr, out.ptr, len(q))
     otk, otv = np.empty(cap, np.uint64), np.empty(cap, np.uint32)
     L2 = O.load()
     assert L2.or_hash_build(O.ptr(keys), O.ptr(vals), n, cap, O.ptr(otk), O.ptr(otv)) == 0
