@@ -308,6 +308,63 @@ __global__ void k_gather(fl_items it, const uint32_t* __restrict__ perm, size_t 
     }
 }
 
+// SplitEngine::split pieces (split_cells.cl:15-132): predicate, then children
+// at the scanned block start, fields copied from the parent.
+__global__ void k_split_pred(fl_mesh_dev m, int max_level, uint32_t* __restrict__ pred) {
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride)
+        pred[i] = (m.flags[i] > 0 && m.state[i] == 0 && m.level[i] < max_level) ? 1u : 0u;
+}
+
+__global__ void k_split_children(fl_mesh_dev m, const uint32_t* __restrict__ pred, const uint32_t* __restrict__ off,
+                                 fl_mesh_out ch, uint32_t* __restrict__ p2c, const float* __restrict__ fin,
+                                 float* __restrict__ fout, uint32_t C) {
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
+        if (!pred[i]) {
+            if (p2c) p2c[i] = FL_INVALID_INDEX;
+            continue;
+        }
+        uint32_t start = off[i] * 8;
+        if (p2c) p2c[i] = start;
+        for (int c = 0; c < 8; ++c) {
+            uint32_t j = start + c;
+            ch.x[j] = (m.x[i] << 1) | (c & 1);
+            ch.y[j] = (m.y[i] << 1) | ((c >> 1) & 1);
+            ch.z[j] = (m.z[i] << 1) | ((c >> 2) & 1);
+            ch.level[j] = (uint8_t)(m.level[i] + 1);
+            ch.state[j] = m.state[i];
+            ch.material[j] = m.material[i];
+            ch.flags[j] = 0;
+            if (ch.case_id) ch.case_id[j] = m.case_id[i];
+            if (fin && fout)
+                for (uint32_t k = 0; k < C; ++k) fout[(size_t)j * C + k] = fin[(size_t)i * C + k];
+        }
+    }
+}
+
+// MergeEngine::merge pieces (merge_cells.cl:123-199): group ids by leader
+// order, parents from the first sibling, fields restricted in child order.
+__global__ void k_merge_parents(fl_mesh_dev m, const uint32_t* __restrict__ members, uint32_t G, fl_mesh_out par,
+                                const float* __restrict__ fin, float* __restrict__ fout, uint32_t C, int rule) {
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x; g < G; g += stride) {
+        uint32_t i = members[g * 8];
+        par.x[g] = m.x[i] >> 1; par.y[g] = m.y[i] >> 1; par.z[g] = m.z[i] >> 1;
+        par.level[g] = (uint8_t)(m.level[i] - 1);
+        par.state[g] = m.state[i];
+        par.material[g] = m.material[i];
+        par.flags[g] = 0;
+        if (par.case_id) par.case_id[g] = m.case_id[i];
+        if (fin && fout)
+            for (uint32_t k = 0; k < C; ++k) {
+                float s = 0.0f;
+                for (int q = 0; q < 8; ++q) s = __fadd_rn(s, fin[(size_t)members[g * 8 + q] * C + k]);
+                fout[(size_t)g * C + k] = rule == 1 ? s : __fmul_rn(s, 0.125f);
+            }
+    }
+}
+
 // Scratch carving helper.
 struct Carver {
     char* p;
@@ -676,6 +733,106 @@ int fl_adapt(fl_ctx* ctx, fl_mesh* mesh, const fl_adapt_config* cfg, float** fie
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "fl_adapt");
     if (stats) *stats = s;
     return (s.balance.converged || !cfg->enforce_2_1_balance) ? FL_OK : FL_E_BALANCE_NOT_CONVERGED;
+}
+
+int fl_split(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, const float* fields, uint32_t C,
+             fl_mesh* children, float* child_fields, uint32_t* parent_to_child, size_t* num_children) {
+    if (!ctx || !mesh || !cfg || !children || !num_children) return FL_E_INVALID_ARG;
+    *num_children = 0;
+    size_t n = mesh->num_cells;
+    if (n == 0) return FL_OK;
+    int rc = fl_scratch_reserve(ctx, 2 * fl_align256(n * 4) + fl_scan_scratch_bytes(n) + 512);
+    if (rc) return rc;
+    Carver cv{(char*)ctx->scratch};
+    uint32_t* pred = cv.take<uint32_t>(n);
+    uint32_t* off = cv.take<uint32_t>(n);
+    uint32_t* total = cv.take<uint32_t>(4);
+    void* ss = cv.p;
+    fl_mesh_dev md{mesh->x, mesh->y, mesh->z, mesh->level, mesh->state, mesh->flags, mesh->material, mesh->case_id, n};
+    unsigned nb = fl_blocks(n, kT, ctx->num_sms * 8);
+    k_split_pred<<<nb, kT, 0, ctx->stream>>>(md, cfg->max_refinement_level, pred);
+    FL_CHECK_LAUNCH(ctx, "k_split_pred");
+    rc = fl_scan_u32_with(ctx, pred, off, n, total, ss);
+    if (rc) return rc;
+    uint32_t h = 0;
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(&h, total, 4, cudaMemcpyDeviceToHost, ctx->stream), "split count");
+    rc = fl_collect_device_status(ctx, "fl_split");
+    if (rc) return rc;
+    size_t nc = (size_t)h * 8;
+    if (nc > children->capacity) {
+        *num_children = nc;
+        return fl_set_error(ctx, FL_E_CAPACITY, "fl_split: children capacity too small (count returned)");
+    }
+    fl_mesh_out o{children->x, children->y, children->z, children->level, children->state, children->flags,
+                  children->material, mesh->case_id ? children->case_id : nullptr};
+    k_split_children<<<nb, kT, 0, ctx->stream>>>(md, pred, off, o, parent_to_child, fields, child_fields, C);
+    FL_CHECK_LAUNCH(ctx, "k_split_children");
+    children->num_cells = nc;
+    *num_children = nc;
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "fl_split");
+    return FL_OK;
+}
+
+int fl_merge(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, const float* fields, uint32_t C,
+             fl_mesh* parents, float* parent_fields, uint32_t* merge_group_id, size_t* num_parents) {
+    if (!ctx || !mesh || !cfg || !parents || !num_parents) return FL_E_INVALID_ARG;
+    if (!fl_domain_config_valid(cfg)) return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_merge: bad key geometry");
+    *num_parents = 0;
+    size_t n = mesh->num_cells;
+    if (n == 0) return FL_OK;
+    uint64_t cap = fl_table_capacity(n);
+    int rc = fl_scratch_reserve(ctx, 256 + fl_align256(n * 8) + fl_align256(cap * 8) + 2 * fl_align256(cap * 4) +
+                                         4 * fl_align256(n * 4) + fl_align256(n * 4 + 64) + fl_scan_scratch_bytes(n) + 512);
+    if (rc) return rc;
+    Carver cv{(char*)ctx->scratch};
+    void* dcase = cv.take<char>(256);
+    uint64_t* keys = cv.take<uint64_t>(n);
+    uint64_t* tk = cv.take<uint64_t>(cap);
+    uint32_t* tv = cv.take<uint32_t>(cap);
+    uint32_t* win = cv.take<uint32_t>(cap);
+    uint32_t* leader = cv.take<uint32_t>(n);
+    uint32_t* gid = cv.take<uint32_t>(n);
+    uint32_t* group_of = merge_group_id ? merge_group_id : cv.take<uint32_t>(n);
+    uint32_t* members = cv.take<uint32_t>(n + 16);
+    uint32_t* total = cv.take<uint32_t>(4);
+    void* ss = cv.p;
+    fl_domain_dev dom = fl_domain_from_config(ctx, cfg, dcase);
+    dom.max_level = cfg->max_refinement_level > 0 ? cfg->max_refinement_level : dom.anchor_level;
+    fl_mesh_dev md{mesh->x, mesh->y, mesh->z, mesh->level, mesh->state, mesh->flags, mesh->material, mesh->case_id, n};
+    rc = fl_launch_cell_keys(ctx, mesh->x, mesh->y, mesh->z, mesh->level, mesh->case_id, dom.depth, dom.anchor_level,
+                             keys, n);
+    if (rc) return rc;
+    rc = fl_hash_build_with(ctx, tk, tv, cap, keys, nullptr, n, win);
+    if (rc) return rc;
+    unsigned nb = fl_blocks(n, kT, ctx->num_sms * 8);
+    int lg = fl_hash_lg(cap);
+    k_leaders<<<nb, kT, 0, ctx->stream>>>(md, dom, tk, tv, lg, cfg->min_refinement_level, 0, nullptr, leader);
+    FL_CHECK_LAUNCH(ctx, "k_leaders");
+    rc = fl_scan_u32_with(ctx, leader, gid, n, total, ss);
+    if (rc) return rc;
+    rc = fl_launch_fill_u32(ctx, group_of, FL_INVALID_INDEX, n);
+    if (rc) return rc;
+    k_members<<<nb, kT, 0, ctx->stream>>>(md, dom, tk, tv, lg, cfg->min_refinement_level, leader, gid, members, group_of);
+    FL_CHECK_LAUNCH(ctx, "k_members");
+    uint32_t G = 0;
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(&G, total, 4, cudaMemcpyDeviceToHost, ctx->stream), "merge count");
+    rc = fl_collect_device_status(ctx, "fl_merge");
+    if (rc) return rc;
+    if (G > parents->capacity) {
+        *num_parents = G;
+        return fl_set_error(ctx, FL_E_CAPACITY, "fl_merge: parents capacity too small (count returned)");
+    }
+    if (G) {
+        fl_mesh_out o{parents->x, parents->y, parents->z, parents->level, parents->state, parents->flags,
+                      parents->material, mesh->case_id ? parents->case_id : nullptr};
+        k_merge_parents<<<fl_blocks(G, kT, ctx->num_sms * 8), kT, 0, ctx->stream>>>(md, members, G, o, fields,
+                                                                                   parent_fields, C, cfg->averaging_rule);
+        FL_CHECK_LAUNCH(ctx, "k_merge_parents");
+    }
+    parents->num_cells = G;
+    *num_parents = G;
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "fl_merge");
+    return FL_OK;
 }
 
 }  // extern "C"

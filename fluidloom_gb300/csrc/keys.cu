@@ -158,6 +158,57 @@ int fl_cell_keys(fl_ctx* ctx, const int32_t* x, const int32_t* y, const int32_t*
     return fl_launch_cell_keys(ctx, x, y, z, level, case_id, depth, anchor_level, keys, n);
 }
 
+// Host restatement of the same codec for host-side callers (CellCoord-style use).
+static const uint8_t h_enc[12][8] = {
+    {8, 17, 27, 18, 47, 38, 28, 37},   {16, 71, 1, 62, 51, 52, 2, 61},
+    {0, 75, 95, 76, 9, 10, 86, 85},    {4, 77, 55, 78, 3, 66, 80, 65},
+    {50, 49, 45, 46, 67, 88, 68, 7},   {6, 57, 39, 72, 5, 58, 84, 83},
+    {12, 11, 29, 90, 79, 32, 30, 89},  {74, 91, 73, 40, 69, 92, 70, 15},
+    {14, 13, 81, 82, 63, 36, 24, 35},  {20, 31, 19, 56, 53, 54, 42, 41},
+    {26, 93, 43, 44, 25, 94, 64, 23},  {22, 87, 21, 60, 33, 48, 34, 59},
+};
+static const uint8_t h_dec[12][8] = {
+    {8, 17, 19, 26, 30, 39, 37, 44},   {16, 2, 6, 52, 53, 63, 59, 65},
+    {0, 12, 13, 73, 75, 87, 86, 90},   {86, 71, 69, 4, 0, 73, 75, 50},
+    {93, 49, 48, 68, 70, 42, 43, 7},   {75, 57, 61, 87, 86, 4, 0, 34},
+    {37, 95, 91, 9, 8, 26, 30, 76},    {43, 74, 72, 89, 93, 68, 70, 15},
+    {30, 82, 83, 39, 37, 9, 8, 60},    {59, 47, 46, 18, 16, 52, 53, 25},
+    {70, 28, 24, 42, 43, 89, 93, 23},  {53, 36, 38, 63, 59, 18, 16, 81},
+};
+
+uint64_t fl_hilbert_encode_host(int32_t x, int32_t y, int32_t z, uint8_t level) {
+    const uint32_t m = (1u << 21) - 1;
+    uint32_t ux = (uint32_t)x & m, uy = (uint32_t)y & m, uz = (uint32_t)z & m;
+    uint64_t h = 0;
+    unsigned s = 0;
+    for (int i = (int)level - 1; i >= 0; --i) {
+        unsigned q = (((uz >> i) & 1u) << 2) | (((uy >> i) & 1u) << 1) | ((ux >> i) & 1u);
+        unsigned v = h_enc[s][q];
+        h = (h << 3) | (v & 7u);
+        s = v >> 3;
+    }
+    unsigned shift = (unsigned)(uint8_t)(64 - level * 3);
+    if (shift < 64) { h <<= shift; h >>= shift; }
+    return h;
+}
+
+void fl_hilbert_decode_host(uint64_t key, uint8_t level, int32_t* x, int32_t* y, int32_t* z) {
+    if (level == 0) { *x = *y = *z = 0; return; }
+    uint64_t t = key << (64 - level * 3);
+    uint32_t ux = 0, uy = 0, uz = 0;
+    unsigned s = 0;
+    for (int l = 0; l < level; ++l) {
+        unsigned v = h_dec[s][(t >> 61) & 7u];
+        unsigned q = v & 7u;
+        s = v >> 3;
+        ux = (ux << 1) | (q & 1u);
+        uy = (uy << 1) | ((q >> 1) & 1u);
+        uz = (uz << 1) | ((q >> 2) & 1u);
+        t <<= 3;
+    }
+    *x = (int32_t)ux; *y = (int32_t)uy; *z = (int32_t)uz;
+}
+
 uint64_t fl_hilbert_get_parent(uint64_t key, uint8_t level) { return level == 0 ? FL_EMPTY_KEY : key >> 3; }
 
 uint64_t fl_hilbert_get_child(uint64_t key, uint8_t level, uint8_t quadrant) {

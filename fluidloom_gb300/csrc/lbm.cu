@@ -138,8 +138,8 @@ __device__ __forceinline__ size_t fidx(size_t cap, int q, size_t b, int s) { ret
 
 // Pull of population q for a site whose source leaves the brick through a
 // non-same-level face/edge/corner, or the domain (oracle: or_lbm.cpp pull()).
-__device__ float pull_slow(const StepArgs& a, const LbmCaseDev& c, uint32_t b, int q, int l, const int64_t* G,
-                           int s_local) {
+__device__ __noinline__ float pull_slow(const StepArgs& a, const LbmCaseDev& c, uint32_t b, int q, int l,
+                                        const int64_t* G, int s_local) {
     int64_t S[3] = {G[0] - CXq(q), G[1] - CYq(q), G[2] - CZq(q)};
     int64_t N[3];
     for (int ax = 0; ax < 3; ++ax) N[ax] = ((int64_t)c.ext[ax] * 8) << l;
@@ -174,8 +174,9 @@ __device__ float pull_slow(const StepArgs& a, const LbmCaseDev& c, uint32_t b, i
         }
         return v;
     }
-    int64_t Sw[3];
-    for (int ax = 0; ax < 3; ++ax) Sw[ax] = c.periodic[ax] ? ((S[ax] % N[ax]) + N[ax]) % N[ax] : S[ax];
+    int64_t Sw[3];  // the source is one site from G: wrapping is one add or subtract
+    for (int ax = 0; ax < 3; ++ax)
+        Sw[ax] = !c.periodic[ax] ? S[ax] : (S[ax] < 0 ? S[ax] + N[ax] : (S[ax] >= N[ax] ? S[ax] - N[ax] : S[ax]));
     if (solid_at(c, Sw[0], Sw[1], Sw[2], l)) return a.R[fidx(a.cap, OPPq(q), b, s_local)];
     int64_t Lc[3] = {S[0] - (int64_t)a.bx[b] * 8, S[1] - (int64_t)a.by[b] * 8, S[2] - (int64_t)a.bz[b] * 8};
     if (Lc[0] >= 0 && Lc[0] < 8 && Lc[1] >= 0 && Lc[1] < 8 && Lc[2] >= 0 && Lc[2] < 8)
@@ -225,93 +226,165 @@ __device__ float pull_slow(const StepArgs& a, const LbmCaseDev& c, uint32_t b, i
     return a.R[fidx(a.cap, OPPq(q), b, s_local)];
 }
 
-// One CTA per brick (persistent over the level's list), 256 threads, two
-// sites per thread.  The 27-entry table holds this brick (centre) and its
-// same-level neighbours; any other relation takes pull_slow.
-__global__ void __launch_bounds__(256, 3) k_collide_stream(StepArgs a) {
+// Could a site of brick b, or a source one site outside it, lie in the sphere?
+// Minimal-image distance on periodic axes; a margin of two sites.
+__device__ __forceinline__ int brick_near_sphere(const LbmCaseDev& c, int32_t bx, int32_t by, int32_t bz, int l) {
+    if (!c.has_sphere) return 0;
+    float inv = 1.0f / (float)(1 << l);
+    int32_t o[3] = {bx * 8, by * 8, bz * 8};
+    float dm = 0.0f;
+    for (int ax = 0; ax < 3; ++ax) {
+        float lo = (float)(o[ax] - 1) * inv, hi = (float)(o[ax] + 9) * inv;
+        float best = 3.0e38f;
+        for (int img = -1; img <= 1; ++img) {
+            if (img != 0 && !c.periodic[ax]) continue;
+            float cc = c.sc[ax] + (float)img * (float)(c.ext[ax] * 8);
+            float cl = cc < lo ? lo : (cc > hi ? hi : cc);
+            float d = cc - cl;
+            best = fminf(best, d * d);
+        }
+        dm += best;
+    }
+    float rr = c.sr + 2.0f * inv;
+    return dm <= rr * rr ? 1 : 0;
+}
+
+// Source of population q one site upstream of global site G, wrapped on
+// periodic axes (|offset| <= 1).
+__device__ __forceinline__ bool solid_source(const LbmCaseDev& c, int q, const int64_t* G, int l) {
+    int64_t S[3] = {G[0] - CXq(q), G[1] - CYq(q), G[2] - CZq(q)};
+    for (int ax = 0; ax < 3; ++ax) {
+        if (!c.periodic[ax]) continue;
+        int64_t N = ((int64_t)c.ext[ax] * 8) << l;
+        S[ax] = S[ax] < 0 ? S[ax] + N : (S[ax] >= N ? S[ax] - N : S[ax]);
+    }
+    return solid_at(c, S[0], S[1], S[2], l);
+}
+
+// One CTA per brick (persistent over the level's list), 128 threads; thread t
+// owns the x-quad x0 = 4(t & 1), y = (t >> 1) & 7, z = t >> 4.  For each
+// population the quad's upstream row is one 128-bit load from this brick or a
+// same-level neighbour; the x-shift comes from the partner lane (the other
+// half of the row) by shuffle, and only the quad at the brick's x face loads
+// one more value from the x-neighbour.  Bricks whose 18 face/edge neighbours
+// are all same-level and that cannot see the sphere take this path with no
+// per-site checks; others check each element and fall back to pull_slow for
+// sources across a level interface, outside the domain or in the sphere.
+template <bool GENERAL>
+__device__ __forceinline__ void gather_quad(const StepArgs& a, const LbmCaseDev& c, const uint32_t* s_nb, uint32_t b,
+                                            int l, int near, int x0, int y, int z, const int64_t* G0,
+                                            float (&f)[Q][4]) {
+    const int lane_odd = x0 != 0;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const int cx = CXq(q), cy = CYq(q), cz = CZq(q);
+        const int sy = y - cy, sz = z - cz;
+        const int dy = sy >> 3, dz = sz >> 3;
+        const int rowoff = (sy & 7) * 8 + (sz & 7) * 64;
+        const uint32_t erow = s_nb[(dz + 1) * 9 + (dy + 1) * 3 + 1];
+        const bool rowok = !GENERAL || erow != kSlow;
+        float4 A = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (rowok) A = __ldg((const float4*)(a.R + fidx(a.cap, q, erow, rowoff + x0)));
+        float v[4];
+        if (cx == 0) {
+            v[0] = A.x; v[1] = A.y; v[2] = A.z; v[3] = A.w;
+        } else if (cx == 1) {
+            float pw = __shfl_xor_sync(0xFFFFFFFFu, A.w, 1);
+            float h = pw;
+            if (!lane_odd) {  // x = -1: last column of the -x neighbour's row
+                uint32_t ex = s_nb[(dz + 1) * 9 + (dy + 1) * 3 + 0];
+                if (!GENERAL || ex != kSlow) h = __ldg(a.R + fidx(a.cap, q, ex, rowoff + 7));
+            }
+            v[0] = h; v[1] = A.x; v[2] = A.y; v[3] = A.z;
+        } else {
+            float px = __shfl_xor_sync(0xFFFFFFFFu, A.x, 1);
+            float h = px;
+            if (lane_odd) {  // x = 8: first column of the +x neighbour's row
+                uint32_t ex = s_nb[(dz + 1) * 9 + (dy + 1) * 3 + 2];
+                if (!GENERAL || ex != kSlow) h = __ldg(a.R + fidx(a.cap, q, ex, rowoff + 0));
+            }
+            v[0] = A.y; v[1] = A.z; v[2] = A.w; v[3] = h;
+        }
+        if (GENERAL) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int xi = x0 + i - cx;  // source x inside [-1, 8]
+                const int dx = xi >> 3;
+                const uint32_t e = (dx == 0) ? erow : s_nb[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)];
+                const int64_t G[3] = {G0[0] + x0 + i, G0[1] + y, G0[2] + z};
+                const int s_own = x0 + i + 8 * y + 64 * z;
+                if (e == kSlow) {
+                    v[i] = pull_slow(a, c, b, q, l, G, s_own);
+                } else if (near && solid_source(c, q, G, l)) {
+                    v[i] = a.R[fidx(a.cap, OPPq(q), b, s_own)];
+                }
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) f[q][i] = v[i];
+    }
+}
+
+__global__ void __launch_bounds__(128, 3) k_collide_stream(StepArgs a) {
     __shared__ uint32_t s_nb[27];
-    __shared__ int s_near;
+    __shared__ int s_flags;  // bit 0: general path, bit 1: near the sphere
     const int l = a.level;
+    const int t = threadIdx.x;
+    const int x0 = (t & 1) * 4, y = (t >> 1) & 7, z = t >> 4;
     for (uint32_t w = blockIdx.x; w < a.count; w += gridDim.x) {
         const uint32_t b = a.list[w];
         const uint16_t cs = a.bcase[b];
         const LbmCaseDev& c = a.cases[cs];
-        if (threadIdx.x < 27) {
-            int d = threadIdx.x;
+        if (t < 27) {
             uint32_t e = b;
-            if (d != 13) {
-                int k = d < 13 ? d : d - 1;
+            if (t != 13) {
+                int k = t < 13 ? t : t - 1;
                 uint32_t nb = a.nbr[((size_t)b * 26 + k) * 4];
                 e = (nb != FL_INVALID_INDEX && a.blevel[nb] == l) ? nb : kSlow;
             }
-            s_nb[d] = e;
+            s_nb[t] = e;
         }
-        if (threadIdx.x == 32) {
-            // could a site of this brick or a source one site outside it be solid?
-            int near = 0;
-            if (c.has_sphere) {
-                float inv = 1.0f / (float)(1 << l);
-                int32_t o[3] = {a.bx[b] * 8, a.by[b] * 8, a.bz[b] * 8};
-                float dm = 0.0f;
-                for (int ax = 0; ax < 3; ++ax) {
-                    float lo = (float)(o[ax] - 1) * inv, hi = (float)(o[ax] + 9) * inv;
-                    float cc = c.sc[ax];
-                    float cl = cc < lo ? lo : (cc > hi ? hi : cc);
-                    dm += (cc - cl) * (cc - cl);
-                    if (c.periodic[ax] && (o[ax] == 0 || o[ax] + 8 >= ((c.ext[ax] * 8) << l))) near = 1;
-                }
-                float rr = c.sr + 2.0f * inv;
-                if (dm <= rr * rr) near = 1;
-            }
-            s_near = near;
+        if (t == 32) s_flags = brick_near_sphere(c, a.bx[b], a.by[b], a.bz[b], l) ? 2 : 0;
+        __syncthreads();
+        if (t < 27) {
+            // corners (both |d| components... three non-zero) are never sources in D3Q19
+            int dxx = t % 3 - 1, dyy = (t / 3) % 3 - 1, dzz = t / 9 - 1;
+            bool corner = dxx != 0 && dyy != 0 && dzz != 0;
+            if (!corner && s_nb[t] == kSlow) atomicOr(&s_flags, 1);
         }
         __syncthreads();
+        const int flags = s_flags;
+        const int near = (flags >> 1) & 1;
+        const int64_t G0[3] = {(int64_t)a.bx[b] * 8, (int64_t)a.by[b] * 8, (int64_t)a.bz[b] * 8};
+        float f[Q][4];
+        if (flags == 0) gather_quad<false>(a, c, s_nb, b, l, 0, x0, y, z, G0, f);
+        else gather_quad<true>(a, c, s_nb, b, l, near, x0, y, z, G0, f);
         const float omega = c.omega[l];
-        const int near = s_near;
-        const int64_t o0 = (int64_t)a.bx[b] * 8, o1 = (int64_t)a.by[b] * 8, o2 = (int64_t)a.bz[b] * 8;
-        for (int s = threadIdx.x; s < 512; s += 256) {
-            const int i = s & 7, j = (s >> 3) & 7, kz = s >> 6;
-            const int64_t G[3] = {o0 + i, o1 + j, o2 + kz};
-            if (near && solid_at(c, G[0], G[1], G[2], l)) {
 #pragma unroll
-                for (int q = 0; q < Q; ++q) a.W[fidx(a.cap, q, b, s)] = Wq(q);
-                continue;
-            }
-            float f[Q];
-#pragma unroll
-            for (int q = 0; q < Q; ++q) {
-                const int sx = i - CXq(q), sy = j - CYq(q), sz = kz - CZq(q);
-                const int d = ((sz >> 3) + 1) * 9 + ((sy >> 3) + 1) * 3 + ((sx >> 3) + 1);
-                const uint32_t e = s_nb[d];
-                if (e != kSlow) {
-                    bool bb = false;
-                    if (near) {
-                        int64_t Sw[3] = {G[0] - CXq(q), G[1] - CYq(q), G[2] - CZq(q)};
-                        for (int ax = 0; ax < 3; ++ax) {
-                            int64_t Nn = ((int64_t)c.ext[ax] * 8) << l;
-                            if (c.periodic[ax]) Sw[ax] = ((Sw[ax] % Nn) + Nn) % Nn;
-                        }
-                        bb = solid_at(c, Sw[0], Sw[1], Sw[2], l);
-                    }
-                    f[q] = bb ? a.R[fidx(a.cap, OPPq(q), b, s)]
-                              : a.R[fidx(a.cap, q, e, (sx & 7) + 8 * (sy & 7) + 64 * (sz & 7))];
-                } else {
-                    f[q] = pull_slow(a, c, b, q, l, G, s);
-                }
-            }
+        for (int i = 0; i < 4; ++i) {
+            bool solid = near && solid_at(c, G0[0] + x0 + i, G0[1] + y, G0[2] + z, l);
             float rho, jx, jy, jz;
-            moments(f, rho, jx, jy, jz);
+            {
+                float g[Q];
+#pragma unroll
+                for (int q = 0; q < Q; ++q) g[q] = f[q][i];
+                moments(g, rho, jx, jy, jz);
+            }
             float inv = 1.0f / rho;
             float ux = jx * inv, uy = jy * inv, uz = jz * inv;
             float base = base_of(ux, uy, uz);
 #pragma unroll
-            for (int q = 0; q < Q; ++q) {
+            for (int q = 0; q < Q; ++q) {  // outputs overwrite the inputs in place
                 float fe = feq1(q, rho, ux, uy, uz, base);
-                float dd = fe - f[q];
+                float dd = fe - f[q][i];
                 dd = omega * dd;
-                a.W[fidx(a.cap, q, b, s)] = f[q] + dd;
+                f[q][i] = solid ? Wq(q) : f[q][i] + dd;
             }
         }
+        const int own = x0 + 8 * y + 64 * z;
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+            *(float4*)(a.W + fidx(a.cap, q, b, own)) = make_float4(f[q][0], f[q][1], f[q][2], f[q][3]);
         __syncthreads();
     }
 }
@@ -895,7 +968,7 @@ void launch_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm = nul
         a.cases = P->d_cases;
         a.dev_status = ctx->dev_status;
         unsigned grid = std::min<unsigned>(cnt, (unsigned)ctx->num_sms * P->grid_mult);
-        k_collide_stream<<<grid, 256, 0, ctx->stream>>>(a);
+        k_collide_stream<<<grid, 128, 0, ctx->stream>>>(a);
         if (tm) {
             cudaEventRecord(e1, ctx->stream);
             tm->ev.push_back(e0);

@@ -81,6 +81,9 @@ int fl_morton8_encode(fl_ctx* ctx, const int32_t* x, const int32_t* y, const int
  * case_id may be NULL. */
 int fl_cell_keys(fl_ctx* ctx, const int32_t* x, const int32_t* y, const int32_t* z, const uint8_t* level,
                  const uint16_t* case_id, int depth, int anchor_level, uint64_t* keys, size_t n);
+/* [host] hilbert::encode / decode for one cell (HilbertCodec.h:29,40). */
+uint64_t fl_hilbert_encode_host(int32_t x, int32_t y, int32_t z, uint8_t level);
+void fl_hilbert_decode_host(uint64_t key, uint8_t level, int32_t* x, int32_t* y, int32_t* z);
 /* [host] hilbert::getParent / getChild / isValid (HilbertCodec.h:49,59,68). */
 uint64_t fl_hilbert_get_parent(uint64_t key, uint8_t level);
 uint64_t fl_hilbert_get_child(uint64_t key, uint8_t level, uint8_t quadrant);
@@ -176,6 +179,20 @@ int fl_balance_enforce(fl_ctx* ctx, fl_mesh* mesh, const fl_adapt_config* cfg, f
  * the cell set changes capacity, as the reference releases and replaces its cl_mem handles. */
 int fl_adapt(fl_ctx* ctx, fl_mesh* mesh, const fl_adapt_config* cfg, float** fields, uint32_t C,
              fl_adapt_stats* stats);
+/* SplitEngine::split (include/fluidloom/adaptation/SplitEngine.h:51-59): children of every cell with
+ * flag > 0, FLUID state and level < max (split_cells.cl:31-33), in parent order, 8 per parent
+ * (child bit 0 = x, 1 = y, 2 = z); child fields (AoS, C per cell, may be NULL) copied from the parent;
+ * parent_to_child[i] = first child index or FL_INVALID (may be NULL).  FL_E_CAPACITY with the
+ * count in *num_children when children->capacity is too small.  Synchronizes. */
+int fl_split(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, const float* fields, uint32_t C,
+             fl_mesh* children, float* child_fields, uint32_t* parent_to_child, size_t* num_children);
+/* MergeEngine::merge (include/fluidloom/adaptation/MergeEngine.h:51-59): complete sibling octets
+ * with flag -1, FLUID, same level, above min level (merge_cells.cl:11-106), numbered in first-sibling
+ * order; parents (level - 1) with fields summed over children 0..7 in order, x0.125 for the arithmetic
+ * rule (FieldAveragingRules.h:31-52); merge_group_id[i] = group or FL_INVALID (may be NULL).
+ * Synchronizes. */
+int fl_merge(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, const float* fields, uint32_t C,
+             fl_mesh* parents, float* parent_fields, uint32_t* merge_group_id, size_t* num_parents);
 /* Neighbour table: nbr[(i*26 + k)*subslots + s] = leaf containing the probe point of direction k
  * (dz outer, dy, dx inner, centre skipped) at sub-slot s, FL_INVALID outside the domain
  * (point-location rule of src/adaptation/kernels/balance_enforce.cl:107-143).  subslots 1 or 4. */

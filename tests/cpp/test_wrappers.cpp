@@ -1,0 +1,118 @@
+// C++ host-side parity checks through include/fluidloom_gb300.hpp, in the
+// shape of the reference's gtest cases (tests/unit/adaptation/*Test.cpp,
+// tests/unit/hilbert/test_hilbert_codec.cpp).  Built and run by
+// tests/test_gpu_cpp.py; prints "ALL PASSED" and exits 0 on success.
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include "fluidloom_gb300.hpp"
+
+using namespace fluidloom;
+using namespace fluidloom::adaptation;
+
+static int failures = 0;
+#define EXPECT_EQ(a, b)                                                                          \
+    do {                                                                                         \
+        auto _a = (a);                                                                           \
+        auto _b = (b);                                                                           \
+        if (!(_a == _b)) {                                                                       \
+            std::printf("%s:%d EXPECT_EQ(%s, %s) failed\n", __FILE__, __LINE__, #a, #b);          \
+            ++failures;                                                                          \
+        }                                                                                        \
+    } while (0)
+#define EXPECT_TRUE(a) EXPECT_EQ(!!(a), true)
+
+int main() {
+    // test_hilbert_codec.cpp:33-58, 108-125
+    EXPECT_EQ(hilbert::encode(0, 0, 0, 1), 0ull);
+    std::vector<int> seen(8, 0);
+    for (int z = 0; z < 2; ++z)
+        for (int y = 0; y < 2; ++y)
+            for (int x = 0; x < 2; ++x) seen[hilbert::encode(x, y, z, 1)]++;
+    for (int i = 0; i < 8; ++i) EXPECT_EQ(seen[i], 1);
+    for (int lv = 1; lv <= 21; ++lv) {
+        int32_t x = (12345 * lv) & ((1 << lv) - 1), y = (777 * lv) & ((1 << lv) - 1), z = (31 * lv) & ((1 << lv) - 1);
+        int32_t a, b, c;
+        hilbert::decode(hilbert::encode(x, y, z, lv), lv, a, b, c);
+        EXPECT_EQ(a, x); EXPECT_EQ(b, y); EXPECT_EQ(c, z);
+        EXPECT_TRUE(hilbert::isValid(hilbert::encode(x, y, z, lv), lv));
+    }
+    Device dev(0);
+    AdaptationConfig cfg;
+    cfg.max_refinement_level = 8;
+    // SplitEngineTest.cpp:35-63
+    {
+        Mesh parents(dev, 1), children(dev, 8);
+        parents.upload({0}, {0}, {0}, {0}, {0}, {1}, {0});
+        SplitEngine se(dev, cfg);
+        EXPECT_EQ(se.split(parents, children), (size_t)8);
+        for (uint8_t l : children.read(children.raw().level)) EXPECT_EQ((int)l, 1);
+    }
+    // MergeEngineTest.cpp:35-71
+    {
+        Mesh kids(dev, 8), parents(dev, 1);
+        std::vector<int32_t> x(8), y(8), z(8);
+        for (int i = 0; i < 8; ++i) { x[i] = i & 1; y[i] = (i >> 1) & 1; z[i] = (i >> 2) & 1; }
+        kids.upload(x, y, z, std::vector<uint8_t>(8, 1), std::vector<uint8_t>(8, 0), std::vector<int32_t>(8, -1),
+                    std::vector<uint32_t>(8, 0));
+        MergeEngine me(dev, cfg);
+        EXPECT_EQ(me.merge(kids, parents), (size_t)1);
+        EXPECT_EQ((int)parents.read(parents.raw().level)[0], 0);
+        EXPECT_EQ(parents.read(parents.raw().x)[0], 0);
+    }
+    // BalanceEnforcerTest.cpp:37-93 (8-level anchors: x = {0, 128} -> native {0, 4})
+    {
+        Mesh m(dev, 2);
+        m.upload({0, 4}, {0, 0}, {0, 0}, {1, 3}, {0, 0}, {0, 0}, {0, 0});
+        AdaptationConfig c8 = cfg;
+        c8.anchor_level = 8;
+        BalanceEnforcer be(dev, c8);
+        BalanceResult r = be.enforce(m);
+        EXPECT_TRUE(r.converged);
+        EXPECT_TRUE(r.total_violations_detected > 0);
+        EXPECT_TRUE(r.total_cells_marked_for_balance > 0);
+        auto f = m.read(m.raw().flags);
+        EXPECT_EQ(f[0], 1);
+        EXPECT_EQ(f[1], 0);
+    }
+    // AdaptationIntegrationTest.cpp:62-128: split then merge through the engine
+    {
+        Mesh m(dev, 1024);
+        m.upload({0}, {0}, {0}, {0}, {0}, {1}, {0});
+        AdaptationEngine eng(dev, cfg);
+        eng.adapt(m);
+        EXPECT_EQ(m.size(), (size_t)8);
+        std::vector<int32_t> fl(8, -1);
+        check(dev.get(), fl_memcpy_h2d(dev.get(), m.raw().flags, fl.data(), 32), "flags");
+        eng.adapt(m);
+        EXPECT_EQ(m.size(), (size_t)1);
+        EXPECT_EQ((int)m.read(m.raw().level)[0], 0);
+    }
+    // a pool step through the runtime nodes
+    {
+        fl_lbm_case c{};
+        c.ext[0] = c.ext[1] = c.ext[2] = 2;
+        int bc[6] = {1, 1, 1, 1, 1, 2};
+        for (int k = 0; k < 6; ++k) c.bc[k] = bc[k];
+        c.wall_u[0] = 0.05f;
+        c.tau0 = 0.56f;
+        c.max_level = 1;
+        c.refine_frac = 0.5f;
+        c.coarsen_frac = 0.1f;
+        runtime::BrickPool pool(dev, {c});
+        runtime::LbmStepNode step(pool, 4);
+        runtime::AdaptMeshNode adapt(pool);
+        step.execute();
+        adapt.execute();
+        step.execute();
+        dev.finish();
+        EXPECT_TRUE(pool.info().num_bricks >= 8);
+    }
+    if (failures) {
+        std::printf("%d FAILURES\n", failures);
+        return 1;
+    }
+    std::printf("ALL PASSED\n");
+    return 0;
+}
