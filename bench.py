@@ -335,6 +335,8 @@ def run_gpu(args):
                 "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": workload_config({"bricks": int(bricks0), "fluid_lups_per_step": int(lups0),
+                                           "bricks_per_level": [int(info.bricks_per_level[l]) for l in range(4)],
+                                           "fluid_sites_per_level": [int(info.fluid_sites_per_level[l]) for l in range(4)],
                                            "parallelism": "replicas" if ws > 1 else "single"}),
                 "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h)},
