@@ -198,6 +198,25 @@ int fl_merge(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, const
  * (point-location rule of src/adaptation/kernels/balance_enforce.cl:107-143).  subslots 1 or 4. */
 int fl_neighbour_rebuild(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, int subslots, uint32_t* nbr);
 
+/* ---- same-GPU ghost pack / unpack, interpolation, restriction (fields AoS, C floats per cell) */
+/* pack_fields / unpack_fields (kernels/halo_pack.cl:3-45): float field <-> byte buffer at a byte offset. */
+int fl_pack_fields(fl_ctx* ctx, const float* field, void* packed, size_t num_cells, size_t field_offset_bytes);
+int fl_unpack_fields(fl_ctx* ctx, const void* packed, float* field, size_t num_cells, size_t field_offset_bytes);
+/* pack_halo direct copy (kernels/halo/pack.cl:8-52): pack[k*C + c] = field[cell_indices[k]*C + c]. */
+int fl_pack_halo(fl_ctx* ctx, const float* field, uint32_t C, const uint32_t* cell_indices, size_t n, float* pack);
+/* unpack_halo with pre-averaged values (kernels/halo/unpack.cl, interpolate_average.cl:12-32). */
+int fl_unpack_halo(fl_ctx* ctx, const float* pack, uint32_t C, const uint32_t* cell_indices, size_t n, float* field);
+/* trilinear_interpolate (kernels/halo/interpolate_trilinear.cl:12-56, default weights
+ * InterpolationParams.h:34-43) for nq fine cells (native coords + level): the 8 cells at the coarser
+ * level around fine / 2, 0.125 each, missing ones contribute nothing.  Single-case meshes, C <= 32. */
+int fl_interp_trilinear(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, const float* field, uint32_t C,
+                        const int32_t* fx, const int32_t* fy, const int32_t* fz, const uint8_t* flevel, size_t nq,
+                        float* out);
+/* Restriction of sibling groups members[g][8] (merge_fields, merge_cells.cl:123-159): children 0..7
+ * summed in order, x0.125 for rule 0 (arithmetic), unscaled for rule 1 (volume weighted). */
+int fl_restrict_groups(fl_ctx* ctx, const float* field, uint32_t C, const uint32_t* members, size_t ngroups, int rule,
+                       float* out);
+
 /* Refine/coarsen flags from a sum of Gaussian blobs over the unit cube (the flag source of the
  * regrid microbenchmark; the reference's flags come from DSL loops, benchmarks/lid_driven_cavity.fl:37-45).
  * blobs: nblobs x {cx, cy, cz, 1/(2 sigma^2), amplitude} (host); flag 1 above hi (below max_level),
