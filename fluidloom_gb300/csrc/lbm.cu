@@ -270,10 +270,15 @@ __device__ __forceinline__ bool solid_source(const LbmCaseDev& c, int q, const i
 // are all same-level and that cannot see the sphere take this path with no
 // per-site checks; others check each element and fall back to pull_slow for
 // sources across a level interface, outside the domain or in the sphere.
+__device__ __forceinline__ int solid_bit(const uint32_t* s_solid, int x, int y, int z) {
+    int i = (x + 1) + 10 * (y + 1) + 100 * (z + 1);
+    return (s_solid[i >> 5] >> (i & 31)) & 1;
+}
+
 template <bool GENERAL>
 __device__ __forceinline__ void gather_quad(const StepArgs& a, const LbmCaseDev& c, const uint32_t* s_nb, uint32_t b,
                                             int l, int near, int x0, int y, int z, const int64_t* G0,
-                                            float (&f)[Q][4]) {
+                                            const uint32_t* s_solid, float (&f)[Q][4]) {
     const int lane_odd = x0 != 0;
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -315,7 +320,7 @@ __device__ __forceinline__ void gather_quad(const StepArgs& a, const LbmCaseDev&
                 const int s_own = x0 + i + 8 * y + 64 * z;
                 if (e == kSlow) {
                     v[i] = pull_slow(a, c, b, q, l, G, s_own);
-                } else if (near && solid_source(c, q, G, l)) {
+                } else if (near && solid_bit(s_solid, xi, sy, sz)) {
                     v[i] = a.R[fidx(a.cap, OPPq(q), b, s_own)];
                 }
             }
@@ -325,67 +330,120 @@ __device__ __forceinline__ void gather_quad(const StepArgs& a, const LbmCaseDev&
     }
 }
 
-__global__ void __launch_bounds__(128, 3) k_collide_stream(StepArgs a) {
+// Collision of the gathered x-quad and the 128-bit stores (shared by both kernels).
+__device__ __forceinline__ void collide_store(const StepArgs& a, const LbmCaseDev& c, uint32_t b, int l, int x0,
+                                              int y, int z, const uint32_t* s_solid, int near, float (&f)[Q][4]) {
+    const float omega = c.omega[l];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        bool solid = near && solid_bit(s_solid, x0 + i, y, z);
+        float rho, jx, jy, jz;
+        {
+            float g[Q];
+#pragma unroll
+            for (int q = 0; q < Q; ++q) g[q] = f[q][i];
+            moments(g, rho, jx, jy, jz);
+        }
+        float inv = 1.0f / rho;
+        float ux = jx * inv, uy = jy * inv, uz = jz * inv;
+        float base = base_of(ux, uy, uz);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {  // outputs overwrite the inputs in place
+            float fe = feq1(q, rho, ux, uy, uz, base);
+            float dd = fe - f[q][i];
+            dd = omega * dd;
+            f[q][i] = solid ? Wq(q) : f[q][i] + dd;
+        }
+    }
+    const int own = x0 + 8 * y + 64 * z;
+#pragma unroll
+    for (int q = 0; q < Q; ++q)
+        *(float4*)(a.W + fidx(a.cap, q, b, own)) = make_float4(f[q][0], f[q][1], f[q][2], f[q][3]);
+}
+
+// Interior bricks: all 18 face/edge neighbours at this level, no sphere in
+// reach.  The 27-entry neighbour row comes precomputed (k_brick_table).
+__global__ void __launch_bounds__(128, 4) k_collide_fast(StepArgs a, const uint32_t* __restrict__ nb27) {
     __shared__ uint32_t s_nb[27];
-    __shared__ int s_flags;  // bit 0: general path, bit 1: near the sphere
     const int l = a.level;
     const int t = threadIdx.x;
     const int x0 = (t & 1) * 4, y = (t >> 1) & 7, z = t >> 4;
     for (uint32_t w = blockIdx.x; w < a.count; w += gridDim.x) {
         const uint32_t b = a.list[w];
-        const uint16_t cs = a.bcase[b];
-        const LbmCaseDev& c = a.cases[cs];
-        if (t < 27) {
-            uint32_t e = b;
-            if (t != 13) {
-                int k = t < 13 ? t : t - 1;
-                uint32_t nb = a.nbr[((size_t)b * 26 + k) * 4];
-                e = (nb != FL_INVALID_INDEX && a.blevel[nb] == l) ? nb : kSlow;
-            }
-            s_nb[t] = e;
-        }
-        if (t == 32) s_flags = brick_near_sphere(c, a.bx[b], a.by[b], a.bz[b], l) ? 2 : 0;
+        if (t < 27) s_nb[t] = nb27[(size_t)b * 28 + t];
         __syncthreads();
-        if (t < 27) {
-            // corners (both |d| components... three non-zero) are never sources in D3Q19
-            int dxx = t % 3 - 1, dyy = (t / 3) % 3 - 1, dzz = t / 9 - 1;
-            bool corner = dxx != 0 && dyy != 0 && dzz != 0;
-            if (!corner && s_nb[t] == kSlow) atomicOr(&s_flags, 1);
-        }
-        __syncthreads();
-        const int flags = s_flags;
-        const int near = (flags >> 1) & 1;
-        const int64_t G0[3] = {(int64_t)a.bx[b] * 8, (int64_t)a.by[b] * 8, (int64_t)a.bz[b] * 8};
+        const LbmCaseDev& c = a.cases[a.bcase[b]];
         float f[Q][4];
-        if (flags == 0) gather_quad<false>(a, c, s_nb, b, l, 0, x0, y, z, G0, f);
-        else gather_quad<true>(a, c, s_nb, b, l, near, x0, y, z, G0, f);
-        const float omega = c.omega[l];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            bool solid = near && solid_at(c, G0[0] + x0 + i, G0[1] + y, G0[2] + z, l);
-            float rho, jx, jy, jz;
-            {
-                float g[Q];
-#pragma unroll
-                for (int q = 0; q < Q; ++q) g[q] = f[q][i];
-                moments(g, rho, jx, jy, jz);
-            }
-            float inv = 1.0f / rho;
-            float ux = jx * inv, uy = jy * inv, uz = jz * inv;
-            float base = base_of(ux, uy, uz);
-#pragma unroll
-            for (int q = 0; q < Q; ++q) {  // outputs overwrite the inputs in place
-                float fe = feq1(q, rho, ux, uy, uz, base);
-                float dd = fe - f[q][i];
-                dd = omega * dd;
-                f[q][i] = solid ? Wq(q) : f[q][i] + dd;
-            }
-        }
-        const int own = x0 + 8 * y + 64 * z;
-#pragma unroll
-        for (int q = 0; q < Q; ++q)
-            *(float4*)(a.W + fidx(a.cap, q, b, own)) = make_float4(f[q][0], f[q][1], f[q][2], f[q][3]);
+        gather_quad<false>(a, c, s_nb, b, l, 0, x0, y, z, nullptr, nullptr, f);
+        collide_store(a, c, b, l, x0, y, z, nullptr, 0, f);
         __syncthreads();
+    }
+}
+
+// Bricks at a level interface, a domain boundary or near the sphere: per
+// element checks, a shared 10^3 solid mask (the brick and its one-site halo)
+// and pull_slow for sources across an interface or outside the domain.
+__global__ void __launch_bounds__(128, 3) k_collide_general(StepArgs a, const uint32_t* __restrict__ nb27) {
+    __shared__ uint32_t s_nb[27];
+    __shared__ uint32_t s_solid[32];
+    __shared__ int s_near;
+    const int l = a.level;
+    const int t = threadIdx.x;
+    const int x0 = (t & 1) * 4, y = (t >> 1) & 7, z = t >> 4;
+    for (uint32_t w = blockIdx.x; w < a.count; w += gridDim.x) {
+        const uint32_t b = a.list[w];
+        const LbmCaseDev& c = a.cases[a.bcase[b]];
+        if (t < 27) s_nb[t] = nb27[(size_t)b * 28 + t];
+        if (t < 32) s_solid[t] = 0u;
+        if (t == 32) s_near = brick_near_sphere(c, a.bx[b], a.by[b], a.bz[b], l);
+        __syncthreads();
+        const int near = s_near;
+        const int64_t G0[3] = {(int64_t)a.bx[b] * 8, (int64_t)a.by[b] * 8, (int64_t)a.bz[b] * 8};
+        if (near) {
+            for (int i = t; i < 1000; i += 128) {
+                int64_t G[3] = {G0[0] + i % 10 - 1, G0[1] + (i / 10) % 10 - 1, G0[2] + i / 100 - 1};
+                for (int ax = 0; ax < 3; ++ax) {
+                    if (!c.periodic[ax]) continue;
+                    int64_t N = ((int64_t)c.ext[ax] * 8) << l;
+                    G[ax] = G[ax] < 0 ? G[ax] + N : (G[ax] >= N ? G[ax] - N : G[ax]);
+                }
+                if (solid_at(c, G[0], G[1], G[2], l)) atomicOr(&s_solid[i >> 5], 1u << (i & 31));
+            }
+            __syncthreads();
+        }
+        float f[Q][4];
+        gather_quad<true>(a, c, s_nb, b, l, near, x0, y, z, G0, s_solid, f);
+        collide_store(a, c, b, l, x0, y, z, s_solid, near, f);
+        __syncthreads();
+    }
+}
+
+// Per brick: the 27-entry same-level neighbour row (centre = the brick,
+// kSlow where the neighbour is missing or at another level) and the class
+// (1 = needs the general kernel).
+__global__ void k_brick_table(size_t n, const uint32_t* __restrict__ nbr, const uint8_t* __restrict__ blevel,
+                              const int32_t* __restrict__ bx, const int32_t* __restrict__ by,
+                              const int32_t* __restrict__ bz, const uint16_t* __restrict__ bcase,
+                              const LbmCaseDev* __restrict__ cases, uint32_t* __restrict__ nb27,
+                              uint8_t* __restrict__ bclass) {
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x; b < n; b += stride) {
+        int l = blevel[b];
+        int general = brick_near_sphere(cases[bcase[b]], bx[b], by[b], bz[b], l);
+        for (int d = 0; d < 27; ++d) {
+            uint32_t e = (uint32_t)b;
+            if (d != 13) {
+                int k = d < 13 ? d : d - 1;
+                uint32_t nb = nbr[(b * 26 + k) * 4];
+                e = (nb != FL_INVALID_INDEX && blevel[nb] == l) ? nb : kSlow;
+                int dx = d % 3 - 1, dy = (d / 3) % 3 - 1, dz = d / 9 - 1;
+                bool corner = dx != 0 && dy != 0 && dz != 0;
+                if (!corner && e == kSlow) general = 1;
+            }
+            nb27[b * 28 + d] = e;
+        }
+        nb27[b * 28 + 27] = 0;
+        bclass[b] = (uint8_t)general;
     }
 }
 
@@ -593,16 +651,26 @@ __global__ void __launch_bounds__(512) k_brick_sums(PoolView p, size_t n, double
     }
 }
 
-// Per case, sum the brick partials in brick order (cases occupy contiguous
-// brick ranges because bricks are sorted by case then key).
-__global__ void k_case_sums(const double* __restrict__ part, const uint32_t* __restrict__ case_begin, int ncases,
-                            double* __restrict__ out) {
-    int cs = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cs >= ncases) return;
-    double acc[4] = {0, 0, 0, 0};
-    for (uint32_t b = case_begin[cs]; b < case_begin[cs + 1]; ++b)
-        for (int k = 0; k < 4; ++k) acc[k] += part[(size_t)b * 4 + k];
-    for (int k = 0; k < 4; ++k) out[cs * 4 + k] = acc[k];
+// Per case (one CTA each): the case's brick partials (a contiguous range,
+// bricks being sorted by case then key) summed in a fixed order — thread t
+// takes bricks t, t+256, ..., then a fixed tree across threads.
+__global__ void __launch_bounds__(256) k_case_sums(const double* __restrict__ part, const uint32_t* __restrict__ case_begin,
+                                                   int ncases, double* __restrict__ out) {
+    __shared__ double red[4][256];
+    for (int cs = blockIdx.x; cs < ncases; cs += gridDim.x) {
+        double acc[4] = {0, 0, 0, 0};
+        for (uint32_t b = case_begin[cs] + threadIdx.x; b < case_begin[cs + 1]; b += 256)
+            for (int k = 0; k < 4; ++k) acc[k] += part[(size_t)b * 4 + k];
+        for (int k = 0; k < 4; ++k) red[k][threadIdx.x] = acc[k];
+        __syncthreads();
+        for (int o = 128; o > 0; o >>= 1) {
+            if (threadIdx.x < o)
+                for (int k = 0; k < 4; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + o];
+            __syncthreads();
+        }
+        if (threadIdx.x < 4) out[cs * 4 + threadIdx.x] = red[threadIdx.x][0];
+        __syncthreads();
+    }
 }
 
 // exp(x) for x <= 0 from the mathematics: x = n ln2 + r with |r| <= ln2/2
@@ -689,6 +757,11 @@ struct fl_pool {
     int maxL = 0;
     uint32_t* list = nullptr;
     std::vector<uint32_t> lvl_off;  // maxL + 2 entries
+    // per level: [fast offset, fast count, general offset, general count] into `list`
+    std::vector<uint32_t> lvl_fast_off, lvl_fast_cnt, lvl_gen_off, lvl_gen_cnt;
+    uint64_t fluid_fast[16] = {0}, fluid_gen[16] = {0};
+    uint32_t* nb27 = nullptr;
+    uint8_t* bclass = nullptr;
     std::vector<uint32_t> case_begin;
     uint32_t* d_case_begin = nullptr;
     float* wmax = nullptr;
@@ -702,7 +775,7 @@ struct fl_pool {
     cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one level-0 step, per level-0 parity
     void* adapt_scratch = nullptr;
     size_t adapt_scratch_bytes = 0;
-    int grid_mult = 3;
+    int grid_mult = 4;
 };
 
 namespace {
@@ -763,14 +836,17 @@ int alloc_brick_arrays(fl_ctx* ctx, fl_pool* P, size_t cap) {
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->wmax, cap * 4, ctx->stream), "pool wmax");
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->part, cap * 32, ctx->stream), "pool partials");
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->fluid, cap * 4, ctx->stream), "pool fluid");
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->nb27, cap * 28 * 4, ctx->stream), "pool nb27");
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->bclass, cap, ctx->stream), "pool classes");
     return FL_OK;
 }
 
 void free_brick_arrays(fl_ctx* ctx, fl_pool* P) {
-    void* ps[5] = {P->nbr, P->list, P->wmax, P->part, P->fluid};
+    void* ps[7] = {P->nbr, P->list, P->wmax, P->part, P->fluid, P->nb27, P->bclass};
     for (void* p : ps)
         if (p) cudaFreeAsync(p, ctx->stream);
     P->nbr = nullptr; P->list = nullptr; P->wmax = nullptr; P->part = nullptr; P->fluid = nullptr;
+    P->nb27 = nullptr; P->bclass = nullptr;
 }
 
 void drop_graph(fl_pool* P) {
@@ -802,9 +878,13 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
                    P->mesh.case_id, n};
     rc = fl_neighbours_with(ctx, md, dom, tk, tv, cap, 4, P->nbr);
     if (rc) return rc;
-    // host-side lists (levels and case ids are small: one byte + two bytes per brick)
-    std::vector<uint8_t> lv(n);
+    k_brick_table<<<fl_blocks(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(
+        n, P->nbr, P->mesh.level, P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.case_id, P->d_cases, P->nb27, P->bclass);
+    FL_CHECK_LAUNCH(ctx, "k_brick_table");
+    // host-side lists (levels, classes and case ids are small: four bytes per brick)
+    std::vector<uint8_t> lv(n), cl(n);
     std::vector<uint16_t> cs(n);
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(cl.data(), P->bclass, n, cudaMemcpyDeviceToHost, ctx->stream), "classes");
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(lv.data(), P->mesh.level, n, cudaMemcpyDeviceToHost, ctx->stream), "levels");
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(cs.data(), P->mesh.case_id, n * 2, cudaMemcpyDeviceToHost, ctx->stream), "cases");
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "topology sync");
@@ -814,8 +894,16 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
         P->lvl_off[lv[i] + 1]++;
     }
     for (int l = 0; l <= P->maxL; ++l) P->lvl_off[l + 1] += P->lvl_off[l];
-    std::vector<uint32_t> list(n), fill(P->lvl_off.begin(), P->lvl_off.end() - 1);
-    for (size_t i = 0; i < n; ++i) list[fill[lv[i]]++] = (uint32_t)i;
+    // within a level: interior bricks first, then the general ones
+    P->lvl_fast_off.assign(P->maxL + 1, 0); P->lvl_fast_cnt.assign(P->maxL + 1, 0);
+    P->lvl_gen_off.assign(P->maxL + 1, 0); P->lvl_gen_cnt.assign(P->maxL + 1, 0);
+    for (size_t i = 0; i < n; ++i) (cl[i] ? P->lvl_gen_cnt : P->lvl_fast_cnt)[lv[i]]++;
+    for (int l = 0; l <= P->maxL; ++l) {
+        P->lvl_fast_off[l] = P->lvl_off[l];
+        P->lvl_gen_off[l] = P->lvl_off[l] + P->lvl_fast_cnt[l];
+    }
+    std::vector<uint32_t> list(n), ff(P->lvl_fast_off), gf(P->lvl_gen_off);
+    for (size_t i = 0; i < n; ++i) list[cl[i] ? gf[lv[i]]++ : ff[lv[i]]++] = (uint32_t)i;
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->list, list.data(), n * 4, cudaMemcpyHostToDevice, ctx->stream), "list");
     P->case_begin.assign(P->cases.size() + 1, 0);
     for (size_t i = 0; i < n; ++i) P->case_begin[cs[i] + 1]++;
@@ -829,10 +917,11 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(fl.data(), P->fluid, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "fluid");
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "topology sync");
     P->lups = 0;
-    for (int l = 0; l < 16; ++l) P->fluid_per_level[l] = 0;
+    for (int l = 0; l < 16; ++l) P->fluid_per_level[l] = P->fluid_fast[l] = P->fluid_gen[l] = 0;
     for (size_t i = 0; i < n; ++i) {
         P->lups += (uint64_t)fl[i] << lv[i];
         P->fluid_per_level[lv[i]] += fl[i];
+        (cl[i] ? P->fluid_gen : P->fluid_fast)[lv[i]] += fl[i];
     }
     drop_graph(P);
     return fl_collect_device_status(ctx, "pool topology");
@@ -941,39 +1030,48 @@ int pool_regrid(fl_ctx* ctx, fl_pool* P, int use_vorticity, fl_adapt_stats* st) 
 struct LaunchTimer {
     std::vector<cudaEvent_t> ev;  // start/stop pairs
     std::vector<uint64_t> sites;  // fluid sites processed by each launch
+    std::vector<int> kind;        // 0 interior kernel, 1 general kernel
 };
 
 void launch_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm = nullptr) {
-    uint32_t off = P->lvl_off[l], cnt = P->lvl_off[l + 1] - P->lvl_off[l];
-    if (cnt) {
+    StepArgs a;
+    a.level = l;
+    a.sub = sub;
+    a.R = P->f[P->parity[l]];
+    a.W = P->f[1 - P->parity[l]];
+    a.Cold = l > 0 ? P->f[1 - P->parity[l - 1]] : nullptr;
+    a.Cnew = l > 0 ? P->f[P->parity[l - 1]] : nullptr;
+    a.Fine = l < 15 ? P->f[P->parity[l + 1]] : nullptr;
+    a.cap = P->cap;
+    a.bx = P->mesh.x; a.by = P->mesh.y; a.bz = P->mesh.z; a.blevel = P->mesh.level; a.bcase = P->mesh.case_id;
+    a.nbr = P->nbr;
+    a.cases = P->d_cases;
+    a.dev_status = ctx->dev_status;
+    for (int kind = 0; kind < 2; ++kind) {
+        uint32_t off = kind ? P->lvl_gen_off[l] : P->lvl_fast_off[l];
+        uint32_t cnt = kind ? P->lvl_gen_cnt[l] : P->lvl_fast_cnt[l];
+        if (!cnt) continue;
         cudaEvent_t e0 = nullptr, e1 = nullptr;
         if (tm) {
             cudaEventCreate(&e0);
             cudaEventCreate(&e1);
             cudaEventRecord(e0, ctx->stream);
         }
-        StepArgs a;
         a.list = P->list + off;
         a.count = cnt;
-        a.level = l;
-        a.sub = sub;
-        a.R = P->f[P->parity[l]];
-        a.W = P->f[1 - P->parity[l]];
-        a.Cold = l > 0 ? P->f[1 - P->parity[l - 1]] : nullptr;
-        a.Cnew = l > 0 ? P->f[P->parity[l - 1]] : nullptr;
-        a.Fine = l < 15 ? P->f[P->parity[l + 1]] : nullptr;
-        a.cap = P->cap;
-        a.bx = P->mesh.x; a.by = P->mesh.y; a.bz = P->mesh.z; a.blevel = P->mesh.level; a.bcase = P->mesh.case_id;
-        a.nbr = P->nbr;
-        a.cases = P->d_cases;
-        a.dev_status = ctx->dev_status;
-        unsigned grid = std::min<unsigned>(cnt, (unsigned)ctx->num_sms * P->grid_mult);
-        k_collide_stream<<<grid, 128, 0, ctx->stream>>>(a);
+        if (kind == 0) {
+            unsigned grid = std::min<unsigned>(cnt, (unsigned)ctx->num_sms * P->grid_mult);
+            k_collide_fast<<<grid, 128, 0, ctx->stream>>>(a, P->nb27);
+        } else {
+            unsigned grid = std::min<unsigned>(cnt, (unsigned)ctx->num_sms * 3);
+            k_collide_general<<<grid, 128, 0, ctx->stream>>>(a, P->nb27);
+        }
         if (tm) {
             cudaEventRecord(e1, ctx->stream);
             tm->ev.push_back(e0);
             tm->ev.push_back(e1);
-            tm->sites.push_back(P->fluid_per_level[l]);
+            tm->sites.push_back(kind ? P->fluid_gen[l] : P->fluid_fast[l]);
+            tm->kind.push_back(kind);
         }
     }
     P->parity[l] ^= 1;
@@ -1188,7 +1286,7 @@ int fl_pool_conservation(fl_ctx* ctx, fl_pool* P, double* out) {
     k_brick_sums<<<fl_blocks(n, 1, ctx->num_sms * 8), 512, 0, ctx->stream>>>(view(P), n, P->part, P->fluid);
     FL_CHECK_LAUNCH(ctx, "k_brick_sums");
     int nc = (int)P->cases.size();
-    k_case_sums<<<(nc + 127) / 128, 128, 0, ctx->stream>>>(P->part, P->d_case_begin, nc, P->cons);
+    k_case_sums<<<std::min(nc, ctx->num_sms * 4), 256, 0, ctx->stream>>>(P->part, P->d_case_begin, nc, P->cons);
     FL_CHECK_LAUNCH(ctx, "k_case_sums");
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(out, P->cons, nc * 32, cudaMemcpyDeviceToHost, ctx->stream), "conservation");
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "conservation");

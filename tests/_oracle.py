@@ -221,10 +221,11 @@ def neighbours(cols, dom, subslots):
     return nbr
 
 
-def random_octree(seed, ext=(2, 2, 2), rounds=3, max_level=6, frac=0.3, balanced=True):
-    """A random leaf set built by repeated oracle regrids with random refine flags."""
+def random_octree(seed, ext=(2, 2, 2), rounds=3, max_level=6, frac=0.3, balanced=True, start_level=2):
+    """A random leaf set built by repeated oracle regrids with random refine flags,
+    starting from a uniform mesh at start_level."""
     rng = np.random.default_rng(seed)
-    cols = uniform_mesh(0, ext)
+    cols = uniform_mesh(start_level, ext)
     dom = domain(ext=ext, max_level=max_level)
     for r in range(rounds):
         n = len(cols["x"])

@@ -137,7 +137,7 @@ def test_split_merge_entry_points_vs_oracle(ctx):
 
 def test_blob_flags_vs_oracle(ctx):
     from fluidloom_gb300.amr import Mesh
-    cols = O.random_octree(50, ext=(1, 1, 1), rounds=4, max_level=7, frac=0.3, balanced=True)
+    cols = O.random_octree(50, ext=(1, 1, 1), rounds=2, max_level=7, frac=0.2, balanced=True, start_level=5)
     blobs = O.gaussian_blobs(7)
     want = O.blob_flags(cols, blobs, 0.05, 0.5, 7)
     m = Mesh(ctx, cols)
