@@ -13,6 +13,8 @@
 #include "common.cuh"
 #include "scan.cuh"
 
+#include <mutex>
+
 namespace {
 
 constexpr int kThreads = 256;
@@ -289,3 +291,75 @@ int fl_apply_permutation(fl_ctx* ctx, const void* src, void* dst, size_t elem_si
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Exclusive scan for callers that cannot allocate device memory.
+//
+// Some callers cannot call cudaMalloc: code running while a CUDA graph is
+// being captured on another thread, host callbacks and FFI hosts that must not
+// allocate on their hot path, and embedders that own every device allocation
+// through their own pool.  For them this entry point takes no context and
+// allocates nothing: the scan's only scratch (one status word per 4,096-element
+// tile, a tile ticket and a timeout word) lives in the file-scope array below,
+// sized for at most kNoAllocMaxN elements (128 KiB + 512 B); every GPU that
+// loads this library keeps that array until the process exits.  The caller
+// passes the input, the output and (optionally) the total.
+namespace {
+
+constexpr size_t kNoAllocMaxN = (size_t)1 << 26;                 // 67,108,864 elements
+constexpr size_t kNoAllocTiles = kNoAllocMaxN / kTile;           // 16,384 tile status words
+constexpr size_t kNoAllocStatusBytes = kNoAllocTiles * 8;        // 128 KiB
+constexpr size_t kNoAllocBytes = kNoAllocStatusBytes + 512;      // + ticket and timeout words
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+// Device address of g_noalloc_scratch per device: the array's name is only a
+// host-side stand-in, so host code must ask the runtime for the address, once
+// per device, with that device current.
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[64] = {nullptr};
+
+int noalloc_scratch(void** out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return FL_E_CUDA;
+    if (dev < 0 || dev >= 64) return FL_E_INVALID_ARG;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) return FL_E_CUDA;
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return FL_OK;
+}
+
+}  // namespace
+
+extern "C" int fl_scan_exclusive_u32_noalloc(const uint32_t* in, uint32_t* out, size_t n, uint32_t* total,
+                                             void* cuda_stream) {
+    if (n > kNoAllocMaxN) return FL_E_CAPACITY;
+    if (n && (!in || !out)) return FL_E_INVALID_ARG;
+    cudaStream_t st = (cudaStream_t)cuda_stream;
+    void* base = nullptr;
+    int rc = noalloc_scratch(&base);
+    if (rc) return rc;
+    if (n == 0) {
+        if (total && cudaMemsetAsync(total, 0, 4, st) != cudaSuccess) return FL_E_CUDA;
+        return FL_OK;
+    }
+    size_t tiles = (n + kTile - 1) / kTile;
+    unsigned long long* status = (unsigned long long*)base;
+    unsigned* ticket = (unsigned*)((char*)base + kNoAllocStatusBytes);
+    uint32_t* timeout = (uint32_t*)((char*)base + kNoAllocStatusBytes + 256);
+    // the array keeps the previous call's contents: clear the words this call reads as zero
+    if (cudaMemsetAsync(status, 0, tiles * 8, st) != cudaSuccess) return FL_E_CUDA;
+    if (cudaMemsetAsync(ticket, 0, 256 + FL_DEVSTAT_WORDS * 4, st) != cudaSuccess) return FL_E_CUDA;
+    k_scan<<<(unsigned)tiles, kThreads, 0, st>>>(in, out, n, status, ticket, total, timeout);
+    if (cudaGetLastError() != cudaSuccess) return FL_E_CUDA;
+    uint32_t expired = 0;  // a pageable destination makes this copy wait for the scan
+    if (cudaMemcpyAsync(&expired, timeout + FL_DEVSTAT_TIMEOUT, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        return FL_E_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return FL_E_CUDA;
+    return expired ? FL_E_DEVICE_TIMEOUT : FL_OK;
+}

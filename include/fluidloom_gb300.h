@@ -94,6 +94,14 @@ int fl_hilbert_is_valid(uint64_t key, uint8_t level);
  * Replaces AdaptationEngine::exclusiveScan (src/adaptation/AdaptationEngine.cpp:360-415).
  * total (device pointer, may be NULL) receives the sum.  in == out is allowed. */
 int fl_scan_exclusive_u32(fl_ctx* ctx, const uint32_t* in, uint32_t* out, size_t n, uint32_t* total);
+/* The same scan for callers that cannot allocate device memory (no counterpart in the reference):
+ * no context, no cudaMalloc/cudaFree or allocating library call; its scratch is a fixed array inside
+ * the library (128 KiB + 512 B per GPU, held until exit), so n is limited to 2^26 (67,108,864)
+ * elements and larger n returns FL_E_CAPACITY.  Runs on cuda_stream (a cudaStream_t, NULL = the
+ * default stream) and returns after the scan finished.  The first call on a device looks up the
+ * array's device address: make that first call before any stream capture.  All calls share the
+ * array, so calls that overlap on the GPU (other threads or streams) race. */
+int fl_scan_exclusive_u32_noalloc(const uint32_t* in, uint32_t* out, size_t n, uint32_t* total, void* cuda_stream);
 /* Stable ascending LSD radix sort of (key, value) pairs in place on bits [begin_bit, end_bit).
  * Replaces RadixSort::sortByKey (include/fluidloom/core/hashmap/RadixSort.h:33-35). */
 int fl_sort_pairs_u64_u32(fl_ctx* ctx, uint64_t* keys, uint32_t* vals, size_t n, int begin_bit, int end_bit);
