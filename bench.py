@@ -275,15 +275,25 @@ def run_gpu(args):
     st = pool.regrid()
     regrid_ms.append(stop())
     # roofline: per-launch CUDA events around every collide-stream launch
-    kms, nla, sites = pool.profile_steps(max(2, min(args.steps, 6)))
+    prof = pool.profile_steps(max(2, min(args.steps, 6)))
+    kms = sum(p[0] for p in prof)
+    nla = sum(p[1] for p in prof)
+    sites = sum(p[2] for p in prof)
     peak, peak_kind = measured_peak()
     achieved = BYTES_PER_LUP * sites / (kms * 1e-3) / 1e9
     tr = ncu_traffic()
+    per_kernel = {}
+    for name, (m, la, st_) in zip(("k_collide_fast", "k_collide_general", "k_collide_solid"), prof):
+        if la:
+            per_kernel[name] = {"launches": la, "avg_launch_ms": round(m / la, 4), "fluid_sites": int(st_),
+                                "achieved_gbs": round(BYTES_PER_LUP * st_ / (m * 1e-3) / 1e9, 1),
+                                "time_share": round(m / kms, 3)}
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": (round(tr * sites / nla) if tr else None),
-                "kernel": "k_collide_stream", "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                "kernel": "collide-stream (k_collide_fast + k_collide_general + k_collide_solid)",
+                "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                 "algorithmic_bytes_per_launch": round(BYTES_PER_LUP * sites / nla), "launches_profiled": nla,
-                "avg_launch_ms": round(kms / nla, 4)}
+                "avg_launch_ms": round(kms / nla, 4), "per_kernel": per_kernel}
     # e2e through the C ABI with pinned host buffers
     inf = pool.info()
     n = inf.num_bricks

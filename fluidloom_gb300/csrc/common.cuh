@@ -26,7 +26,10 @@ struct fl_ctx {
     uint32_t* host_status = nullptr;    // pinned mirror
     std::string last_error;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // fl_ctx_timer_start / stop
+    void* soa = nullptr;                       // structure-of-arrays field manager (fields.cu)
 };
+
+void fl_soa_release_all(fl_ctx* ctx);
 
 // Device status words written by kernels instead of trapping.
 enum {

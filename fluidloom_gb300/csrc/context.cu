@@ -103,6 +103,7 @@ int fl_ctx_create(int device, fl_ctx** out) {
 int fl_ctx_destroy(fl_ctx* ctx) {
     if (!ctx) return FL_OK;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    fl_soa_release_all(ctx);
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->dev_status) cudaFree(ctx->dev_status);
     if (ctx->host_status) cudaFreeHost(ctx->host_status);

@@ -368,36 +368,160 @@ __global__ void __launch_bounds__(128, 4) k_collide_fast(StepArgs a, const uint3
     const int l = a.level;
     const int t = threadIdx.x;
     const int x0 = (t & 1) * 4, y = (t >> 1) & 7, z = t >> 4;
-    for (uint32_t w = blockIdx.x; w < a.count; w += gridDim.x) {
-        const uint32_t b = a.list[w];
-        if (t < 27) s_nb[t] = nb27[(size_t)b * 28 + t];
+    // software pipeline: the next brick's list entry and neighbour row are
+    // loaded while the current brick is gathered and relaxed
+    uint32_t w = blockIdx.x;
+    uint32_t b = w < a.count ? a.list[w] : 0u;
+    uint32_t row = (w < a.count && t < 27) ? nb27[(size_t)b * 28 + t] : 0u;
+    for (; w < a.count; w += gridDim.x) {
+        if (t < 27) s_nb[t] = row;
         __syncthreads();
+        const uint32_t wn = w + gridDim.x;
+        const uint32_t bn = wn < a.count ? a.list[wn] : 0u;
+        if (wn < a.count && t < 27) row = nb27[(size_t)bn * 28 + t];
         const LbmCaseDev& c = a.cases[a.bcase[b]];
         float f[Q][4];
         gather_quad<false>(a, c, s_nb, b, l, 0, x0, y, z, nullptr, nullptr, f);
         collide_store(a, c, b, l, x0, y, z, nullptr, 0, f);
         __syncthreads();
+        b = bn;
     }
 }
 
-// Bricks at a level interface, a domain boundary or near the sphere: per
-// element checks, a shared 10^3 solid mask (the brick and its one-site halo)
-// and pull_slow for sources across an interface or outside the domain.
+// Pull across a level interface, a domain boundary or into the sphere for one
+// element (oracle: or_lbm.cpp pull()), with the brick's 26x4 neighbour table
+// and the neighbours' levels staged in shared memory.
+__device__ __noinline__ float pull_general(const StepArgs& a, const LbmCaseDev& c, uint32_t b, int q, int l,
+                                           const int64_t* G, int s_own, const uint32_t* s_nbr, const uint8_t* s_nlv,
+                                           const uint32_t* s_solid, int near, int lx, int ly, int lz) {
+    const int cx = CXq(q), cy = CYq(q), cz = CZq(q);
+    int64_t S[3] = {G[0] - cx, G[1] - cy, G[2] - cz};
+    int64_t N[3];
+    for (int ax = 0; ax < 3; ++ax) N[ax] = ((int64_t)c.ext[ax] * 8) << l;
+    int out_face[3] = {-1, -1, -1};
+    bool out = false;
+    for (int ax = 0; ax < 3; ++ax) {
+        if (c.periodic[ax]) continue;
+        if (S[ax] < 0) { out_face[ax] = 2 * ax; out = true; }
+        else if (S[ax] >= N[ax]) { out_face[ax] = 2 * ax + 1; out = true; }
+    }
+    if (out) {
+        bool inlet = false, outlet = false;
+        int moving = -1;
+        for (int ax = 0; ax < 3; ++ax) {
+            if (out_face[ax] < 0) continue;
+            int bt = c.bc[out_face[ax]];
+            if (bt == 3) inlet = true;
+            else if (bt == 4) outlet = true;
+            else if (bt == 2 && moving < 0) moving = out_face[ax];
+        }
+        if (inlet) {
+            float base = base_of(c.inlet_u[0], c.inlet_u[1], c.inlet_u[2]);
+            return feq1(q, 1.0f, c.inlet_u[0], c.inlet_u[1], c.inlet_u[2], base);
+        }
+        if (outlet) return a.R[fidx(a.cap, q, b, s_own)];
+        float v = a.R[fidx(a.cap, OPPq(q), b, s_own)];
+        if (moving >= 0) {
+            float cu = cdot(q, c.wall_u[0], c.wall_u[1], c.wall_u[2]);
+            float t = 6.0f * Wq(q);
+            t = t * cu;
+            v = v + t;
+        }
+        return v;
+    }
+    int64_t Sw[3];  // the source is one site from G: wrapping is one add or subtract
+    for (int ax = 0; ax < 3; ++ax)
+        Sw[ax] = !c.periodic[ax] ? S[ax] : (S[ax] < 0 ? S[ax] + N[ax] : (S[ax] >= N[ax] ? S[ax] - N[ax] : S[ax]));
+    if (near && solid_bit(s_solid, lx, ly, lz)) return a.R[fidx(a.cap, OPPq(q), b, s_own)];
+    if (lx >= 0 && lx < 8 && ly >= 0 && ly < 8 && lz >= 0 && lz < 8)
+        return a.R[fidx(a.cap, q, b, lx + 8 * ly + 64 * lz)];
+    int d[3] = {lx < 0 ? -1 : (lx >= 8 ? 1 : 0), ly < 0 ? -1 : (ly >= 8 ? 1 : 0), lz < 0 ? -1 : (lz >= 8 ? 1 : 0)};
+    int L3[3] = {lx, ly, lz};
+    int sub_slot = 0, bit = 0;
+    for (int ax = 0; ax < 3; ++ax)
+        if (d[ax] == 0) { if (L3[ax] >= 4) sub_slot |= 1 << bit; ++bit; }
+    int kk = (d[2] + 1) * 9 + (d[1] + 1) * 3 + (d[0] + 1);
+    int k = kk < 13 ? kk : kk - 1;
+    uint32_t nb = s_nbr[k * 4 + sub_slot];
+    if (nb == FL_INVALID_INDEX) return a.R[fidx(a.cap, OPPq(q), b, s_own)];
+    int ln = s_nlv[k * 4 + sub_slot];
+    int64_t nx = (int64_t)a.bx[nb] * 8, ny = (int64_t)a.by[nb] * 8, nz = (int64_t)a.bz[nb] * 8;
+    if (ln == l) return a.R[fidx(a.cap, q, nb, (int)((Sw[0] - nx) + 8 * (Sw[1] - ny) + 64 * (Sw[2] - nz)))];
+    if (ln == l - 1) {
+        int64_t px = (Sw[0] >> 1) - nx, py = (Sw[1] >> 1) - ny, pz = (Sw[2] >> 1) - nz;
+        if (px < 0 || px > 7 || py < 0 || py > 7 || pz < 0 || pz > 7) {
+            atomicAdd(a.dev_status + FL_DEVSTAT_BOUNDS, 1u);
+            return a.R[fidx(a.cap, OPPq(q), b, s_own)];
+        }
+        size_t i = fidx(a.cap, q, nb, (int)(px + 8 * py + 64 * pz));
+        if (a.sub == 0) return a.Cold[i];
+        float t = a.Cold[i] + a.Cnew[i];
+        return t * 0.5f;
+    }
+    if (ln == l + 1) {
+        float sum = 0.0f;
+        for (int kq = 0; kq < 8; ++kq) {
+            int64_t px = 2 * Sw[0] + (kq & 1) - nx;
+            int64_t py = 2 * Sw[1] + ((kq >> 1) & 1) - ny;
+            int64_t pz = 2 * Sw[2] + ((kq >> 2) & 1) - nz;
+            if (px < 0 || px > 7 || py < 0 || py > 7 || pz < 0 || pz > 7) {
+                atomicAdd(a.dev_status + FL_DEVSTAT_BOUNDS, 1u);
+                return a.R[fidx(a.cap, OPPq(q), b, s_own)];
+            }
+            sum = sum + a.Fine[fidx(a.cap, q, nb, (int)(px + 8 * py + 64 * pz))];
+        }
+        return sum * 0.125f;
+    }
+    atomicAdd(a.dev_status + FL_DEVSTAT_LEVEL_JUMP, 1u);
+    return a.R[fidx(a.cap, OPPq(q), b, s_own)];
+}
+
+// Bricks at a level interface, a domain boundary or near the sphere, in three
+// passes: (1) every element is gathered as in the interior kernel, with
+// missing same-level neighbours replaced by the brick itself so every load
+// stays in bounds, and the elements whose source crosses an interface or the
+// domain boundary, or lies in the sphere, are queued in shared memory;
+// (2) the queue is resolved in parallel by pull_general (independent loads,
+// so their latencies overlap); (3) the collision reads the staged values.
+struct GeneralSmem {
+    float f[Q][512];
+    uint16_t queue[Q * 512];  // q << 9 | site
+    uint32_t nbr[104];
+    uint8_t nlv[104];
+    uint32_t nb27[27];
+    uint32_t safe27[27];
+    uint32_t solid[32];
+    int near;
+    unsigned count;
+};
+
 __global__ void __launch_bounds__(128, 3) k_collide_general(StepArgs a, const uint32_t* __restrict__ nb27) {
-    __shared__ uint32_t s_nb[27];
-    __shared__ uint32_t s_solid[32];
-    __shared__ int s_near;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    GeneralSmem& S = *reinterpret_cast<GeneralSmem*>(smem_raw);
     const int l = a.level;
     const int t = threadIdx.x;
     const int x0 = (t & 1) * 4, y = (t >> 1) & 7, z = t >> 4;
+    const int own = x0 + 8 * y + 64 * z;
     for (uint32_t w = blockIdx.x; w < a.count; w += gridDim.x) {
         const uint32_t b = a.list[w];
         const LbmCaseDev& c = a.cases[a.bcase[b]];
-        if (t < 27) s_nb[t] = nb27[(size_t)b * 28 + t];
-        if (t < 32) s_solid[t] = 0u;
-        if (t == 32) s_near = brick_near_sphere(c, a.bx[b], a.by[b], a.bz[b], l);
+        if (t < 27) {
+            uint32_t e = nb27[(size_t)b * 28 + t];
+            S.nb27[t] = e;
+            S.safe27[t] = e == kSlow ? b : e;
+        }
+        if (t < 104) {
+            uint32_t nb = a.nbr[(size_t)b * 104 + t];
+            S.nbr[t] = nb;
+            S.nlv[t] = nb == FL_INVALID_INDEX ? 0xFF : a.blevel[nb];
+        }
+        if (t < 32) S.solid[t] = 0u;
+        if (t == 32) {
+            S.near = brick_near_sphere(c, a.bx[b], a.by[b], a.bz[b], l);
+            S.count = 0;
+        }
         __syncthreads();
-        const int near = s_near;
+        const int near = S.near;
         const int64_t G0[3] = {(int64_t)a.bx[b] * 8, (int64_t)a.by[b] * 8, (int64_t)a.bz[b] * 8};
         if (near) {
             for (int i = t; i < 1000; i += 128) {
@@ -407,14 +531,81 @@ __global__ void __launch_bounds__(128, 3) k_collide_general(StepArgs a, const ui
                     int64_t N = ((int64_t)c.ext[ax] * 8) << l;
                     G[ax] = G[ax] < 0 ? G[ax] + N : (G[ax] >= N ? G[ax] - N : G[ax]);
                 }
-                if (solid_at(c, G[0], G[1], G[2], l)) atomicOr(&s_solid[i >> 5], 1u << (i & 31));
+                if (solid_at(c, G[0], G[1], G[2], l)) atomicOr(&S.solid[i >> 5], 1u << (i & 31));
             }
             __syncthreads();
         }
-        float f[Q][4];
-        gather_quad<true>(a, c, s_nb, b, l, near, x0, y, z, G0, s_solid, f);
-        collide_store(a, c, b, l, x0, y, z, s_solid, near, f);
+        // pass 1: in-bounds gathers for every element, queue the ones that need pull_general
+        {
+            float f[Q][4];
+            gather_quad<false>(a, c, S.safe27, b, l, 0, x0, y, z, nullptr, nullptr, f);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                const int cx = CXq(q), cy = CYq(q), cz = CZq(q);
+                const int sy = y - cy, sz = z - cz;
+                const int dy = sy >> 3, dz = sz >> 3;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int xi = x0 + i - cx;
+                    const int dx = xi >> 3;
+                    const bool slow = S.nb27[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)] == kSlow ||
+                                      (near && solid_bit(S.solid, xi, sy, sz));
+                    if (slow) {
+                        unsigned k = atomicAdd(&S.count, 1u);
+                        S.queue[k] = (uint16_t)((q << 9) | (own + i));
+                    }
+                }
+                *reinterpret_cast<float4*>(&S.f[q][own]) = make_float4(f[q][0], f[q][1], f[q][2], f[q][3]);
+            }
+        }
         __syncthreads();
+        // pass 2: the queued elements, independently
+        const unsigned nq = S.count;
+        for (unsigned k = t; k < nq; k += 128) {
+            const unsigned e = S.queue[k];
+            const int q = (int)(e >> 9), s = (int)(e & 511);
+            const int xi = (s & 7) - CXq(q), yi = ((s >> 3) & 7) - CYq(q), zi = (s >> 6) - CZq(q);
+            const int64_t G[3] = {G0[0] + (s & 7), G0[1] + ((s >> 3) & 7), G0[2] + (s >> 6)};
+            S.f[q][s] = pull_general(a, c, b, q, l, G, s, S.nbr, S.nlv, S.solid, near, xi, yi, zi);
+        }
+        __syncthreads();
+        // pass 3: collision from shared memory
+        const float omega = c.omega[l];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            float g[Q];
+#pragma unroll
+            for (int q = 0; q < Q; ++q) g[q] = S.f[q][own + i];
+            const bool solid = near && solid_bit(S.solid, x0 + i, y, z);
+            float rho, jx, jy, jz;
+            moments(g, rho, jx, jy, jz);
+            float inv = 1.0f / rho;
+            float ux = jx * inv, uy = jy * inv, uz = jz * inv;
+            float base = base_of(ux, uy, uz);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                float fe = feq1(q, rho, ux, uy, uz, base);
+                float dd = fe - g[q];
+                dd = omega * dd;
+                S.f[q][own + i] = solid ? Wq(q) : g[q] + dd;
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+            *(float4*)(a.W + fidx(a.cap, q, b, own)) = *reinterpret_cast<const float4*>(&S.f[q][own]);
+        __syncthreads();
+    }
+}
+
+// Bricks whose 512 sites all lie in the sphere: rest equilibrium, no reads.
+__global__ void k_collide_solid(StepArgs a) {
+    size_t total = (size_t)a.count * 512;
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
+        uint32_t b = a.list[t >> 9];
+        int s = (int)(t & 511);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) a.W[fidx(a.cap, q, b, s)] = Wq(q);
     }
 }
 
@@ -443,6 +634,14 @@ __global__ void k_brick_table(size_t n, const uint32_t* __restrict__ nbr, const 
             nb27[b * 28 + d] = e;
         }
         nb27[b * 28 + 27] = 0;
+        if (general) {  // all 512 sites solid: the brick only ever holds the rest equilibrium
+            const LbmCaseDev& c = cases[bcase[b]];
+            bool all = c.has_sphere != 0;
+            for (int s = 0; s < 512 && all; ++s)
+                all = solid_at(c, (int64_t)bx[b] * 8 + (s & 7), (int64_t)by[b] * 8 + ((s >> 3) & 7),
+                               (int64_t)bz[b] * 8 + (s >> 6), l);
+            if (all) general = 2;
+        }
         bclass[b] = (uint8_t)general;
     }
 }
@@ -743,9 +942,46 @@ extern "C" int fl_flags_from_blobs(fl_ctx* ctx, fl_mesh* mesh, const float* blob
     return FL_OK;
 }
 
+namespace {
+
+// Keep only the flags of bricks whose case is due for a regrid.
+__global__ void k_mask_flags(size_t n, const uint16_t* __restrict__ bcase, const uint8_t* __restrict__ due,
+                             int32_t* __restrict__ flags) {
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x; b < n; b += stride)
+        if (!due[bcase[b]]) flags[b] = 0;
+}
+
+__global__ void k_keep_bricks(size_t n, const uint16_t* __restrict__ bcase, const uint8_t* __restrict__ active,
+                              uint32_t* __restrict__ keep) {
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x; b < n; b += stride) keep[b] = active[bcase[b]];
+}
+
+// Order-preserving compaction of the brick columns; osrc/okind feed k_remap as survivors.
+__global__ void k_compact_bricks(fl_mesh_dev m, const uint32_t* __restrict__ keep, const uint32_t* __restrict__ off,
+                                 fl_mesh_out o, uint32_t* __restrict__ osrc, uint8_t* __restrict__ okind) {
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
+        if (!keep[i]) continue;
+        uint32_t j = off[i];
+        o.x[j] = m.x[i]; o.y[j] = m.y[i]; o.z[j] = m.z[i];
+        o.level[j] = m.level[i]; o.state[j] = m.state[i]; o.flags[j] = 0; o.material[j] = m.material[i];
+        o.case_id[j] = m.case_id[i];
+        osrc[j] = (uint32_t)i;
+        okind[j] = 8;
+    }
+}
+
+}  // namespace
+
 // ------------------------------------------------------------------ pool
+constexpr int kMaxCases = 4096;  // case ids live in 12 key bits
+
 struct fl_pool {
-    std::vector<fl_lbm_case> cases;
+    std::vector<fl_lbm_case> cases;   // one entry per slot (case id)
+    std::vector<uint8_t> active;      // slot in use
+    uint8_t* d_mask = nullptr;        // per-slot byte mask on the device (regrid / removal)
     std::vector<LbmCaseDev> hcases;
     LbmCaseDev* d_cases = nullptr;
     fl_domain_dev::Case* d_dom = nullptr;
@@ -757,9 +993,9 @@ struct fl_pool {
     int maxL = 0;
     uint32_t* list = nullptr;
     std::vector<uint32_t> lvl_off;  // maxL + 2 entries
-    // per level: [fast offset, fast count, general offset, general count] into `list`
-    std::vector<uint32_t> lvl_fast_off, lvl_fast_cnt, lvl_gen_off, lvl_gen_cnt;
-    uint64_t fluid_fast[16] = {0}, fluid_gen[16] = {0};
+    // per brick class (0 interior, 1 general, 2 all-solid) and level: offset and count into `list`
+    std::vector<uint32_t> cls_off[3], cls_cnt[3];
+    uint64_t fluid_cls[3][16] = {};
     uint32_t* nb27 = nullptr;
     uint8_t* bclass = nullptr;
     std::vector<uint32_t> case_begin;
@@ -894,16 +1130,19 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
         P->lvl_off[lv[i] + 1]++;
     }
     for (int l = 0; l <= P->maxL; ++l) P->lvl_off[l + 1] += P->lvl_off[l];
-    // within a level: interior bricks first, then the general ones
-    P->lvl_fast_off.assign(P->maxL + 1, 0); P->lvl_fast_cnt.assign(P->maxL + 1, 0);
-    P->lvl_gen_off.assign(P->maxL + 1, 0); P->lvl_gen_cnt.assign(P->maxL + 1, 0);
-    for (size_t i = 0; i < n; ++i) (cl[i] ? P->lvl_gen_cnt : P->lvl_fast_cnt)[lv[i]]++;
-    for (int l = 0; l <= P->maxL; ++l) {
-        P->lvl_fast_off[l] = P->lvl_off[l];
-        P->lvl_gen_off[l] = P->lvl_off[l] + P->lvl_fast_cnt[l];
+    // within a level: interior bricks, then general ones, then all-solid ones
+    for (int k = 0; k < 3; ++k) {
+        P->cls_off[k].assign(P->maxL + 1, 0);
+        P->cls_cnt[k].assign(P->maxL + 1, 0);
     }
-    std::vector<uint32_t> list(n), ff(P->lvl_fast_off), gf(P->lvl_gen_off);
-    for (size_t i = 0; i < n; ++i) list[cl[i] ? gf[lv[i]]++ : ff[lv[i]]++] = (uint32_t)i;
+    for (size_t i = 0; i < n; ++i) P->cls_cnt[cl[i] > 2 ? 1 : cl[i]][lv[i]]++;
+    for (int l = 0; l <= P->maxL; ++l) {
+        P->cls_off[0][l] = P->lvl_off[l];
+        P->cls_off[1][l] = P->cls_off[0][l] + P->cls_cnt[0][l];
+        P->cls_off[2][l] = P->cls_off[1][l] + P->cls_cnt[1][l];
+    }
+    std::vector<uint32_t> list(n), fill[3] = {P->cls_off[0], P->cls_off[1], P->cls_off[2]};
+    for (size_t i = 0; i < n; ++i) list[fill[cl[i] > 2 ? 1 : cl[i]][lv[i]]++] = (uint32_t)i;
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->list, list.data(), n * 4, cudaMemcpyHostToDevice, ctx->stream), "list");
     P->case_begin.assign(P->cases.size() + 1, 0);
     for (size_t i = 0; i < n; ++i) P->case_begin[cs[i] + 1]++;
@@ -917,11 +1156,11 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(fl.data(), P->fluid, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "fluid");
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "topology sync");
     P->lups = 0;
-    for (int l = 0; l < 16; ++l) P->fluid_per_level[l] = P->fluid_fast[l] = P->fluid_gen[l] = 0;
+    for (int l = 0; l < 16; ++l) P->fluid_per_level[l] = P->fluid_cls[0][l] = P->fluid_cls[1][l] = P->fluid_cls[2][l] = 0;
     for (size_t i = 0; i < n; ++i) {
         P->lups += (uint64_t)fl[i] << lv[i];
         P->fluid_per_level[lv[i]] += fl[i];
-        (cl[i] ? P->fluid_gen : P->fluid_fast)[lv[i]] += fl[i];
+        P->fluid_cls[cl[i] > 2 ? 1 : cl[i]][lv[i]] += fl[i];
     }
     drop_graph(P);
     return fl_collect_device_status(ctx, "pool topology");
@@ -957,10 +1196,16 @@ int pool_flags(fl_ctx* ctx, fl_pool* P, int use_vorticity) {
 }
 
 // One regrid: flags, adapt (FULL26), population remap into the spare buffer.
-int pool_regrid(fl_ctx* ctx, fl_pool* P, int use_vorticity, fl_adapt_stats* st) {
+int pool_regrid(fl_ctx* ctx, fl_pool* P, int use_vorticity, fl_adapt_stats* st, const uint8_t* due = nullptr) {
     int rc = pool_flags(ctx, P, use_vorticity);
     if (rc) return rc;
     size_t n = P->mesh.num_cells;
+    if (due) {  // cases not due keep flag 0 and come out of the regrid unchanged
+        FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->d_mask, due, P->cases.size(), cudaMemcpyHostToDevice, ctx->stream), "due");
+        k_mask_flags<<<fl_blocks(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(n, P->mesh.case_id, P->d_mask,
+                                                                                  P->mesh.flags);
+        FL_CHECK_LAUNCH(ctx, "k_mask_flags");
+    }
     fl_adapt_config cfg{};
     cfg.max_refinement_level = (uint8_t)P->maxL;
     cfg.min_refinement_level = 0;
@@ -1027,10 +1272,48 @@ int pool_regrid(fl_ctx* ctx, fl_pool* P, int use_vorticity, fl_adapt_stats* st) 
     return rc;
 }
 
+// Grow every per-brick array to new_cap, keeping the first n bricks (both
+// population buffers A and B are copied, so each level's parity stays valid).
+int pool_grow(fl_ctx* ctx, fl_pool* P, size_t new_cap) {
+    if (new_cap <= P->cap) return FL_OK;
+    size_t n = P->mesh.num_cells;
+    fl_mesh m2{};
+    int rc = fl_mesh_alloc(ctx, new_cap, 1, &m2);
+    if (rc) return rc;
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(m2.x, P->mesh.x, n * 4, cudaMemcpyDeviceToDevice, ctx->stream), "grow");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(m2.y, P->mesh.y, n * 4, cudaMemcpyDeviceToDevice, ctx->stream), "grow");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(m2.z, P->mesh.z, n * 4, cudaMemcpyDeviceToDevice, ctx->stream), "grow");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(m2.level, P->mesh.level, n, cudaMemcpyDeviceToDevice, ctx->stream), "grow");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(m2.state, P->mesh.state, n, cudaMemcpyDeviceToDevice, ctx->stream), "grow");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(m2.flags, P->mesh.flags, n * 4, cudaMemcpyDeviceToDevice, ctx->stream), "grow");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(m2.material, P->mesh.material, n * 4, cudaMemcpyDeviceToDevice, ctx->stream), "grow");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(m2.case_id, P->mesh.case_id, n * 2, cudaMemcpyDeviceToDevice, ctx->stream), "grow");
+    m2.num_cells = n;
+    fl_mesh old = P->mesh;
+    fl_mesh_free(ctx, &old);
+    P->mesh = m2;
+    for (int k = 0; k < 3; ++k) {
+        float* nf = nullptr;
+        FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&nf, new_cap * 512 * Q * 4, ctx->stream), "grow populations");
+        if (k < 2)
+            for (int q = 0; q < Q; ++q)
+                FL_TRY_CUDA(ctx, cudaMemcpyAsync(nf + (size_t)q * new_cap * 512, P->f[k] + (size_t)q * P->cap * 512,
+                                                 n * 512 * 4, cudaMemcpyDeviceToDevice, ctx->stream), "grow");
+        cudaFreeAsync(P->f[k], ctx->stream);
+        P->f[k] = nf;
+    }
+    free_brick_arrays(ctx, P);
+    rc = alloc_brick_arrays(ctx, P, new_cap);
+    if (rc) return rc;
+    P->cap = new_cap;
+    drop_graph(P);
+    return FL_OK;
+}
+
 struct LaunchTimer {
     std::vector<cudaEvent_t> ev;  // start/stop pairs
     std::vector<uint64_t> sites;  // fluid sites processed by each launch
-    std::vector<int> kind;        // 0 interior kernel, 1 general kernel
+    std::vector<int> kind;        // 0 interior kernel, 1 general kernel, 2 all-solid bricks
 };
 
 void launch_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm = nullptr) {
@@ -1047,9 +1330,9 @@ void launch_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm = nul
     a.nbr = P->nbr;
     a.cases = P->d_cases;
     a.dev_status = ctx->dev_status;
-    for (int kind = 0; kind < 2; ++kind) {
-        uint32_t off = kind ? P->lvl_gen_off[l] : P->lvl_fast_off[l];
-        uint32_t cnt = kind ? P->lvl_gen_cnt[l] : P->lvl_fast_cnt[l];
+    for (int kind = 0; kind < 3; ++kind) {
+        uint32_t off = P->cls_off[kind][l];
+        uint32_t cnt = P->cls_cnt[kind][l];
         if (!cnt) continue;
         cudaEvent_t e0 = nullptr, e1 = nullptr;
         if (tm) {
@@ -1062,15 +1345,17 @@ void launch_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm = nul
         if (kind == 0) {
             unsigned grid = std::min<unsigned>(cnt, (unsigned)ctx->num_sms * P->grid_mult);
             k_collide_fast<<<grid, 128, 0, ctx->stream>>>(a, P->nb27);
-        } else {
+        } else if (kind == 1) {
             unsigned grid = std::min<unsigned>(cnt, (unsigned)ctx->num_sms * 3);
-            k_collide_general<<<grid, 128, 0, ctx->stream>>>(a, P->nb27);
+            k_collide_general<<<grid, 128, sizeof(GeneralSmem), ctx->stream>>>(a, P->nb27);
+        } else {
+            k_collide_solid<<<fl_blocks((size_t)cnt * 512, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(a);
         }
         if (tm) {
             cudaEventRecord(e1, ctx->stream);
             tm->ev.push_back(e0);
             tm->ev.push_back(e1);
-            tm->sites.push_back(kind ? P->fluid_gen[l] : P->fluid_fast[l]);
+            tm->sites.push_back(P->fluid_cls[kind][l]);
             tm->kind.push_back(kind);
         }
     }
@@ -1091,6 +1376,8 @@ extern "C" {
 
 int fl_pool_create(fl_ctx* ctx, const fl_lbm_case* cases, int ncases, fl_pool** out) {
     if (!ctx || !cases || ncases <= 0 || ncases > 4096 || !out) return FL_E_INVALID_ARG;
+    FL_TRY_CUDA(ctx, cudaFuncSetAttribute(k_collide_general, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)sizeof(GeneralSmem)), "general kernel shared memory");
     *out = nullptr;
     fl_pool* P = new fl_pool();
     P->cases.assign(cases, cases + ncases);
@@ -1112,11 +1399,14 @@ int fl_pool_create(fl_ctx* ctx, const fl_lbm_case* cases, int ncases, fl_pool** 
     }
     int rc = FL_OK;
     auto fail = [&](int r) { fl_pool_destroy(ctx, P); return r; };
-    if (cudaMalloc(&P->d_cases, ncases * sizeof(LbmCaseDev)) != cudaSuccess) return fail(FL_E_OOM);
-    if (cudaMalloc(&P->d_dom, ncases * sizeof(fl_domain_dev::Case)) != cudaSuccess) return fail(FL_E_OOM);
-    if (cudaMalloc(&P->d_case_begin, (ncases + 1) * 4) != cudaSuccess) return fail(FL_E_OOM);
-    if (cudaMalloc(&P->case_max, ncases * 4) != cudaSuccess) return fail(FL_E_OOM);
-    if (cudaMalloc(&P->cons, ncases * 32) != cudaSuccess) return fail(FL_E_OOM);
+    // case tables sized for every slot a pool can hold (cases may be added later)
+    if (cudaMalloc(&P->d_cases, kMaxCases * sizeof(LbmCaseDev)) != cudaSuccess) return fail(FL_E_OOM);
+    if (cudaMalloc(&P->d_dom, kMaxCases * sizeof(fl_domain_dev::Case)) != cudaSuccess) return fail(FL_E_OOM);
+    if (cudaMalloc(&P->d_case_begin, (kMaxCases + 1) * 4) != cudaSuccess) return fail(FL_E_OOM);
+    if (cudaMalloc(&P->case_max, kMaxCases * 4) != cudaSuccess) return fail(FL_E_OOM);
+    if (cudaMalloc(&P->cons, kMaxCases * 32) != cudaSuccess) return fail(FL_E_OOM);
+    if (cudaMalloc(&P->d_mask, kMaxCases) != cudaSuccess) return fail(FL_E_OOM);
+    P->active.assign(ncases, 1);
     cudaMemcpy(P->d_cases, P->hcases.data(), ncases * sizeof(LbmCaseDev), cudaMemcpyHostToDevice);
     cudaMemcpy(P->d_dom, dom.data(), ncases * sizeof(fl_domain_dev::Case), cudaMemcpyHostToDevice);
     // level-0 bricks, unsorted
@@ -1176,6 +1466,7 @@ int fl_pool_destroy(fl_ctx* ctx, fl_pool* P) {
     if (P->d_case_begin) cudaFree(P->d_case_begin);
     if (P->case_max) cudaFree(P->case_max);
     if (P->cons) cudaFree(P->cons);
+    if (P->d_mask) cudaFree(P->d_mask);
     delete P;
     return FL_OK;
 }
@@ -1224,6 +1515,7 @@ int fl_pool_info_get(fl_ctx* ctx, fl_pool* P, fl_pool_info* info) {
     info->num_bricks = P->mesh.num_cells;
     info->capacity = P->cap;
     info->num_cases = (int32_t)P->cases.size();
+    info->num_active_cases = (int32_t)std::count(P->active.begin(), P->active.end(), (uint8_t)1);
     info->max_level = P->maxL;
     for (int l = 0; l <= P->maxL && l < 16; ++l) info->bricks_per_level[l] = P->lvl_off[l + 1] - P->lvl_off[l];
     info->fluid_lups_per_step = P->lups;
@@ -1298,21 +1590,26 @@ int fl_pool_profile_steps(fl_ctx* ctx, fl_pool* P, int nsteps, double* kernel_ms
     if (!ctx || !P || nsteps < 0) return FL_E_INVALID_ARG;
     LaunchTimer tm;
     for (int i = 0; i < nsteps; ++i) step_level(ctx, P, 0, 0, &tm);
-    FL_CHECK_LAUNCH(ctx, "k_collide_stream");
+    FL_CHECK_LAUNCH(ctx, "collide-stream");
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "profile sync");
-    double ms = 0.0;
-    uint64_t sites = 0;
+    double ms[3] = {0.0, 0.0, 0.0};
+    uint64_t sites[3] = {0, 0, 0};
+    uint32_t cnt[3] = {0, 0, 0};
     for (size_t k = 0; k < tm.ev.size(); k += 2) {
         float t = 0.0f;
         cudaEventElapsedTime(&t, tm.ev[k], tm.ev[k + 1]);
-        ms += t;
+        int kind = tm.kind[k / 2];
+        ms[kind] += t;
+        sites[kind] += tm.sites[k / 2];
+        cnt[kind] += 1;
         cudaEventDestroy(tm.ev[k]);
         cudaEventDestroy(tm.ev[k + 1]);
     }
-    for (uint64_t x : tm.sites) sites += x;
-    if (kernel_ms) *kernel_ms = ms;
-    if (launches) *launches = (uint32_t)(tm.ev.size() / 2);
-    if (fluid_sites) *fluid_sites = sites;
+    for (int k = 0; k < 3; ++k) {
+        if (kernel_ms) kernel_ms[k] = ms[k];
+        if (launches) launches[k] = cnt[k];
+        if (fluid_sites) fluid_sites[k] = sites[k];
+    }
     drop_graph(P);
     return fl_collect_device_status(ctx, "fl_pool_profile_steps");
 }
@@ -1339,6 +1636,167 @@ int fl_pool_set_velocities(fl_ctx* ctx, fl_pool* P, const float* wall_u, const f
         if (inlet_u)
             FL_TRY_CUDA(ctx, cudaMemcpyAsync(base + offsetof(LbmCaseDev, inlet_u), inlet_u + 3 * c, 12,
                                              cudaMemcpyHostToDevice, ctx->stream), "velocities");
+    }
+    return FL_OK;
+}
+
+int fl_pool_regrid_cases(fl_ctx* ctx, fl_pool* P, const uint8_t* due, fl_adapt_stats* st) {
+    if (!ctx || !P || !due) return FL_E_INVALID_ARG;
+    int rc = pool_regrid(ctx, P, 1, st, due);
+    if (rc) return rc;
+    return fl_collect_device_status(ctx, "fl_pool_regrid_cases");
+}
+
+int fl_pool_add_cases(fl_ctx* ctx, fl_pool* P, const fl_lbm_case* cases, int ncases, int32_t* ids) {
+    if (!ctx || !P || !cases || ncases <= 0 || !ids) return FL_E_INVALID_ARG;
+    // slots: freed ids first, then ids past the last one used
+    std::vector<int> slot;
+    for (int i = 0; i < (int)P->active.size() && (int)slot.size() < ncases; ++i)
+        if (!P->active[i]) slot.push_back(i);
+    for (int next = (int)P->active.size(); (int)slot.size() < ncases && next < kMaxCases; ++next) slot.push_back(next);
+    if ((int)slot.size() < ncases) return fl_set_error(ctx, FL_E_CAPACITY, "fl_pool_add_cases: no free case slots");
+    // build the new cases exactly as a pool of their own would start
+    fl_pool* T = nullptr;
+    int rc = fl_pool_create(ctx, cases, ncases, &T);
+    if (rc) return rc;
+    size_t n = P->mesh.num_cells, nt = T->mesh.num_cells;
+    if (n + nt > P->cap) {
+        rc = pool_grow(ctx, P, std::max((size_t)((n + nt) * 1.5), n + nt + 64));
+        if (rc) { fl_pool_destroy(ctx, T); return rc; }
+    }
+    // append columns (case ids mapped to the slots) and populations (into A and B)
+    std::vector<uint16_t> tc(nt);
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(tc.data(), T->mesh.case_id, nt * 2, cudaMemcpyDeviceToHost, ctx->stream), "add");
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "add");
+    for (auto& v : tc) v = (uint16_t)slot[v];
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->mesh.case_id + n, tc.data(), nt * 2, cudaMemcpyHostToDevice, ctx->stream), "add");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->mesh.x + n, T->mesh.x, nt * 4, cudaMemcpyDeviceToDevice, ctx->stream), "add");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->mesh.y + n, T->mesh.y, nt * 4, cudaMemcpyDeviceToDevice, ctx->stream), "add");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->mesh.z + n, T->mesh.z, nt * 4, cudaMemcpyDeviceToDevice, ctx->stream), "add");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->mesh.level + n, T->mesh.level, nt, cudaMemcpyDeviceToDevice, ctx->stream), "add");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->mesh.state + n, T->mesh.state, nt, cudaMemcpyDeviceToDevice, ctx->stream), "add");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->mesh.flags + n, T->mesh.flags, nt * 4, cudaMemcpyDeviceToDevice, ctx->stream), "add");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->mesh.material + n, T->mesh.material, nt * 4, cudaMemcpyDeviceToDevice, ctx->stream), "add");
+    for (int k = 0; k < 2; ++k)
+        for (int q = 0; q < Q; ++q)
+            FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->f[k] + ((size_t)q * P->cap + n) * 512, T->f[0] + (size_t)q * T->cap * 512,
+                                             nt * 512 * 4, cudaMemcpyDeviceToDevice, ctx->stream), "add");
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "add");
+    // case tables
+    for (int i = 0; i < ncases; ++i) {
+        int sl = slot[i];
+        if (sl >= (int)P->cases.size()) {
+            P->cases.resize(sl + 1);
+            P->hcases.resize(sl + 1);
+            P->active.resize(sl + 1, 0);
+        }
+        P->cases[sl] = cases[i];
+        to_dev_case(cases[i], P->hcases[sl]);
+        P->active[sl] = 1;
+        fl_domain_dev::Case d;
+        for (int a = 0; a < 3; ++a) { d.ext[a] = cases[i].ext[a]; d.periodic[a] = cases[i].bc[2 * a] == 0; }
+        FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->d_cases + sl, &P->hcases[sl], sizeof(LbmCaseDev), cudaMemcpyHostToDevice,
+                                         ctx->stream), "add tables");
+        FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->d_dom + sl, &d, sizeof(d), cudaMemcpyHostToDevice, ctx->stream), "add tables");
+        FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "add tables");
+        P->maxL = std::max(P->maxL, (int)cases[i].max_level);
+        ids[i] = sl;
+    }
+    fl_pool_destroy(ctx, T);
+    P->mesh.num_cells = n + nt;
+    // one regrid with every flag 0 only re-sorts by (case, key) and rebuilds the topology
+    rc = pool_regrid(ctx, P, -1, nullptr);
+    if (rc) return rc;
+    return fl_collect_device_status(ctx, "fl_pool_add_cases");
+}
+
+int fl_pool_remove_cases(fl_ctx* ctx, fl_pool* P, const int32_t* ids, int nids) {
+    if (!ctx || !P || (nids && !ids)) return FL_E_INVALID_ARG;
+    for (int i = 0; i < nids; ++i) {
+        if (ids[i] < 0 || ids[i] >= (int)P->active.size() || !P->active[ids[i]])
+            return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_pool_remove_cases: not an active case");
+    }
+    for (int i = 0; i < nids; ++i) P->active[ids[i]] = 0;
+    size_t n = P->mesh.num_cells;
+    if (n == 0) return FL_OK;
+    size_t sb = 3 * fl_align256(n * 4) + fl_scan_scratch_bytes(n) + 512;
+    int rc = fl_scratch_reserve(ctx, sb);
+    if (rc) return rc;
+    char* p = (char*)ctx->scratch;
+    uint32_t* keep = (uint32_t*)p; p += fl_align256(n * 4);
+    uint32_t* off = (uint32_t*)p; p += fl_align256(n * 4);
+    uint32_t* total = (uint32_t*)p; p += fl_align256(n * 4);
+    void* ss = p;
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->d_mask, P->active.data(), P->active.size(), cudaMemcpyHostToDevice, ctx->stream),
+                "active");
+    k_keep_bricks<<<fl_blocks(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(n, P->mesh.case_id, P->d_mask, keep);
+    FL_CHECK_LAUNCH(ctx, "k_keep_bricks");
+    rc = fl_scan_u32_with(ctx, keep, off, n, total, ss);
+    if (rc) return rc;
+    uint32_t M = 0;
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(&M, total, 4, cudaMemcpyDeviceToHost, ctx->stream), "kept");
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "kept");
+    fl_mesh out{};
+    rc = fl_mesh_alloc(ctx, P->cap, 1, &out);
+    if (rc) return rc;
+    uint32_t* osrc = nullptr;
+    uint8_t* okind = nullptr;
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&osrc, (M + 1) * 4, ctx->stream), "remove src");
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&okind, M + 1, ctx->stream), "remove kind");
+    fl_mesh_dev md{P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.level, P->mesh.state, P->mesh.flags, P->mesh.material,
+                   P->mesh.case_id, n};
+    fl_mesh_out o{out.x, out.y, out.z, out.level, out.state, out.flags, out.material, out.case_id};
+    k_compact_bricks<<<fl_blocks(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(md, keep, off, o, osrc, okind);
+    FL_CHECK_LAUNCH(ctx, "k_compact_bricks");
+    if (M) {
+        k_remap<<<fl_blocks((size_t)M * 512, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(view(P), M, osrc, okind,
+                                                                                        nullptr, P->f[2], P->cap);
+        FL_CHECK_LAUNCH(ctx, "k_remap");
+    }
+    cudaFreeAsync(osrc, ctx->stream);
+    cudaFreeAsync(okind, ctx->stream);
+    fl_mesh old = P->mesh;
+    fl_mesh_free(ctx, &old);
+    out.num_cells = M;
+    out.capacity = P->cap;
+    P->mesh = out;
+    float* old0 = P->f[0];
+    P->f[0] = P->f[2];
+    P->f[2] = old0;
+    for (int l = 0; l < 16; ++l) P->parity[l] = 0;
+    rc = pool_topology(ctx, P);
+    if (rc) return rc;
+    return fl_collect_device_status(ctx, "fl_pool_remove_cases");
+}
+
+int fl_pool_download_case(fl_ctx* ctx, fl_pool* P, int32_t id, int32_t* x, int32_t* y, int32_t* z, uint8_t* level,
+                          float* f, size_t* nbricks) {
+    if (!ctx || !P || !nbricks || id < 0 || id >= (int)P->active.size() || !P->active[id]) return FL_E_INVALID_ARG;
+    uint32_t b0 = P->case_begin[id], b1 = P->case_begin[id + 1];
+    size_t n = b1 - b0;
+    *nbricks = n;
+    if (!n) return FL_OK;
+    std::vector<uint8_t> lv(n);
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(lv.data(), P->mesh.level + b0, n, cudaMemcpyDeviceToHost, ctx->stream), "dl");
+    if (x) FL_TRY_CUDA(ctx, cudaMemcpyAsync(x, P->mesh.x + b0, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "dl");
+    if (y) FL_TRY_CUDA(ctx, cudaMemcpyAsync(y, P->mesh.y + b0, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "dl");
+    if (z) FL_TRY_CUDA(ctx, cudaMemcpyAsync(z, P->mesh.z + b0, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "dl");
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "dl");
+    if (level) std::memcpy(level, lv.data(), n);
+    if (f) {
+        for (int q = 0; q < Q; ++q) {
+            size_t b = 0;
+            while (b < n) {
+                int par = P->parity[lv[b]];
+                size_t e = b + 1;
+                while (e < n && P->parity[lv[e]] == par) ++e;
+                FL_TRY_CUDA(ctx, cudaMemcpyAsync(f + ((size_t)q * n + b) * 512,
+                                                 P->f[par] + ((size_t)q * P->cap + b0 + b) * 512, (e - b) * 512 * 4,
+                                                 cudaMemcpyDeviceToHost, ctx->stream), "dl f");
+                b = e;
+            }
+        }
+        FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "dl");
     }
     return FL_OK;
 }

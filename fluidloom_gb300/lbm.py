@@ -21,7 +21,7 @@ class PoolInfo(ctypes.Structure):
     _fields_ = [("num_bricks", ctypes.c_size_t), ("capacity", ctypes.c_size_t), ("num_cases", ctypes.c_int32),
                 ("max_level", ctypes.c_int32), ("bricks_per_level", ctypes.c_uint32 * 16),
                 ("fluid_lups_per_step", ctypes.c_uint64), ("population_bytes", ctypes.c_uint64),
-                ("fluid_sites_per_level", ctypes.c_uint64 * 16)]
+                ("fluid_sites_per_level", ctypes.c_uint64 * 16), ("num_active_cases", ctypes.c_int32)]
 
 
 WALL, MOVING, INLET, OUTLET, PERIODIC = 1, 2, 3, 4, 0
@@ -111,14 +111,15 @@ class Pool:
         return fl, wm
 
     def conservation(self):
-        out = np.empty((self.ncases, 4), np.float64)
+        out = np.empty((self.info().num_cases, 4), np.float64)
         self.ctx.call("fl_pool_conservation", self.h, out.ctypes.data_as(P))
         return out
 
     def profile_steps(self, n):
-        ms, la, st = ctypes.c_double(), ctypes.c_uint32(), ctypes.c_uint64()
-        self.ctx.call("fl_pool_profile_steps", self.h, n, ctypes.byref(ms), ctypes.byref(la), ctypes.byref(st))
-        return ms.value, la.value, st.value
+        """Per kernel (interior, general, all-solid): (kernel ms, launches, fluid sites updated)."""
+        ms, la, st = (ctypes.c_double * 3)(), (ctypes.c_uint32 * 3)(), (ctypes.c_uint64 * 3)()
+        self.ctx.call("fl_pool_profile_steps", self.h, n, ms, la, st)
+        return [(ms[k], la[k], st[k]) for k in range(3)]
 
     def upload(self, f):
         f = np.ascontiguousarray(f, np.float32)
@@ -129,6 +130,36 @@ class Pool:
         i = None if inlet_u is None else np.ascontiguousarray(inlet_u, np.float32)
         self.ctx.call("fl_pool_set_velocities", self.h, w.ctypes.data_as(P) if w is not None else None,
                       i.ctypes.data_as(P) if i is not None else None)
+
+    def add_cases(self, cases):
+        arr = (LbmCase * len(cases))(*cases)
+        ids = (ctypes.c_int32 * len(cases))()
+        self.ctx.call("fl_pool_add_cases", self.h, arr, len(cases), ids)
+        self.ncases = self.info().num_cases
+        return list(ids)
+
+    def remove_cases(self, ids):
+        a = (ctypes.c_int32 * len(ids))(*ids)
+        self.ctx.call("fl_pool_remove_cases", self.h, a, len(ids))
+
+    def regrid_cases(self, due_ids):
+        n = self.info().num_cases
+        due = np.zeros(n, np.uint8)
+        due[list(due_ids)] = 1
+        st = AdaptStats()
+        self.ctx.call("fl_pool_regrid_cases", self.h, due.ctypes.data_as(P), ctypes.byref(st))
+        return st
+
+    def case_state(self, cid, with_f=True):
+        nb = ctypes.c_size_t()
+        self.ctx.call("fl_pool_download_case", self.h, cid, None, None, None, None, None, ctypes.byref(nb))
+        n = nb.value
+        x, y, z = (np.empty(n, np.int32) for _ in range(3))
+        lv = np.empty(n, np.uint8)
+        f = np.empty((Q, n, 512), np.float32) if with_f else None
+        self.ctx.call("fl_pool_download_case", self.h, cid, *[a.ctypes.data_as(P) for a in (x, y, z, lv)],
+                      f.ctypes.data_as(P) if with_f else None, ctypes.byref(nb))
+        return {"x": x, "y": y, "z": z, "level": lv}, f
 
     def close(self):
         if self.h:

@@ -1,0 +1,190 @@
+"""Serving: a request loop that admits AMR-LBM jobs as they arrive, merges them
+into the running pool at level-0 step boundaries (continuous batching), keeps
+every case resident on the device until it finishes, and reports aggregate
+MLUPS with p50/p99 time-to-completion against plain sequential GPU runs of the
+same jobs (one job at a time, arrival order).
+
+  python -m fluidloom_gb300.serving [--rate 50] [--duration 60] [--steps 200 2000] [--budget-gb 150]
+
+Jobs (synthetic, seeded): Poisson arrivals; 70 % lid-driven cavities, 30 %
+sphere-in-channel; base size log-uniform between 16^3 and 128x64x64 sites;
+1-3 refinement levels; steps uniform in the given range; regrid every 20
+steps.  Admission is gated by each job's population footprint against the HBM
+budget.  A job's result is its final state; for --check jobs it is compared
+bit for bit with the same job run alone.
+"""
+import argparse
+import collections
+import json
+import time
+
+import numpy as np
+
+from . import Context
+from .lbm import Pool, cavity, sphere_channel
+
+BRICK_BYTES = 3 * 19 * 512 * 4  # three population buffers per brick
+
+
+class Job:
+    __slots__ = ("jid", "arrival", "case", "steps", "regrid_every", "done", "cid", "start", "end", "est_bytes",
+                 "result")
+
+    def __init__(self, jid, arrival, case, steps, regrid_every=20):
+        self.jid, self.arrival, self.case, self.steps, self.regrid_every = jid, arrival, case, steps, regrid_every
+        self.done = 0
+        self.cid = None
+        self.start = self.end = None
+        self.result = None
+        e = case.ext
+        # footprint estimate: level-0 bricks refined into an eighth of the volume per extra level
+        self.est_bytes = int(e[0] * e[1] * e[2] * (1 + 0.125 * 8 ** max(case.max_level, 0) / 2) * BRICK_BYTES)
+
+
+def make_jobs(rate, duration, steps_range, seed=5):
+    rng = np.random.default_rng(seed)
+    t, jobs = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= duration:
+            break
+        lv = int(rng.integers(1, 4))
+        steps = int(rng.integers(steps_range[0], steps_range[1] + 1))
+        if rng.random() < 0.7:
+            edge = int(np.exp(rng.uniform(np.log(16), np.log(64))))
+            edge = int(min(64, max(16, 8 * round(edge / 8))))
+            case = cavity(edge, lv, u_lid=float(rng.uniform(0.02, 0.08)), tau=float(rng.uniform(0.52, 0.8)))
+        else:
+            s = float(np.exp(rng.uniform(0.0, np.log(4.0))))  # channel scale 1..4 -> 32x16x16 .. 128x64x64
+            nx = int(min(128, max(32, 32 * round(s))))
+            ny = nz = nx // 2
+            case = sphere_channel(nx, ny, nz, lv, radius=nx / 16.0, centre=(nx / 4.0, ny / 2.0, nz / 2.0),
+                                  u_in=0.04, tau=0.56, band=nx / 21.0)
+        jobs.append(Job(len(jobs), t, case, steps))
+    return jobs
+
+
+def run_served(ctx, jobs, budget_bytes, check_ids=()):
+    """Continuous batching; returns per-job (arrival, start, end) and the LUPs done."""
+    pending = collections.deque(sorted(jobs, key=lambda j: j.arrival))
+    queue, active = collections.deque(), {}
+    pool = None
+    used = 0
+    lups = 0
+    steps_run = 0
+    t0 = time.perf_counter()
+    while pending or queue or active:
+        now = time.perf_counter() - t0
+        while pending and pending[0].arrival <= now:
+            queue.append(pending.popleft())
+        admit = []
+        while queue and (used + queue[0].est_bytes <= budget_bytes or not active and not admit):
+            j = queue.popleft()
+            used += j.est_bytes
+            admit.append(j)
+        if admit:
+            cases = [j.case for j in admit]
+            if pool is None:
+                pool = Pool(ctx, cases)
+                ids = list(range(len(cases)))
+            else:
+                ids = pool.add_cases(cases)
+            now = time.perf_counter() - t0
+            for j, cid in zip(admit, ids):
+                j.cid, j.start = cid, now
+                active[cid] = j
+        if not active:
+            if pending:
+                time.sleep(max(0.0, min(0.05, pending[0].arrival - (time.perf_counter() - t0))))
+            continue
+        lups += pool.info().fluid_lups_per_step
+        pool.step(1)
+        steps_run += 1
+        due = []
+        for cid, j in active.items():
+            j.done += 1
+            if j.regrid_every and j.done % j.regrid_every == 0 and j.done < j.steps:
+                due.append(cid)
+        if due:
+            pool.regrid_cases(due)
+        fin = [cid for cid, j in active.items() if j.done >= j.steps]
+        if fin:
+            ctx.sync()
+            now = time.perf_counter() - t0
+            for cid in fin:
+                j = active.pop(cid)
+                j.end = now
+                used -= j.est_bytes
+                if j.jid in check_ids:
+                    j.result = pool.case_state(cid)
+            pool.remove_cases(fin)
+    ctx.sync()
+    makespan = time.perf_counter() - t0
+    if pool is not None:
+        pool.close()
+    return lups, makespan, steps_run
+
+
+def run_solo(ctx, job):
+    """The same job alone on the GPU; returns (seconds, LUPs, final state)."""
+    p = Pool(ctx, [job.case])
+    ctx.sync()
+    t0 = time.perf_counter()
+    lups = 0
+    for s in range(1, job.steps + 1):
+        lups += p.info().fluid_lups_per_step
+        p.step(1)
+        if job.regrid_every and s % job.regrid_every == 0 and s < job.steps:
+            p.regrid()
+    ctx.sync()
+    dt = time.perf_counter() - t0
+    state = p.case_state(0)
+    p.close()
+    return dt, lups, state
+
+
+def percentile(v, q):
+    return float(np.percentile(np.asarray(v), q)) if len(v) else None
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--rate", type=float, default=50.0)
+    ap.add_argument("--duration", type=float, default=60.0)
+    ap.add_argument("--steps", type=int, nargs=2, default=[200, 2000])
+    ap.add_argument("--budget-gb", type=float, default=150.0)
+    ap.add_argument("--check", type=int, default=8, help="jobs whose result is compared with their solo run")
+    ap.add_argument("--seed", type=int, default=5)
+    args = ap.parse_args(argv)
+    ctx = Context(0)
+    jobs = make_jobs(args.rate, args.duration, args.steps, args.seed)
+    check_ids = set(range(min(args.check, len(jobs))))
+    lups, makespan, steps_run = run_served(ctx, jobs, args.budget_gb * 1e9, check_ids)
+    lat = [j.end - j.arrival for j in jobs]
+    # plain sequential: each job alone, one after another in arrival order
+    end_prev, lat_plain, solo_s, solo_lups, mismatched = 0.0, [], 0.0, 0, []
+    for j in sorted(jobs, key=lambda j: j.arrival):
+        dt, lu, state = run_solo(ctx, j)
+        solo_s += dt
+        solo_lups += lu
+        start = max(j.arrival, end_prev)
+        end_prev = start + dt
+        lat_plain.append(end_prev - j.arrival)
+        if j.jid in check_ids:
+            g1, f1 = j.result
+            g2, f2 = state
+            same = all(np.array_equal(g1[k], g2[k]) for k in ("x", "y", "z", "level")) and np.array_equal(f1, f2)
+            if not same:
+                mismatched.append(j.jid)
+    res = {"jobs": len(jobs), "rate_per_s": args.rate, "duration_s": args.duration, "steps_range": args.steps,
+           "served_makespan_s": makespan, "served_mlups": lups / makespan / 1e6,
+           "served_p50_s": percentile(lat, 50), "served_p99_s": percentile(lat, 99),
+           "plain_mlups": solo_lups / solo_s / 1e6, "plain_makespan_s": end_prev,
+           "plain_p50_s": percentile(lat_plain, 50), "plain_p99_s": percentile(lat_plain, 99),
+           "pool_steps": steps_run, "checked": sorted(check_ids), "mismatched": mismatched}
+    print(json.dumps(res))
+    return res
+
+
+if __name__ == "__main__":
+    main()

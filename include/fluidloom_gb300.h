@@ -206,6 +206,41 @@ int fl_merge(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, const
  * (point-location rule of src/adaptation/kernels/balance_enforce.cl:107-143).  subslots 1 or 4. */
 int fl_neighbour_rebuild(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, int subslots, uint32_t* nbr);
 
+/* ---- fields: descriptor, registry, structure-of-arrays manager */
+/* FieldDescriptor (include/fluidloom/core/fields/FieldDescriptor.h:40-83).  type: 0 FLOAT32, 1 FLOAT64,
+ * 2 INT32, 3 INT64, 4 UINT8; avg_rule and solid_scheme as the reference enums. */
+typedef struct fl_field_desc {
+    char name[72];          /* 1..64 characters, NUL-terminated */
+    int32_t type;
+    uint16_t num_components; /* 1..32 */
+    uint8_t halo_depth;     /* 0..2 */
+    uint8_t avg_rule;
+    uint8_t solid_scheme;
+    uint8_t reserved[7];
+    uint64_t id;            /* FNV-1a 64 of the name (include/fluidloom/common/Hash.h:13-22) */
+} fl_field_desc;
+
+/* [host] hash::fnv1a_64 and FieldDescriptor's constructor checks (FieldDescriptor.cpp:8-43). */
+uint64_t fl_fnv1a_64(const char* s);
+int fl_field_make(const char* name, int32_t type, uint16_t components, uint8_t halo_depth, uint8_t avg_rule,
+                  uint8_t solid_scheme, fl_field_desc* out);
+size_t fl_field_bytes_per_cell(const fl_field_desc* desc);
+/* [host] FieldRegistry::instance() (src/core/registry/FieldRegistry.cpp:7-66): register returns
+ * FL_E_CAPACITY when the name exists (the reference's false). */
+int fl_field_register(const fl_field_desc* desc);
+int fl_field_lookup_name(const char* name, fl_field_desc* out);
+int fl_field_lookup_id(uint64_t id, fl_field_desc* out);
+size_t fl_field_registry_count(void);
+void fl_field_registry_clear(void);
+/* SOAFieldManager (include/fluidloom/core/fields/SOAFieldManager.h:26-51), per context:
+ * component-major device storage with a 128-byte aligned pitch; handle = field id. */
+int fl_soa_allocate(fl_ctx* ctx, const fl_field_desc* desc, size_t num_cells, uint64_t* handle);
+int fl_soa_resize(fl_ctx* ctx, uint64_t handle, size_t new_num_cells);
+int fl_soa_deallocate(fl_ctx* ctx, uint64_t handle);
+int fl_soa_device_ptr(fl_ctx* ctx, uint64_t handle, uint16_t component, void** out);
+int fl_soa_info(fl_ctx* ctx, uint64_t handle, size_t* num_cells, size_t* pitch_bytes, uint64_t* version);
+size_t fl_soa_total_bytes(fl_ctx* ctx);
+
 /* ---- same-GPU ghost pack / unpack, interpolation, restriction (fields AoS, C floats per cell) */
 /* pack_fields / unpack_fields (kernels/halo_pack.cl:3-45): float field <-> byte buffer at a byte offset. */
 int fl_pack_fields(fl_ctx* ctx, const float* field, void* packed, size_t num_cells, size_t field_offset_bytes);
@@ -264,6 +299,7 @@ typedef struct fl_pool_info {
     uint64_t fluid_lups_per_step;   /* fluid site updates per level-0 step: sum of 2^level */
     uint64_t population_bytes;
     uint64_t fluid_sites_per_level[16];
+    int32_t num_active_cases;       /* num_cases counts slots, including freed ones */
 } fl_pool_info;
 
 /* Build the cases: level-0 bricks, max_level rounds of sphere-band refinement, equilibrium start. */
@@ -283,8 +319,10 @@ int fl_pool_nbr(fl_ctx* ctx, fl_pool* pool, uint32_t* nbr);
 int fl_pool_flags(fl_ctx* ctx, fl_pool* pool, int32_t* flags, float* wmax);
 /* Per case: fluid mass and momentum (FP64, sites weighted by 8^-level) -> out[ncases][4] (host). */
 int fl_pool_conservation(fl_ctx* ctx, fl_pool* pool, double* out);
-/* Advance nsteps with a CUDA event pair around every collide-stream launch (no graphs); returns
- * the summed kernel time, the launch count and the fluid sites those launches updated. */
+/* Advance nsteps with a CUDA event pair around every collide-stream launch (no graphs); returns,
+ * per kernel ([0] interior bricks, [1] interface/boundary/near-sphere bricks, [2] all-solid bricks),
+ * the summed kernel time, the launch count and the fluid sites those launches updated (each output
+ * an array of 3). */
 int fl_pool_profile_steps(fl_ctx* ctx, fl_pool* pool, int nsteps, double* kernel_ms, uint32_t* launches,
                           uint64_t* fluid_sites);
 /* Replace the populations with a host array [19][n][512] (the layout fl_pool_download gives). */
@@ -292,6 +330,18 @@ int fl_pool_upload(fl_ctx* ctx, fl_pool* pool, const float* f);
 /* Per-case moving-wall and inlet velocities ([ncases][3] host arrays, either may be NULL),
  * copied on the stream and used from the next step on. */
 int fl_pool_set_velocities(fl_ctx* ctx, fl_pool* pool, const float* wall_u, const float* inlet_u);
+/* Regrid only the cases whose due[case id] is non-zero (host array of num_cases bytes); the other
+ * cases come out unchanged. */
+int fl_pool_regrid_cases(fl_ctx* ctx, fl_pool* pool, const uint8_t* due, fl_adapt_stats* stats);
+/* Merge new cases into a running pool at a step boundary: each starts exactly as fl_pool_create
+ * would start it alone; ids[i] receives its case id (freed ids are reused). */
+int fl_pool_add_cases(fl_ctx* ctx, fl_pool* pool, const fl_lbm_case* cases, int ncases, int32_t* ids);
+/* Remove finished cases at a step boundary (their bricks are compacted away). */
+int fl_pool_remove_cases(fl_ctx* ctx, fl_pool* pool, const int32_t* ids, int nids);
+/* Host copies of one case's bricks and populations ([19][nbricks][512]); any pointer may be NULL
+ * except nbricks.  Call with f == NULL first to learn nbricks. */
+int fl_pool_download_case(fl_ctx* ctx, fl_pool* pool, int32_t id, int32_t* x, int32_t* y, int32_t* z,
+                          uint8_t* level, float* f, size_t* nbricks);
 /* use_graphs: replay captured CUDA graphs per level-0 step; grid_mult: CTAs per SM (0 keeps). */
 int fl_pool_set_options(fl_ctx* ctx, fl_pool* pool, int use_graphs, int grid_mult);
 

@@ -1,0 +1,73 @@
+"""Cases merged into / removed from a running pool and per-case regrids: every
+case keeps reproducing its solo run bit for bit (the serving pattern's
+correctness condition)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _cases():
+    from fluidloom_gb300 import lbm
+    a = lbm.cavity(16, 1, u_lid=0.06, tau=0.6)
+    b = lbm.sphere_channel(32, 16, 16, 2, radius=2.0, centre=(8.0, 8.0, 8.0), u_in=0.04, band=2.0)
+    c = lbm.cavity(24, 2, u_lid=0.03, tau=0.55)
+    return a, b, c
+
+
+def _state(pool, cid):
+    g, f = pool.case_state(cid)
+    return g, f
+
+
+def _same(p1, c1, p2, c2):
+    g1, f1 = _state(p1, c1)
+    g2, f2 = _state(p2, c2)
+    for k in ("x", "y", "z", "level"):
+        np.testing.assert_array_equal(g1[k], g2[k])
+    np.testing.assert_array_equal(f1, f2)
+
+
+def test_add_remove_and_per_case_regrid_match_solo(ctx):
+    from fluidloom_gb300.lbm import Pool
+    a, b, c = _cases()
+    mix = Pool(ctx, [a])
+    sa, sb, sc = Pool(ctx, [a]), Pool(ctx, [b]), Pool(ctx, [c])
+    # A runs 3 steps, then B and C join
+    mix.step(3)
+    sa.step(3)
+    ids = mix.add_cases([b, c])
+    assert sorted(ids) == [1, 2]
+    ib, ic = ids
+    _same(mix, 0, sa, 0)
+    _same(mix, ib, sb, 0)
+    _same(mix, ic, sc, 0)
+    # 4 more steps; A regrids alone (B, C not due)
+    mix.step(4)
+    for p in (sa, sb, sc):
+        p.step(4)
+    mix.regrid_cases([0])
+    sa.regrid()
+    _same(mix, 0, sa, 0)
+    _same(mix, ib, sb, 0)
+    _same(mix, ic, sc, 0)
+    # A finishes and leaves; B and C continue, B regrids
+    mix.remove_cases([0])
+    mix.step(2)
+    sb.step(2)
+    sc.step(2)
+    mix.regrid_cases([ib])
+    sb.regrid()
+    _same(mix, ib, sb, 0)
+    _same(mix, ic, sc, 0)
+    # a new case reuses the freed id
+    ids2 = mix.add_cases([a])
+    assert ids2 == [0]
+    sa2 = Pool(ctx, [a])
+    mix.step(2)
+    sa2.step(2)
+    sb.step(2)
+    _same(mix, 0, sa2, 0)
+    _same(mix, ib, sb, 0)
+    info = mix.info()
+    assert info.num_active_cases == 3
