@@ -122,42 +122,6 @@ def ncu_traffic():
 
 
 # ---------------------------------------------------------------- GPU arm
-def dist_setup():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if ws > 1:
-        import torch
-        import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
-    return ws, rank, local, dist
-
-
-def dist_max(dist, v):
-    if dist is None:
-        return v
-    import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
-
-
-def dist_sum(dist, v):
-    if dist is None:
-        return v
-    import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
-
-
-def barrier(dist):
-    if dist is not None:
-        dist.barrier()
-
-
 def timer(ctx):
     import ctypes
     ctx.call("fl_ctx_timer_start")
@@ -237,7 +201,9 @@ def run_gpu(args):
     fbuild.build()
     import fluidloom_gb300 as fl
     from fluidloom_gb300.lbm import Pool
-    ws, rank, local, dist = dist_setup()
+    from fluidloom_gb300.replicas import Replicas
+    rep = Replicas()
+    ws, rank, local = rep.world, rep.rank, rep.local
     ctx = fl.Context(local)
     pool = Pool(ctx, [sphere_case()])
     info = pool.info()
@@ -246,7 +212,7 @@ def run_gpu(args):
     for _ in range(args.warmup):
         pool.step(1)
     ctx.sync()
-    barrier(dist)
+    rep.barrier()
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
@@ -266,9 +232,9 @@ def run_gpu(args):
             regrids += 1
     ms = stop()
     clk = clocks.stop()
-    barrier(dist)
-    ms_max = dist_max(dist, ms)
-    lups_all = dist_sum(dist, float(total_lups))
+    rep.barrier()
+    ms_max = rep.max(ms)
+    lups_all = rep.sum(float(total_lups))
     value = lups_all / (ms_max * 1e-3) / 1e6
     # regrid ms per cycle on this workload (one more regrid, timed alone)
     stop = timer(ctx)
@@ -311,7 +277,7 @@ def run_gpu(args):
     e2e_lups = 0
     pool.step(1)  # graph capture for the uploaded state happens in the loop below
     ctx.sync()
-    barrier(dist)
+    rep.barrier()
     t0 = time.perf_counter()
     stop = timer(ctx)
     ctx.call("fl_pool_upload", pool.h, hp)
@@ -324,8 +290,8 @@ def run_gpu(args):
     e2e_ms = stop()
     e2e_wall = time.perf_counter() - t0
     e2e_ms = max(e2e_ms, e2e_wall * 1e3)
-    e2e_ms = dist_max(dist, e2e_ms)
-    e2e_value = dist_sum(dist, float(e2e_lups)) / (e2e_ms * 1e-3) / 1e6
+    e2e_ms = rep.max(e2e_ms)
+    e2e_value = rep.sum(float(e2e_lups)) / (e2e_ms * 1e-3) / 1e6
     h2d = (fbytes + args.steps * 24) / args.steps
     d2h = (fbytes + args.steps * 32) / args.steps
     ctx.call("fl_host_free_pinned", hp)
@@ -354,8 +320,7 @@ def run_gpu(args):
                 "regrid_ms_per_cycle": round(statistics.mean(regrid_ms), 3), "regrids_in_timed_region": regrids,
                 "regrid_microbench": micro}
         print(json.dumps(line))
-    if dist is not None:
-        dist.destroy_process_group()
+    rep.close()
 
 
 def run_reference(args):

@@ -34,7 +34,9 @@ __device__ __forceinline__ void st_status(unsigned long long* p, unsigned long l
 }
 
 // Warp-wide look-back: returns the exclusive prefix of tile `t` (lane 0 holds it).
-__device__ uint32_t lookback(unsigned long long* status, int t, uint32_t* dev_status) {
+// Gives up after `limit` polls of an unpublished window, records
+// FL_DEVSTAT_TIMEOUT and returns the partial prefix.
+__device__ uint32_t lookback_limited(unsigned long long* status, int t, uint32_t* dev_status, unsigned limit) {
     const int lane = threadIdx.x & 31;
     uint32_t prefix = 0;
     int base = t - 1;
@@ -46,7 +48,7 @@ __device__ uint32_t lookback(unsigned long long* status, int t, uint32_t* dev_st
         while (true) {
             bool ready = (s & kFlagMask) != 0;
             if (__all_sync(0xFFFFFFFFu, ready)) break;
-            if (++spins > FL_SPIN_LIMIT) {
+            if (++spins > limit) {
                 if (lane == 0) atomicAdd(dev_status + FL_DEVSTAT_TIMEOUT, 1u);
                 return prefix;
             }
@@ -61,6 +63,16 @@ __device__ uint32_t lookback(unsigned long long* status, int t, uint32_t* dev_st
         base -= 32;
     }
     return prefix;
+}
+
+__device__ __forceinline__ uint32_t lookback(unsigned long long* status, int t, uint32_t* dev_status) {
+    return lookback_limited(status, t, dev_status, FL_SPIN_LIMIT);
+}
+
+// One warp looks back from tile 1 at a tile-0 word that nothing publishes:
+// the wait runs out after `limit` polls and the kernel returns normally.
+__global__ void k_lookback_probe(unsigned long long* status, uint32_t* dev_status, unsigned limit) {
+    lookback_limited(status, 1, dev_status, limit);
 }
 
 template <typename Load>
@@ -230,6 +242,16 @@ int fl_scan_exclusive_u32(fl_ctx* ctx, const uint32_t* in, uint32_t* out, size_t
     int rc = fl_scratch_reserve(ctx, fl_scan_scratch_bytes(n));
     if (rc) return rc;
     return fl_scan_u32_with(ctx, in, out, n, total, ctx->scratch);
+}
+
+int fl_lookback_timeout_probe(fl_ctx* ctx, uint32_t spin_limit) {
+    if (!ctx || spin_limit == 0 || spin_limit > FL_SPIN_LIMIT) return FL_E_INVALID_ARG;
+    int rc = fl_scratch_reserve(ctx, 256);
+    if (rc) return rc;
+    FL_TRY_CUDA(ctx, cudaMemsetAsync(ctx->scratch, 0, 256, ctx->stream), "probe clear");
+    k_lookback_probe<<<1, 32, 0, ctx->stream>>>((unsigned long long*)ctx->scratch, ctx->dev_status, spin_limit);
+    FL_CHECK_LAUNCH(ctx, "k_lookback_probe");
+    return fl_collect_device_status(ctx, "fl_lookback_timeout_probe");
 }
 
 int fl_compact_and_permute(fl_ctx* ctx, const uint64_t* keys, const uint32_t* state, size_t n, uint32_t* perm,

@@ -102,6 +102,11 @@ int fl_scan_exclusive_u32(fl_ctx* ctx, const uint32_t* in, uint32_t* out, size_t
  * array's device address: make that first call before any stream capture.  All calls share the
  * array, so calls that overlap on the GPU (other threads or streams) race. */
 int fl_scan_exclusive_u32_noalloc(const uint32_t* in, uint32_t* out, size_t n, uint32_t* total, void* cuda_stream);
+/* Failure-detection check of the bounded device waits (no reference counterpart: the reference
+ * has no device-side wait limits): one warp polls a look-back word that nothing publishes; after
+ * spin_limit polls it records a timeout and exits, and the call returns FL_E_DEVICE_TIMEOUT with
+ * the context still usable. */
+int fl_lookback_timeout_probe(fl_ctx* ctx, uint32_t spin_limit);
 /* Stable ascending LSD radix sort of (key, value) pairs in place on bits [begin_bit, end_bit).
  * Replaces RadixSort::sortByKey (include/fluidloom/core/hashmap/RadixSort.h:33-35). */
 int fl_sort_pairs_u64_u32(fl_ctx* ctx, uint64_t* keys, uint32_t* vals, size_t n, int begin_bit, int end_bit);
