@@ -132,99 +132,12 @@ struct StepArgs {
     const uint32_t* nbr;  // [n][26][4]
     const LbmCaseDev* cases;
     uint32_t* dev_status;
+    const uint64_t* desc;      // stencil descriptors of the general class (k_slow_table)
+    const uint32_t* desc_off;  // per list position: first descriptor; [count] = end
+    const uint32_t* smask;     // [n][16]: own sites inside the sphere
 };
 
 __device__ __forceinline__ size_t fidx(size_t cap, int q, size_t b, int s) { return ((size_t)q * cap + b) * 512 + s; }
-
-// Pull of population q for a site whose source leaves the brick through a
-// non-same-level face/edge/corner, or the domain (oracle: or_lbm.cpp pull()).
-__device__ __noinline__ float pull_slow(const StepArgs& a, const LbmCaseDev& c, uint32_t b, int q, int l,
-                                        const int64_t* G, int s_local) {
-    int64_t S[3] = {G[0] - CXq(q), G[1] - CYq(q), G[2] - CZq(q)};
-    int64_t N[3];
-    for (int ax = 0; ax < 3; ++ax) N[ax] = ((int64_t)c.ext[ax] * 8) << l;
-    int out_face[3] = {-1, -1, -1};
-    bool out = false;
-    for (int ax = 0; ax < 3; ++ax) {
-        if (c.periodic[ax]) continue;
-        if (S[ax] < 0) { out_face[ax] = 2 * ax; out = true; }
-        else if (S[ax] >= N[ax]) { out_face[ax] = 2 * ax + 1; out = true; }
-    }
-    if (out) {
-        bool inlet = false, outlet = false;
-        int moving = -1;
-        for (int ax = 0; ax < 3; ++ax) {
-            if (out_face[ax] < 0) continue;
-            int bt = c.bc[out_face[ax]];
-            if (bt == 3) inlet = true;
-            else if (bt == 4) outlet = true;
-            else if (bt == 2 && moving < 0) moving = out_face[ax];
-        }
-        if (inlet) {
-            float base = base_of(c.inlet_u[0], c.inlet_u[1], c.inlet_u[2]);
-            return feq1(q, 1.0f, c.inlet_u[0], c.inlet_u[1], c.inlet_u[2], base);
-        }
-        if (outlet) return a.R[fidx(a.cap, q, b, s_local)];
-        float v = a.R[fidx(a.cap, OPPq(q), b, s_local)];
-        if (moving >= 0) {
-            float cu = cdot(q, c.wall_u[0], c.wall_u[1], c.wall_u[2]);
-            float t = 6.0f * Wq(q);
-            t = t * cu;
-            v = v + t;
-        }
-        return v;
-    }
-    int64_t Sw[3];  // the source is one site from G: wrapping is one add or subtract
-    for (int ax = 0; ax < 3; ++ax)
-        Sw[ax] = !c.periodic[ax] ? S[ax] : (S[ax] < 0 ? S[ax] + N[ax] : (S[ax] >= N[ax] ? S[ax] - N[ax] : S[ax]));
-    if (solid_at(c, Sw[0], Sw[1], Sw[2], l)) return a.R[fidx(a.cap, OPPq(q), b, s_local)];
-    int64_t Lc[3] = {S[0] - (int64_t)a.bx[b] * 8, S[1] - (int64_t)a.by[b] * 8, S[2] - (int64_t)a.bz[b] * 8};
-    if (Lc[0] >= 0 && Lc[0] < 8 && Lc[1] >= 0 && Lc[1] < 8 && Lc[2] >= 0 && Lc[2] < 8)
-        return a.R[fidx(a.cap, q, b, (int)(Lc[0] + 8 * Lc[1] + 64 * Lc[2]))];
-    int d[3], sub_slot = 0, bit = 0;
-    for (int ax = 0; ax < 3; ++ax) {
-        d[ax] = Lc[ax] < 0 ? -1 : (Lc[ax] >= 8 ? 1 : 0);
-        if (d[ax] == 0) { if (Lc[ax] >= 4) sub_slot |= 1 << bit; ++bit; }
-    }
-    int kk = (d[2] + 1) * 9 + (d[1] + 1) * 3 + (d[0] + 1);
-    int k = kk < 13 ? kk : kk - 1;
-    uint32_t nb = a.nbr[((size_t)b * 26 + k) * 4 + sub_slot];
-    if (nb == FL_INVALID_INDEX) return a.R[fidx(a.cap, OPPq(q), b, s_local)];
-    int ln = a.blevel[nb];
-    if (ln == l) {
-        int64_t lx = Sw[0] - (int64_t)a.bx[nb] * 8, ly = Sw[1] - (int64_t)a.by[nb] * 8, lz = Sw[2] - (int64_t)a.bz[nb] * 8;
-        return a.R[fidx(a.cap, q, nb, (int)(lx + 8 * ly + 64 * lz))];
-    }
-    if (ln == l - 1) {
-        int64_t lx = (Sw[0] >> 1) - (int64_t)a.bx[nb] * 8, ly = (Sw[1] >> 1) - (int64_t)a.by[nb] * 8,
-                lz = (Sw[2] >> 1) - (int64_t)a.bz[nb] * 8;
-        if (lx < 0 || lx > 7 || ly < 0 || ly > 7 || lz < 0 || lz > 7) {
-            atomicAdd(a.dev_status + FL_DEVSTAT_BOUNDS, 1u);
-            return a.R[fidx(a.cap, OPPq(q), b, s_local)];
-        }
-        size_t i = fidx(a.cap, q, nb, (int)(lx + 8 * ly + 64 * lz));
-        if (a.sub == 0) return a.Cold[i];
-        float t = a.Cold[i] + a.Cnew[i];
-        return t * 0.5f;
-    }
-    if (ln == l + 1) {
-        float sum = 0.0f;
-#pragma unroll
-        for (int kq = 0; kq < 8; ++kq) {
-            int64_t lx = 2 * Sw[0] + (kq & 1) - (int64_t)a.bx[nb] * 8;
-            int64_t ly = 2 * Sw[1] + ((kq >> 1) & 1) - (int64_t)a.by[nb] * 8;
-            int64_t lz = 2 * Sw[2] + ((kq >> 2) & 1) - (int64_t)a.bz[nb] * 8;
-            if (lx < 0 || lx > 7 || ly < 0 || ly > 7 || lz < 0 || lz > 7) {
-                atomicAdd(a.dev_status + FL_DEVSTAT_BOUNDS, 1u);
-                return a.R[fidx(a.cap, OPPq(q), b, s_local)];
-            }
-            sum = sum + a.Fine[fidx(a.cap, q, nb, (int)(lx + 8 * ly + 64 * lz))];
-        }
-        return sum * 0.125f;
-    }
-    atomicAdd(a.dev_status + FL_DEVSTAT_LEVEL_JUMP, 1u);
-    return a.R[fidx(a.cap, OPPq(q), b, s_local)];
-}
 
 // Could a site of brick b, or a source one site outside it, lie in the sphere?
 // Minimal-image distance on periodic axes; a margin of two sites.
@@ -249,125 +162,73 @@ __device__ __forceinline__ int brick_near_sphere(const LbmCaseDev& c, int32_t bx
     return dm <= rr * rr ? 1 : 0;
 }
 
-// Source of population q one site upstream of global site G, wrapped on
-// periodic axes (|offset| <= 1).
-__device__ __forceinline__ bool solid_source(const LbmCaseDev& c, int q, const int64_t* G, int l) {
-    int64_t S[3] = {G[0] - CXq(q), G[1] - CYq(q), G[2] - CZq(q)};
-    for (int ax = 0; ax < 3; ++ax) {
-        if (!c.periodic[ax]) continue;
-        int64_t N = ((int64_t)c.ext[ax] * 8) << l;
-        S[ax] = S[ax] < 0 ? S[ax] + N : (S[ax] >= N ? S[ax] - N : S[ax]);
-    }
-    return solid_at(c, S[0], S[1], S[2], l);
-}
-
-// One CTA per brick (persistent over the level's list), 128 threads; thread t
-// owns the x-quad x0 = 4(t & 1), y = (t >> 1) & 7, z = t >> 4.  For each
-// population the quad's upstream row is one 128-bit load from this brick or a
-// same-level neighbour; the x-shift comes from the partner lane (the other
-// half of the row) by shuffle, and only the quad at the brick's x face loads
-// one more value from the x-neighbour.  Bricks whose 18 face/edge neighbours
-// are all same-level and that cannot see the sphere take this path with no
-// per-site checks; others check each element and fall back to pull_slow for
-// sources across a level interface, outside the domain or in the sphere.
+// Bit (x+1) + 10(y+1) + 100(z+1) of the 10^3 solid mask of a brick and its
+// one-site halo, x, y, z in [-1, 8].
 __device__ __forceinline__ int solid_bit(const uint32_t* s_solid, int x, int y, int z) {
     int i = (x + 1) + 10 * (y + 1) + 100 * (z + 1);
     return (s_solid[i >> 5] >> (i & 31)) & 1;
 }
 
-template <bool GENERAL>
-__device__ __forceinline__ void gather_quad(const StepArgs& a, const LbmCaseDev& c, const uint32_t* s_nb, uint32_t b,
-                                            int l, int near, int x0, int y, int z, const int64_t* G0,
-                                            const uint32_t* s_solid, float (&f)[Q][4]) {
+// The upstream row of population q for the x-quad (x0..x0+3, y, z) of the
+// brick whose 27-entry same-level neighbour row is s_nb: one 128-bit load from
+// this brick or a same-level neighbour, the x-shift from the partner lane (the
+// other half of the row) by shuffle, and one extra scalar load at the brick's
+// x face.  Every entry of s_nb must name a brick (callers replace missing
+// neighbours by the brick itself and overwrite those elements afterwards).
+template <int Q0, int Q1>
+__device__ __forceinline__ void gather_quad(const StepArgs& a, const uint32_t* s_nb, int x0, int y, int z,
+                                            float (&f)[Q][4]) {
     const int lane_odd = x0 != 0;
 #pragma unroll
-    for (int q = 0; q < Q; ++q) {
+    for (int q = Q0; q < Q1; ++q) {
         const int cx = CXq(q), cy = CYq(q), cz = CZq(q);
         const int sy = y - cy, sz = z - cz;
         const int dy = sy >> 3, dz = sz >> 3;
         const int rowoff = (sy & 7) * 8 + (sz & 7) * 64;
         const uint32_t erow = s_nb[(dz + 1) * 9 + (dy + 1) * 3 + 1];
-        const bool rowok = !GENERAL || erow != kSlow;
-        float4 A = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (rowok) A = __ldg((const float4*)(a.R + fidx(a.cap, q, erow, rowoff + x0)));
-        float v[4];
+        const float4 A = __ldg((const float4*)(a.R + fidx(a.cap, q, erow, rowoff + x0)));
         if (cx == 0) {
-            v[0] = A.x; v[1] = A.y; v[2] = A.z; v[3] = A.w;
+            f[q][0] = A.x; f[q][1] = A.y; f[q][2] = A.z; f[q][3] = A.w;
         } else if (cx == 1) {
-            float pw = __shfl_xor_sync(0xFFFFFFFFu, A.w, 1);
-            float h = pw;
-            if (!lane_odd) {  // x = -1: last column of the -x neighbour's row
-                uint32_t ex = s_nb[(dz + 1) * 9 + (dy + 1) * 3 + 0];
-                if (!GENERAL || ex != kSlow) h = __ldg(a.R + fidx(a.cap, q, ex, rowoff + 7));
-            }
-            v[0] = h; v[1] = A.x; v[2] = A.y; v[3] = A.z;
+            float h = __shfl_xor_sync(0xFFFFFFFFu, A.w, 1);
+            if (!lane_odd)  // x = -1: last column of the -x neighbour's row
+                h = __ldg(a.R + fidx(a.cap, q, s_nb[(dz + 1) * 9 + (dy + 1) * 3 + 0], rowoff + 7));
+            f[q][0] = h; f[q][1] = A.x; f[q][2] = A.y; f[q][3] = A.z;
         } else {
-            float px = __shfl_xor_sync(0xFFFFFFFFu, A.x, 1);
-            float h = px;
-            if (lane_odd) {  // x = 8: first column of the +x neighbour's row
-                uint32_t ex = s_nb[(dz + 1) * 9 + (dy + 1) * 3 + 2];
-                if (!GENERAL || ex != kSlow) h = __ldg(a.R + fidx(a.cap, q, ex, rowoff + 0));
-            }
-            v[0] = A.y; v[1] = A.z; v[2] = A.w; v[3] = h;
+            float h = __shfl_xor_sync(0xFFFFFFFFu, A.x, 1);
+            if (lane_odd)  // x = 8: first column of the +x neighbour's row
+                h = __ldg(a.R + fidx(a.cap, q, s_nb[(dz + 1) * 9 + (dy + 1) * 3 + 2], rowoff + 0));
+            f[q][0] = A.y; f[q][1] = A.z; f[q][2] = A.w; f[q][3] = h;
         }
-        if (GENERAL) {
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const int xi = x0 + i - cx;  // source x inside [-1, 8]
-                const int dx = xi >> 3;
-                const uint32_t e = (dx == 0) ? erow : s_nb[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)];
-                const int64_t G[3] = {G0[0] + x0 + i, G0[1] + y, G0[2] + z};
-                const int s_own = x0 + i + 8 * y + 64 * z;
-                if (e == kSlow) {
-                    v[i] = pull_slow(a, c, b, q, l, G, s_own);
-                } else if (near && solid_bit(s_solid, xi, sy, sz)) {
-                    v[i] = a.R[fidx(a.cap, OPPq(q), b, s_own)];
-                }
-            }
-        }
-#pragma unroll
-        for (int i = 0; i < 4; ++i) f[q][i] = v[i];
     }
 }
 
-// Collision of the gathered x-quad and the 128-bit stores (shared by both kernels).
-__device__ __forceinline__ void collide_store(const StepArgs& a, const LbmCaseDev& c, uint32_t b, int l, int x0,
-                                              int y, int z, const uint32_t* s_solid, int near, float (&f)[Q][4]) {
-    const float omega = c.omega[l];
+// BGK relaxation of one site in place (solid sites take the rest equilibrium).
+__device__ __forceinline__ void relax_site(float (&g)[Q], float omega, bool solid) {
+    float rho, jx, jy, jz;
+    moments(g, rho, jx, jy, jz);
+    float inv = 1.0f / rho;
+    float ux = jx * inv, uy = jy * inv, uz = jz * inv;
+    float base = base_of(ux, uy, uz);
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        bool solid = near && solid_bit(s_solid, x0 + i, y, z);
-        float rho, jx, jy, jz;
-        {
-            float g[Q];
-#pragma unroll
-            for (int q = 0; q < Q; ++q) g[q] = f[q][i];
-            moments(g, rho, jx, jy, jz);
-        }
-        float inv = 1.0f / rho;
-        float ux = jx * inv, uy = jy * inv, uz = jz * inv;
-        float base = base_of(ux, uy, uz);
-#pragma unroll
-        for (int q = 0; q < Q; ++q) {  // outputs overwrite the inputs in place
-            float fe = feq1(q, rho, ux, uy, uz, base);
-            float dd = fe - f[q][i];
-            dd = omega * dd;
-            f[q][i] = solid ? Wq(q) : f[q][i] + dd;
-        }
+    for (int q = 0; q < Q; ++q) {
+        float fe = feq1(q, rho, ux, uy, uz, base);
+        float dd = fe - g[q];
+        dd = omega * dd;
+        g[q] = solid ? Wq(q) : g[q] + dd;
     }
-    const int own = x0 + 8 * y + 64 * z;
-#pragma unroll
-    for (int q = 0; q < Q; ++q)
-        *(float4*)(a.W + fidx(a.cap, q, b, own)) = make_float4(f[q][0], f[q][1], f[q][2], f[q][3]);
 }
 
 // Interior bricks: all 18 face/edge neighbours at this level, no sphere in
-// reach.  The 27-entry neighbour row comes precomputed (k_brick_table).
+// reach.  One CTA per brick (persistent over the level's list), 128 threads;
+// thread t owns the x-quad x0 = 4(t & 1), y = (t >> 1) & 7, z = t >> 4.  The
+// 27-entry neighbour row comes precomputed (k_brick_table).
 __global__ void __launch_bounds__(128, 4) k_collide_fast(StepArgs a, const uint32_t* __restrict__ nb27) {
     __shared__ uint32_t s_nb[27];
     const int l = a.level;
     const int t = threadIdx.x;
     const int x0 = (t & 1) * 4, y = (t >> 1) & 7, z = t >> 4;
+    const int own = x0 + 8 * y + 64 * z;
     // software pipeline: the next brick's list entry and neighbour row are
     // loaded while the current brick is gathered and relaxed
     uint32_t w = blockIdx.x;
@@ -379,23 +240,63 @@ __global__ void __launch_bounds__(128, 4) k_collide_fast(StepArgs a, const uint3
         const uint32_t wn = w + gridDim.x;
         const uint32_t bn = wn < a.count ? a.list[wn] : 0u;
         if (wn < a.count && t < 27) row = nb27[(size_t)bn * 28 + t];
-        const LbmCaseDev& c = a.cases[a.bcase[b]];
+        const float omega = a.cases[a.bcase[b]].omega[l];
         float f[Q][4];
-        gather_quad<false>(a, c, s_nb, b, l, 0, x0, y, z, nullptr, nullptr, f);
-        collide_store(a, c, b, l, x0, y, z, nullptr, 0, f);
+        gather_quad<0, Q>(a, s_nb, x0, y, z, f);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            float g[Q];
+#pragma unroll
+            for (int q = 0; q < Q; ++q) g[q] = f[q][i];
+            relax_site(g, omega, false);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) f[q][i] = g[q];
+        }
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+            *(float4*)(a.W + fidx(a.cap, q, b, own)) = make_float4(f[q][0], f[q][1], f[q][2], f[q][3]);
         __syncthreads();
         b = bn;
     }
 }
 
-// Pull across a level interface, a domain boundary or into the sphere for one
-// element (oracle: or_lbm.cpp pull()), with the brick's 26x4 neighbour table
-// and the neighbours' levels staged in shared memory.
-__device__ __noinline__ float pull_general(const StepArgs& a, const LbmCaseDev& c, uint32_t b, int q, int l,
-                                           const int64_t* G, int s_own, const uint32_t* s_nbr, const uint8_t* s_nlv,
-                                           const uint32_t* s_solid, int near, int lx, int ly, int lz) {
-    const int cx = CXq(q), cy = CYq(q), cz = CZq(q);
-    int64_t S[3] = {G[0] - cx, G[1] - cy, G[2] - cz};
+// Stencil descriptors.  For the bricks of the general class, every element
+// (population q of site s) whose upstream source is not a plain same-level
+// load -- a source across a level interface, outside the domain or inside the
+// sphere -- is resolved once per topology into one 64-bit word:
+//   bits  0-31  source element (brick * 512 + site) within its population plane
+//   bits 32-40  site s, bits 41-45 q, bits 46-48 kind
+// so that a step only replays loads and the boundary arithmetic.  The
+// resolution follows the oracle's pull() (or_lbm.cpp) branch for branch.
+enum : uint32_t {
+    kSrcSame = 0,    // R[q][src]: same-level neighbour (across a periodic wrap, or a corner)
+    kSrcCoarse = 1,  // coarser neighbour: Cold[q][src], or (Cold + Cnew) / 2 on the second sub-step
+    kSrcFine = 2,    // finer neighbour: mean of the 2x2x2 children at src + {0,1,8,9,64,65,72,73}
+    kSrcBounce = 3,  // R[opp q][src]: half-way bounce-back (wall, sphere, missing neighbour)
+    kSrcWall = 4,    // R[opp q][src] + 6 w_q (c_q . u_wall): moving wall
+    kSrcInlet = 5,   // feq(1, u_inlet)
+    kSrcOutlet = 6,  // R[q][src]: zero-gradient outlet (own site)
+};
+
+__device__ __forceinline__ uint64_t make_desc(uint32_t kind, int q, int s, uint32_t src) {
+    return (uint64_t)src | ((uint64_t)s << 32) | ((uint64_t)q << 41) | ((uint64_t)kind << 46);
+}
+
+struct BrickTopo {
+    uint32_t nbr[104];  // 26 directions x 4 sub-slots
+    uint8_t nlv[104];   // their levels (0xFF: none)
+    uint32_t nb27[27];
+    uint32_t solid[32];  // 10^3 bits: the brick and its one-site halo
+    int near;
+};
+
+__device__ uint64_t resolve_source(const LbmCaseDev& c, const int32_t* bx, const int32_t* by, const int32_t* bz,
+                                   uint32_t b, int q, int l, int s, const int64_t* G0, const BrickTopo& T,
+                                   uint32_t* dev_status) {
+    const uint32_t own = b * 512u + (uint32_t)s;
+    const int sx = s & 7, sy = (s >> 3) & 7, sz = s >> 6;
+    const int lx = sx - CXq(q), ly = sy - CYq(q), lz = sz - CZq(q);
+    int64_t S[3] = {G0[0] + lx, G0[1] + ly, G0[2] + lz};
     int64_t N[3];
     for (int ax = 0; ax < 3; ++ax) N[ax] = ((int64_t)c.ext[ax] * 8) << l;
     int out_face[3] = {-1, -1, -1};
@@ -406,35 +307,24 @@ __device__ __noinline__ float pull_general(const StepArgs& a, const LbmCaseDev& 
         else if (S[ax] >= N[ax]) { out_face[ax] = 2 * ax + 1; out = true; }
     }
     if (out) {
-        bool inlet = false, outlet = false;
-        int moving = -1;
+        bool inlet = false, outlet = false, moving = false;
         for (int ax = 0; ax < 3; ++ax) {
             if (out_face[ax] < 0) continue;
             int bt = c.bc[out_face[ax]];
             if (bt == 3) inlet = true;
             else if (bt == 4) outlet = true;
-            else if (bt == 2 && moving < 0) moving = out_face[ax];
+            else if (bt == 2) moving = true;
         }
-        if (inlet) {
-            float base = base_of(c.inlet_u[0], c.inlet_u[1], c.inlet_u[2]);
-            return feq1(q, 1.0f, c.inlet_u[0], c.inlet_u[1], c.inlet_u[2], base);
-        }
-        if (outlet) return a.R[fidx(a.cap, q, b, s_own)];
-        float v = a.R[fidx(a.cap, OPPq(q), b, s_own)];
-        if (moving >= 0) {
-            float cu = cdot(q, c.wall_u[0], c.wall_u[1], c.wall_u[2]);
-            float t = 6.0f * Wq(q);
-            t = t * cu;
-            v = v + t;
-        }
-        return v;
+        if (inlet) return make_desc(kSrcInlet, q, s, 0u);
+        if (outlet) return make_desc(kSrcOutlet, q, s, own);
+        return make_desc(moving ? kSrcWall : kSrcBounce, q, s, own);
     }
     int64_t Sw[3];  // the source is one site from G: wrapping is one add or subtract
     for (int ax = 0; ax < 3; ++ax)
         Sw[ax] = !c.periodic[ax] ? S[ax] : (S[ax] < 0 ? S[ax] + N[ax] : (S[ax] >= N[ax] ? S[ax] - N[ax] : S[ax]));
-    if (near && solid_bit(s_solid, lx, ly, lz)) return a.R[fidx(a.cap, OPPq(q), b, s_own)];
+    if (T.near && solid_bit(T.solid, lx, ly, lz)) return make_desc(kSrcBounce, q, s, own);
     if (lx >= 0 && lx < 8 && ly >= 0 && ly < 8 && lz >= 0 && lz < 8)
-        return a.R[fidx(a.cap, q, b, lx + 8 * ly + 64 * lz)];
+        return make_desc(kSrcSame, q, s, b * 512u + (uint32_t)(lx + 8 * ly + 64 * lz));
     int d[3] = {lx < 0 ? -1 : (lx >= 8 ? 1 : 0), ly < 0 ? -1 : (ly >= 8 ? 1 : 0), lz < 0 ? -1 : (lz >= 8 ? 1 : 0)};
     int L3[3] = {lx, ly, lz};
     int sub_slot = 0, bit = 0;
@@ -442,158 +332,230 @@ __device__ __noinline__ float pull_general(const StepArgs& a, const LbmCaseDev& 
         if (d[ax] == 0) { if (L3[ax] >= 4) sub_slot |= 1 << bit; ++bit; }
     int kk = (d[2] + 1) * 9 + (d[1] + 1) * 3 + (d[0] + 1);
     int k = kk < 13 ? kk : kk - 1;
-    uint32_t nb = s_nbr[k * 4 + sub_slot];
-    if (nb == FL_INVALID_INDEX) return a.R[fidx(a.cap, OPPq(q), b, s_own)];
-    int ln = s_nlv[k * 4 + sub_slot];
-    int64_t nx = (int64_t)a.bx[nb] * 8, ny = (int64_t)a.by[nb] * 8, nz = (int64_t)a.bz[nb] * 8;
-    if (ln == l) return a.R[fidx(a.cap, q, nb, (int)((Sw[0] - nx) + 8 * (Sw[1] - ny) + 64 * (Sw[2] - nz)))];
+    uint32_t nb = T.nbr[k * 4 + sub_slot];
+    if (nb == FL_INVALID_INDEX) return make_desc(kSrcBounce, q, s, own);
+    int ln = T.nlv[k * 4 + sub_slot];
+    int64_t nx = (int64_t)bx[nb] * 8, ny = (int64_t)by[nb] * 8, nz = (int64_t)bz[nb] * 8;
+    if (ln == l)
+        return make_desc(kSrcSame, q, s, nb * 512u + (uint32_t)((Sw[0] - nx) + 8 * (Sw[1] - ny) + 64 * (Sw[2] - nz)));
     if (ln == l - 1) {
         int64_t px = (Sw[0] >> 1) - nx, py = (Sw[1] >> 1) - ny, pz = (Sw[2] >> 1) - nz;
         if (px < 0 || px > 7 || py < 0 || py > 7 || pz < 0 || pz > 7) {
-            atomicAdd(a.dev_status + FL_DEVSTAT_BOUNDS, 1u);
-            return a.R[fidx(a.cap, OPPq(q), b, s_own)];
+            atomicAdd(dev_status + FL_DEVSTAT_BOUNDS, 1u);
+            return make_desc(kSrcBounce, q, s, own);
         }
-        size_t i = fidx(a.cap, q, nb, (int)(px + 8 * py + 64 * pz));
-        if (a.sub == 0) return a.Cold[i];
-        float t = a.Cold[i] + a.Cnew[i];
-        return t * 0.5f;
+        return make_desc(kSrcCoarse, q, s, nb * 512u + (uint32_t)(px + 8 * py + 64 * pz));
     }
-    if (ln == l + 1) {
-        float sum = 0.0f;
-        for (int kq = 0; kq < 8; ++kq) {
-            int64_t px = 2 * Sw[0] + (kq & 1) - nx;
-            int64_t py = 2 * Sw[1] + ((kq >> 1) & 1) - ny;
-            int64_t pz = 2 * Sw[2] + ((kq >> 2) & 1) - nz;
-            if (px < 0 || px > 7 || py < 0 || py > 7 || pz < 0 || pz > 7) {
-                atomicAdd(a.dev_status + FL_DEVSTAT_BOUNDS, 1u);
-                return a.R[fidx(a.cap, OPPq(q), b, s_own)];
-            }
-            sum = sum + a.Fine[fidx(a.cap, q, nb, (int)(px + 8 * py + 64 * pz))];
+    if (ln == l + 1) {  // children 2S .. 2S+1 per axis; 2S - n is even, so one test per axis
+        int64_t px = 2 * Sw[0] - nx, py = 2 * Sw[1] - ny, pz = 2 * Sw[2] - nz;
+        if (px < 0 || px > 6 || py < 0 || py > 6 || pz < 0 || pz > 6) {
+            atomicAdd(dev_status + FL_DEVSTAT_BOUNDS, 1u);
+            return make_desc(kSrcBounce, q, s, own);
         }
-        return sum * 0.125f;
+        return make_desc(kSrcFine, q, s, nb * 512u + (uint32_t)(px + 8 * py + 64 * pz));
     }
-    atomicAdd(a.dev_status + FL_DEVSTAT_LEVEL_JUMP, 1u);
-    return a.R[fidx(a.cap, OPPq(q), b, s_own)];
+    atomicAdd(dev_status + FL_DEVSTAT_LEVEL_JUMP, 1u);
+    return make_desc(kSrcBounce, q, s, own);
 }
 
-// Bricks at a level interface, a domain boundary or near the sphere, in three
-// passes: (1) every element is gathered as in the interior kernel, with
-// missing same-level neighbours replaced by the brick itself so every load
-// stays in bounds, and the elements whose source crosses an interface or the
-// domain boundary, or lies in the sphere, are queued in shared memory;
-// (2) the queue is resolved in parallel by pull_general (independent loads,
-// so their latencies overlap); (3) the collision reads the staged values.
-struct GeneralSmem {
-    float f[Q][512];
-    uint16_t queue[Q * 512];  // q << 9 | site
-    uint32_t nbr[104];
-    uint8_t nlv[104];
-    uint32_t nb27[27];
-    uint32_t safe27[27];
-    uint32_t solid[32];
-    int near;
-    unsigned count;
-};
-
-__global__ void __launch_bounds__(128, 3) k_collide_general(StepArgs a, const uint32_t* __restrict__ nb27) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    GeneralSmem& S = *reinterpret_cast<GeneralSmem*>(smem_raw);
-    const int l = a.level;
-    const int t = threadIdx.x;
-    const int x0 = (t & 1) * 4, y = (t >> 1) & 7, z = t >> 4;
-    const int own = x0 + 8 * y + 64 * z;
-    for (uint32_t w = blockIdx.x; w < a.count; w += gridDim.x) {
-        const uint32_t b = a.list[w];
-        const LbmCaseDev& c = a.cases[a.bcase[b]];
-        if (t < 27) {
-            uint32_t e = nb27[(size_t)b * 28 + t];
-            S.nb27[t] = e;
-            S.safe27[t] = e == kSlow ? b : e;
+// Per list position p (one CTA of 512 threads per brick, thread = site): for
+// bricks of the general class, COUNT writes the number of descriptors to
+// cnt[p] and the brick's own-site solid mask (16 words), EMIT writes the
+// descriptors from desc + off[p] in site-major, q-minor order.  Sites inside
+// the sphere get none: their relaxation ignores what they pulled.
+template <bool EMIT>
+__global__ void __launch_bounds__(512) k_slow_table(size_t n, const uint32_t* __restrict__ list,
+                                                    const uint8_t* __restrict__ bclass, const uint32_t* __restrict__ nbr,
+                                                    const uint8_t* __restrict__ blevel, const int32_t* __restrict__ bx,
+                                                    const int32_t* __restrict__ by, const int32_t* __restrict__ bz,
+                                                    const uint16_t* __restrict__ bcase,
+                                                    const LbmCaseDev* __restrict__ cases,
+                                                    const uint32_t* __restrict__ nb27, uint32_t* __restrict__ cnt,
+                                                    uint32_t* __restrict__ smask, const uint32_t* __restrict__ off,
+                                                    uint64_t* __restrict__ desc, uint32_t* dev_status) {
+    __shared__ BrickTopo T;
+    __shared__ uint32_t warp_sum[16];
+    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    for (size_t p = blockIdx.x; p < n; p += gridDim.x) {
+        const uint32_t b = list[p];
+        if (bclass[b] != 1) {
+            if (!EMIT && t == 0) cnt[p] = 0;
+            continue;
         }
+        const int l = blevel[b];
+        const LbmCaseDev& c = cases[bcase[b]];
         if (t < 104) {
-            uint32_t nb = a.nbr[(size_t)b * 104 + t];
-            S.nbr[t] = nb;
-            S.nlv[t] = nb == FL_INVALID_INDEX ? 0xFF : a.blevel[nb];
+            uint32_t nb = nbr[(size_t)b * 104 + t];
+            T.nbr[t] = nb;
+            T.nlv[t] = nb == FL_INVALID_INDEX ? 0xFF : blevel[nb];
         }
-        if (t < 32) S.solid[t] = 0u;
-        if (t == 32) {
-            S.near = brick_near_sphere(c, a.bx[b], a.by[b], a.bz[b], l);
-            S.count = 0;
-        }
+        if (t < 27) T.nb27[t] = nb27[(size_t)b * 28 + t];
+        if (t < 32) T.solid[t] = 0u;
+        if (t == 32) T.near = brick_near_sphere(c, bx[b], by[b], bz[b], l);
         __syncthreads();
-        const int near = S.near;
-        const int64_t G0[3] = {(int64_t)a.bx[b] * 8, (int64_t)a.by[b] * 8, (int64_t)a.bz[b] * 8};
+        const int near = T.near;
+        const int64_t G0[3] = {(int64_t)bx[b] * 8, (int64_t)by[b] * 8, (int64_t)bz[b] * 8};
         if (near) {
-            for (int i = t; i < 1000; i += 128) {
+            for (int i = t; i < 1000; i += 512) {
                 int64_t G[3] = {G0[0] + i % 10 - 1, G0[1] + (i / 10) % 10 - 1, G0[2] + i / 100 - 1};
                 for (int ax = 0; ax < 3; ++ax) {
                     if (!c.periodic[ax]) continue;
                     int64_t N = ((int64_t)c.ext[ax] * 8) << l;
                     G[ax] = G[ax] < 0 ? G[ax] + N : (G[ax] >= N ? G[ax] - N : G[ax]);
                 }
-                if (solid_at(c, G[0], G[1], G[2], l)) atomicOr(&S.solid[i >> 5], 1u << (i & 31));
+                if (solid_at(c, G[0], G[1], G[2], l)) atomicOr(&T.solid[i >> 5], 1u << (i & 31));
             }
-            __syncthreads();
         }
-        // pass 1: in-bounds gathers for every element, queue the ones that need pull_general
+        __syncthreads();
+        const int s = t, x = s & 7, y = (s >> 3) & 7, z = s >> 6;
+        const bool own_solid = near && solid_bit(T.solid, x, y, z);
+        uint32_t slow = 0;  // bit q: element (q, s) needs a descriptor
+        if (!own_solid) {
+#pragma unroll
+            for (int q = 1; q < Q; ++q) {
+                const int xi = x - CXq(q), yi = y - CYq(q), zi = z - CZq(q);
+                const bool sl = T.nb27[((zi >> 3) + 1) * 9 + ((yi >> 3) + 1) * 3 + ((xi >> 3) + 1)] == kSlow ||
+                                (near && solid_bit(T.solid, xi, yi, zi));
+                slow |= (uint32_t)sl << q;
+            }
+        }
+        const uint32_t mine = __popc(slow);
+        // block exclusive scan of the per-site counts
+        uint32_t incl = mine;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (lane == 31) warp_sum[wid] = incl;
+        const uint32_t solid_word = __ballot_sync(0xFFFFFFFFu, own_solid);
+        __syncthreads();
+        uint32_t before = 0, total = 0;
+        for (int k = 0; k < 16; ++k) {
+            uint32_t v = warp_sum[k];
+            before += k < wid ? v : 0u;
+            total += v;
+        }
+        if (!EMIT) {
+            if (t == 0) cnt[p] = total;
+            if (lane == 0) smask[(size_t)b * 16 + wid] = solid_word;
+        } else {
+            uint64_t* out = desc + off[p] + before + (incl - mine);
+            while (slow) {
+                const int q = __ffs(slow) - 1;
+                slow &= slow - 1;
+                *out++ = resolve_source(c, bx, by, bz, b, q, l, s, G0, T, dev_status);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Bricks at a level interface, a domain boundary or near the sphere; one CTA
+// of 256 threads per brick, in three passes: (1) every element is gathered as
+// in the interior kernel into shared memory, with missing same-level
+// neighbours replaced by the brick itself so every load stays in bounds (the
+// two halves of the CTA take populations 0-9 and 10-18 of the same x-quads);
+// (2) the brick's stencil descriptors overwrite the elements whose source is
+// not a plain same-level load; (3) each thread relaxes two adjacent sites and
+// stores them with 64-bit stores.
+constexpr int kGeneralCtasPerSm = 4;
+
+__global__ void __launch_bounds__(256, kGeneralCtasPerSm) k_collide_general(StepArgs a, const uint32_t* __restrict__ nb27) {
+    __shared__ __align__(16) float sf[Q][512];
+    __shared__ uint32_t s_nb[27];
+    const int l = a.level;
+    const int t = threadIdx.x;
+    const int u = t & 127, half = t >> 7;
+    const int x0 = (u & 1) * 4, y = (u >> 1) & 7, z = u >> 4;
+    const int own = x0 + 8 * y + 64 * z;
+    const size_t plane = a.cap * 512;
+    // software pipeline: the next brick's list entry and neighbour row are
+    // loaded while the current brick is processed
+    uint32_t w = blockIdx.x;
+    uint32_t b = w < a.count ? a.list[w] : 0u;
+    uint32_t row = (w < a.count && t < 27) ? nb27[(size_t)b * 28 + t] : 0u;
+    for (; w < a.count; w += gridDim.x) {
+        if (t < 27) s_nb[t] = row == kSlow ? b : row;
+        __syncthreads();
+        const uint32_t wn = w + gridDim.x;
+        const uint32_t bn = wn < a.count ? a.list[wn] : 0u;
+        if (wn < a.count && t < 27) row = nb27[(size_t)bn * 28 + t];
+        const uint32_t d0 = a.desc_off[w], d1 = a.desc_off[w + 1];
+        const uint32_t sw = a.smask[(size_t)b * 16 + (t >> 4)];
+        const float omega = a.cases[a.bcase[b]].omega[l];
+        // pass 1: in-bounds row gathers for every element
         {
             float f[Q][4];
-            gather_quad<false>(a, c, S.safe27, b, l, 0, x0, y, z, nullptr, nullptr, f);
+            if (half == 0) {
+                gather_quad<0, 10>(a, s_nb, x0, y, z, f);
 #pragma unroll
-            for (int q = 0; q < Q; ++q) {
-                const int cx = CXq(q), cy = CYq(q), cz = CZq(q);
-                const int sy = y - cy, sz = z - cz;
-                const int dy = sy >> 3, dz = sz >> 3;
+                for (int q = 0; q < 10; ++q)
+                    *reinterpret_cast<float4*>(&sf[q][own]) = make_float4(f[q][0], f[q][1], f[q][2], f[q][3]);
+            } else {
+                gather_quad<10, Q>(a, s_nb, x0, y, z, f);
 #pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const int xi = x0 + i - cx;
-                    const int dx = xi >> 3;
-                    const bool slow = S.nb27[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)] == kSlow ||
-                                      (near && solid_bit(S.solid, xi, sy, sz));
-                    if (slow) {
-                        unsigned k = atomicAdd(&S.count, 1u);
-                        S.queue[k] = (uint16_t)((q << 9) | (own + i));
-                    }
+                for (int q = 10; q < Q; ++q)
+                    *reinterpret_cast<float4*>(&sf[q][own]) = make_float4(f[q][0], f[q][1], f[q][2], f[q][3]);
+            }
+        }
+        __syncthreads();
+        // pass 2: the brick's descriptors
+        for (uint32_t k = d0 + t; k < d1; k += 256) {
+            const uint64_t d = __ldg(a.desc + k);
+            const uint32_t src = (uint32_t)d;
+            const int s = (int)((d >> 32) & 511u), q = (int)((d >> 41) & 31u);
+            const uint32_t kind = (uint32_t)(d >> 46) & 7u;
+            float v;
+            if (kind == kSrcSame || kind == kSrcOutlet) {
+                v = a.R[q * plane + src];
+            } else if (kind == kSrcBounce) {
+                v = a.R[OPPq(q) * plane + src];
+            } else if (kind == kSrcCoarse) {
+                v = a.Cold[q * plane + src];
+                if (a.sub) {
+                    float tt = v + a.Cnew[q * plane + src];
+                    v = tt * 0.5f;
                 }
-                *reinterpret_cast<float4*>(&S.f[q][own]) = make_float4(f[q][0], f[q][1], f[q][2], f[q][3]);
+            } else if (kind == kSrcFine) {
+                const float* F = a.Fine + q * plane + src;
+                float sum = 0.0f;
+#pragma unroll
+                for (int kq = 0; kq < 8; ++kq) sum = sum + F[(kq & 1) + 8 * ((kq >> 1) & 1) + 64 * (kq >> 2)];
+                v = sum * 0.125f;
+            } else {
+                const LbmCaseDev& c = a.cases[a.bcase[b]];
+                if (kind == kSrcWall) {
+                    v = a.R[OPPq(q) * plane + src];
+                    float cu = cdot(q, c.wall_u[0], c.wall_u[1], c.wall_u[2]);
+                    float tt = 6.0f * Wq(q);
+                    tt = tt * cu;
+                    v = v + tt;
+                } else {
+                    float base = base_of(c.inlet_u[0], c.inlet_u[1], c.inlet_u[2]);
+                    v = feq1(q, 1.0f, c.inlet_u[0], c.inlet_u[1], c.inlet_u[2], base);
+                }
             }
+            sf[q][s] = v;
         }
         __syncthreads();
-        // pass 2: the queued elements, independently
-        const unsigned nq = S.count;
-        for (unsigned k = t; k < nq; k += 128) {
-            const unsigned e = S.queue[k];
-            const int q = (int)(e >> 9), s = (int)(e & 511);
-            const int xi = (s & 7) - CXq(q), yi = ((s >> 3) & 7) - CYq(q), zi = (s >> 6) - CZq(q);
-            const int64_t G[3] = {G0[0] + (s & 7), G0[1] + ((s >> 3) & 7), G0[2] + (s >> 6)};
-            S.f[q][s] = pull_general(a, c, b, q, l, G, s, S.nbr, S.nlv, S.solid, near, xi, yi, zi);
-        }
-        __syncthreads();
-        // pass 3: collision from shared memory
-        const float omega = c.omega[l];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            float g[Q];
-#pragma unroll
-            for (int q = 0; q < Q; ++q) g[q] = S.f[q][own + i];
-            const bool solid = near && solid_bit(S.solid, x0 + i, y, z);
-            float rho, jx, jy, jz;
-            moments(g, rho, jx, jy, jz);
-            float inv = 1.0f / rho;
-            float ux = jx * inv, uy = jy * inv, uz = jz * inv;
-            float base = base_of(ux, uy, uz);
+        // pass 3: relaxation of sites 2t, 2t + 1
+        {
+            const int s0 = 2 * t;
+            float g0[Q], g1[Q];
 #pragma unroll
             for (int q = 0; q < Q; ++q) {
-                float fe = feq1(q, rho, ux, uy, uz, base);
-                float dd = fe - g[q];
-                dd = omega * dd;
-                S.f[q][own + i] = solid ? Wq(q) : g[q] + dd;
+                const float2 v = *reinterpret_cast<const float2*>(&sf[q][s0]);
+                g0[q] = v.x;
+                g1[q] = v.y;
             }
-        }
+            relax_site(g0, omega, (sw >> (s0 & 31)) & 1u);
+            relax_site(g1, omega, (sw >> ((s0 + 1) & 31)) & 1u);
 #pragma unroll
-        for (int q = 0; q < Q; ++q)
-            *(float4*)(a.W + fidx(a.cap, q, b, own)) = *reinterpret_cast<const float4*>(&S.f[q][own]);
+            for (int q = 0; q < Q; ++q) *(float2*)(a.W + fidx(a.cap, q, b, s0)) = make_float2(g0[q], g1[q]);
+        }
         __syncthreads();
+        b = bn;
     }
 }
 
@@ -998,6 +960,12 @@ struct fl_pool {
     uint64_t fluid_cls[3][16] = {};
     uint32_t* nb27 = nullptr;
     uint8_t* bclass = nullptr;
+    uint32_t* slow_cnt = nullptr;   // per list position: descriptors of the brick
+    uint32_t* slow_off = nullptr;   // exclusive prefix of slow_cnt, n + 1 entries
+    uint32_t* smask = nullptr;      // [cap][16] own-site solid bits of general bricks
+    uint64_t* desc = nullptr;       // stencil descriptors
+    size_t desc_cap = 0;
+    uint64_t num_desc = 0;
     std::vector<uint32_t> case_begin;
     uint32_t* d_case_begin = nullptr;
     float* wmax = nullptr;
@@ -1012,6 +980,11 @@ struct fl_pool {
     void* adapt_scratch = nullptr;
     size_t adapt_scratch_bytes = 0;
     int grid_mult = 4;
+    // the general class of a level runs on `side`, concurrently with the
+    // interior and all-solid classes on the context stream (fork/join events)
+    int streams = 2;
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 namespace {
@@ -1074,15 +1047,18 @@ int alloc_brick_arrays(fl_ctx* ctx, fl_pool* P, size_t cap) {
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->fluid, cap * 4, ctx->stream), "pool fluid");
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->nb27, cap * 28 * 4, ctx->stream), "pool nb27");
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->bclass, cap, ctx->stream), "pool classes");
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->slow_cnt, cap * 4, ctx->stream), "pool descriptor counts");
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->slow_off, (cap + 1) * 4, ctx->stream), "pool descriptor offsets");
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->smask, cap * 64, ctx->stream), "pool solid masks");
     return FL_OK;
 }
 
 void free_brick_arrays(fl_ctx* ctx, fl_pool* P) {
-    void* ps[7] = {P->nbr, P->list, P->wmax, P->part, P->fluid, P->nb27, P->bclass};
+    void* ps[10] = {P->nbr, P->list, P->wmax, P->part, P->fluid, P->nb27, P->bclass, P->slow_cnt, P->slow_off, P->smask};
     for (void* p : ps)
         if (p) cudaFreeAsync(p, ctx->stream);
     P->nbr = nullptr; P->list = nullptr; P->wmax = nullptr; P->part = nullptr; P->fluid = nullptr;
-    P->nb27 = nullptr; P->bclass = nullptr;
+    P->nb27 = nullptr; P->bclass = nullptr; P->slow_cnt = nullptr; P->slow_off = nullptr; P->smask = nullptr;
 }
 
 void drop_graph(fl_pool* P) {
@@ -1095,6 +1071,8 @@ void drop_graph(fl_pool* P) {
 // Neighbour table, per-level lists, case ranges and fluid count for the current mesh.
 int pool_topology(fl_ctx* ctx, fl_pool* P) {
     size_t n = P->mesh.num_cells;
+    if (P->cap >= (1u << 23))  // descriptors address elements as brick * 512 + site in 32 bits
+        return fl_set_error(ctx, FL_E_CAPACITY, "a pool holds fewer than 2^23 bricks");
     uint64_t cap = fl_table_capacity(n);
     size_t need = fl_align256(n * 8) + fl_align256(cap * 8) + 2 * fl_align256(cap * 4) + 256;
     int rc = fl_scratch_reserve(ctx, need);
@@ -1144,6 +1122,11 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
     std::vector<uint32_t> list(n), fill[3] = {P->cls_off[0], P->cls_off[1], P->cls_off[2]};
     for (size_t i = 0; i < n; ++i) list[fill[cl[i] > 2 ? 1 : cl[i]][lv[i]]++] = (uint32_t)i;
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->list, list.data(), n * 4, cudaMemcpyHostToDevice, ctx->stream), "list");
+    const unsigned tgrid = (unsigned)std::max<size_t>(1, std::min<size_t>(n, (size_t)ctx->num_sms * 4));
+    k_slow_table<false><<<tgrid, 512, 0, ctx->stream>>>(n, P->list, P->bclass, P->nbr, P->mesh.level, P->mesh.x,
+                                                        P->mesh.y, P->mesh.z, P->mesh.case_id, P->d_cases, P->nb27,
+                                                        P->slow_cnt, P->smask, nullptr, nullptr, ctx->dev_status);
+    FL_CHECK_LAUNCH(ctx, "k_slow_table count");
     P->case_begin.assign(P->cases.size() + 1, 0);
     for (size_t i = 0; i < n; ++i) P->case_begin[cs[i] + 1]++;
     for (size_t c = 0; c < P->cases.size(); ++c) P->case_begin[c + 1] += P->case_begin[c];
@@ -1152,9 +1135,32 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
     // fluid sites per brick -> LUPs per level-0 step
     k_brick_sums<<<fl_blocks(n, 1, ctx->num_sms * 8), 512, 0, ctx->stream>>>(view(P), n, P->part, P->fluid);
     FL_CHECK_LAUNCH(ctx, "k_brick_sums");
-    std::vector<uint32_t> fl(n);
+    std::vector<uint32_t> fl(n), sc(n + 1);
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(fl.data(), P->fluid, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "fluid");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(sc.data(), P->slow_cnt, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "counts");
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "topology sync");
+    // stencil descriptors of the general class: offsets on the host, words on the device
+    uint64_t run = 0;
+    for (size_t i = 0; i < n; ++i) {
+        uint32_t c = sc[i];
+        sc[i] = (uint32_t)run;
+        run += c;
+    }
+    if (run >= (1ull << 32)) return fl_set_error(ctx, FL_E_CAPACITY, "more than 2^32 stencil descriptors");
+    sc[n] = (uint32_t)run;
+    P->num_desc = run;
+    if (run > P->desc_cap) {
+        if (P->desc) cudaFreeAsync(P->desc, ctx->stream);
+        P->desc_cap = run + run / 4 + 1024;
+        FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->desc, P->desc_cap * 8, ctx->stream), "stencil descriptors");
+    }
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->slow_off, sc.data(), (n + 1) * 4, cudaMemcpyHostToDevice, ctx->stream),
+                "descriptor offsets");
+    k_slow_table<true><<<tgrid, 512, 0, ctx->stream>>>(n, P->list, P->bclass, P->nbr, P->mesh.level, P->mesh.x,
+                                                       P->mesh.y, P->mesh.z, P->mesh.case_id, P->d_cases, P->nb27,
+                                                       nullptr, nullptr, P->slow_off, P->desc, ctx->dev_status);
+    FL_CHECK_LAUNCH(ctx, "k_slow_table emit");
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "descriptor sync");  // sc is freed on return
     P->lups = 0;
     for (int l = 0; l < 16; ++l) P->fluid_per_level[l] = P->fluid_cls[0][l] = P->fluid_cls[1][l] = P->fluid_cls[2][l] = 0;
     for (size_t i = 0; i < n; ++i) {
@@ -1330,6 +1336,12 @@ void launch_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm = nul
     a.nbr = P->nbr;
     a.cases = P->d_cases;
     a.dev_status = ctx->dev_status;
+    const bool fork = !tm && P->streams > 1 && P->side && P->cls_cnt[1][l] &&
+                      (P->cls_cnt[0][l] || P->cls_cnt[2][l]);
+    if (fork) {
+        cudaEventRecord(P->ev_fork, ctx->stream);
+        cudaStreamWaitEvent(P->side, P->ev_fork, 0);
+    }
     for (int kind = 0; kind < 3; ++kind) {
         uint32_t off = P->cls_off[kind][l];
         uint32_t cnt = P->cls_cnt[kind][l];
@@ -1346,8 +1358,11 @@ void launch_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm = nul
             unsigned grid = std::min<unsigned>(cnt, (unsigned)ctx->num_sms * P->grid_mult);
             k_collide_fast<<<grid, 128, 0, ctx->stream>>>(a, P->nb27);
         } else if (kind == 1) {
-            unsigned grid = std::min<unsigned>(cnt, (unsigned)ctx->num_sms * 3);
-            k_collide_general<<<grid, 128, sizeof(GeneralSmem), ctx->stream>>>(a, P->nb27);
+            unsigned grid = std::min<unsigned>(cnt, (unsigned)ctx->num_sms * kGeneralCtasPerSm);
+            a.desc = P->desc;
+            a.desc_off = P->slow_off + off;
+            a.smask = P->smask;
+            k_collide_general<<<grid, 256, 0, fork ? P->side : ctx->stream>>>(a, P->nb27);
         } else {
             k_collide_solid<<<fl_blocks((size_t)cnt * 512, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(a);
         }
@@ -1358,6 +1373,10 @@ void launch_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm = nul
             tm->sites.push_back(P->fluid_cls[kind][l]);
             tm->kind.push_back(kind);
         }
+    }
+    if (fork) {
+        cudaEventRecord(P->ev_join, P->side);
+        cudaStreamWaitEvent(ctx->stream, P->ev_join, 0);
     }
     P->parity[l] ^= 1;
 }
@@ -1376,8 +1395,6 @@ extern "C" {
 
 int fl_pool_create(fl_ctx* ctx, const fl_lbm_case* cases, int ncases, fl_pool** out) {
     if (!ctx || !cases || ncases <= 0 || ncases > 4096 || !out) return FL_E_INVALID_ARG;
-    FL_TRY_CUDA(ctx, cudaFuncSetAttribute(k_collide_general, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)sizeof(GeneralSmem)), "general kernel shared memory");
     *out = nullptr;
     fl_pool* P = new fl_pool();
     P->cases.assign(cases, cases + ncases);
@@ -1399,6 +1416,10 @@ int fl_pool_create(fl_ctx* ctx, const fl_lbm_case* cases, int ncases, fl_pool** 
     }
     int rc = FL_OK;
     auto fail = [&](int r) { fl_pool_destroy(ctx, P); return r; };
+    if (cudaStreamCreateWithFlags(&P->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&P->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&P->ev_join, cudaEventDisableTiming) != cudaSuccess)
+        return fail(fl_set_error(ctx, FL_E_CUDA, "fl_pool_create: stream or event creation failed"));
     // case tables sized for every slot a pool can hold (cases may be added later)
     if (cudaMalloc(&P->d_cases, kMaxCases * sizeof(LbmCaseDev)) != cudaSuccess) return fail(FL_E_OOM);
     if (cudaMalloc(&P->d_dom, kMaxCases * sizeof(fl_domain_dev::Case)) != cudaSuccess) return fail(FL_E_OOM);
@@ -1460,6 +1481,7 @@ int fl_pool_destroy(fl_ctx* ctx, fl_pool* P) {
         if (P->f[k]) cudaFreeAsync(P->f[k], ctx->stream);
     if (P->mesh.x) fl_mesh_free(ctx, &P->mesh);
     if (P->adapt_scratch) cudaFreeAsync(P->adapt_scratch, ctx->stream);
+    if (P->desc) cudaFreeAsync(P->desc, ctx->stream);
     cudaStreamSynchronize(ctx->stream);
     if (P->d_cases) cudaFree(P->d_cases);
     if (P->d_dom) cudaFree(P->d_dom);
@@ -1467,6 +1489,9 @@ int fl_pool_destroy(fl_ctx* ctx, fl_pool* P) {
     if (P->case_max) cudaFree(P->case_max);
     if (P->cons) cudaFree(P->cons);
     if (P->d_mask) cudaFree(P->d_mask);
+    if (P->side) cudaStreamDestroy(P->side);
+    if (P->ev_fork) cudaEventDestroy(P->ev_fork);
+    if (P->ev_join) cudaEventDestroy(P->ev_join);
     delete P;
     return FL_OK;
 }
@@ -1805,6 +1830,14 @@ int fl_pool_set_options(fl_ctx* ctx, fl_pool* P, int use_graphs, int grid_mult) 
     if (!ctx || !P) return FL_E_INVALID_ARG;
     P->graphs = use_graphs;
     if (grid_mult > 0) P->grid_mult = grid_mult;
+    drop_graph(P);
+    return FL_OK;
+}
+
+int fl_pool_set_class_streams(fl_ctx* ctx, fl_pool* P, int streams) {
+    if (!ctx || !P || streams < 1 || streams > 2) return FL_E_INVALID_ARG;
+    cudaStreamSynchronize(P->side);
+    P->streams = streams;
     drop_graph(P);
     return FL_OK;
 }

@@ -82,8 +82,10 @@ class Pool:
         self.ctx.call("fl_pool_info_get", self.h, ctypes.byref(i))
         return i
 
-    def set_options(self, graphs=1, grid_mult=0):
+    def set_options(self, graphs=1, grid_mult=0, streams=None):
         self.ctx.call("fl_pool_set_options", self.h, graphs, grid_mult)
+        if streams is not None:
+            self.ctx.call("fl_pool_set_class_streams", self.h, streams)
 
     def bricks(self):
         n = self.info().num_bricks

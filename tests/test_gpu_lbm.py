@@ -61,6 +61,22 @@ def test_graphs_match_direct_launches(ctx):
     np.testing.assert_array_equal(a.populations(), b.populations())
 
 
+@pytest.mark.parametrize("graphs", [0, 1])
+def test_concurrent_class_streams_match_one_stream(ctx, graphs):
+    """General bricks on a second stream (fork/join, inside graphs or not) give the
+    same populations as the three classes in order on one stream, across a regrid."""
+    from fluidloom_gb300.lbm import Pool
+    c = cases_small()[1]
+    a, b = Pool(ctx, [c]), Pool(ctx, [c])
+    a.set_options(graphs=graphs, streams=2)
+    b.set_options(graphs=0, streams=1)
+    for p in (a, b):
+        p.step(4)
+        p.regrid()
+        p.step(3)
+    np.testing.assert_array_equal(a.populations(), b.populations())
+
+
 def test_batch_equals_solo(ctx):
     """Two cases in one pool reproduce their solo runs bit for bit."""
     from fluidloom_gb300.lbm import Pool
