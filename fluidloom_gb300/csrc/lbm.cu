@@ -66,12 +66,20 @@ struct LbmCaseDev {
 
 namespace {
 
+// c_q . u as the sum of its non-zero terms in x, y, z order (c = +-1 is a
+// sign, so no product is formed; c_0 . u = 0) -- the oracle's cdot().
 __device__ __forceinline__ float cdot(int q, float ux, float uy, float uz) {
-    float a = (float)CXq(q) * ux;
-    float b = (float)CYq(q) * uy;
-    float c = (float)CZq(q) * uz;
-    float s = a + b;
-    return s + c;
+    const int c[3] = {CXq(q), CYq(q), CZq(q)};
+    const float t[3] = {c[0] > 0 ? ux : -ux, c[1] > 0 ? uy : -uy, c[2] > 0 ? uz : -uz};
+    float s = 0.0f;
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        if (!c[k]) continue;
+        s = any ? s + t[k] : t[k];
+        any = true;
+    }
+    return s;
 }
 
 __device__ __forceinline__ float base_of(float ux, float uy, float uz) {
@@ -135,6 +143,8 @@ struct StepArgs {
     const uint64_t* desc;      // stencil descriptors of the general class (k_slow_table)
     const uint32_t* desc_off;  // per list position: first descriptor; [count] = end
     const uint32_t* smask;     // [n][16]: own sites inside the sphere
+    const uint4* qmask;        // [n][128]: per x-quad descriptor bits (4q + i) and first descriptor
+    const float* pv;           // descriptor values of this sub-step (k_interface)
 };
 
 __device__ __forceinline__ size_t fidx(size_t cap, int q, size_t b, int s) { return ((size_t)q * cap + b) * 512 + s; }
@@ -274,7 +284,7 @@ enum : uint32_t {
     kSrcFine = 2,    // finer neighbour: mean of the 2x2x2 children at src + {0,1,8,9,64,65,72,73}
     kSrcBounce = 3,  // R[opp q][src]: half-way bounce-back (wall, sphere, missing neighbour)
     kSrcWall = 4,    // R[opp q][src] + 6 w_q (c_q . u_wall): moving wall
-    kSrcInlet = 5,   // feq(1, u_inlet)
+    kSrcInlet = 5,   // feq(1, u_inlet) (src: own element, names the brick)
     kSrcOutlet = 6,  // R[q][src]: zero-gradient outlet (own site)
 };
 
@@ -315,7 +325,7 @@ __device__ uint64_t resolve_source(const LbmCaseDev& c, const int32_t* bx, const
             else if (bt == 4) outlet = true;
             else if (bt == 2) moving = true;
         }
-        if (inlet) return make_desc(kSrcInlet, q, s, 0u);
+        if (inlet) return make_desc(kSrcInlet, q, s, own);
         if (outlet) return make_desc(kSrcOutlet, q, s, own);
         return make_desc(moving ? kSrcWall : kSrcBounce, q, s, own);
     }
@@ -371,7 +381,8 @@ __global__ void __launch_bounds__(512) k_slow_table(size_t n, const uint32_t* __
                                                     const uint16_t* __restrict__ bcase,
                                                     const LbmCaseDev* __restrict__ cases,
                                                     const uint32_t* __restrict__ nb27, uint32_t* __restrict__ cnt,
-                                                    uint32_t* __restrict__ smask, const uint32_t* __restrict__ off,
+                                                    uint32_t* __restrict__ smask, uint4* __restrict__ qmask,
+                                                    const uint32_t* __restrict__ off,
                                                     uint64_t* __restrict__ desc, uint32_t* dev_status) {
     __shared__ BrickTopo T;
     __shared__ uint32_t warp_sum[16];
@@ -436,42 +447,98 @@ __global__ void __launch_bounds__(512) k_slow_table(size_t n, const uint32_t* __
             before += k < wid ? v : 0u;
             total += v;
         }
+        // x-quads are threads 4u .. 4u + 3; a quad's elements are numbered q-major, then site
+        const int i = lane & 3;
+        uint32_t m[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) m[k] = __shfl_sync(0xFFFFFFFFu, slow, (lane & ~3) + k);
+        const uint32_t qbase = __shfl_sync(0xFFFFFFFFu, before + (incl - mine), lane & ~3);
         if (!EMIT) {
             if (t == 0) cnt[p] = total;
             if (lane == 0) smask[(size_t)b * 16 + wid] = solid_word;
+            if (i == 0) {
+                uint32_t wq[3] = {0u, 0u, 0u};
+                for (int q = 0; q < Q; ++q)
+                    for (int k = 0; k < 4; ++k)
+                        wq[(q * 4 + k) >> 5] |= ((m[k] >> q) & 1u) << ((q * 4 + k) & 31);
+                qmask[(size_t)b * 128 + (t >> 2)] = make_uint4(wq[0], wq[1], wq[2], qbase);
+            }
         } else {
-            uint64_t* out = desc + off[p] + before + (incl - mine);
+            uint64_t* out = desc + off[p] + qbase;
             while (slow) {
                 const int q = __ffs(slow) - 1;
                 slow &= slow - 1;
-                *out++ = resolve_source(c, bx, by, bz, b, q, l, s, G0, T, dev_status);
+                const uint32_t below = (1u << q) - 1u;
+                uint32_t rank = 0;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) rank += __popc(m[k] & below) + (k < i ? (m[k] >> q) & 1u : 0u);
+                out[rank] = resolve_source(c, bx, by, bz, b, q, l, s, G0, T, dev_status);
             }
         }
         __syncthreads();
     }
 }
 
-// Bricks at a level interface, a domain boundary or near the sphere; one CTA
-// of 256 threads per brick, in three passes: (1) every element is gathered as
-// in the interior kernel into shared memory, with missing same-level
-// neighbours replaced by the brick itself so every load stays in bounds (the
-// two halves of the CTA take populations 0-9 and 10-18 of the same x-quads);
-// (2) the brick's stencil descriptors overwrite the elements whose source is
-// not a plain same-level load; (3) each thread relaxes two adjacent sites and
-// stores them with 64-bit stores.
-constexpr int kGeneralCtasPerSm = 4;
+// Value of one stencil descriptor at this sub-step.
+__device__ __forceinline__ float desc_value(const StepArgs& a, uint64_t d, size_t plane) {
+    const uint32_t src = (uint32_t)d;
+    const int q = (int)((d >> 41) & 31u);
+    const uint32_t kind = (uint32_t)(d >> 46) & 7u;
+    float v;
+    if (kind == kSrcSame || kind == kSrcOutlet) {
+        v = a.R[q * plane + src];
+    } else if (kind == kSrcBounce) {
+        v = a.R[OPPq(q) * plane + src];
+    } else if (kind == kSrcCoarse) {
+        v = a.Cold[q * plane + src];
+        if (a.sub) {
+            float tt = v + a.Cnew[q * plane + src];
+            v = tt * 0.5f;
+        }
+    } else if (kind == kSrcFine) {
+        const float* F = a.Fine + q * plane + src;
+        float sum = 0.0f;
+#pragma unroll
+        for (int kq = 0; kq < 8; ++kq) sum = sum + F[(kq & 1) + 8 * ((kq >> 1) & 1) + 64 * (kq >> 2)];
+        v = sum * 0.125f;
+    } else {
+        const LbmCaseDev& c = a.cases[a.bcase[src >> 9]];
+        if (kind == kSrcWall) {
+            v = a.R[OPPq(q) * plane + src];
+            float cu = cdot(q, c.wall_u[0], c.wall_u[1], c.wall_u[2]);
+            float tt = 6.0f * Wq(q);
+            tt = tt * cu;
+            v = v + tt;
+        } else {
+            float base = base_of(c.inlet_u[0], c.inlet_u[1], c.inlet_u[2]);
+            v = feq1(q, 1.0f, c.inlet_u[0], c.inlet_u[1], c.inlet_u[2], base);
+        }
+    }
+    return v;
+}
 
-__global__ void __launch_bounds__(256, kGeneralCtasPerSm) k_collide_general(StepArgs a, const uint32_t* __restrict__ nb27) {
-    __shared__ __align__(16) float sf[Q][512];
+// The values of a level's stencil descriptors [d0, d1) at this sub-step,
+// one thread per descriptor, into pv (same indices).
+__global__ void __launch_bounds__(256) k_interface(StepArgs a, uint32_t d0, uint32_t d1, float* __restrict__ pv) {
+    const size_t plane = a.cap * 512;
+    for (uint32_t k = d0 + blockIdx.x * blockDim.x + threadIdx.x; k < d1; k += gridDim.x * blockDim.x)
+        pv[k] = desc_value(a, __ldg(a.desc + k), plane);
+}
+
+// Bricks at a level interface, a domain boundary or near the sphere, in the
+// interior kernel's layout (x-quads in registers, 128 threads, 4 CTAs/SM):
+// the quad's rows are gathered with missing same-level neighbours replaced by
+// the brick itself (every load stays in bounds); each thread then replaces
+// its elements flagged in its quad mask -- bit 4q + i, ordered like the
+// descriptors, from the quad's first descriptor on -- by the descriptor
+// values k_interface computed for this sub-step, and relaxes the quad.  Sites
+// inside the sphere take the rest equilibrium.
+__global__ void __launch_bounds__(128, 4) k_collide_general(StepArgs a, const uint32_t* __restrict__ nb27) {
     __shared__ uint32_t s_nb[27];
     const int l = a.level;
     const int t = threadIdx.x;
-    const int u = t & 127, half = t >> 7;
-    const int x0 = (u & 1) * 4, y = (u >> 1) & 7, z = u >> 4;
+    const int x0 = (t & 1) * 4, y = (t >> 1) & 7, z = t >> 4;
     const int own = x0 + 8 * y + 64 * z;
-    const size_t plane = a.cap * 512;
-    // software pipeline: the next brick's list entry and neighbour row are
-    // loaded while the current brick is processed
     uint32_t w = blockIdx.x;
     uint32_t b = w < a.count ? a.list[w] : 0u;
     uint32_t row = (w < a.count && t < 27) ? nb27[(size_t)b * 28 + t] : 0u;
@@ -481,79 +548,46 @@ __global__ void __launch_bounds__(256, kGeneralCtasPerSm) k_collide_general(Step
         const uint32_t wn = w + gridDim.x;
         const uint32_t bn = wn < a.count ? a.list[wn] : 0u;
         if (wn < a.count && t < 27) row = nb27[(size_t)bn * 28 + t];
-        const uint32_t d0 = a.desc_off[w], d1 = a.desc_off[w + 1];
-        const uint32_t sw = a.smask[(size_t)b * 16 + (t >> 4)];
+        const uint4 qm = a.qmask[(size_t)b * 128 + t];
+        const uint32_t sw = a.smask[(size_t)b * 16 + (own >> 5)];
         const float omega = a.cases[a.bcase[b]].omega[l];
-        // pass 1: in-bounds row gathers for every element
-        {
-            float f[Q][4];
-            if (half == 0) {
-                gather_quad<0, 10>(a, s_nb, x0, y, z, f);
+        float f[Q][4];
+        gather_quad<0, Q>(a, s_nb, x0, y, z, f);
+        const float* pv = a.pv + a.desc_off[w];
+        uint32_t r = qm.w;
+        if (qm.x) {
 #pragma unroll
-                for (int q = 0; q < 10; ++q)
-                    *reinterpret_cast<float4*>(&sf[q][own]) = make_float4(f[q][0], f[q][1], f[q][2], f[q][3]);
-            } else {
-                gather_quad<10, Q>(a, s_nb, x0, y, z, f);
+            for (int q = 0; q < 8; ++q)
 #pragma unroll
-                for (int q = 10; q < Q; ++q)
-                    *reinterpret_cast<float4*>(&sf[q][own]) = make_float4(f[q][0], f[q][1], f[q][2], f[q][3]);
-            }
+                for (int i = 0; i < 4; ++i)
+                    if ((qm.x >> (q * 4 + i)) & 1u) f[q][i] = __ldg(pv + r++);
         }
-        __syncthreads();
-        // pass 2: the brick's descriptors
-        for (uint32_t k = d0 + t; k < d1; k += 256) {
-            const uint64_t d = __ldg(a.desc + k);
-            const uint32_t src = (uint32_t)d;
-            const int s = (int)((d >> 32) & 511u), q = (int)((d >> 41) & 31u);
-            const uint32_t kind = (uint32_t)(d >> 46) & 7u;
-            float v;
-            if (kind == kSrcSame || kind == kSrcOutlet) {
-                v = a.R[q * plane + src];
-            } else if (kind == kSrcBounce) {
-                v = a.R[OPPq(q) * plane + src];
-            } else if (kind == kSrcCoarse) {
-                v = a.Cold[q * plane + src];
-                if (a.sub) {
-                    float tt = v + a.Cnew[q * plane + src];
-                    v = tt * 0.5f;
-                }
-            } else if (kind == kSrcFine) {
-                const float* F = a.Fine + q * plane + src;
-                float sum = 0.0f;
+        if (qm.y) {
 #pragma unroll
-                for (int kq = 0; kq < 8; ++kq) sum = sum + F[(kq & 1) + 8 * ((kq >> 1) & 1) + 64 * (kq >> 2)];
-                v = sum * 0.125f;
-            } else {
-                const LbmCaseDev& c = a.cases[a.bcase[b]];
-                if (kind == kSrcWall) {
-                    v = a.R[OPPq(q) * plane + src];
-                    float cu = cdot(q, c.wall_u[0], c.wall_u[1], c.wall_u[2]);
-                    float tt = 6.0f * Wq(q);
-                    tt = tt * cu;
-                    v = v + tt;
-                } else {
-                    float base = base_of(c.inlet_u[0], c.inlet_u[1], c.inlet_u[2]);
-                    v = feq1(q, 1.0f, c.inlet_u[0], c.inlet_u[1], c.inlet_u[2], base);
-                }
-            }
-            sf[q][s] = v;
+            for (int q = 8; q < 16; ++q)
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                    if ((qm.y >> (q * 4 + i - 32)) & 1u) f[q][i] = __ldg(pv + r++);
         }
-        __syncthreads();
-        // pass 3: relaxation of sites 2t, 2t + 1
-        {
-            const int s0 = 2 * t;
-            float g0[Q], g1[Q];
+        if (qm.z) {
 #pragma unroll
-            for (int q = 0; q < Q; ++q) {
-                const float2 v = *reinterpret_cast<const float2*>(&sf[q][s0]);
-                g0[q] = v.x;
-                g1[q] = v.y;
-            }
-            relax_site(g0, omega, (sw >> (s0 & 31)) & 1u);
-            relax_site(g1, omega, (sw >> ((s0 + 1) & 31)) & 1u);
+            for (int q = 16; q < Q; ++q)
 #pragma unroll
-            for (int q = 0; q < Q; ++q) *(float2*)(a.W + fidx(a.cap, q, b, s0)) = make_float2(g0[q], g1[q]);
+                for (int i = 0; i < 4; ++i)
+                    if ((qm.z >> (q * 4 + i - 64)) & 1u) f[q][i] = __ldg(pv + r++);
         }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            float g[Q];
+#pragma unroll
+            for (int q = 0; q < Q; ++q) g[q] = f[q][i];
+            relax_site(g, omega, (sw >> ((own + i) & 31)) & 1u);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) f[q][i] = g[q];
+        }
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+            *(float4*)(a.W + fidx(a.cap, q, b, own)) = make_float4(f[q][0], f[q][1], f[q][2], f[q][3]);
         __syncthreads();
         b = bn;
     }
@@ -963,8 +997,11 @@ struct fl_pool {
     uint32_t* slow_cnt = nullptr;   // per list position: descriptors of the brick
     uint32_t* slow_off = nullptr;   // exclusive prefix of slow_cnt, n + 1 entries
     uint32_t* smask = nullptr;      // [cap][16] own-site solid bits of general bricks
+    uint4* qmask = nullptr;         // [cap][128] per x-quad descriptor bits and offsets
     uint64_t* desc = nullptr;       // stencil descriptors
+    float* pv = nullptr;            // their values at the current sub-step
     size_t desc_cap = 0;
+    std::vector<uint32_t> lvl_desc;  // per level: first descriptor of its general bricks; [maxL + 1] = end
     uint64_t num_desc = 0;
     std::vector<uint32_t> case_begin;
     uint32_t* d_case_begin = nullptr;
@@ -1050,15 +1087,18 @@ int alloc_brick_arrays(fl_ctx* ctx, fl_pool* P, size_t cap) {
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->slow_cnt, cap * 4, ctx->stream), "pool descriptor counts");
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->slow_off, (cap + 1) * 4, ctx->stream), "pool descriptor offsets");
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->smask, cap * 64, ctx->stream), "pool solid masks");
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->qmask, cap * 128 * sizeof(uint4), ctx->stream), "pool quad masks");
     return FL_OK;
 }
 
 void free_brick_arrays(fl_ctx* ctx, fl_pool* P) {
-    void* ps[10] = {P->nbr, P->list, P->wmax, P->part, P->fluid, P->nb27, P->bclass, P->slow_cnt, P->slow_off, P->smask};
+    void* ps[11] = {P->nbr,  P->list,     P->wmax,     P->part,  P->fluid, P->nb27,
+                    P->bclass, P->slow_cnt, P->slow_off, P->smask, P->qmask};
     for (void* p : ps)
         if (p) cudaFreeAsync(p, ctx->stream);
     P->nbr = nullptr; P->list = nullptr; P->wmax = nullptr; P->part = nullptr; P->fluid = nullptr;
     P->nb27 = nullptr; P->bclass = nullptr; P->slow_cnt = nullptr; P->slow_off = nullptr; P->smask = nullptr;
+    P->qmask = nullptr;
 }
 
 void drop_graph(fl_pool* P) {
@@ -1125,7 +1165,8 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
     const unsigned tgrid = (unsigned)std::max<size_t>(1, std::min<size_t>(n, (size_t)ctx->num_sms * 4));
     k_slow_table<false><<<tgrid, 512, 0, ctx->stream>>>(n, P->list, P->bclass, P->nbr, P->mesh.level, P->mesh.x,
                                                         P->mesh.y, P->mesh.z, P->mesh.case_id, P->d_cases, P->nb27,
-                                                        P->slow_cnt, P->smask, nullptr, nullptr, ctx->dev_status);
+                                                        P->slow_cnt, P->smask, P->qmask, nullptr, nullptr,
+                                                        ctx->dev_status);
     FL_CHECK_LAUNCH(ctx, "k_slow_table count");
     P->case_begin.assign(P->cases.size() + 1, 0);
     for (size_t i = 0; i < n; ++i) P->case_begin[cs[i] + 1]++;
@@ -1149,16 +1190,22 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
     if (run >= (1ull << 32)) return fl_set_error(ctx, FL_E_CAPACITY, "more than 2^32 stencil descriptors");
     sc[n] = (uint32_t)run;
     P->num_desc = run;
+    P->lvl_desc.assign(P->maxL + 2, 0);
+    for (int l = 0; l <= P->maxL; ++l) P->lvl_desc[l] = sc[P->cls_off[1][l]];
+    P->lvl_desc[P->maxL + 1] = sc[n];
     if (run > P->desc_cap) {
         if (P->desc) cudaFreeAsync(P->desc, ctx->stream);
+        if (P->pv) cudaFreeAsync(P->pv, ctx->stream);
         P->desc_cap = run + run / 4 + 1024;
         FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->desc, P->desc_cap * 8, ctx->stream), "stencil descriptors");
+        FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->pv, P->desc_cap * 4, ctx->stream), "descriptor values");
     }
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->slow_off, sc.data(), (n + 1) * 4, cudaMemcpyHostToDevice, ctx->stream),
                 "descriptor offsets");
     k_slow_table<true><<<tgrid, 512, 0, ctx->stream>>>(n, P->list, P->bclass, P->nbr, P->mesh.level, P->mesh.x,
                                                        P->mesh.y, P->mesh.z, P->mesh.case_id, P->d_cases, P->nb27,
-                                                       nullptr, nullptr, P->slow_off, P->desc, ctx->dev_status);
+                                                       nullptr, nullptr, nullptr, P->slow_off, P->desc,
+                                                       ctx->dev_status);
     FL_CHECK_LAUNCH(ctx, "k_slow_table emit");
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "descriptor sync");  // sc is freed on return
     P->lups = 0;
@@ -1358,11 +1405,18 @@ void launch_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm = nul
             unsigned grid = std::min<unsigned>(cnt, (unsigned)ctx->num_sms * P->grid_mult);
             k_collide_fast<<<grid, 128, 0, ctx->stream>>>(a, P->nb27);
         } else if (kind == 1) {
-            unsigned grid = std::min<unsigned>(cnt, (unsigned)ctx->num_sms * kGeneralCtasPerSm);
+            unsigned grid = std::min<unsigned>(cnt, (unsigned)ctx->num_sms * 4);
             a.desc = P->desc;
             a.desc_off = P->slow_off + off;
             a.smask = P->smask;
-            k_collide_general<<<grid, 256, 0, fork ? P->side : ctx->stream>>>(a, P->nb27);
+            a.qmask = P->qmask;
+            a.pv = P->pv;
+            cudaStream_t st = fork ? P->side : ctx->stream;
+            const uint32_t dd0 = P->lvl_desc[l], dd1 = P->lvl_desc[l + 1];
+            if (dd1 > dd0) {
+                k_interface<<<fl_blocks(dd1 - dd0, 256, ctx->num_sms * 8), 256, 0, st>>>(a, dd0, dd1, P->pv);
+            }
+            k_collide_general<<<grid, 128, 0, st>>>(a, P->nb27);
         } else {
             k_collide_solid<<<fl_blocks((size_t)cnt * 512, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(a);
         }
@@ -1482,6 +1536,7 @@ int fl_pool_destroy(fl_ctx* ctx, fl_pool* P) {
     if (P->mesh.x) fl_mesh_free(ctx, &P->mesh);
     if (P->adapt_scratch) cudaFreeAsync(P->adapt_scratch, ctx->stream);
     if (P->desc) cudaFreeAsync(P->desc, ctx->stream);
+    if (P->pv) cudaFreeAsync(P->pv, ctx->stream);
     cudaStreamSynchronize(ctx->stream);
     if (P->d_cases) cudaFree(P->d_cases);
     if (P->d_dom) cudaFree(P->d_dom);

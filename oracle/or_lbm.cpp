@@ -34,12 +34,19 @@ const int OPP[Q] = {0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15, 18
 const float W0 = 1.0f / 3.0f, W1 = 1.0f / 18.0f, W2 = 1.0f / 36.0f;
 inline float wq(int q) { return q == 0 ? W0 : (q < 7 ? W1 : W2); }
 
+// c_q . u as the sum of its non-zero terms in x, y, z order (c = +-1 is a
+// sign, so no product is formed; c_0 . u = 0).
 inline float cdot(int q, float ux, float uy, float uz) {
-    float a = (float)CX[q] * ux;
-    float b = (float)CY[q] * uy;
-    float c = (float)CZ[q] * uz;
-    float s = a + b;
-    return s + c;
+    const float t[3] = {CX[q] > 0 ? ux : -ux, CY[q] > 0 ? uy : -uy, CZ[q] > 0 ? uz : -uz};
+    const int c[3] = {CX[q], CY[q], CZ[q]};
+    float s = 0.0f;
+    bool any = false;
+    for (int k = 0; k < 3; ++k) {
+        if (!c[k]) continue;
+        s = any ? s + t[k] : t[k];
+        any = true;
+    }
+    return s;
 }
 
 inline float feq1(int q, float rho, float ux, float uy, float uz, float base) {
