@@ -50,6 +50,7 @@ __device__ __forceinline__ float Wq(int q) {
 }
 
 constexpr uint32_t kSlow = 0xFFFFFFFEu;
+constexpr int kMaxPoolLevels = 14;  // case max_level is 0..13
 
 }  // namespace
 
@@ -1017,11 +1018,11 @@ struct fl_pool {
     void* adapt_scratch = nullptr;
     size_t adapt_scratch_bytes = 0;
     int grid_mult = 4;
-    // the general class of a level runs on `side`, concurrently with the
-    // interior and all-solid classes on the context stream (fork/join events)
+    // dependency-graph launch order: per level a stream for the general,
+    // interface and all-solid bricks and one for the interior bricks
     int streams = 2;
-    cudaStream_t side = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaStream_t sg[kMaxPoolLevels] = {}, sf[kMaxPoolLevels] = {};
+    cudaEvent_t evg[kMaxPoolLevels][2] = {}, evf[kMaxPoolLevels][2] = {}, ev_root = nullptr;
 };
 
 namespace {
@@ -1369,8 +1370,8 @@ struct LaunchTimer {
     std::vector<int> kind;        // 0 interior kernel, 1 general kernel, 2 all-solid bricks
 };
 
-void launch_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm = nullptr) {
-    StepArgs a;
+StepArgs level_args(fl_ctx* ctx, fl_pool* P, int l, int sub) {
+    StepArgs a{};
     a.level = l;
     a.sub = sub;
     a.R = P->f[P->parity[l]];
@@ -1383,63 +1384,104 @@ void launch_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm = nul
     a.nbr = P->nbr;
     a.cases = P->d_cases;
     a.dev_status = ctx->dev_status;
-    const bool fork = !tm && P->streams > 1 && P->side && P->cls_cnt[1][l] &&
-                      (P->cls_cnt[0][l] || P->cls_cnt[2][l]);
-    if (fork) {
-        cudaEventRecord(P->ev_fork, ctx->stream);
-        cudaStreamWaitEvent(P->side, P->ev_fork, 0);
+    a.desc = P->desc;
+    a.smask = P->smask;
+    a.qmask = P->qmask;
+    a.pv = P->pv;
+    return a;
+}
+
+// One brick class of level l on stream st (kind 0 interior, 1 general with its
+// descriptor values, 2 all-solid), bracketed by timing events when tm is set.
+void launch_class(fl_ctx* ctx, fl_pool* P, StepArgs a, int l, int kind, cudaStream_t st, LaunchTimer* tm) {
+    const uint32_t off = P->cls_off[kind][l], cnt = P->cls_cnt[kind][l];
+    if (!cnt) return;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (tm) {
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, st);
     }
-    for (int kind = 0; kind < 3; ++kind) {
-        uint32_t off = P->cls_off[kind][l];
-        uint32_t cnt = P->cls_cnt[kind][l];
-        if (!cnt) continue;
-        cudaEvent_t e0 = nullptr, e1 = nullptr;
-        if (tm) {
-            cudaEventCreate(&e0);
-            cudaEventCreate(&e1);
-            cudaEventRecord(e0, ctx->stream);
-        }
-        a.list = P->list + off;
-        a.count = cnt;
-        if (kind == 0) {
-            unsigned grid = std::min<unsigned>(cnt, (unsigned)ctx->num_sms * P->grid_mult);
-            k_collide_fast<<<grid, 128, 0, ctx->stream>>>(a, P->nb27);
-        } else if (kind == 1) {
-            unsigned grid = std::min<unsigned>(cnt, (unsigned)ctx->num_sms * 4);
-            a.desc = P->desc;
-            a.desc_off = P->slow_off + off;
-            a.smask = P->smask;
-            a.qmask = P->qmask;
-            a.pv = P->pv;
-            cudaStream_t st = fork ? P->side : ctx->stream;
-            const uint32_t dd0 = P->lvl_desc[l], dd1 = P->lvl_desc[l + 1];
-            if (dd1 > dd0) {
-                k_interface<<<fl_blocks(dd1 - dd0, 256, ctx->num_sms * 8), 256, 0, st>>>(a, dd0, dd1, P->pv);
-            }
-            k_collide_general<<<grid, 128, 0, st>>>(a, P->nb27);
-        } else {
-            k_collide_solid<<<fl_blocks((size_t)cnt * 512, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(a);
-        }
-        if (tm) {
-            cudaEventRecord(e1, ctx->stream);
-            tm->ev.push_back(e0);
-            tm->ev.push_back(e1);
-            tm->sites.push_back(P->fluid_cls[kind][l]);
-            tm->kind.push_back(kind);
-        }
+    a.list = P->list + off;
+    a.count = cnt;
+    if (kind == 0) {
+        unsigned grid = std::min<unsigned>(cnt, (unsigned)ctx->num_sms * P->grid_mult);
+        k_collide_fast<<<grid, 128, 0, st>>>(a, P->nb27);
+    } else if (kind == 1) {
+        a.desc_off = P->slow_off + off;
+        const uint32_t dd0 = P->lvl_desc[l], dd1 = P->lvl_desc[l + 1];
+        if (dd1 > dd0) k_interface<<<fl_blocks(dd1 - dd0, 256, ctx->num_sms * 8), 256, 0, st>>>(a, dd0, dd1, P->pv);
+        k_collide_general<<<std::min<unsigned>(cnt, (unsigned)ctx->num_sms * 4), 128, 0, st>>>(a, P->nb27);
+    } else {
+        k_collide_solid<<<fl_blocks((size_t)cnt * 512, 256, ctx->num_sms * 8), 256, 0, st>>>(a);
     }
-    if (fork) {
-        cudaEventRecord(P->ev_join, P->side);
-        cudaStreamWaitEvent(ctx->stream, P->ev_join, 0);
+    if (tm) {
+        cudaEventRecord(e1, st);
+        tm->ev.push_back(e0);
+        tm->ev.push_back(e1);
+        tm->sites.push_back(P->fluid_cls[kind][l]);
+        tm->kind.push_back(kind);
+    }
+}
+
+// Sub-steps emitted per level within one level-0 step (dependency graph mode).
+struct Dag {
+    int k[kMaxPoolLevels] = {};
+};
+
+// One sub-step of level l.  Without a Dag every class runs in order on the
+// context stream.  With one, level l's general, interface and all-solid bricks
+// (the only bricks other levels read or that read other levels: coarse and
+// fine sources are always interface bricks) run on P->sg[l], after level l's
+// previous interior sub-step and the latest general sub-steps of levels l - 1
+// and l + 1; its interior bricks run on P->sf[l], after level l's previous
+// general sub-step.  Same-stream order covers the rest, including the
+// write-after-read of each level's two population buffers.
+void launch_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm, Dag* dag) {
+    const StepArgs a = level_args(ctx, P, l, sub);
+    if (!dag) {
+        for (int kind = 0; kind < 3; ++kind) launch_class(ctx, P, a, l, kind, ctx->stream, tm);
+    } else {
+        const int k = dag->k[l]++;
+        cudaStream_t sg = P->sg[l], sf = P->sf[l];
+        if (k > 0) cudaStreamWaitEvent(sg, P->evf[l][(k - 1) & 1], 0);
+        if (l > 0 && dag->k[l - 1] > 0) cudaStreamWaitEvent(sg, P->evg[l - 1][(dag->k[l - 1] - 1) & 1], 0);
+        if (l < P->maxL && dag->k[l + 1] > 0) cudaStreamWaitEvent(sg, P->evg[l + 1][(dag->k[l + 1] - 1) & 1], 0);
+        launch_class(ctx, P, a, l, 1, sg, nullptr);
+        launch_class(ctx, P, a, l, 2, sg, nullptr);
+        cudaEventRecord(P->evg[l][k & 1], sg);
+        if (k > 0) cudaStreamWaitEvent(sf, P->evg[l][(k - 1) & 1], 0);
+        launch_class(ctx, P, a, l, 0, sf, nullptr);
+        cudaEventRecord(P->evf[l][k & 1], sf);
     }
     P->parity[l] ^= 1;
 }
 
-void step_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm = nullptr) {
-    launch_level(ctx, P, l, sub, tm);
+void step_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm, Dag* dag) {
+    launch_level(ctx, P, l, sub, tm, dag);
     if (l < P->maxL) {
-        step_level(ctx, P, l + 1, 0, tm);
-        step_level(ctx, P, l + 1, 1, tm);
+        step_level(ctx, P, l + 1, 0, tm, dag);
+        step_level(ctx, P, l + 1, 1, tm, dag);
+    }
+}
+
+// One level-0 step: in order on the context stream, or as the dependency graph
+// forked from and joined back into the context stream.
+void level0_step(fl_ctx* ctx, fl_pool* P, LaunchTimer* tm = nullptr) {
+    if (tm || P->streams < 2) {
+        step_level(ctx, P, 0, 0, tm, nullptr);
+        return;
+    }
+    Dag dag;
+    cudaEventRecord(P->ev_root, ctx->stream);
+    for (int l = 0; l <= P->maxL; ++l) {
+        cudaStreamWaitEvent(P->sg[l], P->ev_root, 0);
+        cudaStreamWaitEvent(P->sf[l], P->ev_root, 0);
+    }
+    step_level(ctx, P, 0, 0, nullptr, &dag);
+    for (int l = 0; l <= P->maxL; ++l) {
+        cudaStreamWaitEvent(ctx->stream, P->evg[l][(dag.k[l] - 1) & 1], 0);
+        cudaStreamWaitEvent(ctx->stream, P->evf[l][(dag.k[l] - 1) & 1], 0);
     }
 }
 
@@ -1470,10 +1512,15 @@ int fl_pool_create(fl_ctx* ctx, const fl_lbm_case* cases, int ncases, fl_pool** 
     }
     int rc = FL_OK;
     auto fail = [&](int r) { fl_pool_destroy(ctx, P); return r; };
-    if (cudaStreamCreateWithFlags(&P->side, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&P->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&P->ev_join, cudaEventDisableTiming) != cudaSuccess)
-        return fail(fl_set_error(ctx, FL_E_CUDA, "fl_pool_create: stream or event creation failed"));
+    bool sok = cudaEventCreateWithFlags(&P->ev_root, cudaEventDisableTiming) == cudaSuccess;
+    for (int l = 0; l < kMaxPoolLevels && sok; ++l) {
+        sok = cudaStreamCreateWithFlags(&P->sg[l], cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&P->sf[l], cudaStreamNonBlocking) == cudaSuccess;
+        for (int j = 0; j < 2 && sok; ++j)
+            sok = cudaEventCreateWithFlags(&P->evg[l][j], cudaEventDisableTiming) == cudaSuccess &&
+                  cudaEventCreateWithFlags(&P->evf[l][j], cudaEventDisableTiming) == cudaSuccess;
+    }
+    if (!sok) return fail(fl_set_error(ctx, FL_E_CUDA, "fl_pool_create: stream or event creation failed"));
     // case tables sized for every slot a pool can hold (cases may be added later)
     if (cudaMalloc(&P->d_cases, kMaxCases * sizeof(LbmCaseDev)) != cudaSuccess) return fail(FL_E_OOM);
     if (cudaMalloc(&P->d_dom, kMaxCases * sizeof(fl_domain_dev::Case)) != cudaSuccess) return fail(FL_E_OOM);
@@ -1544,9 +1591,15 @@ int fl_pool_destroy(fl_ctx* ctx, fl_pool* P) {
     if (P->case_max) cudaFree(P->case_max);
     if (P->cons) cudaFree(P->cons);
     if (P->d_mask) cudaFree(P->d_mask);
-    if (P->side) cudaStreamDestroy(P->side);
-    if (P->ev_fork) cudaEventDestroy(P->ev_fork);
-    if (P->ev_join) cudaEventDestroy(P->ev_join);
+    for (int l = 0; l < kMaxPoolLevels; ++l) {
+        if (P->sg[l]) cudaStreamDestroy(P->sg[l]);
+        if (P->sf[l]) cudaStreamDestroy(P->sf[l]);
+        for (int j = 0; j < 2; ++j) {
+            if (P->evg[l][j]) cudaEventDestroy(P->evg[l][j]);
+            if (P->evf[l][j]) cudaEventDestroy(P->evf[l][j]);
+        }
+    }
+    if (P->ev_root) cudaEventDestroy(P->ev_root);
     delete P;
     return FL_OK;
 }
@@ -1555,7 +1608,7 @@ int fl_pool_step(fl_ctx* ctx, fl_pool* P, int nsteps) {
     if (!ctx || !P || nsteps < 0) return FL_E_INVALID_ARG;
     for (int i = 0; i < nsteps; ++i) {
         if (!P->graphs) {
-            step_level(ctx, P, 0, 0);
+            level0_step(ctx, P);
             FL_CHECK_LAUNCH(ctx, "k_collide_stream");
             continue;
         }
@@ -1568,7 +1621,7 @@ int fl_pool_step(fl_ctx* ctx, fl_pool* P, int nsteps) {
             std::memcpy(saved, P->parity, sizeof(saved));
             cudaGraph_t g;
             FL_TRY_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "capture begin");
-            step_level(ctx, P, 0, 0);
+            level0_step(ctx, P);
             cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
             std::memcpy(P->parity, saved, sizeof(saved));
             FL_TRY_CUDA(ctx, e, "capture end");
@@ -1669,7 +1722,7 @@ int fl_pool_profile_steps(fl_ctx* ctx, fl_pool* P, int nsteps, double* kernel_ms
                           uint64_t* fluid_sites) {
     if (!ctx || !P || nsteps < 0) return FL_E_INVALID_ARG;
     LaunchTimer tm;
-    for (int i = 0; i < nsteps; ++i) step_level(ctx, P, 0, 0, &tm);
+    for (int i = 0; i < nsteps; ++i) level0_step(ctx, P, &tm);
     FL_CHECK_LAUNCH(ctx, "collide-stream");
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "profile sync");
     double ms[3] = {0.0, 0.0, 0.0};
@@ -1891,7 +1944,7 @@ int fl_pool_set_options(fl_ctx* ctx, fl_pool* P, int use_graphs, int grid_mult) 
 
 int fl_pool_set_class_streams(fl_ctx* ctx, fl_pool* P, int streams) {
     if (!ctx || !P || streams < 1 || streams > 2) return FL_E_INVALID_ARG;
-    cudaStreamSynchronize(P->side);
+    cudaStreamSynchronize(ctx->stream);
     P->streams = streams;
     drop_graph(P);
     return FL_OK;

@@ -349,9 +349,12 @@ int fl_pool_download_case(fl_ctx* ctx, fl_pool* pool, int32_t id, int32_t* x, in
                           uint8_t* level, float* f, size_t* nbricks);
 /* use_graphs: replay captured CUDA graphs per level-0 step; grid_mult: CTAs per SM (0 keeps). */
 int fl_pool_set_options(fl_ctx* ctx, fl_pool* pool, int use_graphs, int grid_mult);
-/* streams = 2 (default): each level sub-step runs its general bricks on a second stream,
- * concurrently with its interior and all-solid bricks (fork/join events, also inside the
- * captured graphs); streams = 1: the three classes run in order on the context stream. */
+/* streams = 2 (default): each level-0 step runs as a dependency graph over two streams per
+ * level -- general, interface and all-solid bricks on one, interior bricks on the other --
+ * joined by events (coarse and fine sources are always interface bricks, so only the
+ * general launches of neighbouring levels wait on each other); the graph is forked from and
+ * joined back into the context stream and captured like the rest of the step.
+ * streams = 1: every launch in order on the context stream. */
 int fl_pool_set_class_streams(fl_ctx* ctx, fl_pool* pool, int streams);
 
 #ifdef __cplusplus
