@@ -219,18 +219,18 @@ def run_gpu(args):
     total_lups = 0
     regrids = 0
     regrid_ms = []
-    launches = 0
+    launches0 = ctx.launch_count()
     stop = timer(ctx)
     for k in range(args.steps):
         step_no = args.warmup + k + 1
         inf = pool.info()
         total_lups += inf.fluid_lups_per_step
-        launches += sum(1 << l for l in range(inf.max_level + 1) if inf.bricks_per_level[l])
         pool.step(1)
         if step_no % REGRID_EVERY == 0:
             pool.regrid()
             regrids += 1
     ms = stop()
+    launches = ctx.launch_count() - launches0
     clk = clocks.stop()
     rep.barrier()
     ms_max = rep.max(ms)
@@ -249,14 +249,14 @@ def run_gpu(args):
     achieved = BYTES_PER_LUP * sites / (kms * 1e-3) / 1e9
     tr = ncu_traffic()
     per_kernel = {}
-    for name, (m, la, st_) in zip(("k_collide_fast", "k_collide_general", "k_collide_solid"), prof):
+    for name, (m, la, st_) in zip(("k_collide_fast", "k_interface + k_collide_general", "k_collide_solid"), prof):
         if la:
             per_kernel[name] = {"launches": la, "avg_launch_ms": round(m / la, 4), "fluid_sites": int(st_),
                                 "achieved_gbs": round(BYTES_PER_LUP * st_ / (m * 1e-3) / 1e9, 1),
                                 "time_share": round(m / kms, 3)}
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": (round(tr * sites / nla) if tr else None),
-                "kernel": "collide-stream (k_collide_fast + k_collide_general + k_collide_solid)",
+                "kernel": "collide-stream (k_collide_fast + k_interface + k_collide_general + k_collide_solid)",
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                 "algorithmic_bytes_per_launch": round(BYTES_PER_LUP * sites / nla), "launches_profiled": nla,
                 "avg_launch_ms": round(kms / nla, 4), "per_kernel": per_kernel}
@@ -355,7 +355,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=25)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-microbench", action="store_true")

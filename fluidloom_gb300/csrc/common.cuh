@@ -27,6 +27,7 @@ struct fl_ctx {
     std::string last_error;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // fl_ctx_timer_start / stop
     void* soa = nullptr;                       // structure-of-arrays field manager (fields.cu)
+    uint64_t launches = 0;                     // kernels launched on behalf of this context
 };
 
 void fl_soa_release_all(fl_ctx* ctx);
@@ -53,7 +54,14 @@ int fl_collect_device_status(fl_ctx* ctx, const char* what);
         if (_e != cudaSuccess) return fl_check_cuda((ctx), _e, what); \
     } while (0)
 
-#define FL_CHECK_LAUNCH(ctx, what) FL_TRY_CUDA(ctx, cudaGetLastError(), what)
+// After each kernel launch: counts it and checks the launch.
+#define FL_CHECK_LAUNCH(ctx, what)                    \
+    do {                                              \
+        ++(ctx)->launches;                            \
+        FL_TRY_CUDA(ctx, cudaGetLastError(), what);   \
+    } while (0)
+// After a batch of launches counted by the caller.
+#define FL_CHECK_ERRORS(ctx, what) FL_TRY_CUDA(ctx, cudaGetLastError(), what)
 
 static inline size_t fl_align256(size_t b) { return (b + 255) & ~(size_t)255; }
 

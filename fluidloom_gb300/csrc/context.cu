@@ -196,6 +196,12 @@ int fl_ctx_timer_start(fl_ctx* ctx) {
     return FL_OK;
 }
 
+int fl_ctx_launch_count(fl_ctx* ctx, uint64_t* count) {
+    if (!ctx || !count) return FL_E_INVALID_ARG;
+    *count = ctx->launches;
+    return FL_OK;
+}
+
 int fl_ctx_timer_stop(fl_ctx* ctx, float* ms) {
     if (!ctx || !ms || !ctx->ev0) return FL_E_INVALID_ARG;
     FL_TRY_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream), "event record");

@@ -800,49 +800,74 @@ __global__ void k_remap(PoolView p, size_t M, const uint32_t* __restrict__ osrc,
     }
 }
 
-// Per-brick FP64 partial sums of rho, j (fluid sites, volume 8^-level) and the
-// fluid-site count.
-__global__ void __launch_bounds__(512) k_brick_sums(PoolView p, size_t n, double* __restrict__ part,
+// Double-single (hi, lo) FP32 pairs for the per-brick sums: Knuth's TwoSum
+// (exact rounding error of one addition; needs no FMA contraction) and the
+// pair addition with one renormalisation -- about 2^-44 relative per add.
+struct DS {
+    float hi, lo;
+};
+__device__ __forceinline__ DS ds_add(DS a, DS b) {
+    float s = a.hi + b.hi;
+    float bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (b.hi - bb);
+    e = e + (a.lo + b.lo);
+    float h = s + e;
+    return DS{h, e - (h - s)};
+}
+
+// One CTA of 128 threads per brick (persistent), thread = x-quad: per brick
+// the sums of rho and j over its fluid sites, weighted by the site volume
+// 2^-3l, and the fluid-site count.  Quads accumulate in double-single, warps
+// reduce in double-single by shuffles, the four warp totals in FP64.
+__global__ void __launch_bounds__(128) k_brick_sums(PoolView p, size_t n, double* __restrict__ part,
                                                     uint32_t* __restrict__ fluid) {
-    __shared__ double red[4][16];
-    __shared__ uint32_t redc[16];
+    __shared__ double red[4][4];
+    __shared__ uint32_t redc[4];
+    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    const int x0 = (t & 1) * 4, y = (t >> 1) & 7, z = t >> 4;
+    const int own = x0 + 8 * y + 64 * z;
     for (size_t b = blockIdx.x; b < n; b += gridDim.x) {
-        const int s = threadIdx.x;
         const int l = p.blevel[b];
         const LbmCaseDev& c = p.cases[p.bcase[b]];
         const float* F = cur_buf(p, l);
-        int64_t G[3] = {(int64_t)p.bx[b] * 8 + (s & 7), (int64_t)p.by[b] * 8 + ((s >> 3) & 7),
-                        (int64_t)p.bz[b] * 8 + (s >> 6)};
-        double v[4] = {0, 0, 0, 0};
+        float4 v4[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) v4[q] = __ldg((const float4*)(F + fidx(p.cap, q, b, own)));
+        DS acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
         uint32_t cnt = 0;
-        if (!solid_at(c, G[0], G[1], G[2], l)) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            if (solid_at(c, (int64_t)p.bx[b] * 8 + x0 + i, (int64_t)p.by[b] * 8 + y, (int64_t)p.bz[b] * 8 + z, l))
+                continue;
             float f[Q];
 #pragma unroll
-            for (int q = 0; q < Q; ++q) f[q] = F[fidx(p.cap, q, b, s)];
-            float rho, jx, jy, jz;
-            moments(f, rho, jx, jy, jz);
-            v[0] = rho; v[1] = jx; v[2] = jy; v[3] = jz;
-            cnt = 1;
+            for (int q = 0; q < Q; ++q) f[q] = i == 0 ? v4[q].x : (i == 1 ? v4[q].y : (i == 2 ? v4[q].z : v4[q].w));
+            float m[4];
+            moments(f, m[0], m[1], m[2], m[3]);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) acc[k] = ds_add(acc[k], DS{m[k], 0.f});
+            ++cnt;
         }
+#pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            for (int k = 0; k < 4; ++k) v[k] += __shfl_xor_sync(0xFFFFFFFFu, v[k], o);
-            cnt += __shfl_xor_sync(0xFFFFFFFFu, cnt, o);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                DS other{__shfl_xor_sync(0xFFFFFFFFu, acc[k].hi, o), __shfl_xor_sync(0xFFFFFFFFu, acc[k].lo, o)};
+                acc[k] = ds_add(acc[k], other);
+            }
         }
-        if ((s & 31) == 0) {
-            for (int k = 0; k < 4; ++k) red[k][s >> 5] = v[k];
-            redc[s >> 5] = cnt;
+        cnt = __reduce_add_sync(0xFFFFFFFFu, cnt);
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) red[k][wid] = (double)acc[k].hi + (double)acc[k].lo;
+            redc[wid] = cnt;
         }
         __syncthreads();
-        if (s < 4) {
-            double t = 0.0;
-            for (int w = 0; w < 16; ++w) t += red[s][w];
-            part[b * 4 + s] = t / (double)(1ull << (3 * l));
+        if (t < 4) {
+            double s4 = ((red[t][0] + red[t][1]) + red[t][2]) + red[t][3];
+            part[b * 4 + t] = s4 / (double)(1ull << (3 * l));
         }
-        if (s == 4) {
-            uint32_t t = 0;
-            for (int w = 0; w < 16; ++w) t += redc[w];
-            fluid[b] = t;
-        }
+        if (t == 4) fluid[b] = (redc[0] + redc[1]) + (redc[2] + redc[3]);
         __syncthreads();
     }
 }
@@ -1015,6 +1040,7 @@ struct fl_pool {
     uint64_t fluid_per_level[16] = {0};
     int graphs = 1;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one level-0 step, per level-0 parity
+    uint64_t graph_kernels[2] = {0, 0};             // kernel nodes of each
     void* adapt_scratch = nullptr;
     size_t adapt_scratch_bytes = 0;
     int grid_mult = 4;
@@ -1175,7 +1201,7 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->d_case_begin, P->case_begin.data(), P->case_begin.size() * 4,
                                      cudaMemcpyHostToDevice, ctx->stream), "case ranges");
     // fluid sites per brick -> LUPs per level-0 step
-    k_brick_sums<<<fl_blocks(n, 1, ctx->num_sms * 8), 512, 0, ctx->stream>>>(view(P), n, P->part, P->fluid);
+    k_brick_sums<<<fl_blocks(n, 1, ctx->num_sms * 16), 128, 0, ctx->stream>>>(view(P), n, P->part, P->fluid);
     FL_CHECK_LAUNCH(ctx, "k_brick_sums");
     std::vector<uint32_t> fl(n), sc(n + 1);
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(fl.data(), P->fluid, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "fluid");
@@ -1404,6 +1430,7 @@ void launch_class(fl_ctx* ctx, fl_pool* P, StepArgs a, int l, int kind, cudaStre
     }
     a.list = P->list + off;
     a.count = cnt;
+    ctx->launches += (kind == 1 && P->lvl_desc[l + 1] > P->lvl_desc[l]) ? 2 : 1;
     if (kind == 0) {
         unsigned grid = std::min<unsigned>(cnt, (unsigned)ctx->num_sms * P->grid_mult);
         k_collide_fast<<<grid, 128, 0, st>>>(a, P->nb27);
@@ -1609,7 +1636,7 @@ int fl_pool_step(fl_ctx* ctx, fl_pool* P, int nsteps) {
     for (int i = 0; i < nsteps; ++i) {
         if (!P->graphs) {
             level0_step(ctx, P);
-            FL_CHECK_LAUNCH(ctx, "k_collide_stream");
+            FL_CHECK_ERRORS(ctx, "k_collide_stream");
             continue;
         }
         // One level-0 step changes only level 0's parity (level l >= 1 runs an
@@ -1620,9 +1647,12 @@ int fl_pool_step(fl_ctx* ctx, fl_pool* P, int nsteps) {
             int saved[16];
             std::memcpy(saved, P->parity, sizeof(saved));
             cudaGraph_t g;
+            const uint64_t c0 = ctx->launches;
             FL_TRY_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "capture begin");
             level0_step(ctx, P);
             cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+            P->graph_kernels[p0] = ctx->launches - c0;  // recorded, not launched: counted per replay
+            ctx->launches = c0;
             std::memcpy(P->parity, saved, sizeof(saved));
             FL_TRY_CUDA(ctx, e, "capture end");
             e = cudaGraphInstantiate(&P->graph[p0], g, 0);
@@ -1630,6 +1660,7 @@ int fl_pool_step(fl_ctx* ctx, fl_pool* P, int nsteps) {
             FL_TRY_CUDA(ctx, e, "graph instantiate");
         }
         FL_TRY_CUDA(ctx, cudaGraphLaunch(P->graph[p0], ctx->stream), "graph launch");
+        ctx->launches += P->graph_kernels[p0];
         P->parity[0] ^= 1;
     }
     return FL_OK;
@@ -1708,7 +1739,7 @@ int fl_pool_flags(fl_ctx* ctx, fl_pool* P, int32_t* flags, float* wmax) {
 int fl_pool_conservation(fl_ctx* ctx, fl_pool* P, double* out) {
     if (!ctx || !P || !out) return FL_E_INVALID_ARG;
     size_t n = P->mesh.num_cells;
-    k_brick_sums<<<fl_blocks(n, 1, ctx->num_sms * 8), 512, 0, ctx->stream>>>(view(P), n, P->part, P->fluid);
+    k_brick_sums<<<fl_blocks(n, 1, ctx->num_sms * 16), 128, 0, ctx->stream>>>(view(P), n, P->part, P->fluid);
     FL_CHECK_LAUNCH(ctx, "k_brick_sums");
     int nc = (int)P->cases.size();
     k_case_sums<<<std::min(nc, ctx->num_sms * 4), 256, 0, ctx->stream>>>(P->part, P->d_case_begin, nc, P->cons);
@@ -1723,7 +1754,7 @@ int fl_pool_profile_steps(fl_ctx* ctx, fl_pool* P, int nsteps, double* kernel_ms
     if (!ctx || !P || nsteps < 0) return FL_E_INVALID_ARG;
     LaunchTimer tm;
     for (int i = 0; i < nsteps; ++i) level0_step(ctx, P, &tm);
-    FL_CHECK_LAUNCH(ctx, "collide-stream");
+    FL_CHECK_ERRORS(ctx, "collide-stream");
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "profile sync");
     double ms[3] = {0.0, 0.0, 0.0};
     uint64_t sites[3] = {0, 0, 0};

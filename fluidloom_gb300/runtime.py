@@ -43,6 +43,12 @@ class Context:
     def sync(self):
         self.call("fl_ctx_synchronize")
 
+    def launch_count(self):
+        """Kernels launched on behalf of this context so far (graph replays count their nodes)."""
+        c = ctypes.c_uint64()
+        self.call("fl_ctx_launch_count", ctypes.byref(c))
+        return c.value
+
     def set_stream(self, stream_ptr):
         self.call("fl_ctx_set_stream", ctypes.c_void_p(stream_ptr))
 

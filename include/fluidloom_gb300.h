@@ -63,6 +63,8 @@ int fl_host_free_pinned(fl_ctx* ctx, void* ptr);
 /* CUDA-event timer on the context stream: start records, stop records, waits and returns ms. */
 int fl_ctx_timer_start(fl_ctx* ctx);
 int fl_ctx_timer_stop(fl_ctx* ctx, float* ms);
+/* Kernels this context has launched so far (a replayed graph counts its kernel nodes). */
+int fl_ctx_launch_count(fl_ctx* ctx, uint64_t* count);
 
 /* ---- keys */
 /* hilbert::encode over n cells (include/fluidloom/core/hilbert/HilbertCodec.h:29;
