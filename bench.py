@@ -110,15 +110,18 @@ def measured_peak():
 
 
 def ncu_traffic():
-    """Per-launch DRAM bytes of the collide-stream from the committed ncu summary, scaled per fluid site."""
-    p = os.path.join(ROOT, "profiles", "collide_stream_traffic.json")
+    """DRAM bytes per fluid site update of the collide-stream, from the committed ncu summary
+    (dram__bytes_read.sum + dram__bytes_write.sum of one level-3 sub-step / its fluid sites)."""
+    p = os.path.join(ROOT, "profiles", "collide_stream_sphere_ncu.md")
     if not os.path.exists(p):
         return None
-    try:
-        d = json.load(open(p))
-        return float(d["dram_bytes_per_fluid_site"])
-    except Exception:
-        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_fluid_site:"):
+            try:
+                return float(line.split(":", 1)[1])
+            except ValueError:
+                return None
+    return None
 
 
 # ---------------------------------------------------------------- GPU arm

@@ -9,9 +9,13 @@ same jobs (one job at a time, arrival order).
 Jobs (synthetic, seeded): Poisson arrivals; 70 % lid-driven cavities, 30 %
 sphere-in-channel; base size log-uniform between 16^3 and 128x64x64 sites;
 1-3 refinement levels; steps uniform in the given range; regrid every 20
-steps.  Admission is gated by each job's population footprint against the HBM
-budget.  A job's result is its final state; for --check jobs it is compared
-bit for bit with the same job run alone.
+steps.  Jobs are admitted at pool steps that are multiples of the regrid
+interval, so every resident job's regrids fall on the same pool steps and one
+regrid of the due cases serves them all (each job still regrids every 20 of
+its own steps, exactly as when it runs alone).  Admission is gated by each
+job's population footprint against the HBM budget.  A job's result is its
+final state; for --check jobs it is compared bit for bit with the same job run
+alone.
 """
 import argparse
 import collections
@@ -49,7 +53,7 @@ def make_jobs(rate, duration, steps_range, seed=5):
         if t >= duration:
             break
         lv = int(rng.integers(1, 4))
-        steps = int(rng.integers(steps_range[0], steps_range[1] + 1))
+        steps = int(rng.integers(steps_range[0], steps_range[1] + 1))  # regrid interval 20 for every job
         if rng.random() < 0.7:
             edge = int(np.exp(rng.uniform(np.log(16), np.log(64))))
             edge = int(min(64, max(16, 8 * round(edge / 8))))
@@ -64,21 +68,31 @@ def make_jobs(rate, duration, steps_range, seed=5):
     return jobs
 
 
-def run_served(ctx, jobs, budget_bytes, check_ids=()):
-    """Continuous batching; returns per-job (arrival, start, end) and the LUPs done."""
+def run_served(ctx, jobs, budget_bytes, check_ids=(), regrid_every=20, resident_bytes=None):
+    """Continuous batching; returns the LUPs done, the makespan and the pool steps run.
+
+    Jobs are admitted in arrival order while the resident population footprint
+    stays within min(budget_bytes, resident_bytes): enough resident bricks to
+    keep HBM busy, and no more, so queued jobs start in order instead of all
+    sharing the GPU at once."""
+    cap = budget_bytes if resident_bytes is None else min(budget_bytes, resident_bytes)
     pending = collections.deque(sorted(jobs, key=lambda j: j.arrival))
     queue, active = collections.deque(), {}
     pool = None
     used = 0
     lups = 0
     steps_run = 0
+    phase = 0  # pool steps since the last regrid boundary (restarts whenever the pool empties)
     t0 = time.perf_counter()
     while pending or queue or active:
         now = time.perf_counter() - t0
         while pending and pending[0].arrival <= now:
             queue.append(pending.popleft())
         admit = []
-        while queue and (used + queue[0].est_bytes <= budget_bytes or not active and not admit):
+        if not active:
+            phase = 0
+        boundary = phase % regrid_every == 0
+        while boundary and queue and (used + queue[0].est_bytes <= cap or not active and not admit):
             j = queue.popleft()
             used += j.est_bytes
             admit.append(j)
@@ -100,13 +114,17 @@ def run_served(ctx, jobs, budget_bytes, check_ids=()):
         lups += pool.info().fluid_lups_per_step
         pool.step(1)
         steps_run += 1
+        phase += 1
         due = []
         for cid, j in active.items():
             j.done += 1
             if j.regrid_every and j.done % j.regrid_every == 0 and j.done < j.steps:
                 due.append(cid)
         if due:
-            pool.regrid_cases(due)
+            if len(due) == len(active):
+                pool.regrid()
+            else:
+                pool.regrid_cases(due)
         fin = [cid for cid, j in active.items() if j.done >= j.steps]
         if fin:
             ctx.sync()
@@ -153,13 +171,16 @@ def main(argv=None):
     ap.add_argument("--duration", type=float, default=60.0)
     ap.add_argument("--steps", type=int, nargs=2, default=[200, 2000])
     ap.add_argument("--budget-gb", type=float, default=150.0)
+    ap.add_argument("--resident-gb", type=float, default=6.0,
+                    help="admission stops while the resident population footprint exceeds this")
     ap.add_argument("--check", type=int, default=8, help="jobs whose result is compared with their solo run")
     ap.add_argument("--seed", type=int, default=5)
     args = ap.parse_args(argv)
     ctx = Context(0)
     jobs = make_jobs(args.rate, args.duration, args.steps, args.seed)
     check_ids = set(range(min(args.check, len(jobs))))
-    lups, makespan, steps_run = run_served(ctx, jobs, args.budget_gb * 1e9, check_ids)
+    lups, makespan, steps_run = run_served(ctx, jobs, args.budget_gb * 1e9, check_ids,
+                                           resident_bytes=args.resident_gb * 1e9)
     lat = [j.end - j.arrival for j in jobs]
     # plain sequential: each job alone, one after another in arrival order
     end_prev, lat_plain, solo_s, solo_lups, mismatched = 0.0, [], 0.0, 0, []
@@ -177,6 +198,8 @@ def main(argv=None):
             if not same:
                 mismatched.append(j.jid)
     res = {"jobs": len(jobs), "rate_per_s": args.rate, "duration_s": args.duration, "steps_range": args.steps,
+           "admission": "arrival order, resident footprint <= %.1f GB of a %.0f GB budget" % (
+               args.resident_gb, args.budget_gb),
            "served_makespan_s": makespan, "served_mlups": lups / makespan / 1e6,
            "served_p50_s": percentile(lat, 50), "served_p99_s": percentile(lat, 99),
            "plain_mlups": solo_lups / solo_s / 1e6, "plain_makespan_s": end_prev,

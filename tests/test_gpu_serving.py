@@ -71,3 +71,21 @@ def test_add_remove_and_per_case_regrid_match_solo(ctx):
     _same(mix, ib, sb, 0)
     info = mix.info()
     assert info.num_active_cases == 3
+
+
+def test_served_loop_matches_solo_runs(ctx):
+    """The serving loop (admission at regrid boundaries, shared regrids, removal at
+    completion) leaves every job with the state of its solo run."""
+    from fluidloom_gb300 import lbm, serving
+    a, b, c = _cases()
+    jobs = [serving.Job(0, 0.0, a, 45), serving.Job(1, 0.0, b, 30), serving.Job(2, 0.002, c, 61)]
+    lups, makespan, steps_run = serving.run_served(ctx, jobs, budget_bytes=1e12, check_ids={0, 1, 2})
+    assert lups > 0 and makespan > 0 and steps_run >= 61
+    for j in jobs:
+        assert j.end is not None and j.end >= j.start >= j.arrival
+        _, _, solo = serving.run_solo(ctx, j)
+        g1, f1 = j.result
+        g2, f2 = solo
+        for k in ("x", "y", "z", "level"):
+            np.testing.assert_array_equal(g1[k], g2[k])
+        np.testing.assert_array_equal(f1, f2)
