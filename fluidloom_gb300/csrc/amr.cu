@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(kT) k_detect_face6(fl_mesh_dev m, fl_domain_de
             int64_t p[3] = {anc[0], anc[1], anc[2]};
             p[f >> 1] += (f & 1) ? ss : -1;
             if (!fold3(p, d, dom.anchor_level)) continue;
-            uint32_t r = fl_locate(T.t1, T.t3, tk, tv, lg, shadow, dom, cs, m.case_id != nullptr, p, sl, nullptr);
+            uint32_t r = fl_locate(T.t1, T.t3, tk, tv, lg, shadow, dom, cs, m.case_id != nullptr, p, sl);
             if (r == FL_INVALID_INDEX) continue;
             if ((int)shadow[r] > sl + 1) { viol[i] = 1; ++local; break; }
         }
@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(kT) k_detect_full26(fl_mesh_dev m, fl_domain_d
         int64_t p[3];
         for (int a = 0; a < 3; ++a) p[a] = dv[a] < 0 ? anc[a] - 1 : (dv[a] > 0 ? anc[a] + size : anc[a]);
         if (!fold3(p, d, dom.anchor_level)) continue;
-        uint32_t r = fl_locate(T.t1, T.t3, tk, tv, lg, m.level, dom, cs, m.case_id != nullptr, p, lvl, nullptr);
+        uint32_t r = fl_locate(T.t1, T.t3, tk, tv, lg, nullptr, dom, cs, m.case_id != nullptr, p, lvl);
         if (r == FL_INVALID_INDEX) continue;
         if ((int)shadow[i] >= (int)shadow[r] + 2) { viol[r] = 1; ++local; }
     }
@@ -155,37 +155,49 @@ __device__ bool find_group(const KeyTables& T, const fl_mesh_dev& m, const fl_do
     for (int c = 0; c < 8; ++c) {
         int64_t sx = m.x[i] | (c & 1), sy = m.y[i] | ((c >> 1) & 1), sz = m.z[i] | ((c >> 2) & 1);
         uint64_t key = fl_anchor_key(T.t1, T.t3, dom.depth, cs, m.case_id != nullptr, sx << sh, sy << sh, sz << sh);
-        uint32_t j = fl_hash_lookup(tk, tv, lg, key);
-        if (j == FL_INVALID_INDEX) return false;
-        if (m.level[j] != l || m.flags[j] != -1 || m.state[j] != 0) return false;
+        const uint32_t v = fl_hash_lookup(tk, tv, lg, key);
+        if (v == FL_INVALID_INDEX || fl_packed_level(v) != l) return false;
+        const uint32_t j = fl_packed_idx(v);
+        if (m.flags[j] != -1 || m.state[j] != 0) return false;
         mem[c] = j;
     }
     return true;
 }
 
+// The FULL26 merge condition: no leaf touching the octet from outside ends
+// above its level.  The 8 members x 26 directions probe points take, per axis,
+// only five coordinates -- the last fine point below the octet, the first and
+// last of its lower cell, the first of its upper cell, the first point above
+// -- so the 98 combinations with at least one outside coordinate are exactly
+// the distinct probes outside the octet (the 27 others lie inside it).
 __device__ bool group_balanced(const KeyTables& T, const fl_mesh_dev& m, const fl_domain_dev& dom,
                                const uint64_t* tk, const uint32_t* tv, int lg, const uint8_t* shadow,
                                const uint32_t* mem) {
     uint16_t cs = m.case_id ? m.case_id[mem[0]] : 0;
     const fl_domain_dev::Case& d = dom.c[m.case_id ? cs : 0];
     int l = m.level[mem[0]];
-    for (int c = 0; c < 8; ++c) {
-        size_t j = mem[c];
-        int sh = dom.anchor_level - l;
-        int64_t anc[3] = {(int64_t)m.x[j] << sh, (int64_t)m.y[j] << sh, (int64_t)m.z[j] << sh};
-        int64_t size = (int64_t)1 << sh;
-        for (int k = 0; k < 26; ++k) {
-            int kk = k < 13 ? k : k + 1;
-            int dv[3] = {kk % 3 - 1, (kk / 3) % 3 - 1, kk / 9 - 1};
-            int64_t p[3];
-            for (int a = 0; a < 3; ++a) p[a] = dv[a] < 0 ? anc[a] - 1 : (dv[a] > 0 ? anc[a] + size : anc[a]);
-            if (!fold3(p, d, dom.anchor_level)) continue;
-            uint32_t r = fl_locate(T.t1, T.t3, tk, tv, lg, m.level, dom, cs, m.case_id != nullptr, p, l, nullptr);
-            if (r == FL_INVALID_INDEX) continue;
-            bool inside = false;
-            for (int q = 0; q < 8; ++q) inside |= (mem[q] == r);
-            if (!inside && (int)shadow[r] > l) return false;
-        }
+    int sh = dom.anchor_level - l;
+    int64_t size = (int64_t)1 << sh;
+    int64_t v[3][5];
+    const int64_t b[3] = {(int64_t)m.x[mem[0]] << sh, (int64_t)m.y[mem[0]] << sh, (int64_t)m.z[mem[0]] << sh};
+    for (int a = 0; a < 3; ++a) {
+        v[a][0] = b[a] - 1;
+        v[a][1] = b[a];
+        v[a][2] = b[a] + size - 1;
+        v[a][3] = b[a] + size;
+        v[a][4] = b[a] + 2 * size;
+    }
+    for (int k = 0; k < 125; ++k) {
+        const int ix = k % 5, iy = (k / 5) % 5, iz = k / 25;
+        const bool out = ix == 0 || ix == 4 || iy == 0 || iy == 4 || iz == 0 || iz == 4;
+        if (!out) continue;
+        int64_t p[3] = {v[0][ix], v[1][iy], v[2][iz]};
+        if (!fold3(p, d, dom.anchor_level)) continue;
+        uint32_t r = fl_locate(T.t1, T.t3, tk, tv, lg, nullptr, dom, cs, m.case_id != nullptr, p, l);
+        if (r == FL_INVALID_INDEX) continue;
+        bool inside = false;  // only on a periodic axis of one octet's extent
+        for (int q = 0; q < 8; ++q) inside |= (mem[q] == r);
+        if (!inside && (int)shadow[r] > l) return false;
     }
     return true;
 }
@@ -523,7 +535,7 @@ int fl_adapt_prepare(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cf
     int rc = fl_launch_cell_keys(ctx, mesh->x, mesh->y, mesh->z, mesh->level, mesh->case_id, dom.depth,
                                  dom.anchor_level, w.keys, n);
     if (rc) return rc;
-    rc = fl_hash_build_with(ctx, w.tk, w.tv, w.cap, w.keys, nullptr, n, w.win);  // value = input index
+    rc = fl_hash_build_with(ctx, w.tk, w.tv, w.cap, w.keys, nullptr, n, w.win, mesh->level);  // level | index
     if (rc) return rc;
     FL_TRY_CUDA(ctx, cudaMemsetAsync(w.counters, 0, 64, ctx->stream), "adapt counters");
     if (run_balance) {
@@ -644,7 +656,7 @@ int fl_balance_enforce(fl_ctx* ctx, fl_mesh* mesh, const fl_adapt_config* cfg, f
     rc = fl_launch_cell_keys(ctx, mesh->x, mesh->y, mesh->z, mesh->level, mesh->case_id, dom.depth, dom.anchor_level,
                              keys, n);
     if (rc) return rc;
-    rc = fl_hash_build_with(ctx, tk, tv, cap, keys, nullptr, n, win);
+    rc = fl_hash_build_with(ctx, tk, tv, cap, keys, nullptr, n, win, mesh->level);
     if (rc) return rc;
     fl_mesh_dev md{mesh->x, mesh->y, mesh->z, mesh->level, mesh->state, mesh->flags, mesh->material, mesh->case_id, n};
     fl_balance_result r;
@@ -677,7 +689,7 @@ int fl_neighbour_rebuild(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config
     rc = fl_launch_cell_keys(ctx, mesh->x, mesh->y, mesh->z, mesh->level, mesh->case_id, dom.depth, dom.anchor_level,
                              keys, n);
     if (rc) return rc;
-    rc = fl_hash_build_with(ctx, tk, tv, cap, keys, nullptr, n, win);
+    rc = fl_hash_build_with(ctx, tk, tv, cap, keys, nullptr, n, win, mesh->level);
     if (rc) return rc;
     fl_mesh_dev md{mesh->x, mesh->y, mesh->z, mesh->level, mesh->state, mesh->flags, mesh->material, mesh->case_id, n};
     rc = fl_neighbours_with(ctx, md, dom, tk, tv, cap, subslots, nbr);
@@ -802,7 +814,7 @@ int fl_merge(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, const
     rc = fl_launch_cell_keys(ctx, mesh->x, mesh->y, mesh->z, mesh->level, mesh->case_id, dom.depth, dom.anchor_level,
                              keys, n);
     if (rc) return rc;
-    rc = fl_hash_build_with(ctx, tk, tv, cap, keys, nullptr, n, win);
+    rc = fl_hash_build_with(ctx, tk, tv, cap, keys, nullptr, n, win, mesh->level);
     if (rc) return rc;
     unsigned nb = fl_blocks(n, kT, ctx->num_sms * 8);
     int lg = fl_hash_lg(cap);

@@ -83,8 +83,9 @@ __global__ void __launch_bounds__(256) k_interp(fl_mesh_dev m, fl_domain_dev dom
             int64_t p[3] = {cx + (k & 1), cy + ((k >> 1) & 1), cz + ((k >> 2) & 1)};
             if (p[0] < 0 || p[1] < 0 || p[2] < 0) continue;
             uint64_t key = fl_anchor_key(t1, t3, dom.depth, 0, false, p[0] << sh, p[1] << sh, p[2] << sh);
-            uint32_t j = fl_hash_lookup(tk, tv, lg, key);
-            if (j == FL_INVALID_INDEX || m.level[j] != l) continue;
+            const uint32_t hv = fl_hash_lookup(tk, tv, lg, key);
+            if (hv == FL_INVALID_INDEX || fl_packed_level(hv) != l) continue;
+            const uint32_t j = fl_packed_idx(hv);
             const float* v = field + (size_t)j * C;
             for (uint32_t c = 0; c < C; ++c) o[c] = __fadd_rn(o[c], __fmul_rn(0.125f, v[c]));
         }
@@ -172,7 +173,7 @@ int fl_interp_trilinear(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config*
                                  keys, n);
         if (rc) return rc;
     }
-    rc = fl_hash_build_with(ctx, tk, tv, cap, keys, nullptr, n, win);
+    rc = fl_hash_build_with(ctx, tk, tv, cap, keys, nullptr, n, win, mesh->level);
     if (rc) return rc;
     fl_mesh_dev md{mesh->x, mesh->y, mesh->z, mesh->level, mesh->state, mesh->flags, mesh->material, nullptr, n};
     k_interp<<<fl_blocks(nq, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(md, dom, tk, tv, fl_hash_lg(cap), field, C,

@@ -50,11 +50,14 @@ __global__ void k_hash_insert(uint64_t* __restrict__ tk, uint32_t* __restrict__ 
 }
 
 __global__ void k_hash_values(uint32_t* __restrict__ tv, const uint32_t* __restrict__ win,
-                              const uint32_t* __restrict__ vals, uint64_t cap) {
+                              const uint32_t* __restrict__ vals, const uint8_t* __restrict__ levels, uint64_t cap) {
     size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += stride) {
         uint32_t w = win[i];
-        if (w) tv[i] = vals ? vals[w - 1] : w - 1;
+        if (!w) continue;
+        if (vals) tv[i] = vals[w - 1];
+        else if (levels) tv[i] = ((uint32_t)levels[w - 1] << kPackedIdxBits) | (w - 1);
+        else tv[i] = w - 1;
     }
 }
 
@@ -109,7 +112,7 @@ __global__ void __launch_bounds__(256) k_neighbours(fl_mesh_dev m, fl_domain_dev
         bool in = true;
         for (int a = 0; a < 3; ++a)
             in = in && fold_axis(&p[a], (int64_t)d.ext[a] << dom.anchor_level, d.periodic[a]);
-        if (in) res = fl_locate(t1, t3, tk, tv, lg, m.level, dom, cs, m.case_id != nullptr, p, lvl, m.level);
+        if (in) res = fl_locate(t1, t3, tk, tv, lg, nullptr, dom, cs, m.case_id != nullptr, p, lvl);
         nbr[t] = res;
     }
 }
@@ -123,7 +126,9 @@ int fl_hash_lg(uint64_t cap) {
 }
 
 int fl_hash_build_with(fl_ctx* ctx, uint64_t* tk, uint32_t* tv, uint64_t cap, const uint64_t* keys,
-                       const uint32_t* vals, size_t n, uint32_t* win) {
+                       const uint32_t* vals, size_t n, uint32_t* win, const uint8_t* levels) {
+    if (levels && !vals && n >= ((size_t)1 << kPackedIdxBits))
+        return fl_set_error(ctx, FL_E_CAPACITY, "a mesh of 2^27 or more cells");
     unsigned cb = fl_blocks(cap, 256, ctx->num_sms * 8);
     k_hash_clear<<<cb, 256, 0, ctx->stream>>>(tk, tv, win, cap);
     FL_CHECK_LAUNCH(ctx, "k_hash_clear");
@@ -131,7 +136,7 @@ int fl_hash_build_with(fl_ctx* ctx, uint64_t* tk, uint32_t* tv, uint64_t cap, co
     int lg = fl_hash_lg(cap);
     k_hash_insert<<<fl_blocks(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(tk, win, lg, keys, n, ctx->dev_status);
     FL_CHECK_LAUNCH(ctx, "k_hash_insert");
-    k_hash_values<<<cb, 256, 0, ctx->stream>>>(tv, win, vals, cap);
+    k_hash_values<<<cb, 256, 0, ctx->stream>>>(tv, win, vals, vals ? nullptr : levels, cap);
     FL_CHECK_LAUNCH(ctx, "k_hash_values");
     return FL_OK;
 }

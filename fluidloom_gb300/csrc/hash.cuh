@@ -56,16 +56,25 @@ static __device__ __forceinline__ uint64_t fl_anchor_key(const uint8_t* t1, cons
     return k;
 }
 
-// Point location: the leaf whose `lv` equals l and whose anchor equals p with
-// the low (A - l) bits cleared.  Levels are probed outward from `start`; in a
-// valid leaf set at most one level matches, so the order does not change the
-// answer, only the number of lookups.
+// Tables over a mesh's own cells (built with the mesh's level column) store
+// level << 27 | cell index, so a probe learns the leaf's level without a
+// second random read.  Meshes of such tables hold fewer than 2^27 cells.
+constexpr int kPackedIdxBits = 27;
+constexpr uint32_t kPackedIdxMask = (1u << kPackedIdxBits) - 1;
+static __device__ __forceinline__ uint32_t fl_packed_idx(uint32_t v) {
+    return v == FL_INVALID_INDEX ? FL_INVALID_INDEX : (v & kPackedIdxMask);
+}
+static __device__ __forceinline__ int fl_packed_level(uint32_t v) { return (int)(v >> kPackedIdxBits); }
+
+// Point location: the leaf whose level (packed in the table value, or lv[]
+// when lv is given -- the balance's shadow levels) equals l and whose anchor
+// equals p with the low (A - l) bits cleared.  Levels are probed outward from
+// `start`; in a valid leaf set at most one level matches, so the order does
+// not change the answer, only the number of lookups.  Returns the cell index.
 static __device__ __forceinline__ uint32_t fl_locate(const uint8_t* t1, const uint16_t* t3,
                                                      const uint64_t* __restrict__ tk, const uint32_t* __restrict__ tv,
                                                      int lg, const uint8_t* __restrict__ lv, const fl_domain_dev& dom,
-                                                     uint16_t cs, bool has_case, const int64_t* p, int start,
-                                                     const uint8_t* unused) {
-    (void)unused;
+                                                     uint16_t cs, bool has_case, const int64_t* p, int start) {
     int maxl = dom.max_level;
     if (start > maxl) start = maxl;
     if (start < 0) start = 0;
@@ -77,16 +86,19 @@ static __device__ __forceinline__ uint32_t fl_locate(const uint8_t* t1, const ui
         int sh = dom.anchor_level - l;
         int64_t mask = ~(((int64_t)1 << sh) - 1);
         uint64_t key = fl_anchor_key(t1, t3, dom.depth, cs, has_case, p[0] & mask, p[1] & mask, p[2] & mask);
-        uint32_t idx = fl_hash_lookup(tk, tv, lg, key);
-        if (idx != FL_INVALID_INDEX && lv[idx] == l) return idx;
+        const uint32_t v = fl_hash_lookup(tk, tv, lg, key);
+        if (v == FL_INVALID_INDEX) continue;
+        const uint32_t idx = v & kPackedIdxMask;
+        if ((lv ? (int)lv[idx] : fl_packed_level(v)) == l) return idx;
     }
     return FL_INVALID_INDEX;
 }
 
 int fl_hash_lg(uint64_t cap);
 uint64_t fl_table_capacity(size_t n);
-// Clear + build; `win` is cap uint32 of scratch.
+// Clear + build; `win` is cap uint32 of scratch.  With `levels` (and no vals)
+// the values are levels[i] << 27 | i (n < 2^27, else FL_E_CAPACITY).
 int fl_hash_build_with(fl_ctx* ctx, uint64_t* tk, uint32_t* tv, uint64_t cap, const uint64_t* keys,
-                       const uint32_t* vals, size_t n, uint32_t* win);
+                       const uint32_t* vals, size_t n, uint32_t* win, const uint8_t* levels = nullptr);
 int fl_neighbours_with(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom, const uint64_t* tk,
                        const uint32_t* tv, uint64_t cap, int subslots, uint32_t* nbr);

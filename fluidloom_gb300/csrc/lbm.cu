@@ -1153,7 +1153,7 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
     rc = fl_launch_cell_keys(ctx, P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.level, P->mesh.case_id, dom.depth,
                              dom.anchor_level, keys, n);
     if (rc) return rc;
-    rc = fl_hash_build_with(ctx, tk, tv, cap, keys, nullptr, n, win);
+    rc = fl_hash_build_with(ctx, tk, tv, cap, keys, nullptr, n, win, P->mesh.level);
     if (rc) return rc;
     fl_mesh_dev md{P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.level, P->mesh.state, P->mesh.flags, P->mesh.material,
                    P->mesh.case_id, n};
