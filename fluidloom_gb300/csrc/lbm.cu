@@ -1041,6 +1041,7 @@ struct fl_pool {
     int graphs = 1;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one level-0 step, per level-0 parity
     uint64_t graph_kernels[2] = {0, 0};             // kernel nodes of each
+    uint64_t version = 0;                           // bumped whenever the emitted launches change
     void* adapt_scratch = nullptr;
     size_t adapt_scratch_bytes = 0;
     int grid_mult = 4;
@@ -1129,6 +1130,7 @@ void free_brick_arrays(fl_ctx* ctx, fl_pool* P) {
 }
 
 void drop_graph(fl_pool* P) {
+    ++P->version;
     for (int k = 0; k < 2; ++k) {
         if (P->graph[k]) cudaGraphExecDestroy(P->graph[k]);
         P->graph[k] = nullptr;
@@ -1514,6 +1516,11 @@ void level0_step(fl_ctx* ctx, fl_pool* P, LaunchTimer* tm = nullptr) {
 
 }  // namespace
 
+// Accessors for the execution graph (graph.cu): what a captured step depends
+// on, and the level-0 parity change a replay of n captured steps makes.
+uint64_t fl_pool_launch_key(const fl_pool* P) { return (P->version << 1) | (uint64_t)(P->parity[0] & 1); }
+void fl_pool_advance_parity(fl_pool* P, int nsteps) { P->parity[0] ^= (nsteps & 1); }
+
 extern "C" {
 
 int fl_pool_create(fl_ctx* ctx, const fl_lbm_case* cases, int ncases, fl_pool** out) {
@@ -1633,8 +1640,11 @@ int fl_pool_destroy(fl_ctx* ctx, fl_pool* P) {
 
 int fl_pool_step(fl_ctx* ctx, fl_pool* P, int nsteps) {
     if (!ctx || !P || nsteps < 0) return FL_E_INVALID_ARG;
+    cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
+    FL_TRY_CUDA(ctx, cudaStreamIsCapturing(ctx->stream, &capturing), "capture status");
     for (int i = 0; i < nsteps; ++i) {
-        if (!P->graphs) {
+        // inside a caller's stream capture the launches join that capture directly
+        if (!P->graphs || capturing != cudaStreamCaptureStatusNone) {
             level0_step(ctx, P);
             FL_CHECK_ERRORS(ctx, "k_collide_stream");
             continue;

@@ -359,6 +359,70 @@ int fl_pool_set_options(fl_ctx* ctx, fl_pool* pool, int use_graphs, int grid_mul
  * streams = 1: every launch in order on the context stream. */
 int fl_pool_set_class_streams(fl_ctx* ctx, fl_pool* pool, int streams);
 
+/* ---- Execution graph ----
+ * Replaces the reference runtime: ExecutionNode (include/fluidloom/runtime/nodes/ExecutionNode.h:37-169,
+ * read/write field sets, AMR level, halo depth), HazardAnalyzer::analyzeNodes/enforceHazards
+ * (src/runtime/dependency/HazardAnalyzer.cpp:8-136), DependencyGraph (DependencyGraphBuilder.cpp:12-131:
+ * Kahn's order, cycles rejected) and TopologicalScheduler::execute (TopologicalScheduler.cpp:16-71).
+ * Node kinds follow ExecutionNode::NodeType (KERNEL, HALO_EXCHANGE, BARRIER, ADAPT_MESH) plus the
+ * lattice-Boltzmann step of a pool (the reference's generated lbm_* KernelNodes) and host callbacks. */
+typedef struct fl_graph fl_graph;
+enum {
+    FL_NODE_KERNEL = 0,        /* fn(ctx, stream, user) enqueues asynchronous work on `stream` */
+    FL_NODE_HALO_EXCHANGE = 1, /* one GPU: ordering only (coarse/fine coupling is inside the step) */
+    FL_NODE_BARRIER = 2,       /* ordering only */
+    FL_NODE_ADAPT_MESH = 3,    /* fl_pool_regrid(pool): waits on the host, splits capture segments */
+    FL_NODE_LBM_STEP = 4,      /* fl_pool_step(pool, nsteps) */
+    FL_NODE_HOST = 5           /* host_fn(user) in stream order */
+};
+enum { FL_HAZARD_RAW = 0, FL_HAZARD_WAW = 1, FL_HAZARD_WAR = 2, FL_HAZARD_LEVEL_BARRIER = 3 };
+typedef int (*fl_node_fn)(fl_ctx* ctx, void* stream, void* user);
+typedef void (*fl_host_fn)(void* user);
+typedef struct fl_node_desc {
+    int32_t type;
+    char name[64];
+    int32_t level;       /* AMR level, -1 = none (ExecutionNode::amr_level) */
+    int32_t halo_depth;
+    const char* reads;   /* comma-separated field names, may be NULL (copied) */
+    const char* writes;
+    fl_node_fn fn;
+    fl_host_fn host_fn;
+    void* user;
+    fl_pool* pool;
+    int32_t nsteps;
+} fl_node_desc;
+typedef struct fl_hazard {
+    uint64_t from, to;   /* node ids (insertion order), from < to */
+    int32_t type;        /* FL_HAZARD_* */
+    char field[68];
+} fl_hazard;
+/* ctx may be NULL for a graph that is only analysed and ordered, never executed. */
+int fl_graph_create(fl_ctx* ctx, fl_graph** out);
+int fl_graph_destroy(fl_graph* graph);
+const char* fl_graph_last_error(fl_graph* graph);
+/* ids are 0, 1, 2, ... in insertion order (DependencyGraphBuilder assigns them the same way). */
+int fl_graph_add_node(fl_graph* graph, const fl_node_desc* desc, int64_t* id);
+/* An explicit edge (ExecutionNode::addSuccessor / addPredecessor). */
+int fl_graph_add_edge(fl_graph* graph, int64_t from, int64_t to);
+/* HazardAnalyzer::analyzeNodes + enforceHazards: every RAW, then WAW, WAR and level-barrier pair
+ * (i < j in insertion order) becomes one edge i -> j; count = hazards found, out[] the first cap. */
+int fl_graph_analyze(fl_graph* graph, fl_hazard* out, size_t cap, size_t* count);
+/* The hazards the last fl_graph_analyze found (n = their number, out[] the first cap). */
+int fl_graph_hazards(fl_graph* graph, fl_hazard* out, size_t cap, size_t* n);
+/* Topological order (Kahn, FIFO ready queue); FL_E_INVALID_ARG "Dependency graph contains cycles". */
+int fl_graph_build(fl_graph* graph);
+int fl_graph_order(fl_graph* graph, int64_t* ids, size_t cap, size_t* n);
+int fl_graph_num_edges(fl_graph* graph, size_t* n);
+/* Runs every node once in dependency order on up to 8 streams joined by events, forked from and
+ * joined into the context stream.  use_cuda_graphs: each stretch between ADAPT_MESH nodes is
+ * captured once and replayed while the pools it steps keep their topology and level-0 parity. */
+int fl_graph_execute(fl_graph* graph, int use_cuda_graphs);
+/* Per-node execution count and total time (CUDA events) while profiling is on (eager runs). */
+int fl_graph_set_profiling(fl_graph* graph, int on);
+int fl_graph_node_stats(fl_graph* graph, int64_t id, uint64_t* count, double* total_ms);
+/* Graphviz text of the graph (ExecutionNode::toDOT); len = full length, buf gets up to cap - 1. */
+int fl_graph_dot(fl_graph* graph, char* buf, size_t cap, size_t* len);
+
 #ifdef __cplusplus
 }
 #endif
