@@ -322,5 +322,112 @@ private:
     BrickPool& pool_;
 };
 
+namespace dependency {
+
+// The reference's DependencyGraph + HazardAnalyzer (include/fluidloom/runtime/dependency/
+// DependencyGraph.h:21-107, HazardAnalyzer.h:20-86) over one fl_graph: nodes are added with
+// their read/write field sets and level, analyzeNodes() enforces the hazards as edges,
+// build() computes the topological order (throws on cycles, as the reference does).
+class DependencyGraph {
+public:
+    enum class HazardType { RAW = FL_HAZARD_RAW, WAW = FL_HAZARD_WAW, WAR = FL_HAZARD_WAR,
+                            LEVEL_BARRIER = FL_HAZARD_LEVEL_BARRIER };
+    struct Hazard {
+        size_t from_node_idx, to_node_idx;
+        std::string field_name;
+        HazardType type;
+    };
+
+    explicit DependencyGraph(fl_ctx* ctx = nullptr) : ctx_(ctx) {
+        check(nullptr, fl_graph_create(ctx, &g_), "fl_graph_create");
+    }
+    ~DependencyGraph() { fl_graph_destroy(g_); }
+    DependencyGraph(const DependencyGraph&) = delete;
+    DependencyGraph& operator=(const DependencyGraph&) = delete;
+
+    int64_t addNode(int type, const std::string& name, const std::string& reads, const std::string& writes,
+                    int level = -1, fl_pool* pool = nullptr, int nsteps = 1, fl_node_fn fn = nullptr,
+                    fl_host_fn host_fn = nullptr, void* user = nullptr) {
+        fl_node_desc d{};
+        d.type = type;
+        name.copy(d.name, sizeof(d.name) - 1);
+        d.level = level;
+        d.reads = reads.c_str();
+        d.writes = writes.c_str();
+        d.pool = pool;
+        d.nsteps = nsteps;
+        d.fn = fn;
+        d.host_fn = host_fn;
+        d.user = user;
+        int64_t id = -1;
+        rc(fl_graph_add_node(g_, &d, &id), "addNode");
+        return id;
+    }
+    void addEdge(int64_t from, int64_t to) { rc(fl_graph_add_edge(g_, from, to), "addEdge"); }
+
+    std::vector<Hazard> analyzeNodes() {
+        size_t n = 0;
+        rc(fl_graph_analyze(g_, nullptr, 0, &n), "analyzeNodes");
+        std::vector<fl_hazard> raw(n);
+        rc(fl_graph_hazards(g_, raw.data(), n, &n), "hazards");
+        std::vector<Hazard> out;
+        for (const auto& h : raw) out.push_back({(size_t)h.from, (size_t)h.to, h.field, (HazardType)h.type});
+        return out;
+    }
+    void build() { rc(fl_graph_build(g_), "build"); }
+    std::vector<size_t> getTopologicalOrder() const {
+        size_t n = 0;
+        rc(fl_graph_order(g_, nullptr, 0, &n), "getTopologicalOrder");
+        std::vector<int64_t> ids(n);
+        rc(fl_graph_order(g_, ids.data(), n, &n), "getTopologicalOrder");
+        return std::vector<size_t>(ids.begin(), ids.end());
+    }
+    size_t getNumEdges() const {
+        size_t n = 0;
+        rc(fl_graph_num_edges(g_, &n), "getNumEdges");
+        return n;
+    }
+    std::string toDOT() const {
+        size_t n = 0;
+        rc(fl_graph_dot(g_, nullptr, 0, &n), "toDOT");
+        std::string s(n + 1, '\0');
+        rc(fl_graph_dot(g_, &s[0], n + 1, &n), "toDOT");
+        s.resize(n);
+        return s;
+    }
+    fl_graph* get() const { return g_; }
+    fl_ctx* context() const { return ctx_; }
+
+private:
+    void rc(int st, const char* what) const {
+        if (st != FL_OK) throw FluidLoomError(st, std::string(what) + ": " + fl_graph_last_error(g_));
+    }
+    fl_ctx* ctx_;
+    fl_graph* g_ = nullptr;
+};
+
+}  // namespace dependency
+
+namespace scheduler {
+
+// TopologicalScheduler (include/fluidloom/runtime/scheduler/TopologicalScheduler.h:15-57):
+// runs every node once in dependency order; execute() returns true on success like the
+// reference and records the host-side schedule time.
+class TopologicalScheduler {
+public:
+    explicit TopologicalScheduler(dependency::DependencyGraph& g, bool cuda_graphs = true)
+        : g_(g), cuda_graphs_(cuda_graphs) {}
+    bool execute() {
+        int st = fl_graph_execute(g_.get(), cuda_graphs_ ? 1 : 0);
+        if (st != FL_OK) throw FluidLoomError(st, std::string("execute: ") + fl_graph_last_error(g_.get()));
+        return true;
+    }
+
+private:
+    dependency::DependencyGraph& g_;
+    bool cuda_graphs_;
+};
+
+}  // namespace scheduler
 }  // namespace runtime
 }  // namespace fluidloom

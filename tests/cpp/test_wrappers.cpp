@@ -108,6 +108,38 @@ int main() {
         step.execute();
         dev.finish();
         EXPECT_TRUE(pool.info().num_bricks >= 8);
+        // the same three operations as an execution graph (test_hazard_analyzer.cpp / 
+        // test_topological_scheduler.cpp shapes): hazards chain them, the order is A, B, C
+        runtime::BrickPool pool2(dev, {c});
+        runtime::dependency::DependencyGraph g(dev.get());
+        int64_t a = g.addNode(FL_NODE_LBM_STEP, "lbm", "f", "f", -1, pool2.get(), 4);
+        int64_t b = g.addNode(FL_NODE_ADAPT_MESH, "adapt", "f,mesh", "f,mesh", -1, pool2.get());
+        int64_t d = g.addNode(FL_NODE_LBM_STEP, "lbm2", "f,mesh", "f", -1, pool2.get(), 4);
+        auto hz = g.analyzeNodes();
+        EXPECT_TRUE(hz.size() >= 2);
+        g.build();
+        auto order = g.getTopologicalOrder();
+        EXPECT_EQ(order.size(), (size_t)3);
+        EXPECT_EQ((int64_t)order[0], a);
+        EXPECT_EQ((int64_t)order[1], b);
+        EXPECT_EQ((int64_t)order[2], d);
+        runtime::scheduler::TopologicalScheduler sched(g, true);
+        EXPECT_TRUE(sched.execute());
+        dev.finish();
+        EXPECT_EQ(pool2.info().num_bricks, pool.info().num_bricks);
+        // a cycle is rejected (test_topological_scheduler.cpp:103-126)
+        runtime::dependency::DependencyGraph cyc;
+        int64_t x = cyc.addNode(FL_NODE_KERNEL, "A", "", "");
+        int64_t y = cyc.addNode(FL_NODE_KERNEL, "B", "", "");
+        cyc.addEdge(x, y);
+        cyc.addEdge(y, x);
+        bool threw = false;
+        try {
+            cyc.build();
+        } catch (const FluidLoomError&) {
+            threw = true;
+        }
+        EXPECT_TRUE(threw);
     }
     if (failures) {
         std::printf("%d FAILURES\n", failures);
