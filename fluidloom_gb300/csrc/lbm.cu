@@ -872,6 +872,45 @@ __global__ void __launch_bounds__(128) k_brick_sums(PoolView p, size_t n, double
     }
 }
 
+// Macroscopic fields of every site: rho and u from the current populations
+// (FP32, the collision's moment order); sites inside the sphere report 0.
+__global__ void __launch_bounds__(128) k_macroscopic(PoolView p, size_t n, float* __restrict__ rho,
+                                                     float* __restrict__ ux, float* __restrict__ uy,
+                                                     float* __restrict__ uz) {
+    const int t = threadIdx.x;
+    const int x0 = (t & 1) * 4, y = (t >> 1) & 7, z = t >> 4;
+    const int own = x0 + 8 * y + 64 * z;
+    for (size_t b = blockIdx.x; b < n; b += gridDim.x) {
+        const int l = p.blevel[b];
+        const LbmCaseDev& c = p.cases[p.bcase[b]];
+        const float* F = cur_buf(p, l);
+        float4 v4[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) v4[q] = __ldg((const float4*)(F + fidx(p.cap, q, b, own)));
+        float o[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            float f[Q];
+#pragma unroll
+            for (int q = 0; q < Q; ++q) f[q] = i == 0 ? v4[q].x : (i == 1 ? v4[q].y : (i == 2 ? v4[q].z : v4[q].w));
+            float r, jx, jy, jz;
+            moments(f, r, jx, jy, jz);
+            const bool solid =
+                solid_at(c, (int64_t)p.bx[b] * 8 + x0 + i, (int64_t)p.by[b] * 8 + y, (int64_t)p.bz[b] * 8 + z, l);
+            const float inv = 1.0f / r;
+            o[0][i] = solid ? 0.0f : r;
+            o[1][i] = solid ? 0.0f : jx * inv;
+            o[2][i] = solid ? 0.0f : jy * inv;
+            o[3][i] = solid ? 0.0f : jz * inv;
+        }
+        const size_t at = b * 512 + own;
+        *(float4*)(rho + at) = make_float4(o[0][0], o[0][1], o[0][2], o[0][3]);
+        *(float4*)(ux + at) = make_float4(o[1][0], o[1][1], o[1][2], o[1][3]);
+        *(float4*)(uy + at) = make_float4(o[2][0], o[2][1], o[2][2], o[2][3]);
+        *(float4*)(uz + at) = make_float4(o[3][0], o[3][1], o[3][2], o[3][3]);
+    }
+}
+
 // Per case (one CTA each): the case's brick partials (a contiguous range,
 // bricks being sorted by case then key) summed in a fixed order — thread t
 // takes bricks t, t+256, ..., then a fixed tree across threads.
@@ -1797,6 +1836,61 @@ int fl_pool_upload(fl_ctx* ctx, fl_pool* P, const float* f) {
     for (int l = 0; l < 16; ++l) P->parity[l] = 0;
     drop_graph(P);
     return FL_OK;
+}
+
+int fl_pool_macroscopic(fl_ctx* ctx, fl_pool* P, float* rho, float* ux, float* uy, float* uz) {
+    if (!ctx || !P || !rho || !ux || !uy || !uz) return FL_E_INVALID_ARG;
+    const size_t n = P->mesh.num_cells, sites = n * 512;
+    if (!n) return FL_OK;
+    float* d = nullptr;
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&d, sites * 16, ctx->stream), "macroscopic buffer");
+    k_macroscopic<<<fl_blocks(n, 1, ctx->num_sms * 16), 128, 0, ctx->stream>>>(view(P), n, d, d + sites,
+                                                                               d + 2 * sites, d + 3 * sites);
+    FL_CHECK_LAUNCH(ctx, "k_macroscopic");
+    float* out[4] = {rho, ux, uy, uz};
+    for (int k = 0; k < 4; ++k)
+        FL_TRY_CUDA(ctx, cudaMemcpyAsync(out[k], d + k * sites, sites * 4, cudaMemcpyDeviceToHost, ctx->stream),
+                    "macroscopic download");
+    cudaFreeAsync(d, ctx->stream);
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "macroscopic");
+    return fl_collect_device_status(ctx, "fl_pool_macroscopic");
+}
+
+int fl_pool_load(fl_ctx* ctx, fl_pool* P, size_t n, const int32_t* x, const int32_t* y, const int32_t* z,
+                 const uint8_t* level, const uint16_t* case_id, const float* f) {
+    if (!ctx || !P || !n || !x || !y || !z || !level || !case_id || !f) return FL_E_INVALID_ARG;
+    for (size_t i = 0; i < n; ++i) {
+        const int cs = case_id[i], l = level[i];
+        if (cs >= (int)P->cases.size() || !P->active[cs] || l > P->maxL)
+            return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_pool_load: brick with an unknown case or a level above the pool maximum");
+        const int32_t c[3] = {x[i], y[i], z[i]};
+        for (int a = 0; a < 3; ++a)
+            if (c[a] < 0 || c[a] >= (P->cases[cs].ext[a] << l))
+                return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_pool_load: brick outside its case's domain");
+    }
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "load");
+    if (n > P->cap) {
+        int rc = pool_grow(ctx, P, std::max((size_t)(n * 1.5), n + 64));
+        if (rc) return rc;
+    }
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->mesh.x, x, n * 4, cudaMemcpyHostToDevice, ctx->stream), "load");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->mesh.y, y, n * 4, cudaMemcpyHostToDevice, ctx->stream), "load");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->mesh.z, z, n * 4, cudaMemcpyHostToDevice, ctx->stream), "load");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->mesh.level, level, n, cudaMemcpyHostToDevice, ctx->stream), "load");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->mesh.case_id, case_id, n * 2, cudaMemcpyHostToDevice, ctx->stream), "load");
+    FL_TRY_CUDA(ctx, cudaMemsetAsync(P->mesh.state, 0, n, ctx->stream), "load");
+    FL_TRY_CUDA(ctx, cudaMemsetAsync(P->mesh.flags, 0, n * 4, ctx->stream), "load");
+    FL_TRY_CUDA(ctx, cudaMemsetAsync(P->mesh.material, 0, n * 4, ctx->stream), "load");
+    P->mesh.num_cells = n;
+    for (int q = 0; q < Q; ++q)
+        FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->f[0] + (size_t)q * P->cap * 512, f + (size_t)q * n * 512, n * 512 * 4,
+                                         cudaMemcpyHostToDevice, ctx->stream), "load populations");
+    for (int l = 0; l < 16; ++l) P->parity[l] = 0;
+    // an adapt with every flag 0 only sorts: bricks (and their populations) into key order
+    int rc = pool_regrid(ctx, P, -1, nullptr);
+    if (rc) return rc;
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "load");
+    return fl_collect_device_status(ctx, "fl_pool_load");
 }
 
 int fl_pool_set_velocities(fl_ctx* ctx, fl_pool* P, const float* wall_u, const float* inlet_u) {

@@ -65,6 +65,7 @@ class Pool:
         self.ctx = ctx
         arr = (LbmCase * len(cases))(*cases)
         self.ncases = len(cases)
+        self.cases = [LbmCase.from_buffer_copy(c) for c in cases]  # per case id, for snapshots
         h = ctypes.c_void_p()
         ctx.call("fl_pool_create", arr, len(cases), ctypes.byref(h))
         self.h = h
@@ -138,6 +139,10 @@ class Pool:
         ids = (ctypes.c_int32 * len(cases))()
         self.ctx.call("fl_pool_add_cases", self.h, arr, len(cases), ids)
         self.ncases = self.info().num_cases
+        for c, i in zip(cases, ids):
+            while len(self.cases) <= i:
+                self.cases.append(None)
+            self.cases[i] = LbmCase.from_buffer_copy(c)
         return list(ids)
 
     def remove_cases(self, ids):
@@ -162,6 +167,21 @@ class Pool:
         self.ctx.call("fl_pool_download_case", self.h, cid, *[a.ctypes.data_as(P) for a in (x, y, z, lv)],
                       f.ctypes.data_as(P) if with_f else None, ctypes.byref(nb))
         return {"x": x, "y": y, "z": z, "level": lv}, f
+
+    def macroscopic(self):
+        """Density and velocity of every site, shape (bricks, 512) each (0 inside the sphere)."""
+        n = self.info().num_bricks
+        out = [np.empty((n, 512), np.float32) for _ in range(4)]
+        self.ctx.call("fl_pool_macroscopic", self.h, *[a.ctypes.data_as(P) for a in out])
+        return {"density": out[0], "velocity": np.stack(out[1:], -1)}
+
+    def load(self, bricks, f):
+        """Replace bricks and populations by a saved state (see snapshot.save)."""
+        cols = [np.ascontiguousarray(bricks[k], t) for k, t in
+                (("x", np.int32), ("y", np.int32), ("z", np.int32), ("level", np.uint8), ("case_id", np.uint16))]
+        f = np.ascontiguousarray(f, np.float32)
+        self.ctx.call("fl_pool_load", self.h, ctypes.c_size_t(len(cols[0])), *[a.ctypes.data_as(P) for a in cols],
+                      f.ctypes.data_as(P))
 
     def close(self):
         if self.h:

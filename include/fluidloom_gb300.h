@@ -334,6 +334,16 @@ int fl_pool_profile_steps(fl_ctx* ctx, fl_pool* pool, int nsteps, double* kernel
                           uint64_t* fluid_sites);
 /* Replace the populations with a host array [19][n][512] (the layout fl_pool_download gives). */
 int fl_pool_upload(fl_ctx* ctx, fl_pool* pool, const float* f);
+/* Density and velocity of every site ([nbricks][512] host arrays each, bricks in pool order),
+ * computed on the device from the current populations; sites inside the sphere report 0.
+ * Replaces reading back the reference's density/velocity fields (SOAFieldManager::getDevicePtr,
+ * src/core/fields/SOAFieldManager.cpp:140-160) for output. */
+int fl_pool_macroscopic(fl_ctx* ctx, fl_pool* pool, float* rho, float* ux, float* uy, float* uz);
+/* Replace the pool's bricks and populations by a saved state (bricks of active cases, any order;
+ * f is [19][n][512]): the pool continues exactly as the pool the state came from.  Snapshot /
+ * restart (the reference keeps only placeholders for it, tests/restart/checkpoint_restart_test.cpp:17-60). */
+int fl_pool_load(fl_ctx* ctx, fl_pool* pool, size_t n, const int32_t* x, const int32_t* y, const int32_t* z,
+                 const uint8_t* level, const uint16_t* case_id, const float* f);
 /* Per-case moving-wall and inlet velocities ([ncases][3] host arrays, either may be NULL),
  * copied on the stream and used from the next step on. */
 int fl_pool_set_velocities(fl_ctx* ctx, fl_pool* pool, const float* wall_u, const float* inlet_u);
