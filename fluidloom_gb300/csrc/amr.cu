@@ -51,16 +51,26 @@ __device__ __forceinline__ bool fold3(int64_t* p, const fl_domain_dev::Case& d, 
     return true;
 }
 
-__global__ void k_shadow(fl_mesh_dev m, int mode, uint8_t* __restrict__ shadow) {
-    size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride)
-        shadow[i] = (uint8_t)(m.level[i] + ((mode == 1 && m.flags[i] > 0) ? 1 : 0));
+// Shadow level = the level a cell will have.  FACE6 follows the reference
+// (level + (flag > 0), update_shadow_levels, BalanceEnforcer.cpp:53-62; the
+// first round starts from the levels); FULL26 counts a flag only where the
+// cell will split (fluid, below the maximum level), so a flagged cell at the
+// maximum level does not push its neighbours.
+__device__ __forceinline__ uint8_t shadow_of(const fl_mesh_dev& m, size_t i, int mode, int max_level) {
+    const bool up = mode == 1 ? (m.flags[i] > 0 && m.state[i] == 0 && m.level[i] < max_level) : m.flags[i] > 0;
+    return (uint8_t)(m.level[i] + (up ? 1 : 0));
 }
 
-__global__ void k_shadow_update(fl_mesh_dev m, uint8_t* __restrict__ shadow) {
+__global__ void k_shadow(fl_mesh_dev m, int mode, int max_level, uint8_t* __restrict__ shadow) {
     size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride)
-        shadow[i] = (uint8_t)(m.level[i] + (m.flags[i] > 0 ? 1 : 0));
+        shadow[i] = mode == 0 ? m.level[i] : shadow_of(m, i, mode, max_level);
+}
+
+__global__ void k_shadow_update(fl_mesh_dev m, int mode, int max_level, uint8_t* __restrict__ shadow) {
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride)
+        shadow[i] = shadow_of(m, i, mode, max_level);
 }
 
 // detect_balance_violations (balance_enforce.cl:57-147), exact lookups.
@@ -439,7 +449,7 @@ int fl_balance_run(fl_ctx* ctx, fl_mesh_dev md, int32_t* flags, const fl_domain_
     if (md.n == 0) { r.converged = 1; if (res) *res = r; return FL_OK; }
     unsigned nb = fl_blocks(md.n, kT, ctx->num_sms * 8);
     int lg = fl_hash_lg(cap);
-    k_shadow<<<nb, kT, 0, ctx->stream>>>(md, mode, shadow);
+    k_shadow<<<nb, kT, 0, ctx->stream>>>(md, mode, max_level, shadow);
     FL_CHECK_LAUNCH(ctx, "k_shadow");
     int cap_it = mode == 0 ? max_iters : 4096;
     uint32_t it = 0;
@@ -463,7 +473,7 @@ int fl_balance_run(fl_ctx* ctx, fl_mesh_dev md, int32_t* flags, const fl_domain_
         // k_mark ran after detection regardless; with zero violations it marks nothing
         r.total_cells_marked_for_balance += h[1];
         if (h[1] == 0) { r.converged = 0; r.iterations = it + 1; break; }
-        k_shadow_update<<<nb, kT, 0, ctx->stream>>>(md, shadow);
+        k_shadow_update<<<nb, kT, 0, ctx->stream>>>(md, mode, max_level, shadow);
         FL_CHECK_LAUNCH(ctx, "k_shadow_update");
     }
     if (it == (uint32_t)cap_it) { r.converged = 0; r.iterations = it; }
@@ -545,7 +555,7 @@ int fl_adapt_prepare(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cf
     }
     unsigned nb = fl_blocks(n, kT, ctx->num_sms * 8);
     int lg = fl_hash_lg(w.cap);
-    k_shadow_update<<<nb, kT, 0, ctx->stream>>>(md, w.shadow);
+    k_shadow_update<<<nb, kT, 0, ctx->stream>>>(md, 1, cfg->max_refinement_level, w.shadow);  // final levels
     FL_CHECK_LAUNCH(ctx, "k_shadow_update");
     int check26 = cfg->enforce_2_1_balance && cfg->balance_mode == 1;
     k_leaders<<<nb, kT, 0, ctx->stream>>>(md, dom, w.tk, w.tv, lg, cfg->min_refinement_level, check26, w.shadow,

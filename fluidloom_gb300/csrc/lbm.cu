@@ -1317,10 +1317,17 @@ int pool_flags(fl_ctx* ctx, fl_pool* P, int use_vorticity) {
 }
 
 // One regrid: flags, adapt (FULL26), population remap into the spare buffer.
-int pool_regrid(fl_ctx* ctx, fl_pool* P, int use_vorticity, fl_adapt_stats* st, const uint8_t* due = nullptr) {
-    int rc = pool_flags(ctx, P, use_vorticity);
-    if (rc) return rc;
+// host_flags (one int32 per brick, pool order) replace the computed flags.
+int pool_regrid(fl_ctx* ctx, fl_pool* P, int use_vorticity, fl_adapt_stats* st, const uint8_t* due = nullptr,
+                const int32_t* host_flags = nullptr) {
     size_t n = P->mesh.num_cells;
+    int rc = FL_OK;
+    if (host_flags)
+        FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->mesh.flags, host_flags, n * 4, cudaMemcpyHostToDevice, ctx->stream),
+                    "flags");
+    else
+        rc = pool_flags(ctx, P, use_vorticity);
+    if (rc) return rc;
     if (due) {  // cases not due keep flag 0 and come out of the regrid unchanged
         FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->d_mask, due, P->cases.size(), cudaMemcpyHostToDevice, ctx->stream), "due");
         k_mask_flags<<<fl_blocks(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(n, P->mesh.case_id, P->d_mask,
@@ -1906,6 +1913,13 @@ int fl_pool_set_velocities(fl_ctx* ctx, fl_pool* P, const float* wall_u, const f
                                              cudaMemcpyHostToDevice, ctx->stream), "velocities");
     }
     return FL_OK;
+}
+
+int fl_pool_regrid_flags(fl_ctx* ctx, fl_pool* P, const int32_t* flags, fl_adapt_stats* st) {
+    if (!ctx || !P || !flags) return FL_E_INVALID_ARG;
+    int rc = pool_regrid(ctx, P, 0, st, nullptr, flags);
+    if (rc) return rc;
+    return fl_collect_device_status(ctx, "fl_pool_regrid_flags");
 }
 
 int fl_pool_regrid_cases(fl_ctx* ctx, fl_pool* P, const uint8_t* due, fl_adapt_stats* st) {

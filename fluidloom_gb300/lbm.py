@@ -149,6 +149,13 @@ class Pool:
         a = (ctypes.c_int32 * len(ids))(*ids)
         self.ctx.call("fl_pool_remove_cases", self.h, a, len(ids))
 
+    def regrid_flags(self, flags):
+        """Regrid with one int32 flag per brick (pool order): > 0 split, -1 merge, 0 keep."""
+        fl = np.ascontiguousarray(flags, np.int32)
+        st = AdaptStats()
+        self.ctx.call("fl_pool_regrid_flags", self.h, fl.ctypes.data_as(P), ctypes.byref(st))
+        return st
+
     def regrid_cases(self, due_ids):
         n = self.info().num_cases
         due = np.zeros(n, np.uint8)

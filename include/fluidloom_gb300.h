@@ -347,6 +347,10 @@ int fl_pool_load(fl_ctx* ctx, fl_pool* pool, size_t n, const int32_t* x, const i
 /* Per-case moving-wall and inlet velocities ([ncases][3] host arrays, either may be NULL),
  * copied on the stream and used from the next step on. */
 int fl_pool_set_velocities(fl_ctx* ctx, fl_pool* pool, const float* wall_u, const float* inlet_u);
+/* Regrid with caller-given flags (one int32 per brick in pool order: > 0 split, -1 merge, 0 keep),
+ * 2:1 balanced like every regrid: the refine_flags buffer AdaptMeshNode passes to the
+ * reference's adapt (src/runtime/nodes/AdaptMeshNode.cpp:52-63). */
+int fl_pool_regrid_flags(fl_ctx* ctx, fl_pool* pool, const int32_t* flags, fl_adapt_stats* stats);
 /* Regrid only the cases whose due[case id] is non-zero (host array of num_cases bytes); the other
  * cases come out unchanged. */
 int fl_pool_regrid_cases(fl_ctx* ctx, fl_pool* pool, const uint8_t* due, fl_adapt_stats* stats);

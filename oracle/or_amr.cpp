@@ -126,7 +126,8 @@ extern "C" void or_neighbours(const or_mesh* m, const or_domain* dom, int subslo
 //    Morton-low-bits hash silently misses cells).
 //  mode 1 (FULL26): face+edge+corner balance to a fixed point.  Every leaf
 //    probes its 26 neighbour points at its own size; a leaf n found with
-//    shadow(i) >= shadow(n) + 2 must refine.
+//    shadow(i) >= shadow(n) + 2 must refine, where shadow = level + 1 only
+//    for a cell that will split (flag > 0, fluid, below the maximum level).
 extern "C" int or_balance(or_mesh* m, const or_domain* dom, int mode, int max_level, int max_iters,
                           or_balance_stats* st) {
     std::memset(st, 0, sizeof(*st));
@@ -135,8 +136,11 @@ extern "C" int or_balance(or_mesh* m, const or_domain* dom, int mode, int max_le
     Index ix;
     build_index(m, dom, ix);
     std::vector<uint8_t> shadow(n), viol(n);
-    for (size_t i = 0; i < n; ++i)
-        shadow[i] = mode == 0 ? m->level[i] : (uint8_t)(m->level[i] + (m->flags[i] > 0 ? 1 : 0));
+    // FULL26: a flag raises the shadow level only where the cell will split
+    auto up = [&](size_t i) {
+        return mode == 0 ? m->flags[i] > 0 : (m->flags[i] > 0 && m->state[i] == 0 && m->level[i] < max_level);
+    };
+    for (size_t i = 0; i < n; ++i) shadow[i] = mode == 0 ? m->level[i] : (uint8_t)(m->level[i] + (up(i) ? 1 : 0));
     int cap = mode == 0 ? max_iters : 4096;
     uint32_t it = 0;
     for (; it < (uint32_t)cap; ++it) {
@@ -183,7 +187,7 @@ extern "C" int or_balance(or_mesh* m, const or_domain* dom, int mode, int max_le
         if (it < 64) st->per_iter_marked[it] = marked;
         st->marked += marked;
         if (marked == 0) { st->converged = 0; st->iterations = it + 1; return 0; }
-        for (size_t i = 0; i < n; ++i) shadow[i] = (uint8_t)(m->level[i] + (m->flags[i] > 0 ? 1 : 0));
+        for (size_t i = 0; i < n; ++i) shadow[i] = (uint8_t)(m->level[i] + (up(i) ? 1 : 0));
     }
     st->converged = 0;
     st->iterations = it;
@@ -216,8 +220,8 @@ extern "C" size_t or_adapt(or_mesh* m, const or_domain* dom, const or_adapt_cfg*
     std::vector<uint8_t> split(n, 0), merged(n, 0), leader(n, 0);
     for (size_t i = 0; i < n; ++i)
         split[i] = m->flags[i] > 0 && m->state[i] == 0 && m->level[i] < cfg->max_level;
-    std::vector<uint8_t> shadow(n);
-    for (size_t i = 0; i < n; ++i) shadow[i] = (uint8_t)(m->level[i] + (m->flags[i] > 0 ? 1 : 0));
+    std::vector<uint8_t> shadow(n);  // final levels (the FULL26 merge condition)
+    for (size_t i = 0; i < n; ++i) shadow[i] = (uint8_t)(m->level[i] + (split[i] ? 1 : 0));
     std::vector<uint32_t> members;  // [group][8]
     std::vector<uint32_t> group_of(n, INV);
     for (size_t i = 0; i < n; ++i) {

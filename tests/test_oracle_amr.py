@@ -129,3 +129,23 @@ def test_neighbours_uniform_periodic():
             kk = k if k < 13 else k + 1
             d = (kk % 3 - 1, (kk // 3) % 3 - 1, kk // 9 - 1)
             assert nbr[i, k] == idx[((x + d[0]) % 4, (y + d[1]) % 4, (z + d[2]) % 4)]
+
+
+def test_full26_flag_at_max_level_does_not_push_neighbours():
+    """A flagged cell already at the maximum level will not split, so it must not
+    make its one-level-coarser neighbours refine (FULL26 shadow levels)."""
+    # level-1 octant of a unit domain refined once more: cells at level 2 in
+    # [0, 2)^3 (level-1 cell 0 split), level 1 elsewhere
+    l1 = O.uniform_mesh(1)
+    keep = ~((l1["x"] == 0) & (l1["y"] == 0) & (l1["z"] == 0))
+    l2 = O.uniform_mesh(2)
+    inner = (l2["x"] < 2) & (l2["y"] < 2) & (l2["z"] < 2)
+    cols = {k: np.concatenate([l1[k][keep], l2[k][inner]]) for k in l1}
+    cols["flags"][:] = 0
+    cols["flags"][cols["level"] == 2] = 1  # flagged, but level 2 is the maximum
+    dom = O.domain(ext=(1, 1, 1))
+    flags, st = O.balance(cols, dom, 1, 2)
+    assert st.marked == 0 and (flags[cols["level"] == 1] == 0).all()
+    # with a maximum of 3 the same flags do split, and the level-1 neighbours must follow
+    flags3, st3 = O.balance(cols, dom, 1, 3)
+    assert st3.marked > 0 and (flags3[cols["level"] == 1] == 1).any()
