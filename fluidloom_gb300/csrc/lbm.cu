@@ -369,13 +369,15 @@ __device__ uint64_t resolve_source(const LbmCaseDev& c, const int32_t* bx, const
     return make_desc(kSrcBounce, q, s, own);
 }
 
-// Per list position p (one CTA of 512 threads per brick, thread = site): for
-// bricks of the general class, COUNT writes the number of descriptors to
-// cnt[p] and the brick's own-site solid mask (16 words), EMIT writes the
-// descriptors from desc + off[p] in site-major, q-minor order.  Sites inside
-// the sphere get none: their relaxation ignores what they pulled.
+// Per general brick (one CTA of 512 threads per brick, thread = site; gen
+// lists the bricks' positions p in the level lists): COUNT writes the number
+// of descriptors to cnt[p], the brick's own-site solid mask (16 words), its
+// per-quad masks and its fluid-site count; EMIT writes the descriptors from
+// desc + off[p], quad-major, then q, then site.  Sites inside the sphere get
+// none: their relaxation ignores what they pulled.
 template <bool EMIT>
-__global__ void __launch_bounds__(512) k_slow_table(size_t n, const uint32_t* __restrict__ list,
+__global__ void __launch_bounds__(512, 2) k_slow_table(size_t ng, const uint32_t* __restrict__ gen,
+                                                       const uint32_t* __restrict__ list,
                                                     const uint8_t* __restrict__ bclass, const uint32_t* __restrict__ nbr,
                                                     const uint8_t* __restrict__ blevel, const int32_t* __restrict__ bx,
                                                     const int32_t* __restrict__ by, const int32_t* __restrict__ bz,
@@ -384,16 +386,16 @@ __global__ void __launch_bounds__(512) k_slow_table(size_t n, const uint32_t* __
                                                     const uint32_t* __restrict__ nb27, uint32_t* __restrict__ cnt,
                                                     uint32_t* __restrict__ smask, uint4* __restrict__ qmask,
                                                     const uint32_t* __restrict__ off,
-                                                    uint64_t* __restrict__ desc, uint32_t* dev_status) {
+                                                    uint64_t* __restrict__ desc, uint32_t* __restrict__ fluid,
+                                                    uint32_t* dev_status) {
     __shared__ BrickTopo T;
     __shared__ uint32_t warp_sum[16];
+    __shared__ uint32_t solid_count;
     const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-    for (size_t p = blockIdx.x; p < n; p += gridDim.x) {
+    (void)bclass;
+    for (size_t j = blockIdx.x; j < ng; j += gridDim.x) {
+        const size_t p = gen[j];
         const uint32_t b = list[p];
-        if (bclass[b] != 1) {
-            if (!EMIT && t == 0) cnt[p] = 0;
-            continue;
-        }
         const int l = blevel[b];
         const LbmCaseDev& c = cases[bcase[b]];
         if (t < 104) {
@@ -404,6 +406,7 @@ __global__ void __launch_bounds__(512) k_slow_table(size_t n, const uint32_t* __
         if (t < 27) T.nb27[t] = nb27[(size_t)b * 28 + t];
         if (t < 32) T.solid[t] = 0u;
         if (t == 32) T.near = brick_near_sphere(c, bx[b], by[b], bz[b], l);
+        if (t == 0) solid_count = 0;  // thread 0 also reads it last, after the final barrier
         __syncthreads();
         const int near = T.near;
         const int64_t G0[3] = {(int64_t)bx[b] * 8, (int64_t)by[b] * 8, (int64_t)bz[b] * 8};
@@ -456,7 +459,10 @@ __global__ void __launch_bounds__(512) k_slow_table(size_t n, const uint32_t* __
         const uint32_t qbase = __shfl_sync(0xFFFFFFFFu, before + (incl - mine), lane & ~3);
         if (!EMIT) {
             if (t == 0) cnt[p] = total;
-            if (lane == 0) smask[(size_t)b * 16 + wid] = solid_word;
+            if (lane == 0) {
+                smask[(size_t)b * 16 + wid] = solid_word;
+                atomicAdd(&solid_count, (uint32_t)__popc(solid_word));
+            }
             if (i == 0) {
                 uint32_t wq[3] = {0u, 0u, 0u};
                 for (int q = 0; q < Q; ++q)
@@ -477,6 +483,7 @@ __global__ void __launch_bounds__(512) k_slow_table(size_t n, const uint32_t* __
             }
         }
         __syncthreads();
+        if (!EMIT && t == 0) fluid[b] = 512u - solid_count;
     }
 }
 
@@ -1080,6 +1087,7 @@ struct fl_pool {
     int graphs = 1;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one level-0 step, per level-0 parity
     uint64_t graph_kernels[2] = {0, 0};             // kernel nodes of each
+    bool graph_ok[2] = {false, false};              // graph[k] matches the current pool
     uint64_t version = 0;                           // bumped whenever the emitted launches change
     void* adapt_scratch = nullptr;
     size_t adapt_scratch_bytes = 0;
@@ -1145,7 +1153,7 @@ int pool_reserve_bricks(fl_ctx* ctx, fl_pool* P, size_t need) {
 
 int alloc_brick_arrays(fl_ctx* ctx, fl_pool* P, size_t cap) {
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->nbr, cap * 26 * 4 * 4, ctx->stream), "pool nbr");
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->list, cap * 4, ctx->stream), "pool list");
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->list, cap * 8, ctx->stream), "pool list");  // list + general positions
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->wmax, cap * 4, ctx->stream), "pool wmax");
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->part, cap * 32, ctx->stream), "pool partials");
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->fluid, cap * 4, ctx->stream), "pool fluid");
@@ -1168,11 +1176,19 @@ void free_brick_arrays(fl_ctx* ctx, fl_pool* P) {
     P->qmask = nullptr;
 }
 
+// The captured steps no longer match the pool: mark them stale.  The next
+// capture updates the instantiated graph in place when its shape is unchanged
+// (cudaGraphExecUpdate) instead of instantiating anew.
 void drop_graph(fl_pool* P) {
     ++P->version;
+    P->graph_ok[0] = P->graph_ok[1] = false;
+}
+
+void free_graphs(fl_pool* P) {
     for (int k = 0; k < 2; ++k) {
         if (P->graph[k]) cudaGraphExecDestroy(P->graph[k]);
         P->graph[k] = nullptr;
+        P->graph_ok[k] = false;
     }
 }
 
@@ -1229,25 +1245,36 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
     }
     std::vector<uint32_t> list(n), fill[3] = {P->cls_off[0], P->cls_off[1], P->cls_off[2]};
     for (size_t i = 0; i < n; ++i) list[fill[cl[i] > 2 ? 1 : cl[i]][lv[i]]++] = (uint32_t)i;
-    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->list, list.data(), n * 4, cudaMemcpyHostToDevice, ctx->stream), "list");
-    const unsigned tgrid = (unsigned)std::max<size_t>(1, std::min<size_t>(n, (size_t)ctx->num_sms * 4));
-    k_slow_table<false><<<tgrid, 512, 0, ctx->stream>>>(n, P->list, P->bclass, P->nbr, P->mesh.level, P->mesh.x,
-                                                        P->mesh.y, P->mesh.z, P->mesh.case_id, P->d_cases, P->nb27,
-                                                        P->slow_cnt, P->smask, P->qmask, nullptr, nullptr,
-                                                        ctx->dev_status);
-    FL_CHECK_LAUNCH(ctx, "k_slow_table count");
+    // general bricks' list positions (appended after the list in the same upload)
+    std::vector<uint32_t> gen;
+    for (int l = 0; l <= P->maxL; ++l)
+        for (uint32_t k = 0; k < P->cls_cnt[1][l]; ++k) gen.push_back(P->cls_off[1][l] + k);
+    const size_t ng = gen.size();
+    list.insert(list.end(), gen.begin(), gen.end());
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->list, list.data(), (n + ng) * 4, cudaMemcpyHostToDevice, ctx->stream), "list");
+    const uint32_t* d_gen = P->list + n;
+    FL_TRY_CUDA(ctx, cudaMemsetAsync(P->slow_cnt, 0, n * 4, ctx->stream), "descriptor counts");
+    const unsigned tgrid = (unsigned)std::max<size_t>(1, std::min<size_t>(ng, (size_t)ctx->num_sms * 2));
+    if (ng) {
+        k_slow_table<false><<<tgrid, 512, 0, ctx->stream>>>(ng, d_gen, P->list, P->bclass, P->nbr, P->mesh.level,
+                                                            P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.case_id,
+                                                            P->d_cases, P->nb27, P->slow_cnt, P->smask, P->qmask,
+                                                            nullptr, nullptr, P->fluid, ctx->dev_status);
+        FL_CHECK_LAUNCH(ctx, "k_slow_table count");
+    }
     P->case_begin.assign(P->cases.size() + 1, 0);
     for (size_t i = 0; i < n; ++i) P->case_begin[cs[i] + 1]++;
     for (size_t c = 0; c < P->cases.size(); ++c) P->case_begin[c + 1] += P->case_begin[c];
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->d_case_begin, P->case_begin.data(), P->case_begin.size() * 4,
                                      cudaMemcpyHostToDevice, ctx->stream), "case ranges");
-    // fluid sites per brick -> LUPs per level-0 step
-    k_brick_sums<<<fl_blocks(n, 1, ctx->num_sms * 16), 128, 0, ctx->stream>>>(view(P), n, P->part, P->fluid);
-    FL_CHECK_LAUNCH(ctx, "k_brick_sums");
+    // fluid sites per brick -> LUPs per level-0 step: interior bricks are all
+    // fluid, all-solid bricks none, general bricks counted by k_slow_table
     std::vector<uint32_t> fl(n), sc(n + 1);
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(fl.data(), P->fluid, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "fluid");
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(sc.data(), P->slow_cnt, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "counts");
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "topology sync");
+    for (size_t i = 0; i < n; ++i)
+        if (cl[i] != 1) fl[i] = cl[i] == 0 ? 512u : 0u;
     // stencil descriptors of the general class: offsets on the host, words on the device
     uint64_t run = 0;
     for (size_t i = 0; i < n; ++i) {
@@ -1270,11 +1297,13 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
     }
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->slow_off, sc.data(), (n + 1) * 4, cudaMemcpyHostToDevice, ctx->stream),
                 "descriptor offsets");
-    k_slow_table<true><<<tgrid, 512, 0, ctx->stream>>>(n, P->list, P->bclass, P->nbr, P->mesh.level, P->mesh.x,
-                                                       P->mesh.y, P->mesh.z, P->mesh.case_id, P->d_cases, P->nb27,
-                                                       nullptr, nullptr, nullptr, P->slow_off, P->desc,
-                                                       ctx->dev_status);
-    FL_CHECK_LAUNCH(ctx, "k_slow_table emit");
+    if (ng) {
+        k_slow_table<true><<<tgrid, 512, 0, ctx->stream>>>(ng, d_gen, P->list, P->bclass, P->nbr, P->mesh.level,
+                                                           P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.case_id,
+                                                           P->d_cases, P->nb27, nullptr, nullptr, nullptr, P->slow_off,
+                                                           P->desc, nullptr, ctx->dev_status);
+        FL_CHECK_LAUNCH(ctx, "k_slow_table emit");
+    }
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "descriptor sync");  // sc is freed on return
     P->lups = 0;
     for (int l = 0; l < 16; ++l) P->fluid_per_level[l] = P->fluid_cls[0][l] = P->fluid_cls[1][l] = P->fluid_cls[2][l] = 0;
@@ -1656,7 +1685,7 @@ int fl_pool_create(fl_ctx* ctx, const fl_lbm_case* cases, int ncases, fl_pool** 
 int fl_pool_destroy(fl_ctx* ctx, fl_pool* P) {
     if (!ctx || !P) return FL_E_INVALID_ARG;
     cudaStreamSynchronize(ctx->stream);
-    drop_graph(P);
+    free_graphs(P);
     free_brick_arrays(ctx, P);
     for (int k = 0; k < 3; ++k)
         if (P->f[k]) cudaFreeAsync(P->f[k], ctx->stream);
@@ -1699,7 +1728,7 @@ int fl_pool_step(fl_ctx* ctx, fl_pool* P, int nsteps) {
         // even number of sub-steps), so two captured graphs, one per level-0
         // parity, replay every step until the topology changes.
         int p0 = P->parity[0];
-        if (!P->graph[p0]) {
+        if (!P->graph_ok[p0]) {
             int saved[16];
             std::memcpy(saved, P->parity, sizeof(saved));
             cudaGraph_t g;
@@ -1711,9 +1740,20 @@ int fl_pool_step(fl_ctx* ctx, fl_pool* P, int nsteps) {
             ctx->launches = c0;
             std::memcpy(P->parity, saved, sizeof(saved));
             FL_TRY_CUDA(ctx, e, "capture end");
-            e = cudaGraphInstantiate(&P->graph[p0], g, 0);
+            bool updated = false;
+            if (P->graph[p0]) {
+                cudaGraphExecUpdateResultInfo info;
+                updated = cudaGraphExecUpdate(P->graph[p0], g, &info) == cudaSuccess;
+                if (!updated) {
+                    cudaGetLastError();  // a failed update leaves no sticky error; clear the last one
+                    cudaGraphExecDestroy(P->graph[p0]);
+                    P->graph[p0] = nullptr;
+                }
+            }
+            if (!updated) e = cudaGraphInstantiate(&P->graph[p0], g, 0);
             cudaGraphDestroy(g);
             FL_TRY_CUDA(ctx, e, "graph instantiate");
+            P->graph_ok[p0] = true;
         }
         FL_TRY_CUDA(ctx, cudaGraphLaunch(P->graph[p0], ctx->stream), "graph launch");
         ctx->launches += P->graph_kernels[p0];
