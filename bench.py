@@ -262,7 +262,11 @@ def run_gpu(args):
                 "kernel": "collide-stream (k_collide_fast + k_interface + k_collide_general + k_collide_solid)",
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                 "algorithmic_bytes_per_launch": round(BYTES_PER_LUP * sites / nla), "launches_profiled": nla,
-                "avg_launch_ms": round(kms / nla, 4), "per_kernel": per_kernel}
+                "avg_launch_ms": round(kms / nla, 4), "per_kernel": per_kernel,
+                # the timed steps themselves (dependency graph, regrids included): algorithmic
+                # collide-stream bytes over the timed region
+                "timed_region_achieved": round(value * 1e6 * BYTES_PER_LUP / 1e9, 1),
+                "timed_region_frac": round(value * 1e6 * BYTES_PER_LUP / 1e9 / peak, 4)}
     # e2e through the C ABI with pinned host buffers
     inf = pool.info()
     n = inf.num_bricks

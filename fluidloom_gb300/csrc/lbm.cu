@@ -918,15 +918,19 @@ __global__ void __launch_bounds__(128) k_macroscopic(PoolView p, size_t n, float
     }
 }
 
-// Per case (one CTA each): the case's brick partials (a contiguous range,
-// bricks being sorted by case then key) summed in a fixed order — thread t
-// takes bricks t, t+256, ..., then a fixed tree across threads.
-__global__ void __launch_bounds__(256) k_case_sums(const double* __restrict__ part, const uint32_t* __restrict__ case_begin,
-                                                   int ncases, double* __restrict__ out) {
+// Per chunk of up to 1024 consecutive bricks of one case (one CTA each): the
+// bricks' partials summed in a fixed order -- thread t takes bricks t, t+256,
+// ..., then a fixed tree across threads.  Chunks start at each case's first
+// brick, so a case's sums do not depend on the other cases of the pool.
+constexpr uint32_t kChunkBricks = 1024;
+
+__global__ void __launch_bounds__(256) k_chunk_sums(const double* __restrict__ part, const uint2* __restrict__ chunks,
+                                                    uint32_t nchunks, double* __restrict__ chunk_part) {
     __shared__ double red[4][256];
-    for (int cs = blockIdx.x; cs < ncases; cs += gridDim.x) {
+    for (uint32_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const uint2 r = chunks[c];
         double acc[4] = {0, 0, 0, 0};
-        for (uint32_t b = case_begin[cs] + threadIdx.x; b < case_begin[cs + 1]; b += 256)
+        for (uint32_t b = r.x + threadIdx.x; b < r.y; b += 256)
             for (int k = 0; k < 4; ++k) acc[k] += part[(size_t)b * 4 + k];
         for (int k = 0; k < 4; ++k) red[k][threadIdx.x] = acc[k];
         __syncthreads();
@@ -935,9 +939,20 @@ __global__ void __launch_bounds__(256) k_case_sums(const double* __restrict__ pa
                 for (int k = 0; k < 4; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + o];
             __syncthreads();
         }
-        if (threadIdx.x < 4) out[cs * 4 + threadIdx.x] = red[threadIdx.x][0];
+        if (threadIdx.x < 4) chunk_part[(size_t)c * 4 + threadIdx.x] = red[threadIdx.x][0];
         __syncthreads();
     }
+}
+
+// Per case (thread = case and component): its chunks' sums in chunk order.
+__global__ void k_case_sums(const double* __restrict__ chunk_part, const uint32_t* __restrict__ case_chunk,
+                            int ncases, double* __restrict__ out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ncases * 4) return;
+    const int cs = t >> 2, k = t & 3;
+    double s = 0.0;
+    for (uint32_t c = case_chunk[cs]; c < case_chunk[cs + 1]; ++c) s += chunk_part[(size_t)c * 4 + k];
+    out[t] = s;
 }
 
 // exp(x) for x <= 0 from the mathematics: x = n ln2 + r with |r| <= ln2/2
@@ -1077,6 +1092,10 @@ struct fl_pool {
     uint64_t num_desc = 0;
     std::vector<uint32_t> case_begin;
     uint32_t* d_case_begin = nullptr;
+    uint2* d_chunks = nullptr;            // brick ranges of <= 1024 bricks, each within one case
+    uint32_t* d_case_chunk = nullptr;     // per case: first chunk; [ncases] = end
+    double* chunk_part = nullptr;
+    uint32_t nchunks = 0;
     float* wmax = nullptr;
     unsigned* case_max = nullptr;
     double* part = nullptr;
@@ -1163,17 +1182,20 @@ int alloc_brick_arrays(fl_ctx* ctx, fl_pool* P, size_t cap) {
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->slow_off, (cap + 1) * 4, ctx->stream), "pool descriptor offsets");
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->smask, cap * 64, ctx->stream), "pool solid masks");
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->qmask, cap * 128 * sizeof(uint4), ctx->stream), "pool quad masks");
+    const size_t max_chunks = cap / kChunkBricks + kMaxCases + 1;  // one partial chunk per case at most
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->d_chunks, max_chunks * sizeof(uint2), ctx->stream), "pool chunks");
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->chunk_part, max_chunks * 32, ctx->stream), "pool chunk sums");
     return FL_OK;
 }
 
 void free_brick_arrays(fl_ctx* ctx, fl_pool* P) {
-    void* ps[11] = {P->nbr,  P->list,     P->wmax,     P->part,  P->fluid, P->nb27,
-                    P->bclass, P->slow_cnt, P->slow_off, P->smask, P->qmask};
+    void* ps[13] = {P->nbr,  P->list,     P->wmax,     P->part,  P->fluid, P->nb27,     P->bclass,
+                    P->slow_cnt, P->slow_off, P->smask, P->qmask, P->d_chunks, P->chunk_part};
     for (void* p : ps)
         if (p) cudaFreeAsync(p, ctx->stream);
     P->nbr = nullptr; P->list = nullptr; P->wmax = nullptr; P->part = nullptr; P->fluid = nullptr;
     P->nb27 = nullptr; P->bclass = nullptr; P->slow_cnt = nullptr; P->slow_off = nullptr; P->smask = nullptr;
-    P->qmask = nullptr;
+    P->qmask = nullptr; P->d_chunks = nullptr; P->chunk_part = nullptr;
 }
 
 // The captured steps no longer match the pool: mark them stale.  The next
@@ -1267,6 +1289,22 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
     for (size_t c = 0; c < P->cases.size(); ++c) P->case_begin[c + 1] += P->case_begin[c];
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->d_case_begin, P->case_begin.data(), P->case_begin.size() * 4,
                                      cudaMemcpyHostToDevice, ctx->stream), "case ranges");
+    {  // conservation-sum chunks
+        std::vector<uint2> chunks;
+        std::vector<uint32_t> case_chunk(P->cases.size() + 1, 0);
+        for (size_t c = 0; c < P->cases.size(); ++c) {
+            case_chunk[c] = (uint32_t)chunks.size();
+            for (uint32_t b = P->case_begin[c]; b < P->case_begin[c + 1]; b += kChunkBricks)
+                chunks.push_back(make_uint2(b, std::min(b + kChunkBricks, P->case_begin[c + 1])));
+        }
+        case_chunk[P->cases.size()] = (uint32_t)chunks.size();
+        P->nchunks = (uint32_t)chunks.size();
+        if (P->nchunks)
+            FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->d_chunks, chunks.data(), chunks.size() * sizeof(uint2),
+                                             cudaMemcpyHostToDevice, ctx->stream), "chunks");
+        FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->d_case_chunk, case_chunk.data(), case_chunk.size() * 4,
+                                         cudaMemcpyHostToDevice, ctx->stream), "case chunks");
+    }
     // fluid sites per brick -> LUPs per level-0 step: interior bricks are all
     // fluid, all-solid bricks none, general bricks counted by k_slow_table
     std::vector<uint32_t> fl(n), sc(n + 1);
@@ -1634,6 +1672,7 @@ int fl_pool_create(fl_ctx* ctx, const fl_lbm_case* cases, int ncases, fl_pool** 
     if (cudaMalloc(&P->d_cases, kMaxCases * sizeof(LbmCaseDev)) != cudaSuccess) return fail(FL_E_OOM);
     if (cudaMalloc(&P->d_dom, kMaxCases * sizeof(fl_domain_dev::Case)) != cudaSuccess) return fail(FL_E_OOM);
     if (cudaMalloc(&P->d_case_begin, (kMaxCases + 1) * 4) != cudaSuccess) return fail(FL_E_OOM);
+    if (cudaMalloc(&P->d_case_chunk, (kMaxCases + 1) * 4) != cudaSuccess) return fail(FL_E_OOM);
     if (cudaMalloc(&P->case_max, kMaxCases * 4) != cudaSuccess) return fail(FL_E_OOM);
     if (cudaMalloc(&P->cons, kMaxCases * 32) != cudaSuccess) return fail(FL_E_OOM);
     if (cudaMalloc(&P->d_mask, kMaxCases) != cudaSuccess) return fail(FL_E_OOM);
@@ -1697,6 +1736,7 @@ int fl_pool_destroy(fl_ctx* ctx, fl_pool* P) {
     if (P->d_cases) cudaFree(P->d_cases);
     if (P->d_dom) cudaFree(P->d_dom);
     if (P->d_case_begin) cudaFree(P->d_case_begin);
+    if (P->d_case_chunk) cudaFree(P->d_case_chunk);
     if (P->case_max) cudaFree(P->case_max);
     if (P->cons) cudaFree(P->cons);
     if (P->d_mask) cudaFree(P->d_mask);
@@ -1838,7 +1878,12 @@ int fl_pool_conservation(fl_ctx* ctx, fl_pool* P, double* out) {
     k_brick_sums<<<fl_blocks(n, 1, ctx->num_sms * 16), 128, 0, ctx->stream>>>(view(P), n, P->part, P->fluid);
     FL_CHECK_LAUNCH(ctx, "k_brick_sums");
     int nc = (int)P->cases.size();
-    k_case_sums<<<std::min(nc, ctx->num_sms * 4), 256, 0, ctx->stream>>>(P->part, P->d_case_begin, nc, P->cons);
+    if (P->nchunks) {
+        k_chunk_sums<<<std::min<uint32_t>(P->nchunks, (uint32_t)ctx->num_sms * 8), 256, 0, ctx->stream>>>(
+            P->part, P->d_chunks, P->nchunks, P->chunk_part);
+        FL_CHECK_LAUNCH(ctx, "k_chunk_sums");
+    }
+    k_case_sums<<<(nc * 4 + 255) / 256, 256, 0, ctx->stream>>>(P->chunk_part, P->d_case_chunk, nc, P->cons);
     FL_CHECK_LAUNCH(ctx, "k_case_sums");
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(out, P->cons, nc * 32, cudaMemcpyDeviceToHost, ctx->stream), "conservation");
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "conservation");
