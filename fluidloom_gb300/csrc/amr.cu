@@ -431,7 +431,7 @@ size_t fl_adapt_scratch_bytes(size_t n, uint64_t cap) {
     size_t b = 0;
     b += fl_align256(n * 8);                 // old keys
     b += fl_align256(n * 4);                 // iota
-    b += fl_align256(cap * 8) + 2 * fl_align256(cap * 4);  // table + win
+    b += fl_align256(cap * 16) + fl_align256(cap * 4);  // 16-byte-slot table + win
     b += 2 * fl_align256(n);                 // shadow, viol
     b += 4 * fl_align256(n * 4);             // leader, gid, group_of, cnt/off
     b += fl_align256(n * 4);                 // members (n/8 groups * 8)
@@ -496,8 +496,8 @@ static AdaptWork carve_adapt(void* scratch, size_t n, bool with_case) {
     w.cap = fl_table_capacity(n);
     Carver cv{(char*)scratch};
     w.keys = cv.take<uint64_t>(n);
-    w.tk = cv.take<uint64_t>(w.cap);
-    w.tv = cv.take<uint32_t>(w.cap);
+    w.tk = cv.take<uint64_t>(2 * w.cap);
+    w.tv = nullptr;  // 16-byte slots
     w.win = cv.take<uint32_t>(w.cap);
     w.shadow = cv.take<uint8_t>(n);
     w.viol = cv.take<uint8_t>(n);
@@ -650,14 +650,14 @@ int fl_balance_enforce(fl_ctx* ctx, fl_mesh* mesh, const fl_adapt_config* cfg, f
     if (res) *res = fl_balance_result{};
     if (n == 0) { if (res) res->converged = 1; return FL_OK; }
     uint64_t cap = fl_table_capacity(n);
-    size_t need = fl_align256(n * 8) + fl_align256(cap * 8) + 2 * fl_align256(cap * 4) + 2 * fl_align256(n) + 512 + 256;
+    size_t need = fl_align256(n * 8) + fl_align256(cap * 16) + fl_align256(cap * 4) + 2 * fl_align256(n) + 512 + 256;
     int rc = fl_scratch_reserve(ctx, need);
     if (rc) return rc;
     Carver cv{(char*)ctx->scratch};
     void* dcase = cv.take<char>(256);
     uint64_t* keys = cv.take<uint64_t>(n);
-    uint64_t* tk = cv.take<uint64_t>(cap);
-    uint32_t* tv = cv.take<uint32_t>(cap);
+    uint64_t* tk = cv.take<uint64_t>(2 * cap);
+    uint32_t* tv = nullptr;  // 16-byte slots
     uint32_t* win = cv.take<uint32_t>(cap);
     uint8_t* shadow = cv.take<uint8_t>(n);
     uint8_t* viol = cv.take<uint8_t>(n);
@@ -686,13 +686,13 @@ int fl_neighbour_rebuild(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config
     size_t n = mesh->num_cells;
     if (n == 0) return FL_OK;
     uint64_t cap = fl_table_capacity(n);
-    int rc = fl_scratch_reserve(ctx, 256 + fl_align256(n * 8) + fl_align256(cap * 8) + 2 * fl_align256(cap * 4) + 256);
+    int rc = fl_scratch_reserve(ctx, 256 + fl_align256(n * 8) + fl_align256(cap * 16) + fl_align256(cap * 4) + 256);
     if (rc) return rc;
     Carver cv{(char*)ctx->scratch};
     void* dcase = cv.take<char>(256);
     uint64_t* keys = cv.take<uint64_t>(n);
-    uint64_t* tk = cv.take<uint64_t>(cap);
-    uint32_t* tv = cv.take<uint32_t>(cap);
+    uint64_t* tk = cv.take<uint64_t>(2 * cap);
+    uint32_t* tv = nullptr;  // 16-byte slots
     uint32_t* win = cv.take<uint32_t>(cap);
     fl_domain_dev dom = fl_domain_from_config(ctx, cfg, dcase);
     dom.max_level = cfg->max_refinement_level;
@@ -803,14 +803,14 @@ int fl_merge(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, const
     size_t n = mesh->num_cells;
     if (n == 0) return FL_OK;
     uint64_t cap = fl_table_capacity(n);
-    int rc = fl_scratch_reserve(ctx, 256 + fl_align256(n * 8) + fl_align256(cap * 8) + 2 * fl_align256(cap * 4) +
+    int rc = fl_scratch_reserve(ctx, 256 + fl_align256(n * 8) + fl_align256(cap * 16) + fl_align256(cap * 4) +
                                          4 * fl_align256(n * 4) + fl_align256(n * 4 + 64) + fl_scan_scratch_bytes(n) + 512);
     if (rc) return rc;
     Carver cv{(char*)ctx->scratch};
     void* dcase = cv.take<char>(256);
     uint64_t* keys = cv.take<uint64_t>(n);
-    uint64_t* tk = cv.take<uint64_t>(cap);
-    uint32_t* tv = cv.take<uint32_t>(cap);
+    uint64_t* tk = cv.take<uint64_t>(2 * cap);
+    uint32_t* tv = nullptr;  // 16-byte slots
     uint32_t* win = cv.take<uint32_t>(cap);
     uint32_t* leader = cv.take<uint32_t>(n);
     uint32_t* gid = cv.take<uint32_t>(n);

@@ -159,13 +159,13 @@ int fl_interp_trilinear(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config*
     if (mesh->case_id) return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_interp_trilinear: single-case meshes only");
     size_t n = mesh->num_cells;
     uint64_t cap = fl_table_capacity(n ? n : 1);
-    int rc = fl_scratch_reserve(ctx, 256 + fl_align256(n * 8 + 8) + fl_align256(cap * 8) + 2 * fl_align256(cap * 4));
+    int rc = fl_scratch_reserve(ctx, 256 + fl_align256(n * 8 + 8) + fl_align256(cap * 16) + fl_align256(cap * 4));
     if (rc) return rc;
     char* p = (char*)ctx->scratch;
     void* dcase = p; p += 256;
     uint64_t* keys = (uint64_t*)p; p += fl_align256(n * 8 + 8);
-    uint64_t* tk = (uint64_t*)p; p += fl_align256(cap * 8);
-    uint32_t* tv = (uint32_t*)p; p += fl_align256(cap * 4);
+    uint64_t* tk = (uint64_t*)p; p += fl_align256(cap * 16);
+    uint32_t* tv = nullptr;  // 16-byte slots
     uint32_t* win = (uint32_t*)p;
     fl_domain_dev dom = fl_domain_from_config(ctx, cfg, dcase);
     if (n) {

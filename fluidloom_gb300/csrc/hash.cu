@@ -22,13 +22,17 @@ __global__ void k_hash_clear(uint64_t* __restrict__ tk, uint32_t* __restrict__ t
                              uint64_t cap) {
     size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += stride) {
-        tk[i] = FL_EMPTY_KEY;
-        tv[i] = FL_INVALID_INDEX;
+        if (tv) {
+            tk[i] = FL_EMPTY_KEY;
+            tv[i] = FL_INVALID_INDEX;
+        } else {
+            reinterpret_cast<ulonglong2*>(tk)[i] = make_ulonglong2(FL_EMPTY_KEY, FL_INVALID_INDEX);
+        }
         if (win) win[i] = 0u;
     }
 }
 
-__global__ void k_hash_insert(uint64_t* __restrict__ tk, uint32_t* __restrict__ win, int lg,
+__global__ void k_hash_insert(uint64_t* __restrict__ tk, int slot_words, uint32_t* __restrict__ win, int lg,
                               const uint64_t* __restrict__ keys, size_t n, uint32_t* dev_status) {
     size_t stride = (size_t)gridDim.x * blockDim.x;
     const uint64_t mask = (1ull << lg) - 1;
@@ -38,7 +42,7 @@ __global__ void k_hash_insert(uint64_t* __restrict__ tk, uint32_t* __restrict__ 
         uint64_t s = fl_hash_slot(k, lg);
         int p = 0;
         for (; p < kProbeLimit; ++p) {
-            unsigned long long prev = atomicCAS((unsigned long long*)(tk + s), FL_EMPTY_KEY, k);
+            unsigned long long prev = atomicCAS((unsigned long long*)(tk + s * slot_words), FL_EMPTY_KEY, k);
             if (prev == FL_EMPTY_KEY || prev == k) {
                 atomicMax(win + s, (uint32_t)(i + 1));
                 break;
@@ -49,15 +53,18 @@ __global__ void k_hash_insert(uint64_t* __restrict__ tk, uint32_t* __restrict__ 
     }
 }
 
-__global__ void k_hash_values(uint32_t* __restrict__ tv, const uint32_t* __restrict__ win,
+__global__ void k_hash_values(uint64_t* __restrict__ tk, uint32_t* __restrict__ tv, const uint32_t* __restrict__ win,
                               const uint32_t* __restrict__ vals, const uint8_t* __restrict__ levels, uint64_t cap) {
     size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += stride) {
         uint32_t w = win[i];
         if (!w) continue;
-        if (vals) tv[i] = vals[w - 1];
-        else if (levels) tv[i] = ((uint32_t)levels[w - 1] << kPackedIdxBits) | (w - 1);
-        else tv[i] = w - 1;
+        uint32_t v;
+        if (vals) v = vals[w - 1];
+        else if (levels) v = ((uint32_t)levels[w - 1] << kPackedIdxBits) | (w - 1);
+        else v = w - 1;
+        if (tv) tv[i] = v;
+        else tk[2 * i + 1] = v;
     }
 }
 
@@ -134,9 +141,10 @@ int fl_hash_build_with(fl_ctx* ctx, uint64_t* tk, uint32_t* tv, uint64_t cap, co
     FL_CHECK_LAUNCH(ctx, "k_hash_clear");
     if (n == 0) return FL_OK;
     int lg = fl_hash_lg(cap);
-    k_hash_insert<<<fl_blocks(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(tk, win, lg, keys, n, ctx->dev_status);
+    k_hash_insert<<<fl_blocks(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(tk, tv ? 1 : 2, win, lg, keys, n,
+                                                                                 ctx->dev_status);
     FL_CHECK_LAUNCH(ctx, "k_hash_insert");
-    k_hash_values<<<cb, 256, 0, ctx->stream>>>(tv, win, vals, vals ? nullptr : levels, cap);
+    k_hash_values<<<cb, 256, 0, ctx->stream>>>(tk, tv, win, vals, vals ? nullptr : levels, cap);
     FL_CHECK_LAUNCH(ctx, "k_hash_values");
     return FL_OK;
 }

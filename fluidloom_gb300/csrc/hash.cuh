@@ -33,12 +33,27 @@ static __device__ __forceinline__ uint64_t fl_hash_slot(uint64_t key, int lg) {
     return lg ? (h >> (64 - lg)) : 0ull;
 }
 
+// Two layouts: the API tables keep keys and values in separate arrays (tk, tv,
+// HashTableManager's getKeysDevicePtr / getValuesDevicePtr); the tables the
+// library builds for itself store each slot as 16 bytes -- key, value, padding
+// -- so one probe reads one 32-byte sector instead of two.  tv == nullptr marks
+// such a table, tk then pointing at 2 * capacity words.
 // hash_query (kernels/hashmap/hash_query.cl:22-56) with the slot rule above.
 static __device__ __forceinline__ uint32_t fl_hash_lookup(const uint64_t* __restrict__ tk,
                                                           const uint32_t* __restrict__ tv, int lg, uint64_t key) {
     if (key == FL_EMPTY_KEY) return FL_INVALID_INDEX;
     const uint64_t mask = (1ull << lg) - 1;
     uint64_t s = fl_hash_slot(key, lg);
+    if (!tv) {
+        const ulonglong2* S = reinterpret_cast<const ulonglong2*>(tk);
+        for (int p = 0; p < 256; ++p) {
+            const ulonglong2 w = __ldg(S + s);
+            if (w.x == key) return (uint32_t)w.y;
+            if (w.x == FL_EMPTY_KEY) return FL_INVALID_INDEX;
+            s = (s + 1) & mask;
+        }
+        return FL_INVALID_INDEX;
+    }
     for (int p = 0; p < 256; ++p) {
         uint64_t k = __ldg((const unsigned long long*)(tk + s));
         if (k == key) return __ldg(tv + s);
@@ -96,8 +111,9 @@ static __device__ __forceinline__ uint32_t fl_locate(const uint8_t* t1, const ui
 
 int fl_hash_lg(uint64_t cap);
 uint64_t fl_table_capacity(size_t n);
-// Clear + build; `win` is cap uint32 of scratch.  With `levels` (and no vals)
-// the values are levels[i] << 27 | i (n < 2^27, else FL_E_CAPACITY).
+// Clear + build; `win` is cap uint32 of scratch; tv == nullptr builds the
+// 16-byte-slot layout in tk (2 * cap words).  With `levels` (and no vals) the
+// values are levels[i] << 27 | i (n < 2^27, else FL_E_CAPACITY).
 int fl_hash_build_with(fl_ctx* ctx, uint64_t* tk, uint32_t* tv, uint64_t cap, const uint64_t* keys,
                        const uint32_t* vals, size_t n, uint32_t* win, const uint8_t* levels = nullptr);
 int fl_neighbours_with(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom, const uint64_t* tk,

@@ -1220,13 +1220,13 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
     if (P->cap >= (1u << 23))  // descriptors address elements as brick * 512 + site in 32 bits
         return fl_set_error(ctx, FL_E_CAPACITY, "a pool holds fewer than 2^23 bricks");
     uint64_t cap = fl_table_capacity(n);
-    size_t need = fl_align256(n * 8) + fl_align256(cap * 8) + 2 * fl_align256(cap * 4) + 256;
+    size_t need = fl_align256(n * 8) + fl_align256(cap * 16) + fl_align256(cap * 4) + 256;
     int rc = fl_scratch_reserve(ctx, need);
     if (rc) return rc;
     char* p = (char*)ctx->scratch;
     uint64_t* keys = (uint64_t*)p; p += fl_align256(n * 8);
-    uint64_t* tk = (uint64_t*)p; p += fl_align256(cap * 8);
-    uint32_t* tv = (uint32_t*)p; p += fl_align256(cap * 4);
+    uint64_t* tk = (uint64_t*)p; p += fl_align256(cap * 16);
+    uint32_t* tv = nullptr;  // 16-byte slots
     uint32_t* win = (uint32_t*)p;
     fl_domain_dev dom = pool_domain(P);
     rc = fl_launch_cell_keys(ctx, P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.level, P->mesh.case_id, dom.depth,
