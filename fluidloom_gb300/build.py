@@ -3,9 +3,9 @@
 Every translation unit is compiled for sm_103a only
 (-gencode arch=compute_103a,code=sm_103a), in parallel, then linked as one
 shared library with the CUDA runtime linked statically.  The collide-stream
-unit is built with -fmad=false so its FP32 arithmetic is the plain IEEE
-sequence of operations (no contraction), like the CPU restatement it is
-checked against.
+unit is built with -fmad=false (and its host code with -ffp-contract=off) so
+its FP32 arithmetic is the plain IEEE sequence of operations (no contraction),
+like the CPU restatement it is checked against.
 """
 import concurrent.futures as cf
 import os
@@ -20,7 +20,7 @@ LIB_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIB_DIR, "libfluidloom_gb300.so")
 OBJ_DIR = os.path.join(LIB_DIR, "obj")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NO_FMA_UNITS = {"lbm.cu"}
+NO_FMA_UNITS = {"lbm.cu", "geometry.cu"}
 
 
 def nvcc():
@@ -46,8 +46,8 @@ def _compile(src, verbose_ptxas=False):
     cmd = [nvcc()] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                              "-I", os.path.join(ROOT, "include"), "-I", CSRC, "-c",
                              os.path.join(CSRC, src), "-o", obj]
-    if src in NO_FMA_UNITS:
-        cmd.insert(1, "-fmad=false")
+    if src in NO_FMA_UNITS:  # device and host code alike (the host compiler may contract on Arm)
+        cmd[1:1] = ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]
     if verbose_ptxas:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -373,6 +373,41 @@ int fl_pool_set_options(fl_ctx* ctx, fl_pool* pool, int use_graphs, int grid_mul
  * streams = 1: every launch in order on the context stream. */
 int fl_pool_set_class_streams(fl_ctx* ctx, fl_pool* pool, int streams);
 
+/* ---- Geometry placement ----
+ * Replaces src/geometry: GeometryDescriptor (include/fluidloom/geometry/GeometryDescriptor.h:19-113),
+ * ImplicitEvaluator::isInside / evaluate (implicit/ImplicitEvaluator.cpp:8-98), SimpleSTLVoxelizer::voxelize
+ * (voxelizer/SimpleSTLVoxelizer.cpp:119-247) and GeometryPlacer::processGeometry
+ * (placer/GeometryPlacer.cpp:55-118).  Types in GeometryDescriptor::Type order; rotation is carried
+ * but, as in the reference, not applied. */
+enum { FL_GEOM_STL = 0, FL_GEOM_IMPLICIT = 1, FL_GEOM_BOX = 2, FL_GEOM_SPHERE = 3, FL_GEOM_CYLINDER = 4 };
+typedef struct fl_geometry_desc {
+    int32_t type;
+    int32_t material_id;
+    float translate[3];
+    float scale[3];       /* > 0 */
+    float rotate[3];      /* degrees; not applied */
+    float radius, height, width, length;
+} fl_geometry_desc;
+/* computeTransformedAABB: box6 = min xyz, max xyz. */
+int fl_geometry_aabb(const fl_geometry_desc* geom, float* box6);
+/* isInside at n points (device float arrays), inside[i] = 0/1 (device). */
+int fl_geometry_inside(fl_ctx* ctx, const fl_geometry_desc* geom, const float* x, const float* y, const float* z,
+                       size_t n, uint8_t* inside);
+/* ImplicitEvaluator::evaluate: cells (device int32 arrays) tested at their centres coord + 0.5. */
+int fl_geometry_evaluate(fl_ctx* ctx, const fl_geometry_desc* geom, const int32_t* x, const int32_t* y,
+                         const int32_t* z, size_t n, uint8_t* inside);
+/* SimpleSTLVoxelizer::voxelize of a triangle mesh (host array [ntri][9]: v1, v2, v3): the cells of the
+ * inclusive grid range of the transformed mesh bounds whose centre lies inside (+x ray casting), in
+ * z, y, x order, into device arrays of cap entries; count = cells found (FL_E_CAPACITY if > cap). */
+int fl_stl_voxelize(fl_ctx* ctx, const float* triangles, size_t ntri, const fl_geometry_desc* geom, float cell_size,
+                    int32_t* x, int32_t* y, int32_t* z, size_t cap, size_t* count);
+/* GeometryPlacer::processGeometry: STL -> fl_stl_voxelize; implicit -> candidates of the transformed AABB
+ * clipped to domain_box6 ([floor, ceil) cells) evaluated at their centres; material[] = material_id and
+ * key[] = hilbert::encode(x, y, z) at level 8 (any output may be NULL except x, y, z). */
+int fl_geometry_process(fl_ctx* ctx, const fl_geometry_desc* geom, const float* triangles, size_t ntri,
+                        float cell_size, const float* domain_box6, int32_t* x, int32_t* y, int32_t* z,
+                        int32_t* material, uint64_t* key, size_t cap, size_t* count);
+
 /* ---- Execution graph ----
  * Replaces the reference runtime: ExecutionNode (include/fluidloom/runtime/nodes/ExecutionNode.h:37-169,
  * read/write field sets, AMR level, halo depth), HazardAnalyzer::analyzeNodes/enforceHazards

@@ -8,7 +8,7 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SOURCES = ["or_keys_prims.cpp", "or_amr.cpp", "or_lbm.cpp"]
+SOURCES = ["or_keys_prims.cpp", "or_amr.cpp", "or_lbm.cpp", "or_geometry.cpp"]
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboracle.so")
 

@@ -118,6 +118,24 @@ void or_pool_populations(void* h, float* out);
 void or_pool_conservation(void* h, double* out);
 uint64_t or_pool_fluid_lups(void* h);
 
+/* Geometry placement (or_geometry.cpp).  type: 0 STL, 1 implicit function, 2 box, 3 sphere, 4 cylinder. */
+typedef struct or_geometry {
+    int32_t type;
+    int32_t material_id;
+    float translate[3];
+    float scale[3];
+    float rotate[3];
+    float radius, height, width, length;
+} or_geometry;
+void or_geometry_aabb(const or_geometry* g, float* box6);
+void or_geometry_inside(const or_geometry* g, const float* x, const float* y, const float* z, size_t n, uint8_t* out);
+void or_geometry_evaluate(const or_geometry* g, const int32_t* x, const int32_t* y, const int32_t* z, size_t n,
+                          uint8_t* out);
+size_t or_stl_voxelize(const float* tris, size_t ntri, const or_geometry* g, float cell, int32_t* ox, int32_t* oy,
+                       int32_t* oz, size_t cap);
+size_t or_geometry_candidates(const or_geometry* g, float cell, const float* dom, int32_t* ox, int32_t* oy,
+                              int32_t* oz, size_t cap);
+
 #ifdef __cplusplus
 }
 #endif

@@ -312,3 +312,64 @@ def blob_flags(cols, blobs, lo, hi, max_level):
     b = np.ascontiguousarray(blobs, np.float32)
     L.or_blob_flags(*[ptr(a) for a in keep], n, ptr(b), len(b), lo, hi, max_level, ptr(out))
     return out
+
+
+# ---------------------------------------------------------------- geometry
+
+def geometry_struct(d):
+    """The oracle's or_geometry has the C layout of fl_geometry_desc."""
+    return ctypes.byref(d)
+
+
+def _geo_lib():
+    L = load()
+    if not getattr(L, "_geo_set", False):
+        L.or_geometry_aabb.argtypes = [P, P]
+        L.or_geometry_inside.argtypes = [P, P, P, P, ctypes.c_size_t, P]
+        L.or_geometry_evaluate.argtypes = [P, P, P, P, ctypes.c_size_t, P]
+        L.or_stl_voxelize.restype = ctypes.c_size_t
+        L.or_stl_voxelize.argtypes = [P, ctypes.c_size_t, P, ctypes.c_float, P, P, P, ctypes.c_size_t]
+        L.or_geometry_candidates.restype = ctypes.c_size_t
+        L.or_geometry_candidates.argtypes = [P, ctypes.c_float, P, P, P, P, ctypes.c_size_t]
+        L._geo_set = True
+    return L
+
+
+def geometry_aabb(d):
+    b = np.zeros(6, np.float32)
+    _geo_lib().or_geometry_aabb(ctypes.byref(d), ptr(b))
+    return b
+
+
+def geometry_inside(d, pts):
+    pts = np.asarray(pts, np.float32).reshape(-1, 3)
+    cols = [np.ascontiguousarray(pts[:, a]) for a in range(3)]
+    out = np.zeros(len(pts), np.uint8)
+    _geo_lib().or_geometry_inside(ctypes.byref(d), *[ptr(c) for c in cols], len(pts), ptr(out))
+    return out.astype(bool)
+
+
+def geometry_evaluate(d, cells):
+    cells = np.asarray(cells, np.int32).reshape(-1, 3)
+    cols = [np.ascontiguousarray(cells[:, a]) for a in range(3)]
+    out = np.zeros(len(cells), np.uint8)
+    _geo_lib().or_geometry_evaluate(ctypes.byref(d), *[ptr(c) for c in cols], len(cells), ptr(out))
+    return out.astype(bool)
+
+
+def _cells_out(fn, cap=1 << 22):
+    x, y, z = (np.zeros(cap, np.int32) for _ in range(3))
+    n = fn(ptr(x), ptr(y), ptr(z), cap)
+    return np.stack([x[:n], y[:n], z[:n]], -1)
+
+
+def stl_voxelize(tris, d, cell):
+    t = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+    return _cells_out(lambda px, py, pz, cap: _geo_lib().or_stl_voxelize(ptr(t), len(t), ctypes.byref(d), cell,
+                                                                          px, py, pz, cap))
+
+
+def geometry_candidates(d, cell, dom):
+    b = np.asarray(dom, np.float32)
+    return _cells_out(lambda px, py, pz, cap: _geo_lib().or_geometry_candidates(ctypes.byref(d), cell, ptr(b),
+                                                                                px, py, pz, cap))
