@@ -63,6 +63,10 @@ struct LbmCaseDev {
     float omega[20];
     int32_t max_level, has_sphere;
     float sc[3], sr, refine_frac, coarsen_frac, band;
+    // solid voxels of the case grid at mask_level (bit (z * Ny + y) * Nx + x,
+    // N = ext * 8 << mask_level), or nullptr
+    const uint32_t* mask;
+    int32_t mask_level, mask_pad;
 };
 
 namespace {
@@ -114,16 +118,37 @@ __device__ __forceinline__ void moments(const float* f, float& rho, float& jx, f
     rho = r; jx = a; jy = b; jz = c;
 }
 
+// Voxel of the case's solid mask under the centre of level-l site (sx, sy, sz):
+// a coarser site samples the voxel at its centre (the upper of the two middle
+// ones), a finer site the voxel that holds it; sites outside the case grid are
+// fluid.
+__device__ __forceinline__ bool mask_at(const LbmCaseDev& c, int64_t sx, int64_t sy, int64_t sz, int l) {
+    const int64_t G[3] = {sx, sy, sz};
+    int64_t v[3], N[3];
+    const int sh = c.mask_level - l;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (G[a] < 0 || G[a] >= ((int64_t)c.ext[a] * 8 << l)) return false;
+        N[a] = (int64_t)c.ext[a] * 8 << c.mask_level;
+        v[a] = sh >= 0 ? (G[a] << sh) + (sh ? (int64_t)1 << (sh - 1) : 0) : G[a] >> -sh;
+    }
+    const uint64_t i = ((uint64_t)v[2] * (uint64_t)N[1] + (uint64_t)v[1]) * (uint64_t)N[0] + (uint64_t)v[0];
+    return (__ldg(c.mask + (i >> 5)) >> (i & 31)) & 1u;
+}
+
+// A site is solid inside the case's sphere or on a voxel of its solid mask.
 __device__ __forceinline__ bool solid_at(const LbmCaseDev& c, int64_t sx, int64_t sy, int64_t sz, int l) {
-    if (!c.has_sphere) return false;
-    float inv = 1.0f / (float)(1 << l);
-    float px = ((float)sx + 0.5f) * inv, py = ((float)sy + 0.5f) * inv, pz = ((float)sz + 0.5f) * inv;
-    float dx = px - c.sc[0], dy = py - c.sc[1], dz = pz - c.sc[2];
-    float d2 = dx * dx;
-    d2 = d2 + dy * dy;
-    d2 = d2 + dz * dz;
-    float r2 = c.sr * c.sr;
-    return d2 < r2;
+    if (c.has_sphere) {
+        float inv = 1.0f / (float)(1 << l);
+        float px = ((float)sx + 0.5f) * inv, py = ((float)sy + 0.5f) * inv, pz = ((float)sz + 0.5f) * inv;
+        float dx = px - c.sc[0], dy = py - c.sc[1], dz = pz - c.sc[2];
+        float d2 = dx * dx;
+        d2 = d2 + dy * dy;
+        d2 = d2 + dz * dz;
+        float r2 = c.sr * c.sr;
+        if (d2 < r2) return true;
+    }
+    return c.mask != nullptr && mask_at(c, sx, sy, sz, l);
 }
 
 struct StepArgs {
@@ -383,7 +408,8 @@ __global__ void __launch_bounds__(512, 2) k_slow_table(size_t ng, const uint32_t
                                                     const int32_t* __restrict__ by, const int32_t* __restrict__ bz,
                                                     const uint16_t* __restrict__ bcase,
                                                     const LbmCaseDev* __restrict__ cases,
-                                                    const uint32_t* __restrict__ nb27, uint32_t* __restrict__ cnt,
+                                                    const uint32_t* __restrict__ nb27,
+                                                    const uint8_t* __restrict__ mnear, uint32_t* __restrict__ cnt,
                                                     uint32_t* __restrict__ smask, uint4* __restrict__ qmask,
                                                     const uint32_t* __restrict__ off,
                                                     uint64_t* __restrict__ desc, uint32_t* __restrict__ fluid,
@@ -405,7 +431,7 @@ __global__ void __launch_bounds__(512, 2) k_slow_table(size_t ng, const uint32_t
         }
         if (t < 27) T.nb27[t] = nb27[(size_t)b * 28 + t];
         if (t < 32) T.solid[t] = 0u;
-        if (t == 32) T.near = brick_near_sphere(c, bx[b], by[b], bz[b], l);
+        if (t == 32) T.near = brick_near_sphere(c, bx[b], by[b], bz[b], l) | (mnear ? mnear[b] & 1 : 0);
         if (t == 0) solid_count = 0;  // thread 0 also reads it last, after the final barrier
         __syncthreads();
         const int near = T.near;
@@ -613,18 +639,56 @@ __global__ void k_collide_solid(StepArgs a) {
     }
 }
 
+// Per brick of a case with a solid mask (one warp per brick): bit 0 when a site
+// of the brick or of its one-site halo (periodic axes wrapped) is solid, bit 1
+// when all 512 of its own sites are; 0 for bricks of the other cases.
+__global__ void k_mask_near(size_t n, const uint8_t* __restrict__ blevel, const int32_t* __restrict__ bx,
+                            const int32_t* __restrict__ by, const int32_t* __restrict__ bz,
+                            const uint16_t* __restrict__ bcase, const LbmCaseDev* __restrict__ cases,
+                            uint8_t* __restrict__ mnear) {
+    const int lane = threadIdx.x & 31;
+    const size_t warps = (size_t)gridDim.x * (blockDim.x >> 5);
+    for (size_t b = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); b < n; b += warps) {
+        const LbmCaseDev& c = cases[bcase[b]];
+        if (!c.mask) {
+            if (lane == 0) mnear[b] = 0;
+            continue;
+        }
+        const int l = blevel[b];
+        const int64_t G0[3] = {(int64_t)bx[b] * 8, (int64_t)by[b] * 8, (int64_t)bz[b] * 8};
+        bool any = false, all = true;
+        for (int i = lane; i < 1000; i += 32) {
+            const int h[3] = {i % 10, (i / 10) % 10, i / 100};
+            int64_t G[3];
+            for (int ax = 0; ax < 3; ++ax) {
+                G[ax] = G0[ax] + h[ax] - 1;
+                if (!c.periodic[ax]) continue;
+                const int64_t N = ((int64_t)c.ext[ax] * 8) << l;
+                G[ax] = G[ax] < 0 ? G[ax] + N : (G[ax] >= N ? G[ax] - N : G[ax]);
+            }
+            const bool sol = solid_at(c, G[0], G[1], G[2], l);
+            const bool own = h[0] >= 1 && h[0] <= 8 && h[1] >= 1 && h[1] <= 8 && h[2] >= 1 && h[2] <= 8;
+            any = any || sol;
+            all = all && (sol || !own);
+        }
+        any = __any_sync(0xFFFFFFFFu, any);
+        all = __all_sync(0xFFFFFFFFu, all);
+        if (lane == 0) mnear[b] = (uint8_t)((any ? 1 : 0) | (all ? 2 : 0));
+    }
+}
+
 // Per brick: the 27-entry same-level neighbour row (centre = the brick,
 // kSlow where the neighbour is missing or at another level) and the class
 // (1 = needs the general kernel).
 __global__ void k_brick_table(size_t n, const uint32_t* __restrict__ nbr, const uint8_t* __restrict__ blevel,
                               const int32_t* __restrict__ bx, const int32_t* __restrict__ by,
                               const int32_t* __restrict__ bz, const uint16_t* __restrict__ bcase,
-                              const LbmCaseDev* __restrict__ cases, uint32_t* __restrict__ nb27,
-                              uint8_t* __restrict__ bclass) {
+                              const LbmCaseDev* __restrict__ cases, const uint8_t* __restrict__ mnear,
+                              uint32_t* __restrict__ nb27, uint8_t* __restrict__ bclass) {
     size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x; b < n; b += stride) {
         int l = blevel[b];
-        int general = brick_near_sphere(cases[bcase[b]], bx[b], by[b], bz[b], l);
+        int general = brick_near_sphere(cases[bcase[b]], bx[b], by[b], bz[b], l) | (mnear ? mnear[b] & 1 : 0);
         for (int d = 0; d < 27; ++d) {
             uint32_t e = (uint32_t)b;
             if (d != 13) {
@@ -640,10 +704,15 @@ __global__ void k_brick_table(size_t n, const uint32_t* __restrict__ nbr, const 
         nb27[b * 28 + 27] = 0;
         if (general) {  // all 512 sites solid: the brick only ever holds the rest equilibrium
             const LbmCaseDev& c = cases[bcase[b]];
-            bool all = c.has_sphere != 0;
-            for (int s = 0; s < 512 && all; ++s)
-                all = solid_at(c, (int64_t)bx[b] * 8 + (s & 7), (int64_t)by[b] * 8 + ((s >> 3) & 7),
-                               (int64_t)bz[b] * 8 + (s >> 6), l);
+            bool all;
+            if (c.mask) {
+                all = mnear && ((mnear[b] >> 1) & 1);
+            } else {
+                all = c.has_sphere != 0;
+                for (int s = 0; s < 512 && all; ++s)
+                    all = solid_at(c, (int64_t)bx[b] * 8 + (s & 7), (int64_t)by[b] * 8 + ((s >> 3) & 7),
+                                   (int64_t)bz[b] * 8 + (s >> 6), l);
+            }
             if (all) general = 2;
         }
         bclass[b] = (uint8_t)general;
@@ -669,6 +738,7 @@ struct PoolView {
     size_t cap;
     int parity[16];
     const LbmCaseDev* cases;
+    const uint8_t* mnear;  // k_mask_near bits of the current mesh, or nullptr (no case has a mask)
 };
 
 __device__ __forceinline__ const float* cur_buf(const PoolView& p, int l) { return p.parity[l] ? p.f1 : p.f0; }
@@ -750,16 +820,17 @@ __device__ bool in_band(const LbmCaseDev& c, int32_t bx, int32_t by, int32_t bz,
     return dmin <= ro * ro && dmax >= ri * ri;
 }
 
-// Brick refine/coarsen flags (oracle: compute_flags): band bricks refine to
-// the case's max level; otherwise refine above refine_frac * case max |omega|,
-// coarsen below coarsen_frac * case max.
+// Brick refine/coarsen flags (oracle: compute_flags): band bricks (near the
+// sphere's surface, or holding both solid and fluid mask sites in the brick and
+// its halo) refine to the case's max level; otherwise refine above
+// refine_frac * case max |omega|, coarsen below coarsen_frac * case max.
 __global__ void k_flags(PoolView p, size_t n, const float* __restrict__ wmax, const unsigned* __restrict__ case_max,
                         int use_vorticity, int32_t* __restrict__ flags) {
     size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x; b < n; b += stride) {
         const LbmCaseDev& c = p.cases[p.bcase[b]];
         int l = p.blevel[b];
-        bool band = in_band(c, p.bx[b], p.by[b], p.bz[b], l);
+        bool band = in_band(c, p.bx[b], p.by[b], p.bz[b], l) || (c.mask && p.mnear && (p.mnear[b] & 3) == 1);
         float wm = use_vorticity ? wmax[b] : 0.0f;
         float cm = use_vorticity ? __uint_as_float(case_max[p.bcase[b]]) : 0.0f;
         int32_t fl = 0;
@@ -1035,6 +1106,20 @@ __global__ void k_mask_flags(size_t n, const uint16_t* __restrict__ bcase, const
         if (!due[bcase[b]]) flags[b] = 0;
 }
 
+// Solid-mask bits of the cells (x, y, z) inside the nx * ny * nz grid; cells
+// outside it are ignored.
+__global__ void k_mask_cells(const int32_t* __restrict__ x, const int32_t* __restrict__ y,
+                             const int32_t* __restrict__ z, size_t n, int64_t nx, int64_t ny, int64_t nz,
+                             uint32_t* __restrict__ words) {
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const int64_t a = x[i], b = y[i], c = z[i];
+        if (a < 0 || b < 0 || c < 0 || a >= nx || b >= ny || c >= nz) continue;
+        const uint64_t bit = ((uint64_t)c * (uint64_t)ny + (uint64_t)b) * (uint64_t)nx + (uint64_t)a;
+        atomicOr(words + (bit >> 5), 1u << (bit & 31));
+    }
+}
+
 __global__ void k_keep_bricks(size_t n, const uint16_t* __restrict__ bcase, const uint8_t* __restrict__ active,
                               uint32_t* __restrict__ keep) {
     size_t stride = (size_t)gridDim.x * blockDim.x;
@@ -1081,6 +1166,9 @@ struct fl_pool {
     uint64_t fluid_cls[3][16] = {};
     uint32_t* nb27 = nullptr;
     uint8_t* bclass = nullptr;
+    uint8_t* mnear = nullptr;       // k_mask_near bits per brick (valid while any_mask)
+    std::vector<uint32_t*> dmask;   // per slot: its solid-mask words on the device, or nullptr
+    bool any_mask = false;
     uint32_t* slow_cnt = nullptr;   // per list position: descriptors of the brick
     uint32_t* slow_off = nullptr;   // exclusive prefix of slow_cnt, n + 1 entries
     uint32_t* smask = nullptr;      // [cap][16] own-site solid bits of general bricks
@@ -1161,6 +1249,7 @@ PoolView view(fl_pool* P) {
     v.cap = P->cap;
     for (int l = 0; l < 16; ++l) v.parity[l] = P->parity[l];
     v.cases = P->d_cases;
+    v.mnear = P->any_mask ? P->mnear : nullptr;
     return v;
 }
 
@@ -1178,6 +1267,7 @@ int alloc_brick_arrays(fl_ctx* ctx, fl_pool* P, size_t cap) {
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->fluid, cap * 4, ctx->stream), "pool fluid");
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->nb27, cap * 28 * 4, ctx->stream), "pool nb27");
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->bclass, cap, ctx->stream), "pool classes");
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->mnear, cap, ctx->stream), "pool mask bits");
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->slow_cnt, cap * 4, ctx->stream), "pool descriptor counts");
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->slow_off, (cap + 1) * 4, ctx->stream), "pool descriptor offsets");
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->smask, cap * 64, ctx->stream), "pool solid masks");
@@ -1189,13 +1279,13 @@ int alloc_brick_arrays(fl_ctx* ctx, fl_pool* P, size_t cap) {
 }
 
 void free_brick_arrays(fl_ctx* ctx, fl_pool* P) {
-    void* ps[13] = {P->nbr,  P->list,     P->wmax,     P->part,  P->fluid, P->nb27,     P->bclass,
-                    P->slow_cnt, P->slow_off, P->smask, P->qmask, P->d_chunks, P->chunk_part};
+    void* ps[14] = {P->nbr,      P->list,     P->wmax,  P->part,  P->fluid,    P->nb27,       P->bclass,
+                    P->slow_cnt, P->slow_off, P->smask, P->qmask, P->d_chunks, P->chunk_part, P->mnear};
     for (void* p : ps)
         if (p) cudaFreeAsync(p, ctx->stream);
     P->nbr = nullptr; P->list = nullptr; P->wmax = nullptr; P->part = nullptr; P->fluid = nullptr;
     P->nb27 = nullptr; P->bclass = nullptr; P->slow_cnt = nullptr; P->slow_off = nullptr; P->smask = nullptr;
-    P->qmask = nullptr; P->d_chunks = nullptr; P->chunk_part = nullptr;
+    P->qmask = nullptr; P->d_chunks = nullptr; P->chunk_part = nullptr; P->mnear = nullptr;
 }
 
 // The captured steps no longer match the pool: mark them stale.  The next
@@ -1238,8 +1328,15 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
                    P->mesh.case_id, n};
     rc = fl_neighbours_with(ctx, md, dom, tk, tv, cap, 4, P->nbr);
     if (rc) return rc;
+    const uint8_t* mnear = P->any_mask ? P->mnear : nullptr;
+    if (mnear) {
+        k_mask_near<<<fl_blocks(n * 32, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(
+            n, P->mesh.level, P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.case_id, P->d_cases, P->mnear);
+        FL_CHECK_LAUNCH(ctx, "k_mask_near");
+    }
     k_brick_table<<<fl_blocks(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(
-        n, P->nbr, P->mesh.level, P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.case_id, P->d_cases, P->nb27, P->bclass);
+        n, P->nbr, P->mesh.level, P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.case_id, P->d_cases, mnear, P->nb27,
+        P->bclass);
     FL_CHECK_LAUNCH(ctx, "k_brick_table");
     // host-side lists (levels, classes and case ids are small: four bytes per brick)
     std::vector<uint8_t> lv(n), cl(n);
@@ -1280,8 +1377,8 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
     if (ng) {
         k_slow_table<false><<<tgrid, 512, 0, ctx->stream>>>(ng, d_gen, P->list, P->bclass, P->nbr, P->mesh.level,
                                                             P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.case_id,
-                                                            P->d_cases, P->nb27, P->slow_cnt, P->smask, P->qmask,
-                                                            nullptr, nullptr, P->fluid, ctx->dev_status);
+                                                            P->d_cases, P->nb27, mnear, P->slow_cnt, P->smask,
+                                                            P->qmask, nullptr, nullptr, P->fluid, ctx->dev_status);
         FL_CHECK_LAUNCH(ctx, "k_slow_table count");
     }
     P->case_begin.assign(P->cases.size() + 1, 0);
@@ -1338,8 +1435,8 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
     if (ng) {
         k_slow_table<true><<<tgrid, 512, 0, ctx->stream>>>(ng, d_gen, P->list, P->bclass, P->nbr, P->mesh.level,
                                                            P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.case_id,
-                                                           P->d_cases, P->nb27, nullptr, nullptr, nullptr, P->slow_off,
-                                                           P->desc, nullptr, ctx->dev_status);
+                                                           P->d_cases, P->nb27, mnear, nullptr, nullptr, nullptr,
+                                                           P->slow_off, P->desc, nullptr, ctx->dev_status);
         FL_CHECK_LAUNCH(ctx, "k_slow_table emit");
     }
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "descriptor sync");  // sc is freed on return
@@ -1634,6 +1731,57 @@ void level0_step(fl_ctx* ctx, fl_pool* P, LaunchTimer* tm = nullptr) {
 uint64_t fl_pool_launch_key(const fl_pool* P) { return (P->version << 1) | (uint64_t)(P->parity[0] & 1); }
 void fl_pool_advance_parity(fl_pool* P, int nsteps) { P->parity[0] ^= (nsteps & 1); }
 
+namespace {
+
+// The solid-mask grid of active case `id` at `level` (ext * 8 << level voxels per axis).
+int mask_grid(fl_ctx* ctx, fl_pool* P, int id, int level, uint64_t* N) {
+    if (!ctx || !P) return FL_E_INVALID_ARG;
+    if (id < 0 || id >= (int)P->active.size() || !P->active[id])
+        return fl_set_error(ctx, FL_E_INVALID_ARG, "solid mask: not an active case");
+    if (level < 0 || level >= kMaxPoolLevels) return fl_set_error(ctx, FL_E_INVALID_ARG, "solid mask: level out of range");
+    for (int a = 0; a < 3; ++a) N[a] = (uint64_t)P->cases[id].ext[a] * 8 << level;
+    if (N[0] * N[1] * N[2] > (1ull << 38)) return fl_set_error(ctx, FL_E_CAPACITY, "solid mask: more than 2^38 voxels");
+    return FL_OK;
+}
+
+// Make `words` (device memory the pool now owns, or nullptr) the solid mask of
+// case `id` and rebuild the topology: classes, descriptors and fluid counts
+// follow the new solid sites; the populations are left as they are (solid
+// sites take the rest state at the next step).
+int install_mask(fl_ctx* ctx, fl_pool* P, int id, int level, uint32_t* words) {
+    if (P->dmask.size() < P->cases.size()) P->dmask.resize(P->cases.size(), nullptr);
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "solid mask");
+    if (P->dmask[id]) cudaFree(P->dmask[id]);
+    P->dmask[id] = words;
+    P->hcases[id].mask = words;
+    P->hcases[id].mask_level = words ? level : 0;
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->d_cases + id, &P->hcases[id], sizeof(LbmCaseDev), cudaMemcpyHostToDevice,
+                                     ctx->stream), "solid mask case");
+    P->any_mask = false;
+    for (size_t c = 0; c < P->dmask.size(); ++c)
+        if (P->dmask[c] && c < P->active.size() && P->active[c]) P->any_mask = true;
+    int rc = pool_topology(ctx, P);
+    if (rc) return rc;
+    return fl_collect_device_status(ctx, "solid mask");
+}
+
+// Free the solid masks of slots that are no longer active.
+void release_masks(fl_ctx* ctx, fl_pool* P) {
+    bool any = false;
+    for (size_t c = 0; c < P->dmask.size(); ++c) {
+        if (P->dmask[c] && !(c < P->active.size() && P->active[c])) {
+            cudaFree(P->dmask[c]);
+            P->dmask[c] = nullptr;
+            P->hcases[c].mask = nullptr;
+            cudaMemcpyAsync(P->d_cases + c, &P->hcases[c], sizeof(LbmCaseDev), cudaMemcpyHostToDevice, ctx->stream);
+        }
+        any = any || P->dmask[c] != nullptr;
+    }
+    P->any_mask = any;
+}
+
+}  // namespace
+
 extern "C" {
 
 int fl_pool_create(fl_ctx* ctx, const fl_lbm_case* cases, int ncases, fl_pool** out) {
@@ -1740,6 +1888,8 @@ int fl_pool_destroy(fl_ctx* ctx, fl_pool* P) {
     if (P->case_max) cudaFree(P->case_max);
     if (P->cons) cudaFree(P->cons);
     if (P->d_mask) cudaFree(P->d_mask);
+    for (uint32_t* m : P->dmask)
+        if (m) cudaFree(m);
     for (int l = 0; l < kMaxPoolLevels; ++l) {
         if (P->sg[l]) cudaStreamDestroy(P->sg[l]);
         if (P->sf[l]) cudaStreamDestroy(P->sf[l]);
@@ -2000,6 +2150,60 @@ int fl_pool_set_velocities(fl_ctx* ctx, fl_pool* P, const float* wall_u, const f
     return FL_OK;
 }
 
+int fl_pool_set_solid_mask(fl_ctx* ctx, fl_pool* P, int32_t id, int32_t level, const uint32_t* bits, size_t nwords) {
+    uint64_t N[3];
+    int rc = mask_grid(ctx, P, id, level, N);
+    if (rc) return rc;
+    if (!bits) return install_mask(ctx, P, id, 0, nullptr);
+    const uint64_t words = (N[0] * N[1] * N[2] + 31) / 32;
+    if (nwords != words) return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_pool_set_solid_mask: nwords != ceil(Nx*Ny*Nz/32)");
+    uint32_t* d = nullptr;
+    if (cudaMalloc(&d, words * 4) != cudaSuccess) return fl_set_error(ctx, FL_E_OOM, "solid mask");
+    if (cudaMemcpyAsync(d, bits, words * 4, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess) {
+        cudaFree(d);
+        return fl_set_error(ctx, FL_E_CUDA, "solid mask upload");
+    }
+    return install_mask(ctx, P, id, level, d);
+}
+
+int fl_pool_set_solid_cells(fl_ctx* ctx, fl_pool* P, int32_t id, int32_t level, const int32_t* x, const int32_t* y,
+                            const int32_t* z, size_t n) {
+    uint64_t N[3];
+    int rc = mask_grid(ctx, P, id, level, N);
+    if (rc) return rc;
+    if (n && (!x || !y || !z)) return FL_E_INVALID_ARG;
+    const uint64_t words = (N[0] * N[1] * N[2] + 31) / 32;
+    uint32_t* d = nullptr;
+    if (cudaMalloc(&d, words * 4) != cudaSuccess) return fl_set_error(ctx, FL_E_OOM, "solid mask");
+    cudaMemsetAsync(d, 0, words * 4, ctx->stream);
+    if (n) {
+        k_mask_cells<<<fl_blocks(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(x, y, z, n, (int64_t)N[0],
+                                                                                   (int64_t)N[1], (int64_t)N[2], d);
+        if (cudaPeekAtLastError() != cudaSuccess) {
+            cudaFree(d);
+            return fl_set_error(ctx, FL_E_CUDA, "k_mask_cells launch");
+        }
+        ++ctx->launches;
+    }
+    return install_mask(ctx, P, id, level, d);
+}
+
+int fl_pool_get_solid_mask(fl_ctx* ctx, fl_pool* P, int32_t id, int32_t* level, uint32_t* bits, size_t nwords) {
+    if (!ctx || !P || !level || id < 0 || id >= (int)P->active.size() || !P->active[id])
+        return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_pool_get_solid_mask: not an active case");
+    const bool has = id < (int)P->dmask.size() && P->dmask[id];
+    *level = has ? P->hcases[id].mask_level : -1;
+    if (!has || !bits) return FL_OK;
+    uint64_t N[3];
+    int rc = mask_grid(ctx, P, id, *level, N);
+    if (rc) return rc;
+    const uint64_t words = (N[0] * N[1] * N[2] + 31) / 32;
+    if (nwords < words) return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_pool_get_solid_mask: buffer too small");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(bits, P->dmask[id], words * 4, cudaMemcpyDeviceToHost, ctx->stream), "mask");
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "mask");
+    return FL_OK;
+}
+
 int fl_pool_regrid_flags(fl_ctx* ctx, fl_pool* P, const int32_t* flags, fl_adapt_stats* st) {
     if (!ctx || !P || !flags) return FL_E_INVALID_ARG;
     int rc = pool_regrid(ctx, P, 0, st, nullptr, flags);
@@ -2084,6 +2288,7 @@ int fl_pool_remove_cases(fl_ctx* ctx, fl_pool* P, const int32_t* ids, int nids) 
             return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_pool_remove_cases: not an active case");
     }
     for (int i = 0; i < nids; ++i) P->active[ids[i]] = 0;
+    release_masks(ctx, P);
     size_t n = P->mesh.num_cells;
     if (n == 0) return FL_OK;
     size_t sb = 3 * fl_align256(n * 4) + fl_scan_scratch_bytes(n) + 512;

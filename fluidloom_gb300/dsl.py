@@ -26,7 +26,10 @@ same by kernel name (src/parsing/SimulationBuilder.cpp:192-363):
   * `if timestep % N == 0 { adapt_mesh() ... }` regrids every N steps (any
     period-guarded `print` / `write_vtk` / `write_hdf5` fires with the same rule);
   * in `initial_condition`, uniform `density[i]` / `velocity[i]` assignments set
-    the initial state, `place_geometry` a sphere, and a per-cell loop writing
+    the initial state, `place_geometry` the case's sphere (the first unscaled
+    one) or solid-mask geometry (further spheres, boxes, cylinders, STL meshes:
+    voxelised on the GPU into the case's mask at --mask-level, the mesh then
+    pre-refined around them), and a per-cell loop writing
     `refine_flag[i] = k` under a condition (evaluated per brick at its centre,
     `cell_position(i)`) followed by `adapt_mesh()` pre-refines up to k levels;
   * `write_vtk(fields..., path)` writes a VTK PolyData file (fluidloom_gb300.io),
@@ -511,8 +514,10 @@ class Scenario:
     """A parsed script bound to case parameters (BASELINE-like defaults when the
     script does not set them)."""
 
-    def __init__(self, tree, ext=None, max_level=None, tau=None, regrid_every=None):
+    def __init__(self, tree, ext=None, max_level=None, tau=None, regrid_every=None, base_dir=".", mask_level=None):
         self.tree = tree
+        self.base_dir = base_dir
+        self.solids = []  # placed geometries other than the case sphere: dicts of GeometryDescriptor fields
         self.fields = dict(tree["fields"])
         imports = " ".join(tree["imports"]).lower()
         self.lattice = "D3Q19"
@@ -535,6 +540,7 @@ class Scenario:
         self.tau = tau if tau is not None else 0.56
         if regrid_every:
             self.regrid_every = regrid_every
+        self.mask_level = mask_level if mask_level is not None else min(self.max_level, 2)
 
     def _analyse(self):
         env = Env({"timestep": 0, "num_cells": 0})
@@ -557,18 +563,42 @@ class Scenario:
                         pass
 
     def _place(self, args, env):
-        kw = {}
+        """place_geometry(NAME) or place_geometry(type=..., ...): the first unscaled sphere becomes the
+        case's sphere; other spheres, boxes, cylinders and STL meshes become solid-mask geometry."""
         if len(args) == 1 and args[0][0] is None and args[0][1][0] == "name":  # place_geometry(NAME)
             g = self.tree["geometries"].get(args[0][1][1])
             if g is None:
                 raise ParseError("place_geometry: unknown geometry %r" % args[0][1][1])
-            kw = {"type": g.get("type"), "radius": g.get("radius"),
-                  "center": evaluate(g["translate"], env) if "translate" in g else None}
+            kw = {k: (evaluate(v, env) if isinstance(v, tuple) else v) for k, v in g.items()}
         else:
             kw = _kw(args, env)
-        if str(kw.get("type", "")).lower() != "sphere":
-            raise ParseError("place_geometry: only spheres are placed by this build")
-        self.sphere = (tuple(float(x) for x in np.asarray(kw["center"]).reshape(-1)[:3]), float(kw["radius"]))
+        kind = str(kw.get("type", "")).lower()
+        vec = lambda v, d: tuple(float(x) for x in np.asarray(v if v is not None else d, float).reshape(-1)[:3])
+        t = vec(kw.get("translate", kw.get("center")), (0.0, 0.0, 0.0))
+        scale = vec(kw.get("scale"), (1.0, 1.0, 1.0))
+        if kind == "sphere" and self.sphere is None and scale == (1.0, 1.0, 1.0) and not self.solids:
+            self.sphere = (t, float(kw["radius"]))
+            return
+        if kind not in ("sphere", "box", "cylinder", "stl"):
+            raise ParseError("place_geometry: type %r is not placed by this build" % kind)
+        if kind == "stl" and not kw.get("source"):
+            raise ParseError("place_geometry: an stl geometry needs a source file")
+        self.solids.append({"type": kind, "translate": t, "scale": scale, "source": kw.get("source"),
+                            **{k: float(kw.get(k, 1.0)) for k in ("radius", "height", "width", "length")}})
+
+    def solid_geometries(self):
+        """(GeometryDesc, triangles or None) of the solids in voxel units of the mask level:
+        translate and scale times 2^mask_level (script coordinates are level-0 sites)."""
+        from . import geometry as G
+        s = float(1 << self.mask_level)
+        out = []
+        for g in self.solids:
+            kind = {"sphere": G.SPHERE, "box": G.BOX, "cylinder": G.CYLINDER, "stl": G.STL}[g["type"]]
+            d = G.make(kind, translate=[v * s for v in g["translate"]], scale=[v * s for v in g["scale"]],
+                       radius=g["radius"], height=g["height"], width=g["width"], length=g["length"])
+            tris = G.load_stl(os.path.join(self.base_dir, g["source"])) if kind == G.STL else None
+            out.append((d, tris))
+        return out
 
     def _loop_statement(self, st, env, period):
         k = st[0]
@@ -619,6 +649,8 @@ class Scenario:
                                band=0.0)
             c.inlet_u[:] = list(u)
             c.init_u[:] = list(self.init_u) if any(self.init_u) else list(u)
+            if self.sphere is None and self.solids:  # the placed geometry is the obstacle
+                c.has_sphere = 0
         if self.rule:
             c.refine_frac = self.rule["refine"] if self.rule["refine"] is not None else c.refine_frac
             c.coarsen_frac = self.rule["coarsen"] if self.rule["coarsen"] is not None else c.coarsen_frac
@@ -638,6 +670,13 @@ class Runner:
         self.timestep = 0
         self.lups = 0
         self.regrids = 0
+        self.solid_cells = 0
+        if scenario.solids:
+            from . import geometry
+            self.solid_cells = geometry.place(ctx, self.pool, 0, scenario.mask_level, scenario.solid_geometries())
+            for _ in range(scenario.max_level):  # at rest only the mask band refines, as the sphere's at creation
+                self.pool.regrid()
+                self.regrids += 1
 
     def env(self):
         info = self.pool.info()
@@ -759,11 +798,13 @@ def main(argv=None):
     ap.add_argument("--max-level", type=int)
     ap.add_argument("--tau", type=float)
     ap.add_argument("--regrid-every", type=int)
+    ap.add_argument("--mask-level", type=int, help="level of the solid-mask grid of placed geometries")
     ap.add_argument("--out", default="fl_output")
     args = ap.parse_args(argv)
     from . import Context
     tree = parse(open(args.script).read())
-    sc = Scenario(tree, args.ext, args.max_level, args.tau, args.regrid_every)
+    sc = Scenario(tree, args.ext, args.max_level, args.tau, args.regrid_every,
+                  base_dir=os.path.dirname(os.path.abspath(args.script)), mask_level=args.mask_level)
     ctx = Context(0)
     r = Runner(ctx, sc, args.out)
     r.initial()
@@ -771,7 +812,7 @@ def main(argv=None):
     r.final()
     info = r.pool.info()
     res = {"script": os.path.basename(args.script), "kind": sc.kind, "lattice": sc.lattice, "note": sc.note,
-           "steps": args.steps, "regrids": r.regrids, "bricks": int(info.num_bricks), "seconds": secs,
+           "steps": args.steps, "regrids": r.regrids, "solid_cells": r.solid_cells, "bricks": int(info.num_bricks), "seconds": secs,
            "mlups": r.lups / secs / 1e6 if secs > 0 else None, "kernels": sc.runs}
     print(json.dumps(res))
     return res

@@ -99,3 +99,44 @@ def process(ctx, d, cell_size, domain_box, tris=None, cap=1 << 22):
              ctypes.c_float(cell_size), box, *[o.ptr for o in out], key.ptr, ctypes.c_size_t(cap), ctypes.byref(n))
     k = n.value
     return np.stack([o.to_host()[:k] for o in out[:3]], -1), out[3].to_host()[:k], key.to_host()[:k]
+
+
+
+def _cell_bound(ctx, d, t, dims):
+    """Cells fl_geometry_process can return for one geometry on the grid `dims`."""
+    if d.type == STL:  # the whole inclusive grid range of the transformed mesh bounds
+        if not len(t):
+            return 0
+        v = t.reshape(-1, 3).astype(np.float64) * np.array(d.scale) + np.array(d.translate)
+        lo, hi = v.min(0), v.max(0)
+        return int(np.prod(np.ceil(hi) - np.floor(lo) + 2))
+    b = np.array(aabb(ctx, d), np.float64)  # clipped to the grid, cells [floor, ceil)
+    lo, hi = np.maximum(b[:3], 0.0), np.minimum(b[3:], dims)
+    return int(np.prod(np.maximum(np.ceil(hi) - np.floor(lo), 0.0)))
+
+
+def place(ctx, pool, case_id, level, geoms):
+    """Place geometries as solid into one case of a pool.  `geoms` is a list of
+    (GeometryDesc, triangles or None), each written in voxel units of the
+    case's level-`level` grid; their cells (cell size 1; implicit shapes
+    clipped to the grid) are made on the GPU by fl_geometry_process into one
+    device buffer and handed to fl_pool_set_solid_cells without leaving the
+    device (the mask is their union).  Returns the number of cells placed."""
+    nz, ny, nx = pool.mask_shape(case_id, level)
+    dims = np.array([nx, ny, nz], np.float64)
+    items = []
+    for d, tris in geoms:
+        t = np.ascontiguousarray(tris if tris is not None else np.zeros((0, 9)), np.float32).reshape(-1, 9)
+        items.append((d, t, _cell_bound(ctx, d, t, dims)))
+    cap = max(1, sum(k for _, _, k in items))
+    out = [DeviceArray(ctx, (cap,), np.int32) for _ in range(3)]
+    box = (ctypes.c_float * 6)(0.0, 0.0, 0.0, float(nx), float(ny), float(nz))
+    used = 0
+    for d, t, k in items:
+        n = ctypes.c_size_t()
+        at = [ctypes.c_void_p(o.ptr.value + 4 * used) for o in out]
+        ctx.call("fl_geometry_process", ctypes.byref(d), t.ctypes.data_as(ctypes.c_void_p), ctypes.c_size_t(len(t)),
+                 ctypes.c_float(1.0), box, *at, None, None, ctypes.c_size_t(cap - used), ctypes.byref(n))
+        used += n.value
+    pool.set_solid_cells(case_id, level, out[0].ptr, out[1].ptr, out[2].ptr, used)
+    return used

@@ -17,6 +17,20 @@ class LbmCase(ctypes.Structure):
                 ("init_u", ctypes.c_float * 3)]
 
 
+def pack_mask(mask):
+    """Solid-mask words of a bool grid (Nz, Ny, Nx): bit (z*Ny + y)*Nx + x, 32 to a uint32."""
+    b = np.packbits(np.ascontiguousarray(mask, bool).reshape(-1), bitorder="little")
+    b = np.concatenate([b, np.zeros((-b.size) % 4, np.uint8)])
+    return b.view("<u4").astype(np.uint32)
+
+
+def unpack_mask(words, shape):
+    """The bool grid of pack_mask's words."""
+    n = int(np.prod(shape))
+    bits = np.unpackbits(np.ascontiguousarray(words, "<u4").view(np.uint8), bitorder="little")[:n]
+    return bits.astype(bool).reshape(shape)
+
+
 class PoolInfo(ctypes.Structure):
     _fields_ = [("num_bricks", ctypes.c_size_t), ("capacity", ctypes.c_size_t), ("num_cases", ctypes.c_int32),
                 ("max_level", ctypes.c_int32), ("bricks_per_level", ctypes.c_uint32 * 16),
@@ -133,6 +147,39 @@ class Pool:
         i = None if inlet_u is None else np.ascontiguousarray(inlet_u, np.float32)
         self.ctx.call("fl_pool_set_velocities", self.h, w.ctypes.data_as(P) if w is not None else None,
                       i.ctypes.data_as(P) if i is not None else None)
+
+    def mask_shape(self, case_id, level):
+        """(Nz, Ny, Nx) of a case's solid-mask grid at `level` (N = ext * 8 << level)."""
+        c = self.cases[case_id]
+        return tuple((int(c.ext[a]) * 8) << level for a in (2, 1, 0))
+
+    def set_solid_mask(self, case_id, level, mask):
+        """Solid voxels of one case at `level` (bool (Nz, Ny, Nx)), OR-ed with its sphere; None removes them."""
+        if mask is None:
+            self.ctx.call("fl_pool_set_solid_mask", self.h, case_id, 0, None, ctypes.c_size_t(0))
+            return
+        mask = np.asarray(mask, bool)
+        if mask.shape != self.mask_shape(case_id, level):
+            raise ValueError("mask shape %s, want %s" % (mask.shape, self.mask_shape(case_id, level)))
+        w = pack_mask(mask)
+        self.ctx.call("fl_pool_set_solid_mask", self.h, case_id, level, w.ctypes.data_as(P), ctypes.c_size_t(w.size))
+
+    def set_solid_cells(self, case_id, level, x, y, z, n):
+        """Solid mask from n cells of the level-`level` grid given as device columns (pointers)."""
+        cols = [v if isinstance(v, P) else P(v) for v in (x, y, z)]
+        self.ctx.call("fl_pool_set_solid_cells", self.h, case_id, level, *cols, ctypes.c_size_t(n))
+
+    def solid_mask(self, case_id):
+        """(level, bool (Nz, Ny, Nx)) of the case's solid mask, or (-1, None)."""
+        lv = ctypes.c_int32()
+        self.ctx.call("fl_pool_get_solid_mask", self.h, case_id, ctypes.byref(lv), None, ctypes.c_size_t(0))
+        if lv.value < 0:
+            return -1, None
+        shape = self.mask_shape(case_id, lv.value)
+        w = np.empty((int(np.prod(shape)) + 31) // 32, np.uint32)
+        self.ctx.call("fl_pool_get_solid_mask", self.h, case_id, ctypes.byref(lv), w.ctypes.data_as(P),
+                      ctypes.c_size_t(w.size))
+        return lv.value, unpack_mask(w, shape)
 
     def add_cases(self, cases):
         arr = (LbmCase * len(cases))(*cases)

@@ -347,6 +347,23 @@ int fl_pool_load(fl_ctx* ctx, fl_pool* pool, size_t n, const int32_t* x, const i
 /* Per-case moving-wall and inlet velocities ([ncases][3] host arrays, either may be NULL),
  * copied on the stream and used from the next step on. */
 int fl_pool_set_velocities(fl_ctx* ctx, fl_pool* pool, const float* wall_u, const float* inlet_u);
+/* Solid voxels of one case, OR-ed with its sphere: bit (z * Ny + y) * Nx + x of `bits` (host,
+ * nwords = ceil(Nx * Ny * Nz / 32), N = ext * 8 << level) marks voxel (x, y, z) of the case's grid
+ * at `level`.  A site of level l samples the voxel under its centre (the upper middle voxel
+ * when l < level).  bits == NULL removes the mask.  Classes, descriptors and fluid counts are
+ * rebuilt; populations are unchanged (solid sites take the rest state at the next step), and the
+ * next regrid refines bricks holding both solid and fluid sites (their own or in a one-site
+ * halo) to max_level.  Uploads the solid cells the reference's builder generates from its
+ * geometries but leaves on the host (src/parsing/SimulationBuilder.cpp:112-126). */
+int fl_pool_set_solid_mask(fl_ctx* ctx, fl_pool* pool, int32_t case_id, int32_t level, const uint32_t* bits,
+                           size_t nwords);
+/* The same from n solid cells given as DEVICE columns x, y, z of the level-`level` grid, e.g.
+ * the cells fl_geometry_process gives for a geometry written in level-`level` voxel units with
+ * cell_size 1; cells outside the case grid are ignored. */
+int fl_pool_set_solid_cells(fl_ctx* ctx, fl_pool* pool, int32_t case_id, int32_t level, const int32_t* x,
+                            const int32_t* y, const int32_t* z, size_t n);
+/* The case's mask level (-1: none) and, when bits != NULL, its words (nwords at least the mask's). */
+int fl_pool_get_solid_mask(fl_ctx* ctx, fl_pool* pool, int32_t case_id, int32_t* level, uint32_t* bits, size_t nwords);
 /* Regrid with caller-given flags (one int32 per brick in pool order: > 0 split, -1 merge, 0 keep),
  * 2:1 balanced like every regrid: the refine_flags buffer AdaptMeshNode passes to the
  * reference's adapt (src/runtime/nodes/AdaptMeshNode.cpp:52-63). */

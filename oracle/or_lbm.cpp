@@ -88,6 +88,8 @@ inline int dir_index(int dx, int dy, int dz) {
 struct CaseInfo {
     int periodic[3];
     float omega[20];
+    int mask_level = 0;
+    std::vector<uint32_t> mask;  // solid voxels at mask_level, bit (z * Ny + y) * Nx + x; empty: none
 };
 
 struct Pool {
@@ -114,16 +116,36 @@ struct Pool {
 
 inline size_t fidx(size_t n, int q, size_t b, int s) { return ((size_t)q * n + b) * 512 + s; }
 
-inline bool solid_at(const or_lbm_case& c, int64_t sx, int64_t sy, int64_t sz, int l) {
-    if (!c.has_sphere) return false;
-    float inv = 1.0f / (float)(1 << l);
-    float px = ((float)sx + 0.5f) * inv, py = ((float)sy + 0.5f) * inv, pz = ((float)sz + 0.5f) * inv;
-    float dx = px - c.sphere_c[0], dy = py - c.sphere_c[1], dz = pz - c.sphere_c[2];
-    float d2 = dx * dx;
-    d2 = d2 + dy * dy;
-    d2 = d2 + dz * dz;
-    float r2 = c.sphere_r * c.sphere_r;
-    return d2 < r2;
+// Mask voxel under the centre of level-l site (sx, sy, sz): a coarser site
+// samples the voxel at its centre (the upper of the two middle ones), a finer
+// site the voxel holding it; sites outside the case grid are fluid.
+inline bool mask_at(const or_lbm_case& c, const CaseInfo& ci, int64_t sx, int64_t sy, int64_t sz, int l) {
+    const int64_t G[3] = {sx, sy, sz};
+    int64_t v[3], N[3];
+    const int sh = ci.mask_level - l;
+    for (int a = 0; a < 3; ++a) {
+        if (G[a] < 0 || G[a] >= ((int64_t)c.ext[a] * 8 << l)) return false;
+        N[a] = (int64_t)c.ext[a] * 8 << ci.mask_level;
+        if (sh >= 0) v[a] = G[a] * ((int64_t)1 << sh) + (sh > 0 ? (int64_t)1 << (sh - 1) : 0);
+        else v[a] = G[a] / ((int64_t)1 << -sh);
+    }
+    const uint64_t i = ((uint64_t)v[2] * (uint64_t)N[1] + (uint64_t)v[1]) * (uint64_t)N[0] + (uint64_t)v[0];
+    return (ci.mask[i >> 5] >> (i & 31)) & 1u;
+}
+
+// Solid: inside the case's sphere or on a voxel of its solid mask.
+inline bool solid_at(const or_lbm_case& c, const CaseInfo& ci, int64_t sx, int64_t sy, int64_t sz, int l) {
+    if (c.has_sphere) {
+        float inv = 1.0f / (float)(1 << l);
+        float px = ((float)sx + 0.5f) * inv, py = ((float)sy + 0.5f) * inv, pz = ((float)sz + 0.5f) * inv;
+        float dx = px - c.sphere_c[0], dy = py - c.sphere_c[1], dz = pz - c.sphere_c[2];
+        float d2 = dx * dx;
+        d2 = d2 + dy * dy;
+        d2 = d2 + dz * dz;
+        float r2 = c.sphere_r * c.sphere_r;
+        if (d2 < r2) return true;
+    }
+    return !ci.mask.empty() && mask_at(c, ci, sx, sy, sz, l);
 }
 
 // Pull of population q into site G (global level-l coords) of brick b.
@@ -167,7 +189,7 @@ float pull(const Pool& P, size_t b, int q, int l, int sub, const int64_t* G, con
     }
     int64_t Sw[3];
     for (int a = 0; a < 3; ++a) Sw[a] = ci.periodic[a] ? ((S[a] % N[a]) + N[a]) % N[a] : S[a];
-    if (solid_at(c, Sw[0], Sw[1], Sw[2], l)) return R[fidx(P.n, OPP[q], b, s_local)];
+    if (solid_at(c, ci, Sw[0], Sw[1], Sw[2], l)) return R[fidx(P.n, OPP[q], b, s_local)];
     // local coordinates of the (unwrapped) source relative to brick b
     int64_t L[3] = {S[0] - (int64_t)P.x[b] * 8, S[1] - (int64_t)P.y[b] * 8, S[2] - (int64_t)P.z[b] * 8};
     if (L[0] >= 0 && L[0] < 8 && L[1] >= 0 && L[1] < 8 && L[2] >= 0 && L[2] < 8)
@@ -216,11 +238,12 @@ void collide_stream(Pool& P, int l, int sub, int nthreads) {
     for (long long b = 0; b < nb; ++b) {
         if (P.level[b] != l) continue;
         const or_lbm_case& c = P.cases[P.cs[b]];
-        float omega = P.info[P.cs[b]].omega[l];
+        const CaseInfo& ci = P.info[P.cs[b]];
+        float omega = ci.omega[l];
         for (int s = 0; s < 512; ++s) {
             int64_t G[3] = {(int64_t)P.x[b] * 8 + (s & 7), (int64_t)P.y[b] * 8 + ((s >> 3) & 7),
                             (int64_t)P.z[b] * 8 + (s >> 6)};
-            if (solid_at(c, G[0], G[1], G[2], l)) {
+            if (solid_at(c, ci, G[0], G[1], G[2], l)) {
                 for (int q = 0; q < Q; ++q) Wt[fidx(P.n, q, b, s)] = wq(q);
                 continue;
             }
@@ -300,7 +323,7 @@ bool in_band(const or_lbm_case& c, int32_t bx, int32_t by, int32_t bz, int l) {
 inline void site_u(const Pool& P, const float* F, size_t b, int s, int l, float* u) {
     const or_lbm_case& c = P.cases[P.cs[b]];
     int64_t G[3] = {(int64_t)P.x[b] * 8 + (s & 7), (int64_t)P.y[b] * 8 + ((s >> 3) & 7), (int64_t)P.z[b] * 8 + (s >> 6)};
-    if (solid_at(c, G[0], G[1], G[2], l)) { u[0] = u[1] = u[2] = 0.0f; return; }
+    if (solid_at(c, P.info[P.cs[b]], G[0], G[1], G[2], l)) { u[0] = u[1] = u[2] = 0.0f; return; }
     float f[Q];
     for (int q = 0; q < Q; ++q) f[q] = F[fidx(P.n, q, b, s)];
     float rho, jx, jy, jz;
@@ -338,6 +361,33 @@ void brick_vorticity(const Pool& P, size_t b, float* wmax) {
     *wmax = m;
 }
 
+// A brick of a masked case whose own sites and one-site halo (periodic axes
+// wrapped) hold both solid and fluid sites: some halo site solid, not all own
+// sites solid.
+bool mask_mixed(const Pool& P, size_t b) {
+    const or_lbm_case& c = P.cases[P.cs[b]];
+    const CaseInfo& ci = P.info[P.cs[b]];
+    if (ci.mask.empty()) return false;
+    const int l = P.level[b];
+    const int64_t G0[3] = {(int64_t)P.x[b] * 8, (int64_t)P.y[b] * 8, (int64_t)P.z[b] * 8};
+    bool any = false, all = true;
+    for (int i = 0; i < 1000; ++i) {
+        const int h[3] = {i % 10, (i / 10) % 10, i / 100};
+        int64_t G[3];
+        for (int a = 0; a < 3; ++a) {
+            G[a] = G0[a] + h[a] - 1;
+            if (!ci.periodic[a]) continue;
+            const int64_t N = ((int64_t)c.ext[a] * 8) << l;
+            G[a] = G[a] < 0 ? G[a] + N : (G[a] >= N ? G[a] - N : G[a]);
+        }
+        const bool sol = solid_at(c, ci, G[0], G[1], G[2], l);
+        const bool own = h[0] >= 1 && h[0] <= 8 && h[1] >= 1 && h[1] <= 8 && h[2] >= 1 && h[2] <= 8;
+        any = any || sol;
+        all = all && (sol || !own);
+    }
+    return any && !all;
+}
+
 void compute_flags(Pool& P, bool use_vorticity, float* out_wmax) {
     std::vector<float> wm(P.n, 0.0f);
     if (use_vorticity) {
@@ -349,7 +399,7 @@ void compute_flags(Pool& P, bool use_vorticity, float* out_wmax) {
     for (size_t b = 0; b < P.n; ++b) {
         const or_lbm_case& c = P.cases[P.cs[b]];
         int l = P.level[b];
-        bool band = in_band(c, P.x[b], P.y[b], P.z[b], l);
+        bool band = in_band(c, P.x[b], P.y[b], P.z[b], l) || mask_mixed(P, b);
         float cm = cmax[P.cs[b]];
         int32_t fl = 0;
         if (band) fl = l < c.max_level ? 1 : 0;
@@ -523,6 +573,14 @@ void* or_pool_new(const or_lbm_case* cases, int ncases) {
 
 void or_pool_free(void* h) { delete (Pool*)h; }
 
+// The case's solid mask (fl_pool_set_solid_mask): bits == NULL removes it.
+void or_pool_set_mask(void* h, int case_id, int level, const uint32_t* bits, size_t nwords) {
+    Pool& P = *(Pool*)h;
+    CaseInfo& ci = P.info[case_id];
+    ci.mask_level = bits ? level : 0;
+    ci.mask.assign(bits, bits ? bits + nwords : bits);
+}
+
 void or_pool_steps(void* h, int nsteps, int nthreads) {
     Pool& P = *(Pool*)h;
     for (int i = 0; i < nsteps; ++i) step_level(P, 0, 0, nthreads);
@@ -572,7 +630,7 @@ void or_pool_conservation(void* h, double* out) {
         double acc[4] = {0, 0, 0, 0};
         for (int s = 0; s < 512; ++s) {
             int64_t G[3] = {(int64_t)P.x[b] * 8 + (s & 7), (int64_t)P.y[b] * 8 + ((s >> 3) & 7), (int64_t)P.z[b] * 8 + (s >> 6)};
-            if (solid_at(c, G[0], G[1], G[2], l)) continue;
+            if (solid_at(c, P.info[P.cs[b]], G[0], G[1], G[2], l)) continue;
             float f[Q];
             for (int q = 0; q < Q; ++q) f[q] = F[fidx(P.n, q, b, s)];
             float rho, jx, jy, jz;
@@ -593,7 +651,7 @@ uint64_t or_pool_fluid_lups(void* h) {
         uint64_t cnt = 0;
         for (int s = 0; s < 512; ++s) {
             int64_t G[3] = {(int64_t)P.x[b] * 8 + (s & 7), (int64_t)P.y[b] * 8 + ((s >> 3) & 7), (int64_t)P.z[b] * 8 + (s >> 6)};
-            if (!solid_at(c, G[0], G[1], G[2], l)) ++cnt;
+            if (!solid_at(c, P.info[P.cs[b]], G[0], G[1], G[2], l)) ++cnt;
         }
         t += cnt << l;
     }

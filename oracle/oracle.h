@@ -117,6 +117,8 @@ void or_pool_nbr(void* h, uint32_t* out);
 void or_pool_populations(void* h, float* out);
 void or_pool_conservation(void* h, double* out);
 uint64_t or_pool_fluid_lups(void* h);
+/* Solid voxels of one case at `level` (bit (z * Ny + y) * Nx + x); bits == NULL removes them. */
+void or_pool_set_mask(void* h, int case_id, int level, const uint32_t* bits, size_t nwords);
 
 /* Geometry placement (or_geometry.cpp).  type: 0 STL, 1 implicit function, 2 box, 3 sphere, 4 cylinder. */
 typedef struct or_geometry {

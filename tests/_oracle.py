@@ -101,6 +101,7 @@ def load():
         L.or_pool_conservation.argtypes = [P, P]
         L.or_pool_fluid_lups.restype = ctypes.c_uint64
         L.or_pool_fluid_lups.argtypes = [P]
+        L.or_pool_set_mask.argtypes = [P, ctypes.c_int, ctypes.c_int, P, ctypes.c_size_t]
         _lib = L
     return _lib
 
@@ -288,6 +289,15 @@ class OraclePool:
 
     def lups(self):
         return load().or_pool_fluid_lups(self.h)
+
+    def set_mask(self, case_id, level, words):
+        """Solid-mask words (uint32, bit (z*Ny + y)*Nx + x) of one case; None removes them."""
+        if words is None:
+            load().or_pool_set_mask(self.h, case_id, 0, None, 0)
+            return
+        self._mask = getattr(self, "_mask", {})
+        self._mask[case_id] = w = np.ascontiguousarray(words, np.uint32)
+        load().or_pool_set_mask(self.h, case_id, level, ptr(w), w.size)
 
     def __del__(self):
         try:

@@ -81,3 +81,32 @@ def test_reference_benchmark_scripts_parse_and_map():
     sph = dsl.Scenario(dsl.parse(open(os.path.join(REF_BENCH, "flow_past_sphere.fl")).read()))
     assert sph.kind == "channel" and sph.inlet == (0.1, 0.0, 0.0) and sph.regrid_every == 50
     assert sph.rule["field"] == "q_criterion"
+
+
+def test_placed_solids_map_to_mask_geometry(tmp_path):
+    from fluidloom_gb300 import geometry as G
+    sc = dsl.Scenario(dsl.parse(open(os.path.join(SCEN, "obstacles.fl")).read()), ext=(8, 8, 8), max_level=2)
+    assert sc.kind == "channel" and sc.sphere is None and sc.mask_level == 2
+    assert [g["type"] for g in sc.solids] == ["box", "cylinder"]
+    assert sc.case().has_sphere == 0
+    (box, t0), (cyl, t1) = sc.solid_geometries()
+    assert t0 is None and t1 is None
+    assert box.type == G.BOX and list(box.translate) == [96.0, 120.0, 128.0] and list(box.scale) == [4.0] * 3
+    assert (box.width, box.height, box.length) == (6.0, 10.0, 8.0)
+    assert cyl.type == G.CYLINDER and cyl.radius == 3.0 and list(cyl.translate) == [176.0, 128.0, 96.0]
+    # a second sphere, a scaled sphere and an STL file become mask geometry; implicit functions are refused
+    G.write_stl(str(tmp_path / "tet.stl"), [[0, 0, 0, 1, 0, 0, 0, 1, 0], [0, 0, 0, 0, 0, 1, 1, 0, 0],
+                                            [0, 0, 0, 0, 1, 0, 0, 0, 1], [1, 0, 0, 0, 0, 1, 0, 1, 0]])
+    src = """
+        geometry a { type: sphere  radius: 4.0  translate: (16.0, 16.0, 16.0) }
+        geometry b { type: sphere  radius: 2.0  translate: (40.0, 16.0, 16.0) }
+        geometry c { type: stl  source: "tet.stl"  scale: (8.0, 8.0, 8.0)  translate: (50.0, 20.0, 20.0) }
+        initial_condition: { place_geometry(a)  place_geometry(b)  place_geometry(c) }
+        time_loop: { run lbm_step()  run apply_inlet_velocity(velocity_inlet = (0.03, 0.0, 0.0)) }"""
+    sc = dsl.Scenario(dsl.parse(src), ext=(8, 4, 4), max_level=1, base_dir=str(tmp_path))
+    assert sc.sphere == ((16.0, 16.0, 16.0), 4.0) and [g["type"] for g in sc.solids] == ["sphere", "stl"]
+    assert sc.mask_level == 1 and sc.case().has_sphere == 1
+    (_, none), (stl, tris) = sc.solid_geometries()
+    assert none is None and stl.type == G.STL and tris.shape == (4, 9) and list(stl.scale) == [16.0] * 3
+    with pytest.raises(dsl.ParseError, match="not placed"):
+        dsl.Scenario(dsl.parse("initial_condition: { place_geometry(type = \"implicit\") }"))

@@ -65,3 +65,30 @@ def test_sphere_script_prerefines_near_the_sphere(ctx, tmp_path):
     assert np.all(np.abs(c[fine] - 8.0) < 8.0)
     secs = r.run(6)
     assert secs > 0 and r.lups > 0
+
+
+def test_obstacle_script_equals_direct_pool(ctx, tmp_path):
+    """Box and cylinder of a script become the case's solid mask (GPU voxelised),
+    the mesh is pre-refined around them, and the run equals the same steps on a
+    pool built directly."""
+    from fluidloom_gb300 import geometry
+    from fluidloom_gb300.lbm import Pool
+    sc = dsl.Scenario(dsl.parse(open(os.path.join(SCEN, "obstacles.fl")).read()), ext=(8, 8, 8), max_level=1,
+                      mask_level=1)
+    r = dsl.Runner(ctx, sc, str(tmp_path), log=lambda *_: None)
+    r.initial()
+    r.run(30)
+    ref = Pool(ctx, [sc.case()])
+    n = geometry.place(ctx, ref, 0, 1, sc.solid_geometries())
+    ref.regrid()
+    ref.step(25)
+    ref.regrid()
+    ref.step(5)
+    assert r.solid_cells == n > 0
+    lv, m = r.pool.solid_mask(0)
+    assert lv == 1 and m.sum() == n
+    a, b = r.pool.bricks(), ref.bricks()
+    for k in ("x", "y", "z", "level"):
+        np.testing.assert_array_equal(a[k], b[k])
+    assert (a["level"] == 1).any()
+    np.testing.assert_array_equal(r.pool.populations(), ref.populations())
