@@ -17,7 +17,7 @@ import os
 
 import numpy as np
 
-from .lbm import LbmCase, Pool
+from .lbm import LbmCase, Pool, pack_mask, unpack_mask
 
 
 def _site_points(bricks):
@@ -124,7 +124,13 @@ def save_snapshot(pool, path):
     active = np.zeros(len(pool.cases), bool)
     active[np.unique(b["case_id"])] = True
     cases = np.frombuffer(b"".join(bytes(c) if c is not None else bytes(LbmCase()) for c in pool.cases), np.uint8)
-    np.savez(path, version=np.int32(1), cases=cases, active=active, f=f, **b)
+    masks = {}
+    for c in np.flatnonzero(active):
+        lv, m = pool.solid_mask(int(c))
+        if lv >= 0:
+            masks["mask_level_%d" % c] = np.int32(lv)
+            masks["mask_words_%d" % c] = pack_mask(m)
+    np.savez(path, version=np.int32(1), cases=cases, active=active, f=f, **b, **masks)
     return path
 
 
@@ -141,6 +147,10 @@ def load_snapshot(ctx, path):
     if gone:
         pool.remove_cases(gone)
     pool.load({k: z[k] for k in ("x", "y", "z", "level", "case_id")}, z["f"])
+    for c in np.flatnonzero(z["active"]):
+        if "mask_level_%d" % c in z.files:
+            lv = int(z["mask_level_%d" % c])
+            pool.set_solid_mask(int(c), lv, unpack_mask(z["mask_words_%d" % c], pool.mask_shape(int(c), lv)))
     return pool
 
 

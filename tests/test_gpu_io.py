@@ -47,6 +47,23 @@ def test_snapshot_restart_continues_bit_for_bit(ctx, tmp_path):
     np.testing.assert_array_equal(p.conservation()[1:], q.conservation()[1:])
 
 
+def test_snapshot_keeps_solid_masks(ctx, tmp_path):
+    from fluidloom_gb300.lbm import Pool
+    cav, sph, _ = _cases()
+    p = Pool(ctx, [cav, sph])
+    m = np.zeros(p.mask_shape(1, 1), bool)
+    m[10:20, 8:24, 40:50] = True
+    p.set_solid_mask(1, 1, m)
+    _advance(p)
+    q = io.load_snapshot(ctx, io.save_snapshot(p, str(tmp_path / "masked.npz")))
+    lv, back = q.solid_mask(1)
+    assert lv == 1 and np.array_equal(back, m) and q.solid_mask(0) == (-1, None)
+    assert q.info().fluid_lups_per_step == p.info().fluid_lups_per_step
+    for r in (p, q):
+        _advance(r)
+    _same(p, q)
+
+
 def _moments(f):
     """The kernels' FP32 moment order (rho, then j by pairs) in numpy float32."""
     r = f[0].copy()
