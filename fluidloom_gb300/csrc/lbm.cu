@@ -1199,6 +1199,14 @@ struct fl_pool {
     void* adapt_scratch = nullptr;
     size_t adapt_scratch_bytes = 0;
     int grid_mult = 4;
+    // All-solid bricks only ever hold the rest equilibrium: once both
+    // population buffers of a level hold it (two sub-steps after any change of
+    // the bricks or populations), rewriting it changes nothing and its launch
+    // is left out.  solid_due[l] counts the level's sub-steps that must still
+    // write them; emit_solid forces the launch (a caller's stream capture,
+    // which may be replayed at any time).
+    int solid_due[kMaxPoolLevels] = {};
+    bool emit_solid = false;
     // dependency-graph launch order: per level a stream for the general,
     // interface and all-solid bricks and one for the interior bricks
     int streams = 2;
@@ -1290,10 +1298,13 @@ void free_brick_arrays(fl_ctx* ctx, fl_pool* P) {
 
 // The captured steps no longer match the pool: mark them stale.  The next
 // capture updates the instantiated graph in place when its shape is unchanged
-// (cudaGraphExecUpdate) instead of instantiating anew.
+// (cudaGraphExecUpdate) instead of instantiating anew.  Every change of the
+// bricks or populations passes here, so it also makes each level write its
+// all-solid bricks for its next two sub-steps (both buffers).
 void drop_graph(fl_pool* P) {
     ++P->version;
     P->graph_ok[0] = P->graph_ok[1] = false;
+    for (int l = 0; l < kMaxPoolLevels; ++l) P->solid_due[l] = 2;
 }
 
 void free_graphs(fl_pool* P) {
@@ -1678,8 +1689,10 @@ struct Dag {
 // write-after-read of each level's two population buffers.
 void launch_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm, Dag* dag) {
     const StepArgs a = level_args(ctx, P, l, sub);
+    const bool solid = P->emit_solid || P->solid_due[l] > 0;
+    if (!P->emit_solid && P->solid_due[l] > 0) --P->solid_due[l];
     if (!dag) {
-        for (int kind = 0; kind < 3; ++kind) launch_class(ctx, P, a, l, kind, ctx->stream, tm);
+        for (int kind = 0; kind < (solid ? 3 : 2); ++kind) launch_class(ctx, P, a, l, kind, ctx->stream, tm);
     } else {
         const int k = dag->k[l]++;
         cudaStream_t sg = P->sg[l], sf = P->sf[l];
@@ -1687,7 +1700,7 @@ void launch_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm, Dag*
         if (l > 0 && dag->k[l - 1] > 0) cudaStreamWaitEvent(sg, P->evg[l - 1][(dag->k[l - 1] - 1) & 1], 0);
         if (l < P->maxL && dag->k[l + 1] > 0) cudaStreamWaitEvent(sg, P->evg[l + 1][(dag->k[l + 1] - 1) & 1], 0);
         launch_class(ctx, P, a, l, 1, sg, nullptr);
-        launch_class(ctx, P, a, l, 2, sg, nullptr);
+        if (solid) launch_class(ctx, P, a, l, 2, sg, nullptr);
         cudaEventRecord(P->evg[l][k & 1], sg);
         if (k > 0) cudaStreamWaitEvent(sf, P->evg[l][(k - 1) & 1], 0);
         launch_class(ctx, P, a, l, 0, sf, nullptr);
@@ -1907,9 +1920,13 @@ int fl_pool_step(fl_ctx* ctx, fl_pool* P, int nsteps) {
     if (!ctx || !P || nsteps < 0) return FL_E_INVALID_ARG;
     cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
     FL_TRY_CUDA(ctx, cudaStreamIsCapturing(ctx->stream, &capturing), "capture status");
+    P->emit_solid = capturing != cudaStreamCaptureStatusNone;
     for (int i = 0; i < nsteps; ++i) {
-        // inside a caller's stream capture the launches join that capture directly
-        if (!P->graphs || capturing != cudaStreamCaptureStatusNone) {
+        // inside a caller's stream capture the launches join that capture
+        // directly; the steps that still write all-solid bricks run uncaptured
+        bool settled = true;
+        for (int l = 0; l <= P->maxL; ++l) settled = settled && P->solid_due[l] == 0;
+        if (!P->graphs || capturing != cudaStreamCaptureStatusNone || !settled) {
             level0_step(ctx, P);
             FL_CHECK_ERRORS(ctx, "k_collide_stream");
             continue;
