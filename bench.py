@@ -136,13 +136,13 @@ def timer(ctx):
     return stop
 
 
-def regrid_microbench(ctx, seed=1):
-    """16.7M-leaf regrid: blob flags, FULL26 balance to a fixed point, split/merge,
-    key sort, rebuild; neighbour table; and a 16.7M 63-bit key sort alone."""
+def regrid_microbench(ctx, seed=1, L=8):
+    """16.7M-leaf regrid (a uniform level-L mesh, 8^L leaves): blob flags, FULL26
+    balance to a fixed point, split/merge, key sort, rebuild; neighbour table; and
+    a 63-bit key sort of the result alone."""
     import ctypes
     from fluidloom_gb300 import DeviceArray
     from fluidloom_gb300.amr import AdaptConfig, AdaptStats, Mesh
-    L = 8
     n1 = 1 << L
     idx = np.arange(n1 ** 3, dtype=np.int64)
     cols = {"x": (idx % n1).astype(np.int32), "y": ((idx // n1) % n1).astype(np.int32),
@@ -152,11 +152,11 @@ def regrid_microbench(ctx, seed=1):
     s = rng.uniform(0.02, 0.1, 64)
     blobs = np.ascontiguousarray(np.concatenate([c, (1 / (2 * s * s))[:, None], np.ones((64, 1))], 1), np.float32)
     m = Mesh(ctx, cols)
-    cfg = AdaptConfig.make(max_level=9, min_level=0, balance_mode=1)
+    cfg = AdaptConfig.make(max_level=L + 1, min_level=0, balance_mode=1)
     out = {}
     stop = timer(ctx)
     ctx.call("fl_flags_from_blobs", ctypes.byref(m.m), blobs.ctypes.data_as(ctypes.c_void_p), 64,
-             ctypes.c_float(0.05), ctypes.c_float(0.5), 9)
+             ctypes.c_float(0.05), ctypes.c_float(0.5), L + 1)
     out["flags_ms"] = stop()
     st = AdaptStats()
     fp = ctypes.c_void_p(0)
@@ -367,9 +367,19 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-microbench", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--microbench-only", action="store_true",
+                    help="run only the 2^24-leaf regrid microbench (one warm-up pass, one timed) and print it")
+    ap.add_argument("--microbench-level", type=int, default=8,
+                    help="level of the microbench's uniform start mesh (8: 2^24 leaves; 7 makes a small case)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.microbench_only:
+        from fluidloom_gb300 import Context
+        ctx = Context(0)
+        regrid_microbench(ctx, L=args.microbench_level)
+        print(json.dumps({"regrid_microbench": regrid_microbench(ctx, L=args.microbench_level)}))
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -51,6 +51,12 @@ __device__ __forceinline__ bool fold3(int64_t* p, const fl_domain_dev::Case& d, 
     return true;
 }
 
+__device__ __forceinline__ bool fold3_32(int32_t* p, const fl_domain_dev::Case& d, int A) {
+    bool in = true;
+    for (int a = 0; a < 3; ++a) in = in && fl_fold32(p[a], d.ext[a] << A, d.periodic[a]);
+    return in;
+}
+
 // Shadow level = the level a cell will have.  FACE6 follows the reference
 // (level + (flag > 0), update_shadow_levels, BalanceEnforcer.cpp:53-62; the
 // first round starts from the levels); FULL26 counts a flag only where the
@@ -105,31 +111,33 @@ __global__ void __launch_bounds__(kT) k_detect_face6(fl_mesh_dev m, fl_domain_de
     if (local) atomicAdd(count, local);
 }
 
-__global__ void __launch_bounds__(kT) k_detect_full26(fl_mesh_dev m, fl_domain_dev dom, const uint64_t* __restrict__ tk,
-                                                      const uint32_t* __restrict__ tv, int lg,
-                                                      const uint8_t* __restrict__ shadow, uint8_t* __restrict__ viol,
-                                                      uint32_t* __restrict__ count) {
-    __shared__ KeyTables T;
-    fl_keys_fill_tables(T.t1, T.t3, false);
+// Every leaf probes its 26 neighbour points at its own size through the
+// sorted locator (32 cells x 26 directions per block); a leaf found two or
+// more shadow levels coarser is a violation.
+__global__ void __launch_bounds__(kProbeThreads, 2) k_detect_full26(fl_mesh_dev m, fl_domain_dev dom, fl_locator L,
+                                                                    const uint8_t* __restrict__ shadow,
+                                                                    uint8_t* __restrict__ viol,
+                                                                    uint32_t* __restrict__ count) {
+    __shared__ uint8_t t1[96];
+    __shared__ uint16_t t3c[12 * 512];
+    fl_keys_fill_tables_cat(t1, t3c);
     __syncthreads();
-    size_t total = m.n * 26;
-    size_t stride = (size_t)gridDim.x * blockDim.x;
+    const fl_probe P = fl_probe_make(t1, t3c, L, dom);
+    const int cl = threadIdx.x / 26, k = threadIdx.x - cl * 26;
+    const int kk = k < 13 ? k : k + 1;
+    const int dv[3] = {kk % 3 - 1, (kk / 3) % 3 - 1, kk / 9 - 1};
     uint32_t local = 0;
-    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
-        size_t i = t / 26;
-        int k = (int)(t - i * 26);
-        uint16_t cs = m.case_id ? m.case_id[i] : 0;
+    for (size_t base = (size_t)blockIdx.x * 32; base < m.n; base += (size_t)gridDim.x * 32) {
+        const size_t i = base + cl;
+        if (i >= m.n) continue;
+        const uint16_t cs = m.case_id ? m.case_id[i] : 0;
         const fl_domain_dev::Case& d = dom.c[m.case_id ? cs : 0];
-        int lvl = m.level[i];
-        int sh = dom.anchor_level - lvl;
-        int64_t anc[3] = {(int64_t)m.x[i] << sh, (int64_t)m.y[i] << sh, (int64_t)m.z[i] << sh};
-        int64_t size = (int64_t)1 << sh;
-        int kk = k < 13 ? k : k + 1;
-        int dv[3] = {kk % 3 - 1, (kk / 3) % 3 - 1, kk / 9 - 1};
-        int64_t p[3];
-        for (int a = 0; a < 3; ++a) p[a] = dv[a] < 0 ? anc[a] - 1 : (dv[a] > 0 ? anc[a] + size : anc[a]);
-        if (!fold3(p, d, dom.anchor_level)) continue;
-        uint32_t r = fl_locate(T.t1, T.t3, tk, tv, lg, nullptr, dom, cs, m.case_id != nullptr, p, lvl);
+        const int sh = dom.anchor_level - m.level[i];
+        const int32_t size = 1 << sh;
+        int32_t p[3] = {m.x[i] << sh, m.y[i] << sh, m.z[i] << sh};
+        for (int a = 0; a < 3; ++a) p[a] += dv[a] < 0 ? -1 : (dv[a] > 0 ? size : 0);
+        if (!fold3_32(p, d, dom.anchor_level)) continue;
+        const uint32_t r = fl_probe_point(P, m.case_id != nullptr, cs, (uint32_t)p[0], (uint32_t)p[1], (uint32_t)p[2]);
         if (r == FL_INVALID_INDEX) continue;
         if ((int)shadow[i] >= (int)shadow[r] + 2) { viol[r] = 1; ++local; }
     }
@@ -153,9 +161,11 @@ __global__ void k_clear_u8(uint8_t* p, size_t n) {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) p[i] = 0;
 }
 
-// Sibling lookup for a first sibling; returns false if the octet is not mergeable.
-__device__ bool find_group(const KeyTables& T, const fl_mesh_dev& m, const fl_domain_dev& dom,
-                           const uint64_t* tk, const uint32_t* tv, int lg, size_t i, int min_level, uint32_t* mem) {
+// Sibling lookup for a first sibling; returns false if the octet is not
+// mergeable.  A sibling is the leaf holding its anchor point when that leaf has
+// the octet's level.
+__device__ bool find_group(const fl_probe& P, const fl_mesh_dev& m, const fl_domain_dev& dom, size_t i,
+                           int min_level, uint32_t* mem) {
     if (m.flags[i] != -1 || m.state[i] != 0) return false;
     if ((m.x[i] & 1) || (m.y[i] & 1) || (m.z[i] & 1)) return false;
     int l = m.level[i];
@@ -163,11 +173,10 @@ __device__ bool find_group(const KeyTables& T, const fl_mesh_dev& m, const fl_do
     uint16_t cs = m.case_id ? m.case_id[i] : 0;
     int sh = dom.anchor_level - l;
     for (int c = 0; c < 8; ++c) {
-        int64_t sx = m.x[i] | (c & 1), sy = m.y[i] | ((c >> 1) & 1), sz = m.z[i] | ((c >> 2) & 1);
-        uint64_t key = fl_anchor_key(T.t1, T.t3, dom.depth, cs, m.case_id != nullptr, sx << sh, sy << sh, sz << sh);
-        const uint32_t v = fl_hash_lookup(tk, tv, lg, key);
-        if (v == FL_INVALID_INDEX || fl_packed_level(v) != l) return false;
-        const uint32_t j = fl_packed_idx(v);
+        const uint32_t sx = (uint32_t)(m.x[i] | (c & 1)) << sh, sy = (uint32_t)(m.y[i] | ((c >> 1) & 1)) << sh,
+                       sz = (uint32_t)(m.z[i] | ((c >> 2) & 1)) << sh;
+        const uint32_t j = fl_probe_point(P, m.case_id != nullptr, cs, sx, sy, sz);
+        if (j == FL_INVALID_INDEX || m.level[j] != l) return false;
         if (m.flags[j] != -1 || m.state[j] != 0) return false;
         mem[c] = j;
     }
@@ -180,16 +189,15 @@ __device__ bool find_group(const KeyTables& T, const fl_mesh_dev& m, const fl_do
 // last of its lower cell, the first of its upper cell, the first point above
 // -- so the 98 combinations with at least one outside coordinate are exactly
 // the distinct probes outside the octet (the 27 others lie inside it).
-__device__ bool group_balanced(const KeyTables& T, const fl_mesh_dev& m, const fl_domain_dev& dom,
-                               const uint64_t* tk, const uint32_t* tv, int lg, const uint8_t* shadow,
-                               const uint32_t* mem) {
+__device__ bool group_balanced(const fl_probe& P, const fl_mesh_dev& m, const fl_domain_dev& dom,
+                               const uint8_t* shadow, const uint32_t* mem) {
     uint16_t cs = m.case_id ? m.case_id[mem[0]] : 0;
     const fl_domain_dev::Case& d = dom.c[m.case_id ? cs : 0];
     int l = m.level[mem[0]];
     int sh = dom.anchor_level - l;
-    int64_t size = (int64_t)1 << sh;
-    int64_t v[3][5];
-    const int64_t b[3] = {(int64_t)m.x[mem[0]] << sh, (int64_t)m.y[mem[0]] << sh, (int64_t)m.z[mem[0]] << sh};
+    int32_t size = 1 << sh;
+    int32_t v[3][5];
+    const int32_t b[3] = {m.x[mem[0]] << sh, m.y[mem[0]] << sh, m.z[mem[0]] << sh};
     for (int a = 0; a < 3; ++a) {
         v[a][0] = b[a] - 1;
         v[a][1] = b[a];
@@ -201,9 +209,9 @@ __device__ bool group_balanced(const KeyTables& T, const fl_mesh_dev& m, const f
         const int ix = k % 5, iy = (k / 5) % 5, iz = k / 25;
         const bool out = ix == 0 || ix == 4 || iy == 0 || iy == 4 || iz == 0 || iz == 4;
         if (!out) continue;
-        int64_t p[3] = {v[0][ix], v[1][iy], v[2][iz]};
-        if (!fold3(p, d, dom.anchor_level)) continue;
-        uint32_t r = fl_locate(T.t1, T.t3, tk, tv, lg, nullptr, dom, cs, m.case_id != nullptr, p, l);
+        int32_t p[3] = {v[0][ix], v[1][iy], v[2][iz]};
+        if (!fold3_32(p, d, dom.anchor_level)) continue;
+        uint32_t r = fl_probe_point(P, m.case_id != nullptr, cs, (uint32_t)p[0], (uint32_t)p[1], (uint32_t)p[2]);
         if (r == FL_INVALID_INDEX) continue;
         bool inside = false;  // only on a periodic axis of one octet's extent
         for (int q = 0; q < 8; ++q) inside |= (mem[q] == r);
@@ -212,34 +220,37 @@ __device__ bool group_balanced(const KeyTables& T, const fl_mesh_dev& m, const f
     return true;
 }
 
-__global__ void __launch_bounds__(kT) k_leaders(fl_mesh_dev m, fl_domain_dev dom, const uint64_t* __restrict__ tk,
-                                                const uint32_t* __restrict__ tv, int lg, int min_level, int check26,
-                                                const uint8_t* __restrict__ shadow, uint32_t* __restrict__ is_leader) {
-    __shared__ KeyTables T;
-    fl_keys_fill_tables(T.t1, T.t3, false);
+__global__ void __launch_bounds__(kT) k_leaders(fl_mesh_dev m, fl_domain_dev dom, fl_locator L, int min_level,
+                                                int check26, const uint8_t* __restrict__ shadow,
+                                                uint32_t* __restrict__ is_leader) {
+    __shared__ uint8_t t1[96];
+    __shared__ uint16_t t3c[12 * 512];
+    fl_keys_fill_tables_cat(t1, t3c);
     __syncthreads();
+    const fl_probe P = fl_probe_make(t1, t3c, L, dom);
     size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
         uint32_t mem[8];
-        bool ok = find_group(T, m, dom, tk, tv, lg, i, min_level, mem);
-        if (ok && check26) ok = group_balanced(T, m, dom, tk, tv, lg, shadow, mem);
+        bool ok = find_group(P, m, dom, i, min_level, mem);
+        if (ok && check26) ok = group_balanced(P, m, dom, shadow, mem);
         is_leader[i] = ok ? 1u : 0u;
     }
 }
 
-__global__ void __launch_bounds__(kT) k_members(fl_mesh_dev m, fl_domain_dev dom, const uint64_t* __restrict__ tk,
-                                                const uint32_t* __restrict__ tv, int lg, int min_level,
+__global__ void __launch_bounds__(kT) k_members(fl_mesh_dev m, fl_domain_dev dom, fl_locator L, int min_level,
                                                 const uint32_t* __restrict__ is_leader,
                                                 const uint32_t* __restrict__ gid, uint32_t* __restrict__ members,
                                                 uint32_t* __restrict__ group_of) {
-    __shared__ KeyTables T;
-    fl_keys_fill_tables(T.t1, T.t3, false);
+    __shared__ uint8_t t1[96];
+    __shared__ uint16_t t3c[12 * 512];
+    fl_keys_fill_tables_cat(t1, t3c);
     __syncthreads();
+    const fl_probe P = fl_probe_make(t1, t3c, L, dom);
     size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
         if (!is_leader[i]) continue;
         uint32_t mem[8];
-        find_group(T, m, dom, tk, tv, lg, i, min_level, mem);
+        find_group(P, m, dom, i, min_level, mem);
         uint32_t g = gid[i];
         for (int c = 0; c < 8; ++c) {
             members[(size_t)g * 8 + c] = mem[c];
@@ -437,14 +448,14 @@ size_t fl_adapt_scratch_bytes(size_t n, uint64_t cap) {
     b += fl_align256(n * 4);                 // members (n/8 groups * 8)
     b += fl_align256(64);                    // counters
     b += fl_align256(M * 4) * 5 + fl_align256(M) * 3 + fl_align256(M * 2) + fl_align256(M * 8) * 1;  // items
-    b += fl_scan_scratch_bytes(n) + fl_sort_scratch_bytes(M, 8) + 4096;
+    b += fl_scan_scratch_bytes(n) + fl_align256(fl_locator_scratch_bytes(n)) + fl_sort_scratch_bytes(M, 8) + 4096;
     return b;
 }
 
 // Balance over a mesh with an already-built table (shared by fl_balance_enforce and fl_adapt).
 int fl_balance_run(fl_ctx* ctx, fl_mesh_dev md, int32_t* flags, const fl_domain_dev& dom, const uint64_t* tk,
-                   const uint32_t* tv, uint64_t cap, int mode, int max_level, int max_iters, uint8_t* shadow,
-                   uint8_t* viol, uint32_t* counters, fl_balance_result* res) {
+                   const uint32_t* tv, uint64_t cap, const fl_locator* L, int mode, int max_level, int max_iters,
+                   uint8_t* shadow, uint8_t* viol, uint32_t* counters, fl_balance_result* res) {
     fl_balance_result r{};
     if (md.n == 0) { r.converged = 1; if (res) *res = r; return FL_OK; }
     unsigned nb = fl_blocks(md.n, kT, ctx->num_sms * 8);
@@ -460,8 +471,8 @@ int fl_balance_run(fl_ctx* ctx, fl_mesh_dev md, int32_t* flags, const fl_domain_
             k_detect_face6<<<nb, kT, 0, ctx->stream>>>(md, dom, tk, tv, lg, shadow, viol, counters);
         } else {
             k_clear_u8<<<nb, kT, 0, ctx->stream>>>(viol, md.n);
-            k_detect_full26<<<fl_blocks(md.n * 26, kT, ctx->num_sms * 8), kT, 0, ctx->stream>>>(md, dom, tk, tv, lg,
-                                                                                              shadow, viol, counters);
+            const unsigned pb = (unsigned)std::min<size_t>((md.n + 31) / 32, (size_t)ctx->num_sms * 2);
+            k_detect_full26<<<pb, kProbeThreads, 0, ctx->stream>>>(md, dom, *L, shadow, viol, counters);
         }
         FL_CHECK_LAUNCH(ctx, "k_detect");
         k_mark<<<nb, kT, 0, ctx->stream>>>(md, flags, viol, max_level, counters + 1);
@@ -489,6 +500,7 @@ struct AdaptWork {
     uint32_t* leader; uint32_t* gid; uint32_t* group_of; uint32_t* cnt; uint32_t* members; uint32_t* counters;
     fl_items it;
     void* scan_scratch; void* sort_scratch;
+    void* locator;  // fl_locator_build scratch
 };
 
 static AdaptWork carve_adapt(void* scratch, size_t n, bool with_case) {
@@ -515,6 +527,7 @@ static AdaptWork carve_adapt(void* scratch, size_t n, bool with_case) {
     w.it.material = cv.take<uint32_t>(Mcap);
     w.it.key = cv.take<uint64_t>(Mcap);
     w.scan_scratch = cv.take<char>(fl_scan_scratch_bytes(n));
+    w.locator = cv.take<char>(fl_locator_scratch_bytes(n));
     w.sort_scratch = cv.p;
     return w;
 }
@@ -542,31 +555,37 @@ int fl_adapt_prepare(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cf
     AdaptWork w = carve_adapt(scratch, n, mesh->case_id != nullptr);
     fl_mesh_dev md{mesh->x, mesh->y, mesh->z, mesh->level, mesh->state, mesh->flags, mesh->material,
                    mesh->case_id, n};
-    int rc = fl_launch_cell_keys(ctx, mesh->x, mesh->y, mesh->z, mesh->level, mesh->case_id, dom.depth,
+    // the sorted locator serves FULL26 detection and merge grouping; the
+    // FACE6 detection (shadow-level probes) keeps the hash table
+    fl_locator L;
+    int rc = fl_locator_build(ctx, md, dom, w.locator, &L);
+    if (rc) return rc;
+    if (run_balance && cfg->balance_mode == 0) {
+        rc = fl_launch_cell_keys(ctx, mesh->x, mesh->y, mesh->z, mesh->level, mesh->case_id, dom.depth,
                                  dom.anchor_level, w.keys, n);
-    if (rc) return rc;
-    rc = fl_hash_build_with(ctx, w.tk, w.tv, w.cap, w.keys, nullptr, n, w.win, mesh->level);  // level | index
-    if (rc) return rc;
+        if (rc) return rc;
+        rc = fl_hash_build_with(ctx, w.tk, w.tv, w.cap, w.keys, nullptr, n, w.win, mesh->level);  // level | index
+        if (rc) return rc;
+    }
     FL_TRY_CUDA(ctx, cudaMemsetAsync(w.counters, 0, 64, ctx->stream), "adapt counters");
     if (run_balance) {
-        rc = fl_balance_run(ctx, md, mesh->flags, dom, w.tk, w.tv, w.cap, cfg->balance_mode, cfg->max_refinement_level,
-                            (int)cfg->max_balance_iterations, w.shadow, w.viol, w.counters + 8, &s.balance);
+        rc = fl_balance_run(ctx, md, mesh->flags, dom, w.tk, w.tv, w.cap, &L, cfg->balance_mode,
+                            cfg->max_refinement_level, (int)cfg->max_balance_iterations, w.shadow, w.viol,
+                            w.counters + 8, &s.balance);
         if (rc) return rc;
     }
     unsigned nb = fl_blocks(n, kT, ctx->num_sms * 8);
-    int lg = fl_hash_lg(w.cap);
     k_shadow_update<<<nb, kT, 0, ctx->stream>>>(md, 1, cfg->max_refinement_level, w.shadow);  // final levels
     FL_CHECK_LAUNCH(ctx, "k_shadow_update");
     int check26 = cfg->enforce_2_1_balance && cfg->balance_mode == 1;
-    k_leaders<<<nb, kT, 0, ctx->stream>>>(md, dom, w.tk, w.tv, lg, cfg->min_refinement_level, check26, w.shadow,
-                                          w.leader);
+    k_leaders<<<nb, kT, 0, ctx->stream>>>(md, dom, L, cfg->min_refinement_level, check26, w.shadow, w.leader);
     FL_CHECK_LAUNCH(ctx, "k_leaders");
     rc = fl_scan_u32_with(ctx, w.leader, w.gid, n, w.counters + 2, w.scan_scratch);
     if (rc) return rc;
     rc = fl_launch_fill_u32(ctx, w.group_of, FL_INVALID_INDEX, n);
     if (rc) return rc;
-    k_members<<<nb, kT, 0, ctx->stream>>>(md, dom, w.tk, w.tv, lg, cfg->min_refinement_level, w.leader, w.gid,
-                                          w.members, w.group_of);
+    k_members<<<nb, kT, 0, ctx->stream>>>(md, dom, L, cfg->min_refinement_level, w.leader, w.gid, w.members,
+                                          w.group_of);
     FL_CHECK_LAUNCH(ctx, "k_members");
     k_counts<<<nb, kT, 0, ctx->stream>>>(md, cfg->max_refinement_level, w.leader, w.group_of, w.cnt);
     FL_CHECK_LAUNCH(ctx, "k_counts");
@@ -649,8 +668,10 @@ int fl_balance_enforce(fl_ctx* ctx, fl_mesh* mesh, const fl_adapt_config* cfg, f
     size_t n = mesh->num_cells;
     if (res) *res = fl_balance_result{};
     if (n == 0) { if (res) res->converged = 1; return FL_OK; }
-    uint64_t cap = fl_table_capacity(n);
-    size_t need = fl_align256(n * 8) + fl_align256(cap * 16) + fl_align256(cap * 4) + 2 * fl_align256(n) + 512 + 256;
+    const bool face6 = cfg->balance_mode == 0;  // FACE6 probes shadow levels through the hash table
+    uint64_t cap = face6 ? fl_table_capacity(n) : 0;
+    size_t need = fl_align256(n * 8) + fl_align256(cap * 16) + fl_align256(cap * 4) + 2 * fl_align256(n) + 512 + 256 +
+                  (face6 ? 0 : fl_locator_scratch_bytes(n));
     int rc = fl_scratch_reserve(ctx, need);
     if (rc) return rc;
     Carver cv{(char*)ctx->scratch};
@@ -663,14 +684,19 @@ int fl_balance_enforce(fl_ctx* ctx, fl_mesh* mesh, const fl_adapt_config* cfg, f
     uint8_t* viol = cv.take<uint8_t>(n);
     uint32_t* counters = cv.take<uint32_t>(16);
     fl_domain_dev dom = fl_domain_from_config(ctx, cfg, dcase);
-    rc = fl_launch_cell_keys(ctx, mesh->x, mesh->y, mesh->z, mesh->level, mesh->case_id, dom.depth, dom.anchor_level,
-                             keys, n);
-    if (rc) return rc;
-    rc = fl_hash_build_with(ctx, tk, tv, cap, keys, nullptr, n, win, mesh->level);
-    if (rc) return rc;
     fl_mesh_dev md{mesh->x, mesh->y, mesh->z, mesh->level, mesh->state, mesh->flags, mesh->material, mesh->case_id, n};
+    fl_locator L{};
+    if (face6) {
+        rc = fl_launch_cell_keys(ctx, mesh->x, mesh->y, mesh->z, mesh->level, mesh->case_id, dom.depth,
+                                 dom.anchor_level, keys, n);
+        if (rc) return rc;
+        rc = fl_hash_build_with(ctx, tk, tv, cap, keys, nullptr, n, win, mesh->level);
+    } else {
+        rc = fl_locator_build(ctx, md, dom, cv.p, &L);
+    }
+    if (rc) return rc;
     fl_balance_result r;
-    rc = fl_balance_run(ctx, md, mesh->flags, dom, tk, tv, cap, cfg->balance_mode, cfg->max_refinement_level,
+    rc = fl_balance_run(ctx, md, mesh->flags, dom, tk, tv, cap, &L, cfg->balance_mode, cfg->max_refinement_level,
                         (int)cfg->max_balance_iterations, shadow, viol, counters, &r);
     if (rc) return rc;
     rc = fl_collect_device_status(ctx, "fl_balance_enforce");
@@ -685,24 +711,17 @@ int fl_neighbour_rebuild(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config
         return fl_set_error(ctx, FL_E_INVALID_ARG, "key geometry: need anchor_level <= key_depth <= 21, max level <= anchor_level, ext << anchor_level <= 2^key_depth");
     size_t n = mesh->num_cells;
     if (n == 0) return FL_OK;
-    uint64_t cap = fl_table_capacity(n);
-    int rc = fl_scratch_reserve(ctx, 256 + fl_align256(n * 8) + fl_align256(cap * 16) + fl_align256(cap * 4) + 256);
+    int rc = fl_scratch_reserve(ctx, 256 + fl_locator_scratch_bytes(n));
     if (rc) return rc;
     Carver cv{(char*)ctx->scratch};
     void* dcase = cv.take<char>(256);
-    uint64_t* keys = cv.take<uint64_t>(n);
-    uint64_t* tk = cv.take<uint64_t>(2 * cap);
-    uint32_t* tv = nullptr;  // 16-byte slots
-    uint32_t* win = cv.take<uint32_t>(cap);
     fl_domain_dev dom = fl_domain_from_config(ctx, cfg, dcase);
     dom.max_level = cfg->max_refinement_level;
-    rc = fl_launch_cell_keys(ctx, mesh->x, mesh->y, mesh->z, mesh->level, mesh->case_id, dom.depth, dom.anchor_level,
-                             keys, n);
-    if (rc) return rc;
-    rc = fl_hash_build_with(ctx, tk, tv, cap, keys, nullptr, n, win, mesh->level);
-    if (rc) return rc;
     fl_mesh_dev md{mesh->x, mesh->y, mesh->z, mesh->level, mesh->state, mesh->flags, mesh->material, mesh->case_id, n};
-    rc = fl_neighbours_with(ctx, md, dom, tk, tv, cap, subslots, nbr);
+    fl_locator L;
+    rc = fl_locator_build(ctx, md, dom, cv.p, &L);
+    if (rc) return rc;
+    rc = fl_neighbours_sorted(ctx, md, dom, L, subslots, nbr);
     if (rc) return rc;
     return fl_collect_device_status(ctx, "fl_neighbour_rebuild");
 }
@@ -802,16 +821,12 @@ int fl_merge(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, const
     *num_parents = 0;
     size_t n = mesh->num_cells;
     if (n == 0) return FL_OK;
-    uint64_t cap = fl_table_capacity(n);
-    int rc = fl_scratch_reserve(ctx, 256 + fl_align256(n * 8) + fl_align256(cap * 16) + fl_align256(cap * 4) +
-                                         4 * fl_align256(n * 4) + fl_align256(n * 4 + 64) + fl_scan_scratch_bytes(n) + 512);
+    int rc = fl_scratch_reserve(ctx, 256 + fl_align256(fl_locator_scratch_bytes(n)) + 4 * fl_align256(n * 4) +
+                                         fl_align256(n * 4 + 64) + fl_scan_scratch_bytes(n) + 512);
     if (rc) return rc;
     Carver cv{(char*)ctx->scratch};
     void* dcase = cv.take<char>(256);
-    uint64_t* keys = cv.take<uint64_t>(n);
-    uint64_t* tk = cv.take<uint64_t>(2 * cap);
-    uint32_t* tv = nullptr;  // 16-byte slots
-    uint32_t* win = cv.take<uint32_t>(cap);
+    void* loc = cv.take<char>(fl_locator_scratch_bytes(n));
     uint32_t* leader = cv.take<uint32_t>(n);
     uint32_t* gid = cv.take<uint32_t>(n);
     uint32_t* group_of = merge_group_id ? merge_group_id : cv.take<uint32_t>(n);
@@ -819,22 +834,18 @@ int fl_merge(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, const
     uint32_t* total = cv.take<uint32_t>(4);
     void* ss = cv.p;
     fl_domain_dev dom = fl_domain_from_config(ctx, cfg, dcase);
-    dom.max_level = cfg->max_refinement_level > 0 ? cfg->max_refinement_level : dom.anchor_level;
     fl_mesh_dev md{mesh->x, mesh->y, mesh->z, mesh->level, mesh->state, mesh->flags, mesh->material, mesh->case_id, n};
-    rc = fl_launch_cell_keys(ctx, mesh->x, mesh->y, mesh->z, mesh->level, mesh->case_id, dom.depth, dom.anchor_level,
-                             keys, n);
-    if (rc) return rc;
-    rc = fl_hash_build_with(ctx, tk, tv, cap, keys, nullptr, n, win, mesh->level);
+    fl_locator L;
+    rc = fl_locator_build(ctx, md, dom, loc, &L);
     if (rc) return rc;
     unsigned nb = fl_blocks(n, kT, ctx->num_sms * 8);
-    int lg = fl_hash_lg(cap);
-    k_leaders<<<nb, kT, 0, ctx->stream>>>(md, dom, tk, tv, lg, cfg->min_refinement_level, 0, nullptr, leader);
+    k_leaders<<<nb, kT, 0, ctx->stream>>>(md, dom, L, cfg->min_refinement_level, 0, nullptr, leader);
     FL_CHECK_LAUNCH(ctx, "k_leaders");
     rc = fl_scan_u32_with(ctx, leader, gid, n, total, ss);
     if (rc) return rc;
     rc = fl_launch_fill_u32(ctx, group_of, FL_INVALID_INDEX, n);
     if (rc) return rc;
-    k_members<<<nb, kT, 0, ctx->stream>>>(md, dom, tk, tv, lg, cfg->min_refinement_level, leader, gid, members, group_of);
+    k_members<<<nb, kT, 0, ctx->stream>>>(md, dom, L, cfg->min_refinement_level, leader, gid, members, group_of);
     FL_CHECK_LAUNCH(ctx, "k_members");
     uint32_t G = 0;
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(&G, total, 4, cudaMemcpyDeviceToHost, ctx->stream), "merge count");

@@ -13,6 +13,7 @@
 #include "common.cuh"
 #include "hash.cuh"
 #include "keys.cuh"
+#include "scan.cuh"
 
 namespace {
 
@@ -75,56 +76,158 @@ __global__ void k_hash_query(const uint64_t* __restrict__ tk, const uint32_t* __
         out[i] = fl_hash_lookup(tk, tv, lg, q[i]);
 }
 
-__device__ __forceinline__ int fold_axis(int64_t* p, int64_t ext, int periodic) {
-    if (*p < 0 || *p >= ext) {
-        if (!periodic) return 0;
-        *p = ((*p % ext) + ext) % ext;
+// Run start of every leaf: its anchor's key with the low 3(A - l) bits
+// cleared (the case id above bit 3 * depth); ids[i] = i; flags[1] = the
+// deepest level.
+__global__ void __launch_bounds__(256) k_run_keys(fl_mesh_dev m, fl_domain_dev dom, uint64_t* __restrict__ keys,
+                                                  uint32_t* __restrict__ ids, uint32_t* __restrict__ flags) {
+    __shared__ uint8_t t1[96];
+    __shared__ uint16_t t3c[12 * 512];
+    fl_keys_fill_tables_cat(t1, t3c);
+    __syncthreads();
+    int deepest = 0;
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
+        const int sh = dom.anchor_level - m.level[i];
+        uint64_t k = fl_hilbert_encode_cat(t1, t3c, (uint32_t)m.x[i] << sh, (uint32_t)m.y[i] << sh,
+                                           (uint32_t)m.z[i] << sh, dom.depth);
+        k &= ~((1ull << (3 * sh)) - 1);
+        if (m.case_id) k |= (uint64_t)m.case_id[i] << (3 * dom.depth);
+        keys[i] = k;
+        ids[i] = (uint32_t)i;
+        deepest = max(deepest, (int)m.level[i]);
     }
-    return 1;
+    deepest = __reduce_max_sync(0xFFFFFFFFu, deepest);
+    if ((threadIdx.x & 31) == 0 && deepest > 0) atomicMax(flags + 1, (uint32_t)deepest);
 }
 
-// nbr[(i*26 + k)*S + s] = leaf containing the probe point of direction k,
-// sub-slot s; the point-location rule of balance_enforce.cl:107-143 (the cell
-// whose level is l and whose anchor is the point with the low (A - l) bits
-// cleared), probed outward from the cell's own level.
-__global__ void __launch_bounds__(256) k_neighbours(fl_mesh_dev m, fl_domain_dev dom, const uint64_t* __restrict__ tk,
-                                                    const uint32_t* __restrict__ tv, int lg, int S,
-                                                    uint32_t* __restrict__ nbr, uint32_t* dev_status) {
-    __shared__ uint8_t t1[96];
-    __shared__ uint16_t t3[12 * 512];
-    fl_keys_fill_tables(t1, t3, false);
-    __syncthreads();
-    size_t total = m.n * 26 * (size_t)S;
+// flag = 1 when some run start is smaller than the one before it.
+__global__ void k_check_sorted(const uint64_t* __restrict__ keys, size_t n, uint32_t* __restrict__ flag) {
     size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
-        size_t i = t / (26 * S);
-        int r = (int)(t - i * 26 * S);
-        int k = r / S, s = r - k * S;
-        uint16_t cs = m.case_id ? m.case_id[i] : 0;
+    bool bad = false;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x + 1; i < n; i += stride)
+        bad = bad || keys[i] < keys[i - 1];
+    if (__syncthreads_or(bad) && threadIdx.x == 0) *flag = 1u;
+}
+
+// dir[b] = first run whose bucket is >= b, b in [0, nb]: run i fills the
+// buckets after its predecessor's up to its own (run n stands for bucket nb).
+// A warp fills its 32 runs' ranges together, so a wide gap in the keys (between
+// cases, say) costs 1/32 of its length in one warp.
+__global__ void k_locator_dir(const uint64_t* __restrict__ keys, size_t n, int log2nb, uint32_t* __restrict__ dir) {
+    const uint64_t nb = 1ull << log2nb;
+    const uint64_t k0 = keys[0], span = keys[n - 1] - k0;
+    const int bits = span ? 64 - __clzll((long long)span) : 0;
+    const int shift = bits > log2nb ? bits - log2nb : 0;
+    const int lane = threadIdx.x & 31;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t base = (size_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base <= n; base += stride) {
+        const size_t i = base + lane;
+        uint64_t bl = 1, bh = 0;  // empty unless i <= n
+        if (i <= n) {
+            bh = i < n ? (keys[i] - k0) >> shift : nb;
+            bl = i > 0 ? ((keys[i - 1] - k0) >> shift) + 1 : 0;
+        }
+        for (int j = 0; j < 32; ++j) {
+            const uint64_t lo = __shfl_sync(0xFFFFFFFFu, bl, j), hi = __shfl_sync(0xFFFFFFFFu, bh, j);
+            for (uint64_t b = lo + lane; b <= hi; b += 32) dir[b] = (uint32_t)(base + j);
+        }
+    }
+}
+
+// Blocks of kProbeThreads: 32 / S cells x 26 directions x S sub-slots, so a
+// thread's direction and sub-slot are fixed and a cell's 26 * S probes sit in
+// consecutive threads (one coalesced row of nbr).
+
+template <int S>
+__global__ void __launch_bounds__(kProbeThreads, 2) k_neighbours_sorted(fl_mesh_dev m, fl_domain_dev dom,
+                                                                        fl_locator L, uint32_t* __restrict__ nbr) {
+    constexpr int kCells = 32 / S;
+    __shared__ uint8_t t1[96];
+    __shared__ uint16_t t3c[12 * 512];
+    fl_keys_fill_tables_cat(t1, t3c);
+    __syncthreads();
+    const fl_probe P = fl_probe_make(t1, t3c, L, dom);
+    const int cl = threadIdx.x / (26 * S);
+    const int r = threadIdx.x - cl * (26 * S);
+    const int k = r / S, s = r - k * S;
+    const int kk = k < 13 ? k : k + 1;
+    const int dv[3] = {kk % 3 - 1, (kk / 3) % 3 - 1, kk / 9 - 1};
+    for (size_t base = (size_t)blockIdx.x * kCells; base < m.n; base += (size_t)gridDim.x * kCells) {
+        const size_t i = base + cl;
+        if (i >= m.n) continue;
+        const uint16_t cs = m.case_id ? m.case_id[i] : 0;
         const fl_domain_dev::Case& d = dom.c[m.case_id ? cs : 0];
-        int lvl = m.level[i];
-        int sh = dom.anchor_level - lvl;
-        int64_t anc[3] = {(int64_t)m.x[i] << sh, (int64_t)m.y[i] << sh, (int64_t)m.z[i] << sh};
-        int64_t size = (int64_t)1 << sh;
-        int kk = k < 13 ? k : k + 1;
-        int dv[3] = {kk % 3 - 1, (kk / 3) % 3 - 1, kk / 9 - 1};
-        int64_t p[3];
+        const int sh = dom.anchor_level - m.level[i];
+        const int32_t anc[3] = {m.x[i] << sh, m.y[i] << sh, m.z[i] << sh};
+        const int32_t size = 1 << sh;
+        int32_t p[3];
         int bit = 0;
+        bool in = true;
         for (int a = 0; a < 3; ++a) {
             if (dv[a] < 0) p[a] = anc[a] - 1;
             else if (dv[a] > 0) p[a] = anc[a] + size;
             else { p[a] = anc[a] + (((s >> bit) & 1) ? (size >> 1) : 0); ++bit; }
+            in = in && fl_fold32(p[a], d.ext[a] << dom.anchor_level, d.periodic[a]);
         }
-        uint32_t res = FL_INVALID_INDEX;
-        bool in = true;
-        for (int a = 0; a < 3; ++a)
-            in = in && fold_axis(&p[a], (int64_t)d.ext[a] << dom.anchor_level, d.periodic[a]);
-        if (in) res = fl_locate(t1, t3, tk, tv, lg, nullptr, dom, cs, m.case_id != nullptr, p, lvl);
-        nbr[t] = res;
+        nbr[i * (26 * S) + r] =
+            in ? fl_probe_point(P, m.case_id != nullptr, cs, (uint32_t)p[0], (uint32_t)p[1], (uint32_t)p[2])
+               : FL_INVALID_INDEX;
     }
 }
 
+int locator_log2nb(size_t n) {
+    int lg = 0;
+    while ((1ull << lg) < n) ++lg;
+    return lg > 11 ? lg - 1 : 10;
+}
+
 }  // namespace
+
+size_t fl_locator_scratch_bytes(size_t n) {
+    const size_t nb = (size_t)1 << locator_log2nb(n);
+    return fl_align256(n * 8) + fl_align256(n * 4) + fl_align256((nb + 1) * 4) + 256 + fl_sort_scratch_bytes(n, 8);
+}
+
+int fl_locator_build(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom, void* scratch, fl_locator* L) {
+    const size_t n = m.n;
+    const int log2nb = locator_log2nb(n);
+    char* p = (char*)scratch;
+    uint64_t* keys = (uint64_t*)p; p += fl_align256(n * 8);
+    uint32_t* ids = (uint32_t*)p; p += fl_align256(n * 4);
+    uint32_t* dir = (uint32_t*)p; p += fl_align256((((size_t)1 << log2nb) + 1) * 4);
+    uint32_t* flag = (uint32_t*)p; p += 256;
+    *L = fl_locator{keys, nullptr, dir, m.level, n, log2nb, 0};
+    if (n == 0) return FL_OK;
+    FL_TRY_CUDA(ctx, cudaMemsetAsync(flag, 0, 8, ctx->stream), "locator");
+    k_run_keys<<<fl_blocks(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(m, dom, keys, ids, flag);
+    FL_CHECK_LAUNCH(ctx, "k_run_keys");
+    k_check_sorted<<<fl_blocks(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(keys, n, flag);
+    FL_CHECK_LAUNCH(ctx, "k_check_sorted");
+    uint32_t hf[2] = {0, 0};  // unsorted, deepest level
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(hf, flag, 8, cudaMemcpyDeviceToHost, ctx->stream), "locator");
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "locator");
+    L->cut = dom.anchor_level > (int)hf[1] ? dom.anchor_level - (int)hf[1] : 0;
+    if (hf[0]) {  // stable: equal run starts keep mesh order, so the last of them is found
+        int rc = fl_sort_pairs_with(ctx, keys, ids, n, 0, 64, p);
+        if (rc) return rc;
+        L->ids = ids;
+    }
+    k_locator_dir<<<fl_blocks(n + 1, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(keys, n, log2nb, dir);
+    FL_CHECK_LAUNCH(ctx, "k_locator_dir");
+    return FL_OK;
+}
+
+int fl_neighbours_sorted(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom, const fl_locator& L,
+                         int subslots, uint32_t* nbr) {
+    if (m.n == 0) return FL_OK;
+    const size_t cells = (size_t)(32 / subslots);
+    const unsigned grid = (unsigned)std::min<size_t>((m.n + cells - 1) / cells, (size_t)ctx->num_sms * 2);
+    if (subslots == 4) k_neighbours_sorted<4><<<grid, kProbeThreads, 0, ctx->stream>>>(m, dom, L, nbr);
+    else k_neighbours_sorted<1><<<grid, kProbeThreads, 0, ctx->stream>>>(m, dom, L, nbr);
+    FL_CHECK_LAUNCH(ctx, "k_neighbours_sorted");
+    return FL_OK;
+}
 
 int fl_hash_lg(uint64_t cap) {
     int lg = 0;
@@ -146,16 +249,6 @@ int fl_hash_build_with(fl_ctx* ctx, uint64_t* tk, uint32_t* tv, uint64_t cap, co
     FL_CHECK_LAUNCH(ctx, "k_hash_insert");
     k_hash_values<<<cb, 256, 0, ctx->stream>>>(tk, tv, win, vals, vals ? nullptr : levels, cap);
     FL_CHECK_LAUNCH(ctx, "k_hash_values");
-    return FL_OK;
-}
-
-int fl_neighbours_with(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom, const uint64_t* tk,
-                       const uint32_t* tv, uint64_t cap, int subslots, uint32_t* nbr) {
-    if (m.n == 0) return FL_OK;
-    size_t total = m.n * 26 * (size_t)subslots;
-    k_neighbours<<<fl_blocks(total, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(m, dom, tk, tv, fl_hash_lg(cap),
-                                                                                 subslots, nbr, ctx->dev_status);
-    FL_CHECK_LAUNCH(ctx, "k_neighbours");
     return FL_OK;
 }
 

@@ -109,6 +109,118 @@ static __device__ __forceinline__ uint32_t fl_locate(const uint8_t* t1, const ui
     return FL_INVALID_INDEX;
 }
 
+// Sorted point locator.  On the depth-D Hilbert curve a leaf of level l covers
+// one aligned run of 8^(A-l) finest keys, starting at its anchor's key with the
+// low 3(A-l) bits cleared; with the runs in ascending order, the leaf holding
+// a point is the predecessor of the point's key, if the key falls inside its
+// run.  A linear directory over the key span (bucket b starts at the first run
+// whose (start - k0) >> shift >= b) narrows the search to one bucket.
+// Consecutive threads probe neighbouring points, whose keys lie close
+// together, so the reads hit L1/L2 where a hash table scatters them.
+struct fl_locator {
+    const uint64_t* keys;  // ascending run starts (case id above bit 3 * depth)
+    const uint32_t* ids;   // cell of each run; nullptr: runs in mesh order
+    const uint32_t* dir;   // (1 << log2nb) + 1 bucket starts
+    const uint8_t* level;  // mesh levels by cell index
+    size_t n;
+    int log2nb;
+    int cut;               // anchor_level - the deepest leaf level: every run is >= 8^cut keys
+};
+
+struct fl_locator_base {
+    uint64_t k0;
+    int shift;
+};
+
+static __device__ __forceinline__ fl_locator_base fl_locator_base_of(const fl_locator& L) {
+    fl_locator_base B{0, 0};
+    if (L.n == 0) return B;
+    B.k0 = __ldg((const unsigned long long*)L.keys);
+    const uint64_t span = __ldg((const unsigned long long*)(L.keys + L.n - 1)) - B.k0;
+    const int bits = span ? 64 - __clzll((long long)span) : 0;
+    B.shift = bits > L.log2nb ? bits - L.log2nb : 0;
+    return B;
+}
+
+// The leaf whose run holds key q (a point's full-depth key with its case
+// bits), FL_INVALID_INDEX if none or if that leaf lies below max_level.
+static __device__ __forceinline__ uint32_t fl_locate_sorted(const fl_locator& L, const fl_locator_base& B,
+                                                            int anchor_level, int max_level, uint64_t q) {
+    if (L.n == 0 || q < B.k0) return FL_INVALID_INDEX;
+    const uint64_t nb = 1ull << L.log2nb;
+    uint64_t b = (q - B.k0) >> B.shift;
+    if (b >= nb) b = nb - 1;
+    const uint32_t lo = __ldg(L.dir + b), hi = __ldg(L.dir + b + 1);
+    uint32_t j;
+    if (lo >= hi || __ldg((const unsigned long long*)(L.keys + lo)) > q) {
+        if (lo == 0) return FL_INVALID_INDEX;
+        j = lo - 1;  // the last run of the buckets before b
+    } else {
+        uint32_t a = lo, c = hi;  // keys[a] <= q; the predecessor lies in [a, c)
+        while (c - a > 1) {
+            const uint32_t m = (a + c) >> 1;
+            if (__ldg((const unsigned long long*)(L.keys + m)) <= q) a = m;
+            else c = m;
+        }
+        j = a;
+    }
+    const uint32_t id = L.ids ? __ldg(L.ids + j) : j;
+    const int l = __ldg(L.level + id);
+    if (l > max_level) return FL_INVALID_INDEX;
+    const int sh = 3 * (anchor_level - l);
+    const uint64_t run = sh >= 64 ? ~0ull : (1ull << sh);
+    return q - __ldg((const unsigned long long*)(L.keys + j)) < run ? id : FL_INVALID_INDEX;
+}
+
+// Threads of a probe block: 32 cells x 26 directions.
+constexpr int kProbeThreads = 832;
+
+// Per-kernel state of sorted-locator probes (tables in shared memory).
+struct fl_probe {
+    const uint8_t* t1;
+    const uint16_t* t3c;
+    fl_locator L;
+    fl_locator_base B;
+    int depth, anchor_level, max_level;
+};
+
+static __device__ __forceinline__ fl_probe fl_probe_make(const uint8_t* t1, const uint16_t* t3c, const fl_locator& L,
+                                                         const fl_domain_dev& dom) {
+    fl_probe P{t1, t3c, L, fl_locator_base_of(L), dom.depth, dom.anchor_level, dom.max_level};
+    return P;
+}
+
+// The leaf holding point (px, py, pz) (anchor units, inside the case) of case
+// cs.  Runs start on multiples of 8^cut, so the key needs only the levels
+// above cut: the point shifted down by cut, encoded at depth - cut levels and
+// shifted back has the same predecessor as the full key.
+static __device__ __forceinline__ uint32_t fl_probe_point(const fl_probe& P, bool has_case, uint16_t cs, uint32_t px,
+                                                          uint32_t py, uint32_t pz) {
+    const int cut = P.L.cut;
+    uint64_t q = fl_hilbert_encode_cat(P.t1, P.t3c, px >> cut, py >> cut, pz >> cut, P.depth - cut) << (3 * cut);
+    if (has_case) q |= (uint64_t)cs << (3 * P.depth);
+    return fl_locate_sorted(P.L, P.B, P.anchor_level, P.max_level, q);
+}
+
+// A probe coordinate one cell or less outside [0, n): wrapped on a periodic
+// axis, false on a closed one.
+static __device__ __forceinline__ bool fl_fold32(int32_t& p, int32_t n, int periodic) {
+    if (p >= 0 && p < n) return true;
+    if (!periodic) return false;
+    while (p < 0) p += n;
+    while (p >= n) p -= n;
+    return true;
+}
+
+// Scratch of fl_locator_build for n cells.
+size_t fl_locator_scratch_bytes(size_t n);
+// Run starts of the mesh's leaves, sorted (with their cell ids) when the mesh
+// is not already in key order, and the bucket directory; L points into scratch.
+int fl_locator_build(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom, void* scratch, fl_locator* L);
+// nbr[(i*26 + k)*S + s] through the sorted locator.
+int fl_neighbours_sorted(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom, const fl_locator& L,
+                         int subslots, uint32_t* nbr);
+
 int fl_hash_lg(uint64_t cap);
 uint64_t fl_table_capacity(size_t n);
 // Clear + build; `win` is cap uint32 of scratch; tv == nullptr builds the
@@ -116,5 +228,3 @@ uint64_t fl_table_capacity(size_t n);
 // values are levels[i] << 27 | i (n < 2^27, else FL_E_CAPACITY).
 int fl_hash_build_with(fl_ctx* ctx, uint64_t* tk, uint32_t* tv, uint64_t cap, const uint64_t* keys,
                        const uint32_t* vals, size_t n, uint32_t* win, const uint8_t* levels = nullptr);
-int fl_neighbours_with(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom, const uint64_t* tk,
-                       const uint32_t* tv, uint64_t cap, int subslots, uint32_t* nbr);

@@ -38,6 +38,49 @@ static __device__ __forceinline__ void fl_keys_fill_tables(uint8_t* t1, uint16_t
     }
 }
 
+// The three-level encode table re-indexed by concatenated coordinate bits:
+// t3c[s*512 + (x3 << 6 | y3 << 3 | z3)] holds what t3 holds for the interleaved
+// input of the same three levels, so an encoder reads each 9-bit step straight
+// from the coordinates without interleaving them first.
+static __device__ __forceinline__ void fl_keys_fill_tables_cat(uint8_t* t1, uint16_t* t3c) {
+    for (int i = threadIdx.x; i < 96; i += blockDim.x) t1[i] = c_enc[i >> 3][i & 7];
+    for (int i = threadIdx.x; i < 12 * 512; i += blockDim.x) {
+        unsigned s = i >> 9, out = 0;
+        const unsigned x3 = (i >> 6) & 7u, y3 = (i >> 3) & 7u, z3 = i & 7u;
+        for (int k = 2; k >= 0; --k) {
+            unsigned q = (((z3 >> k) & 1u) << 2) | (((y3 >> k) & 1u) << 1) | ((x3 >> k) & 1u);
+            unsigned v = c_enc[s][q];
+            out = (out << 3) | (v & 7u);
+            s = v >> 3;
+        }
+        t3c[i] = (uint16_t)((s << 9) | out);
+    }
+}
+
+// hilbert::encode of the low `level` bits of x, y, z with the re-indexed table
+// (same keys as fl_hilbert_encode_dev).
+static __device__ __forceinline__ uint64_t fl_hilbert_encode_cat(const uint8_t* t1, const uint16_t* t3c, uint32_t x,
+                                                                 uint32_t y, uint32_t z, int level) {
+    uint64_t h = 0;
+    unsigned s = 0;
+    int i = level;
+    for (int k = 0; k < level % 3; ++k) {  // leading single levels
+        --i;
+        unsigned q = (((z >> i) & 1u) << 2) | (((y >> i) & 1u) << 1) | ((x >> i) & 1u);
+        unsigned v = t1[s * 8 + q];
+        h = (h << 3) | (v & 7u);
+        s = v >> 3;
+    }
+    while (i > 0) {
+        i -= 3;
+        unsigned c = (((x >> i) & 7u) << 6) | (((y >> i) & 7u) << 3) | ((z >> i) & 7u);
+        unsigned v = t3c[s * 512 + c];
+        h = (h << 9) | (v & 511u);
+        s = v >> 9;
+    }
+    return h;
+}
+
 // Interleave up to 21 bits of three coordinates: bit i of x -> 3i, y -> 3i+1, z -> 3i+2.
 static __device__ __forceinline__ uint64_t interleave3(uint32_t x, uint32_t y, uint32_t z) {
     auto sp = [](uint64_t v) {

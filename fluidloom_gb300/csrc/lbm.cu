@@ -1320,24 +1320,15 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
     size_t n = P->mesh.num_cells;
     if (P->cap >= (1u << 23))  // descriptors address elements as brick * 512 + site in 32 bits
         return fl_set_error(ctx, FL_E_CAPACITY, "a pool holds fewer than 2^23 bricks");
-    uint64_t cap = fl_table_capacity(n);
-    size_t need = fl_align256(n * 8) + fl_align256(cap * 16) + fl_align256(cap * 4) + 256;
-    int rc = fl_scratch_reserve(ctx, need);
+    int rc = fl_scratch_reserve(ctx, fl_locator_scratch_bytes(n));
     if (rc) return rc;
-    char* p = (char*)ctx->scratch;
-    uint64_t* keys = (uint64_t*)p; p += fl_align256(n * 8);
-    uint64_t* tk = (uint64_t*)p; p += fl_align256(cap * 16);
-    uint32_t* tv = nullptr;  // 16-byte slots
-    uint32_t* win = (uint32_t*)p;
     fl_domain_dev dom = pool_domain(P);
-    rc = fl_launch_cell_keys(ctx, P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.level, P->mesh.case_id, dom.depth,
-                             dom.anchor_level, keys, n);
-    if (rc) return rc;
-    rc = fl_hash_build_with(ctx, tk, tv, cap, keys, nullptr, n, win, P->mesh.level);
-    if (rc) return rc;
     fl_mesh_dev md{P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.level, P->mesh.state, P->mesh.flags, P->mesh.material,
                    P->mesh.case_id, n};
-    rc = fl_neighbours_with(ctx, md, dom, tk, tv, cap, 4, P->nbr);
+    fl_locator L;
+    rc = fl_locator_build(ctx, md, dom, ctx->scratch, &L);
+    if (rc) return rc;
+    rc = fl_neighbours_sorted(ctx, md, dom, L, 4, P->nbr);
     if (rc) return rc;
     const uint8_t* mnear = P->any_mask ? P->mnear : nullptr;
     if (mnear) {

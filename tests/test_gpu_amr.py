@@ -105,10 +105,15 @@ def test_balance_vs_oracle(ctx, mode):
         (wst.converged, wst.iterations, wst.violations, wst.marked)
 
 
+@pytest.mark.parametrize("order", ["key order", "shuffled"])
 @pytest.mark.parametrize("sub,periodic", [(1, (0, 0, 0)), (4, (0, 0, 0)), (4, (1, 0, 1))])
-def test_neighbours_vs_oracle(ctx, sub, periodic):
+def test_neighbours_vs_oracle(ctx, sub, periodic, order):
+    """The locator sorts the leaves' key runs itself when the mesh is not in key order."""
     from fluidloom_gb300 import DeviceArray
     cols = O.random_octree(20 + sub, ext=(2, 2, 2), rounds=3, max_level=5, frac=0.25, balanced=True)
+    if order == "shuffled":  # random_octree builds its leaves in key order
+        perm = np.random.default_rng(7).permutation(len(cols["x"]))
+        cols = {k: np.ascontiguousarray(v[perm]) for k, v in cols.items()}
     want = O.neighbours(cols, O.domain(ext=(2, 2, 2), max_level=5, periodic=periodic), sub)
     m = mesh(ctx, cols)
     nbr = DeviceArray(ctx, (len(cols["x"]) * 26 * sub,), np.uint32)
