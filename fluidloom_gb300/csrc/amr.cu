@@ -161,65 +161,38 @@ __global__ void k_clear_u8(uint8_t* p, size_t n) {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) p[i] = 0;
 }
 
-// Sibling lookup for a first sibling; returns false if the octet is not
-// mergeable.  A sibling is the leaf holding its anchor point when that leaf has
-// the octet's level.
-__device__ bool find_group(const fl_probe& P, const fl_mesh_dev& m, const fl_domain_dev& dom, size_t i,
-                           int min_level, uint32_t* mem) {
-    if (m.flags[i] != -1 || m.state[i] != 0) return false;
-    if ((m.x[i] & 1) || (m.y[i] & 1) || (m.z[i] & 1)) return false;
-    int l = m.level[i];
-    if (l <= min_level) return false;
-    uint16_t cs = m.case_id ? m.case_id[i] : 0;
-    int sh = dom.anchor_level - l;
-    for (int c = 0; c < 8; ++c) {
-        const uint32_t sx = (uint32_t)(m.x[i] | (c & 1)) << sh, sy = (uint32_t)(m.y[i] | ((c >> 1) & 1)) << sh,
-                       sz = (uint32_t)(m.z[i] | ((c >> 2) & 1)) << sh;
-        const uint32_t j = fl_probe_point(P, m.case_id != nullptr, cs, sx, sy, sz);
-        if (j == FL_INVALID_INDEX || m.level[j] != l) return false;
-        if (m.flags[j] != -1 || m.state[j] != 0) return false;
-        mem[c] = j;
-    }
-    return true;
+// A merge candidate: a FLUID first sibling (all coordinates even) flagged -1
+// above min_level.
+__device__ __forceinline__ bool merge_candidate(const fl_mesh_dev& m, size_t i, int min_level) {
+    return m.flags[i] == -1 && m.state[i] == 0 && !((m.x[i] | m.y[i] | m.z[i]) & 1) && m.level[i] > min_level;
 }
 
-// The FULL26 merge condition: no leaf touching the octet from outside ends
-// above its level.  The 8 members x 26 directions probe points take, per axis,
-// only five coordinates -- the last fine point below the octet, the first and
-// last of its lower cell, the first of its upper cell, the first point above
-// -- so the 98 combinations with at least one outside coordinate are exactly
-// the distinct probes outside the octet (the 27 others lie inside it).
-__device__ bool group_balanced(const fl_probe& P, const fl_mesh_dev& m, const fl_domain_dev& dom,
-                               const uint8_t* shadow, const uint32_t* mem) {
-    uint16_t cs = m.case_id ? m.case_id[mem[0]] : 0;
-    const fl_domain_dev::Case& d = dom.c[m.case_id ? cs : 0];
-    int l = m.level[mem[0]];
-    int sh = dom.anchor_level - l;
-    int32_t size = 1 << sh;
-    int32_t v[3][5];
-    const int32_t b[3] = {m.x[mem[0]] << sh, m.y[mem[0]] << sh, m.z[mem[0]] << sh};
-    for (int a = 0; a < 3; ++a) {
-        v[a][0] = b[a] - 1;
-        v[a][1] = b[a];
-        v[a][2] = b[a] + size - 1;
-        v[a][3] = b[a] + size;
-        v[a][4] = b[a] + 2 * size;
-    }
-    for (int k = 0; k < 125; ++k) {
-        const int ix = k % 5, iy = (k / 5) % 5, iz = k / 25;
-        const bool out = ix == 0 || ix == 4 || iy == 0 || iy == 4 || iz == 0 || iz == 4;
-        if (!out) continue;
-        int32_t p[3] = {v[0][ix], v[1][iy], v[2][iz]};
-        if (!fold3_32(p, d, dom.anchor_level)) continue;
-        uint32_t r = fl_probe_point(P, m.case_id != nullptr, cs, (uint32_t)p[0], (uint32_t)p[1], (uint32_t)p[2]);
-        if (r == FL_INVALID_INDEX) continue;
-        bool inside = false;  // only on a periodic axis of one octet's extent
-        for (int q = 0; q < 8; ++q) inside |= (mem[q] == r);
-        if (!inside && (int)shadow[r] > l) return false;
-    }
-    return true;
+// Lane c < 8 of a warp: sibling c of candidate i (the leaf holding its anchor
+// point, if that leaf has the octet's level), FL_INVALID_INDEX otherwise;
+// `ok` tells whether it is a mergeable member (flag -1, FLUID).
+__device__ __forceinline__ uint32_t sibling_of(const fl_probe& P, const fl_mesh_dev& m, const fl_domain_dev& dom,
+                                               size_t i, int c, bool* ok) {
+    const int l = m.level[i];
+    const uint16_t cs = m.case_id ? m.case_id[i] : 0;
+    const int sh = dom.anchor_level - l;
+    const uint32_t sx = (uint32_t)(m.x[i] | (c & 1)) << sh, sy = (uint32_t)(m.y[i] | ((c >> 1) & 1)) << sh,
+                   sz = (uint32_t)(m.z[i] | ((c >> 2) & 1)) << sh;
+    uint32_t j = fl_probe_point(P, m.case_id != nullptr, cs, sx, sy, sz);
+    if (j != FL_INVALID_INDEX && m.level[j] != l) j = FL_INVALID_INDEX;
+    *ok = j != FL_INVALID_INDEX && m.flags[j] == -1 && m.state[j] == 0;
+    return j;
 }
 
+// Leaders, one warp per candidate: 32 cells are screened a lane each, then
+// each candidate is checked by the whole warp -- lanes 0-7 locate its eight
+// siblings (all must be mergeable leaves of its level) and, for the FULL26
+// merge condition, the 98 probe points around the octet are spread over the
+// lanes: no leaf touching the octet from outside may end above its level.
+// The probe points take, per axis, only five coordinates -- the last fine
+// point below the octet, the first and last of its lower cell, the first of
+// its upper cell, the first point above -- so the 98 combinations with at
+// least one outside coordinate are exactly the distinct probes outside the
+// octet (the 27 others lie inside it).
 __global__ void __launch_bounds__(kT) k_leaders(fl_mesh_dev m, fl_domain_dev dom, fl_locator L, int min_level,
                                                 int check26, const uint8_t* __restrict__ shadow,
                                                 uint32_t* __restrict__ is_leader) {
@@ -228,16 +201,55 @@ __global__ void __launch_bounds__(kT) k_leaders(fl_mesh_dev m, fl_domain_dev dom
     fl_keys_fill_tables_cat(t1, t3c);
     __syncthreads();
     const fl_probe P = fl_probe_make(t1, t3c, L, dom);
-    size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
-        uint32_t mem[8];
-        bool ok = find_group(P, m, dom, i, min_level, mem);
-        if (ok && check26) ok = group_balanced(P, m, dom, shadow, mem);
-        is_leader[i] = ok ? 1u : 0u;
+    const int lane = threadIdx.x & 31;
+    const size_t warps = (size_t)gridDim.x * (blockDim.x >> 5);
+    for (size_t base = ((size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; base < m.n;
+         base += warps * 32) {
+        const size_t mine = base + lane;
+        const bool cand = mine < m.n && merge_candidate(m, mine, min_level);
+        if (mine < m.n && !cand) is_leader[mine] = 0u;
+        for (unsigned cm = __ballot_sync(0xFFFFFFFFu, cand); cm; cm &= cm - 1) {
+            const size_t i = base + (__ffs(cm) - 1);
+            bool ok = true;
+            uint32_t j = FL_INVALID_INDEX;
+            if (lane < 8) j = sibling_of(P, m, dom, i, lane, &ok);
+            bool leader = __all_sync(0xFFFFFFFFu, ok);
+            if (leader && check26) {
+                uint32_t mem[8];
+                for (int c = 0; c < 8; ++c) mem[c] = __shfl_sync(0xFFFFFFFFu, j, c);
+                const uint16_t cs = m.case_id ? m.case_id[i] : 0;
+                const fl_domain_dev::Case& d = dom.c[m.case_id ? cs : 0];
+                const int l = m.level[i];
+                const int sh = dom.anchor_level - l;
+                const int32_t size = 1 << sh;
+                const int32_t b[3] = {m.x[i] << sh, m.y[i] << sh, m.z[i] << sh};
+                bool bad = false;
+                for (int k = lane; k < 125; k += 32) {
+                    const int ix = k % 5, iy = (k / 5) % 5, iz = k / 25;
+                    if (!(ix == 0 || ix == 4 || iy == 0 || iy == 4 || iz == 0 || iz == 4)) continue;
+                    const int id[3] = {ix, iy, iz};
+                    int32_t p[3];
+                    for (int a = 0; a < 3; ++a) {
+                        const int t = id[a];
+                        p[a] = t == 0 ? b[a] - 1 : (t == 1 ? b[a] : (t == 2 ? b[a] + size - 1 : (t == 3 ? b[a] + size : b[a] + 2 * size)));
+                    }
+                    if (!fold3_32(p, d, dom.anchor_level)) continue;
+                    const uint32_t r =
+                        fl_probe_point(P, m.case_id != nullptr, cs, (uint32_t)p[0], (uint32_t)p[1], (uint32_t)p[2]);
+                    if (r == FL_INVALID_INDEX) continue;
+                    bool inside = false;  // only on a periodic axis of one octet's extent
+                    for (int q = 0; q < 8; ++q) inside |= (mem[q] == r);
+                    if (!inside && (int)shadow[r] > l) bad = true;
+                }
+                leader = !__any_sync(0xFFFFFFFFu, bad);
+            }
+            if (lane == 0) is_leader[i] = leader ? 1u : 0u;
+        }
     }
 }
 
-__global__ void __launch_bounds__(kT) k_members(fl_mesh_dev m, fl_domain_dev dom, fl_locator L, int min_level,
+// Members of each leader's group, one warp per leader (lane c < 8: sibling c).
+__global__ void __launch_bounds__(kT) k_members(fl_mesh_dev m, fl_domain_dev dom, fl_locator L,
                                                 const uint32_t* __restrict__ is_leader,
                                                 const uint32_t* __restrict__ gid, uint32_t* __restrict__ members,
                                                 uint32_t* __restrict__ group_of) {
@@ -246,15 +258,21 @@ __global__ void __launch_bounds__(kT) k_members(fl_mesh_dev m, fl_domain_dev dom
     fl_keys_fill_tables_cat(t1, t3c);
     __syncthreads();
     const fl_probe P = fl_probe_make(t1, t3c, L, dom);
-    size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
-        if (!is_leader[i]) continue;
-        uint32_t mem[8];
-        find_group(P, m, dom, i, min_level, mem);
-        uint32_t g = gid[i];
-        for (int c = 0; c < 8; ++c) {
-            members[(size_t)g * 8 + c] = mem[c];
-            group_of[mem[c]] = g;
+    const int lane = threadIdx.x & 31;
+    const size_t warps = (size_t)gridDim.x * (blockDim.x >> 5);
+    for (size_t base = ((size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; base < m.n;
+         base += warps * 32) {
+        const size_t mine = base + lane;
+        const bool lead = mine < m.n && is_leader[mine];
+        for (unsigned cm = __ballot_sync(0xFFFFFFFFu, lead); cm; cm &= cm - 1) {
+            const size_t i = base + (__ffs(cm) - 1);
+            if (lane < 8) {
+                bool ok;
+                const uint32_t j = sibling_of(P, m, dom, i, lane, &ok);
+                const uint32_t g = gid[i];
+                members[(size_t)g * 8 + lane] = j;
+                group_of[j] = g;
+            }
         }
     }
 }
@@ -578,14 +596,14 @@ int fl_adapt_prepare(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cf
     k_shadow_update<<<nb, kT, 0, ctx->stream>>>(md, 1, cfg->max_refinement_level, w.shadow);  // final levels
     FL_CHECK_LAUNCH(ctx, "k_shadow_update");
     int check26 = cfg->enforce_2_1_balance && cfg->balance_mode == 1;
-    k_leaders<<<nb, kT, 0, ctx->stream>>>(md, dom, L, cfg->min_refinement_level, check26, w.shadow, w.leader);
+    const unsigned wb = fl_blocks((n + 31) / 32 * 32, kT, ctx->num_sms * 8);  // a warp per 32 cells
+    k_leaders<<<wb, kT, 0, ctx->stream>>>(md, dom, L, cfg->min_refinement_level, check26, w.shadow, w.leader);
     FL_CHECK_LAUNCH(ctx, "k_leaders");
     rc = fl_scan_u32_with(ctx, w.leader, w.gid, n, w.counters + 2, w.scan_scratch);
     if (rc) return rc;
     rc = fl_launch_fill_u32(ctx, w.group_of, FL_INVALID_INDEX, n);
     if (rc) return rc;
-    k_members<<<nb, kT, 0, ctx->stream>>>(md, dom, L, cfg->min_refinement_level, w.leader, w.gid, w.members,
-                                          w.group_of);
+    k_members<<<wb, kT, 0, ctx->stream>>>(md, dom, L, w.leader, w.gid, w.members, w.group_of);
     FL_CHECK_LAUNCH(ctx, "k_members");
     k_counts<<<nb, kT, 0, ctx->stream>>>(md, cfg->max_refinement_level, w.leader, w.group_of, w.cnt);
     FL_CHECK_LAUNCH(ctx, "k_counts");
@@ -838,14 +856,14 @@ int fl_merge(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, const
     fl_locator L;
     rc = fl_locator_build(ctx, md, dom, loc, &L);
     if (rc) return rc;
-    unsigned nb = fl_blocks(n, kT, ctx->num_sms * 8);
-    k_leaders<<<nb, kT, 0, ctx->stream>>>(md, dom, L, cfg->min_refinement_level, 0, nullptr, leader);
+    const unsigned wb = fl_blocks((n + 31) / 32 * 32, kT, ctx->num_sms * 8);  // a warp per 32 cells
+    k_leaders<<<wb, kT, 0, ctx->stream>>>(md, dom, L, cfg->min_refinement_level, 0, nullptr, leader);
     FL_CHECK_LAUNCH(ctx, "k_leaders");
     rc = fl_scan_u32_with(ctx, leader, gid, n, total, ss);
     if (rc) return rc;
     rc = fl_launch_fill_u32(ctx, group_of, FL_INVALID_INDEX, n);
     if (rc) return rc;
-    k_members<<<nb, kT, 0, ctx->stream>>>(md, dom, L, cfg->min_refinement_level, leader, gid, members, group_of);
+    k_members<<<wb, kT, 0, ctx->stream>>>(md, dom, L, leader, gid, members, group_of);
     FL_CHECK_LAUNCH(ctx, "k_members");
     uint32_t G = 0;
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(&G, total, 4, cudaMemcpyDeviceToHost, ctx->stream), "merge count");

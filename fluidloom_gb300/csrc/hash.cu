@@ -112,8 +112,8 @@ __global__ void k_check_sorted(const uint64_t* __restrict__ keys, size_t n, uint
 
 // dir[b] = first run whose bucket is >= b, b in [0, nb]: run i fills the
 // buckets after its predecessor's up to its own (run n stands for bucket nb).
-// A warp fills its 32 runs' ranges together, so a wide gap in the keys (between
-// cases, say) costs 1/32 of its length in one warp.
+// A wide range (a gap in the keys, between cases say) is filled by the whole
+// warp, so it costs 1/32 of its length.
 __global__ void k_locator_dir(const uint64_t* __restrict__ keys, size_t n, int log2nb, uint32_t* __restrict__ dir) {
     const uint64_t nb = 1ull << log2nb;
     const uint64_t k0 = keys[0], span = keys[n - 1] - k0;
@@ -128,7 +128,13 @@ __global__ void k_locator_dir(const uint64_t* __restrict__ keys, size_t n, int l
             bh = i < n ? (keys[i] - k0) >> shift : nb;
             bl = i > 0 ? ((keys[i - 1] - k0) >> shift) + 1 : 0;
         }
-        for (int j = 0; j < 32; ++j) {
+        // short ranges (the common case: one or two buckets) by their own lane,
+        // coalesced across the warp; long ones by the whole warp
+        const bool wide = bl <= bh && bh - bl >= 4;
+        if (!wide)
+            for (uint64_t b = bl; b <= bh; ++b) dir[b] = (uint32_t)i;
+        for (unsigned w = __ballot_sync(0xFFFFFFFFu, wide); w; w &= w - 1) {
+            const int j = __ffs(w) - 1;
             const uint64_t lo = __shfl_sync(0xFFFFFFFFu, bl, j), hi = __shfl_sync(0xFFFFFFFFu, bh, j);
             for (uint64_t b = lo + lane; b <= hi; b += 32) dir[b] = (uint32_t)(base + j);
         }
