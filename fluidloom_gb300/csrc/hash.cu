@@ -76,29 +76,36 @@ __global__ void k_hash_query(const uint64_t* __restrict__ tk, const uint32_t* __
         out[i] = fl_hash_lookup(tk, tv, lg, q[i]);
 }
 
-// Run start of every leaf: its anchor's key with the low 3(A - l) bits
-// cleared (the case id above bit 3 * depth); ids[i] = i; flags[1] = the
-// deepest level.
-__global__ void __launch_bounds__(256) k_run_keys(fl_mesh_dev m, fl_domain_dev dom, uint64_t* __restrict__ keys,
-                                                  uint32_t* __restrict__ ids, uint32_t* __restrict__ flags) {
+// flags[1] = the deepest leaf level.
+__global__ void k_deepest(const uint8_t* __restrict__ level, size_t n, uint32_t* __restrict__ flags) {
+    int deepest = 0;
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        deepest = max(deepest, (int)level[i]);
+    deepest = __reduce_max_sync(0xFFFFFFFFu, deepest);
+    if ((threadIdx.x & 31) == 0 && deepest > 0) atomicMax(flags + 1, (uint32_t)deepest);
+}
+
+// Run start of every leaf divided by 8^cut: the anchor shifted down by cut,
+// encoded at depth - cut levels, the low 3(A - l - cut) bits cleared (the case
+// id above bit 3 * (depth - cut)); ids[i] = i.
+__global__ void __launch_bounds__(256) k_run_keys(fl_mesh_dev m, fl_domain_dev dom, int cut,
+                                                  uint64_t* __restrict__ keys, uint32_t* __restrict__ ids) {
     __shared__ uint8_t t1[96];
     __shared__ uint16_t t3c[12 * 512];
     fl_keys_fill_tables_cat(t1, t3c);
     __syncthreads();
-    int deepest = 0;
+    const int dc = dom.depth - cut;
     size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
         const int sh = dom.anchor_level - m.level[i];
-        uint64_t k = fl_hilbert_encode_cat(t1, t3c, (uint32_t)m.x[i] << sh, (uint32_t)m.y[i] << sh,
-                                           (uint32_t)m.z[i] << sh, dom.depth);
-        k &= ~((1ull << (3 * sh)) - 1);
-        if (m.case_id) k |= (uint64_t)m.case_id[i] << (3 * dom.depth);
+        uint64_t k = fl_hilbert_encode_cat(t1, t3c, ((uint32_t)m.x[i] << sh) >> cut, ((uint32_t)m.y[i] << sh) >> cut,
+                                           ((uint32_t)m.z[i] << sh) >> cut, dc);
+        k &= ~((1ull << (3 * (sh - cut))) - 1);
+        if (m.case_id) k |= (uint64_t)m.case_id[i] << (3 * dc);
         keys[i] = k;
         ids[i] = (uint32_t)i;
-        deepest = max(deepest, (int)m.level[i]);
     }
-    deepest = __reduce_max_sync(0xFFFFFFFFu, deepest);
-    if ((threadIdx.x & 31) == 0 && deepest > 0) atomicMax(flags + 1, (uint32_t)deepest);
 }
 
 // flag = 1 when some run start is smaller than the one before it.
@@ -206,14 +213,18 @@ int fl_locator_build(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom
     *L = fl_locator{keys, nullptr, dir, m.level, n, log2nb, 0};
     if (n == 0) return FL_OK;
     FL_TRY_CUDA(ctx, cudaMemsetAsync(flag, 0, 8, ctx->stream), "locator");
-    k_run_keys<<<fl_blocks(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(m, dom, keys, ids, flag);
-    FL_CHECK_LAUNCH(ctx, "k_run_keys");
-    k_check_sorted<<<fl_blocks(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(keys, n, flag);
-    FL_CHECK_LAUNCH(ctx, "k_check_sorted");
+    k_deepest<<<fl_blocks(n, 256, ctx->num_sms * 4), 256, 0, ctx->stream>>>(m.level, n, flag);
+    FL_CHECK_LAUNCH(ctx, "k_deepest");
     uint32_t hf[2] = {0, 0};  // unsorted, deepest level
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(hf, flag, 8, cudaMemcpyDeviceToHost, ctx->stream), "locator");
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "locator");
     L->cut = dom.anchor_level > (int)hf[1] ? dom.anchor_level - (int)hf[1] : 0;
+    k_run_keys<<<fl_blocks(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(m, dom, L->cut, keys, ids);
+    FL_CHECK_LAUNCH(ctx, "k_run_keys");
+    k_check_sorted<<<fl_blocks(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(keys, n, flag);
+    FL_CHECK_LAUNCH(ctx, "k_check_sorted");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(hf, flag, 4, cudaMemcpyDeviceToHost, ctx->stream), "locator");
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "locator");
     if (hf[0]) {  // stable: equal run starts keep mesh order, so the last of them is found
         int rc = fl_sort_pairs_with(ctx, keys, ids, n, 0, 64, p);
         if (rc) return rc;

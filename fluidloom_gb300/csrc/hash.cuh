@@ -113,18 +113,21 @@ static __device__ __forceinline__ uint32_t fl_locate(const uint8_t* t1, const ui
 // one aligned run of 8^(A-l) finest keys, starting at its anchor's key with the
 // low 3(A-l) bits cleared; with the runs in ascending order, the leaf holding
 // a point is the predecessor of the point's key, if the key falls inside its
-// run.  A linear directory over the key span (bucket b starts at the first run
-// whose (start - k0) >> shift >= b) narrows the search to one bucket.
-// Consecutive threads probe neighbouring points, whose keys lie close
-// together, so the reads hit L1/L2 where a hash table scatters them.
+// run.  Every run starts on a multiple of 8^cut (cut = A - the deepest leaf
+// level), so keys are kept divided by 8^cut: the key of a point is then the
+// encoding of the point shifted down by cut at depth - cut levels.  A linear
+// directory over the key span (bucket b starts at the first run whose
+// (start - k0) >> shift >= b) narrows the search to one bucket.  Consecutive
+// threads probe neighbouring points, whose keys lie close together, so the
+// reads hit L1/L2 where a hash table scatters them.
 struct fl_locator {
-    const uint64_t* keys;  // ascending run starts (case id above bit 3 * depth)
+    const uint64_t* keys;  // ascending run starts / 8^cut, case id above bit 3 * (depth - cut)
     const uint32_t* ids;   // cell of each run; nullptr: runs in mesh order
     const uint32_t* dir;   // (1 << log2nb) + 1 bucket starts
     const uint8_t* level;  // mesh levels by cell index
     size_t n;
     int log2nb;
-    int cut;               // anchor_level - the deepest leaf level: every run is >= 8^cut keys
+    int cut;               // anchor_level - the deepest leaf level
 };
 
 struct fl_locator_base {
@@ -142,24 +145,28 @@ static __device__ __forceinline__ fl_locator_base fl_locator_base_of(const fl_lo
     return B;
 }
 
-// The leaf whose run holds key q (a point's full-depth key with its case
-// bits), FL_INVALID_INDEX if none or if that leaf lies below max_level.
-static __device__ __forceinline__ uint32_t fl_locate_sorted(const fl_locator& L, const fl_locator_base& B,
-                                                            int anchor_level, int max_level, uint64_t q) {
+// The leaf whose run holds key q (a point's key as above, with its case
+// bits), FL_INVALID_INDEX if none or if that leaf lies below max_level; top =
+// anchor_level - cut.
+static __device__ __forceinline__ uint32_t fl_locate_sorted(const fl_locator& L, const fl_locator_base& B, int top,
+                                                            int max_level, uint64_t q) {
     if (L.n == 0 || q < B.k0) return FL_INVALID_INDEX;
     const uint64_t nb = 1ull << L.log2nb;
     uint64_t b = (q - B.k0) >> B.shift;
     if (b >= nb) b = nb - 1;
     const uint32_t lo = __ldg(L.dir + b), hi = __ldg(L.dir + b + 1);
     uint32_t j;
-    if (lo >= hi || __ldg((const unsigned long long*)(L.keys + lo)) > q) {
+    uint64_t kj = lo < hi ? __ldg((const unsigned long long*)(L.keys + lo)) : ~0ull;
+    if (kj > q) {
         if (lo == 0) return FL_INVALID_INDEX;
         j = lo - 1;  // the last run of the buckets before b
+        kj = __ldg((const unsigned long long*)(L.keys + j));
     } else {
-        uint32_t a = lo, c = hi;  // keys[a] <= q; the predecessor lies in [a, c)
+        uint32_t a = lo, c = hi;  // keys[a] = kj <= q; the predecessor lies in [a, c)
         while (c - a > 1) {
             const uint32_t m = (a + c) >> 1;
-            if (__ldg((const unsigned long long*)(L.keys + m)) <= q) a = m;
+            const uint64_t km = __ldg((const unsigned long long*)(L.keys + m));
+            if (km <= q) { a = m; kj = km; }
             else c = m;
         }
         j = a;
@@ -167,9 +174,9 @@ static __device__ __forceinline__ uint32_t fl_locate_sorted(const fl_locator& L,
     const uint32_t id = L.ids ? __ldg(L.ids + j) : j;
     const int l = __ldg(L.level + id);
     if (l > max_level) return FL_INVALID_INDEX;
-    const int sh = 3 * (anchor_level - l);
+    const int sh = 3 * (top - l);
     const uint64_t run = sh >= 64 ? ~0ull : (1ull << sh);
-    return q - __ldg((const unsigned long long*)(L.keys + j)) < run ? id : FL_INVALID_INDEX;
+    return q - kj < run ? id : FL_INVALID_INDEX;
 }
 
 // Threads of a probe block: 32 cells x 26 directions.
@@ -181,25 +188,22 @@ struct fl_probe {
     const uint16_t* t3c;
     fl_locator L;
     fl_locator_base B;
-    int depth, anchor_level, max_level;
+    int cut, depth_cut, top, max_level;  // L.cut, depth - cut, anchor_level - cut
 };
 
 static __device__ __forceinline__ fl_probe fl_probe_make(const uint8_t* t1, const uint16_t* t3c, const fl_locator& L,
                                                          const fl_domain_dev& dom) {
-    fl_probe P{t1, t3c, L, fl_locator_base_of(L), dom.depth, dom.anchor_level, dom.max_level};
+    fl_probe P{t1, t3c, L, fl_locator_base_of(L), L.cut, dom.depth - L.cut, dom.anchor_level - L.cut,
+               dom.max_level};
     return P;
 }
 
-// The leaf holding point (px, py, pz) (anchor units, inside the case) of case
-// cs.  Runs start on multiples of 8^cut, so the key needs only the levels
-// above cut: the point shifted down by cut, encoded at depth - cut levels and
-// shifted back has the same predecessor as the full key.
+// The leaf holding point (px, py, pz) (anchor units, inside the case) of case cs.
 static __device__ __forceinline__ uint32_t fl_probe_point(const fl_probe& P, bool has_case, uint16_t cs, uint32_t px,
                                                           uint32_t py, uint32_t pz) {
-    const int cut = P.L.cut;
-    uint64_t q = fl_hilbert_encode_cat(P.t1, P.t3c, px >> cut, py >> cut, pz >> cut, P.depth - cut) << (3 * cut);
-    if (has_case) q |= (uint64_t)cs << (3 * P.depth);
-    return fl_locate_sorted(P.L, P.B, P.anchor_level, P.max_level, q);
+    uint64_t q = fl_hilbert_encode_cat(P.t1, P.t3c, px >> P.cut, py >> P.cut, pz >> P.cut, P.depth_cut);
+    if (has_case) q |= (uint64_t)cs << (3 * P.depth_cut);
+    return fl_locate_sorted(P.L, P.B, P.top, P.max_level, q);
 }
 
 // A probe coordinate one cell or less outside [0, n): wrapped on a periodic
