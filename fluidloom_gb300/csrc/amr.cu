@@ -277,46 +277,56 @@ __global__ void __launch_bounds__(kT) k_members(fl_mesh_dev m, fl_domain_dev dom
     }
 }
 
-// Output count per old cell.
-__global__ void k_counts(fl_mesh_dev m, int max_level, const uint32_t* __restrict__ is_leader,
-                         const uint32_t* __restrict__ group_of, uint32_t* __restrict__ cnt) {
+// Output count per old cell, in visiting order (order[t] = the cell visited
+// t-th, or t when order is null).
+__global__ void k_counts(fl_mesh_dev m, int max_level, const uint32_t* __restrict__ order,
+                         const uint32_t* __restrict__ is_leader, const uint32_t* __restrict__ group_of,
+                         uint32_t* __restrict__ cnt) {
     size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < m.n; t += stride) {
+        const size_t i = order ? order[t] : t;
         bool split = m.flags[i] > 0 && m.state[i] == 0 && m.level[i] < max_level;
         uint32_t c;
         if (split) c = 8;
         else if (group_of[i] != FL_INVALID_INDEX) c = is_leader[i] ? 1u : 0u;
         else c = 1;
-        cnt[i] = c;
+        cnt[t] = c;
     }
 }
 
-// Intermediate items in old-index order + their keys.
+// The new cells in key order, with no sort: the old cells are visited in key
+// order (the locator's order) and every new cell lies inside the run of the
+// old cell that makes it -- a survivor in its own run, the children of a split
+// cell in its run, placed by their Hilbert digit under the cell's curve state,
+// a merged group's parent at its leader's place (the eight members' runs are
+// consecutive and the other seven emit nothing).
 __global__ void __launch_bounds__(kT) k_emit(fl_mesh_dev m, fl_domain_dev dom, int max_level,
-                                             const uint32_t* __restrict__ off, const uint32_t* __restrict__ is_leader,
+                                             const uint32_t* __restrict__ order, const uint32_t* __restrict__ off,
+                                             const uint32_t* __restrict__ is_leader,
                                              const uint32_t* __restrict__ group_of, fl_items it) {
-    __shared__ KeyTables T;
-    fl_keys_fill_tables(T.t1, T.t3, false);
+    __shared__ uint8_t t1[96];
+    __shared__ uint16_t t3c[12 * 512];
+    fl_keys_fill_tables_cat(t1, t3c);
     __syncthreads();
     size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < m.n; t += stride) {
+        const size_t i = order ? order[t] : t;
         uint16_t cs = m.case_id ? m.case_id[i] : 0;
         bool split = m.flags[i] > 0 && m.state[i] == 0 && m.level[i] < max_level;
-        uint32_t o = off[i];
+        uint32_t o = off[t];
         auto put = [&](uint32_t j, int32_t x, int32_t y, int32_t z, uint8_t l, uint32_t src, uint8_t kind) {
             it.x[j] = x; it.y[j] = y; it.z[j] = z; it.level[j] = l;
             it.state[j] = m.state[i]; it.material[j] = m.material[i];
             if (it.case_id) it.case_id[j] = cs;
             it.src[j] = src; it.kind[j] = kind;
-            int sh = dom.anchor_level - l;
-            it.key[j] = fl_anchor_key(T.t1, T.t3, dom.depth, cs, m.case_id != nullptr, (int64_t)x << sh,
-                                      (int64_t)y << sh, (int64_t)z << sh);
-            it.pos[j] = j;
         };
         if (split) {
+            const int l = m.level[i];
+            const unsigned st = fl_hilbert_state_cat(t1, t3c, (uint32_t)m.x[i], (uint32_t)m.y[i], (uint32_t)m.z[i],
+                                                     dom.depth - dom.anchor_level + l);
             for (int c = 0; c < 8; ++c)
-                put(o + c, (m.x[i] << 1) | (c & 1), (m.y[i] << 1) | ((c >> 1) & 1), (m.z[i] << 1) | ((c >> 2) & 1),
-                    (uint8_t)(m.level[i] + 1), (uint32_t)i, (uint8_t)c);
+                put(o + (t1[st * 8 + c] & 7u), (m.x[i] << 1) | (c & 1), (m.y[i] << 1) | ((c >> 1) & 1),
+                    (m.z[i] << 1) | ((c >> 2) & 1), (uint8_t)(l + 1), (uint32_t)i, (uint8_t)c);
         } else if (group_of[i] != FL_INVALID_INDEX) {
             if (is_leader[i])
                 put(o, m.x[i] >> 1, m.y[i] >> 1, m.z[i] >> 1, (uint8_t)(m.level[i] - 1), group_of[i], 9);
@@ -328,12 +338,12 @@ __global__ void __launch_bounds__(kT) k_emit(fl_mesh_dev m, fl_domain_dev dom, i
 
 // Final gather in key order; fields AoS (C per cell) with the reference's
 // prolongation (copy) and restriction (ordered sum, x0.125 for rule 0).
-__global__ void k_gather(fl_items it, const uint32_t* __restrict__ perm, size_t M, fl_mesh_out out,
+__global__ void k_gather(fl_items it, size_t M, fl_mesh_out out,
                          const float* __restrict__ fin, float* __restrict__ fout, uint32_t C, int rule,
                          const uint32_t* __restrict__ members, uint32_t* __restrict__ osrc, uint8_t* __restrict__ okind) {
     size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < M; j += stride) {
-        uint32_t p = perm[j];
+        const size_t p = j;
         out.x[j] = it.x[p]; out.y[j] = it.y[p]; out.z[j] = it.z[p];
         out.level[j] = it.level[p]; out.state[j] = it.state[p]; out.material[j] = it.material[p];
         out.flags[j] = 0;
@@ -465,8 +475,8 @@ size_t fl_adapt_scratch_bytes(size_t n, uint64_t cap) {
     b += 4 * fl_align256(n * 4);             // leader, gid, group_of, cnt/off
     b += fl_align256(n * 4);                 // members (n/8 groups * 8)
     b += fl_align256(64);                    // counters
-    b += fl_align256(M * 4) * 5 + fl_align256(M) * 3 + fl_align256(M * 2) + fl_align256(M * 8) * 1;  // items
-    b += fl_scan_scratch_bytes(n) + fl_align256(fl_locator_scratch_bytes(n)) + fl_sort_scratch_bytes(M, 8) + 4096;
+    b += fl_align256(M * 4) * 5 + fl_align256(M) * 3 + fl_align256(M * 2);  // items
+    b += fl_scan_scratch_bytes(n) + fl_align256(fl_locator_scratch_bytes(n)) + 4096;
     return b;
 }
 
@@ -517,7 +527,7 @@ struct AdaptWork {
     uint8_t* shadow; uint8_t* viol;
     uint32_t* leader; uint32_t* gid; uint32_t* group_of; uint32_t* cnt; uint32_t* members; uint32_t* counters;
     fl_items it;
-    void* scan_scratch; void* sort_scratch;
+    void* scan_scratch;
     void* locator;  // fl_locator_build scratch
 };
 
@@ -539,14 +549,12 @@ static AdaptWork carve_adapt(void* scratch, size_t n, bool with_case) {
     w.counters = cv.take<uint32_t>(16);
     size_t Mcap = n * 8 + 8;
     w.it.x = cv.take<int32_t>(Mcap); w.it.y = cv.take<int32_t>(Mcap); w.it.z = cv.take<int32_t>(Mcap);
-    w.it.src = cv.take<uint32_t>(Mcap); w.it.pos = cv.take<uint32_t>(Mcap);
+    w.it.src = cv.take<uint32_t>(Mcap);
     w.it.level = cv.take<uint8_t>(Mcap); w.it.state = cv.take<uint8_t>(Mcap); w.it.kind = cv.take<uint8_t>(Mcap);
     w.it.case_id = with_case ? cv.take<uint16_t>(Mcap) : nullptr;
     w.it.material = cv.take<uint32_t>(Mcap);
-    w.it.key = cv.take<uint64_t>(Mcap);
     w.scan_scratch = cv.take<char>(fl_scan_scratch_bytes(n));
     w.locator = cv.take<char>(fl_locator_scratch_bytes(n));
-    w.sort_scratch = cv.p;
     return w;
 }
 
@@ -605,13 +613,14 @@ int fl_adapt_prepare(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cf
     if (rc) return rc;
     k_members<<<wb, kT, 0, ctx->stream>>>(md, dom, L, w.leader, w.gid, w.members, w.group_of);
     FL_CHECK_LAUNCH(ctx, "k_members");
-    k_counts<<<nb, kT, 0, ctx->stream>>>(md, cfg->max_refinement_level, w.leader, w.group_of, w.cnt);
+    k_counts<<<nb, kT, 0, ctx->stream>>>(md, cfg->max_refinement_level, L.ids, w.leader, w.group_of, w.cnt);
     FL_CHECK_LAUNCH(ctx, "k_counts");
     k_count_kinds<<<nb, kT, 0, ctx->stream>>>(md, cfg->max_refinement_level, w.group_of, w.counters);
     FL_CHECK_LAUNCH(ctx, "k_count_kinds");
     rc = fl_scan_u32_with(ctx, w.cnt, w.cnt, n, w.counters + 3, w.scan_scratch);
     if (rc) return rc;
-    k_emit<<<nb, kT, 0, ctx->stream>>>(md, dom, cfg->max_refinement_level, w.cnt, w.leader, w.group_of, w.it);
+    k_emit<<<nb, kT, 0, ctx->stream>>>(md, dom, cfg->max_refinement_level, L.ids, w.cnt, w.leader, w.group_of,
+                                       w.it);
     FL_CHECK_LAUNCH(ctx, "k_emit");
     uint32_t hc[6] = {0, 0, 0, 0, 0, 0};
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(hc, w.counters, 24, cudaMemcpyDeviceToHost, ctx->stream), "adapt counts");
@@ -635,13 +644,9 @@ int fl_adapt_finish(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg
     size_t n = mesh->num_cells;
     if (n == 0 || M == 0) return FL_OK;
     AdaptWork w = carve_adapt(scratch, n, mesh->case_id != nullptr);
-    int end_bit = 3 * dom.depth + (mesh->case_id ? 12 : 0);
-    if (end_bit > 64) end_bit = 64;
-    int rc = fl_sort_pairs_with(ctx, w.it.key, w.it.pos, M, 0, end_bit, w.sort_scratch);
-    if (rc) return rc;
     fl_mesh_out o{out->x, out->y, out->z, out->level, out->state, out->flags, out->material,
                   mesh->case_id ? out->case_id : nullptr};
-    k_gather<<<fl_blocks(M, kT, ctx->num_sms * 8), kT, 0, ctx->stream>>>(w.it, w.it.pos, M, o, fields, out_fields, C,
+    k_gather<<<fl_blocks(M, kT, ctx->num_sms * 8), kT, 0, ctx->stream>>>(w.it, M, o, fields, out_fields, C,
                                                                          cfg->averaging_rule, w.members, osrc, okind);
     FL_CHECK_LAUNCH(ctx, "k_gather");
     if (omembers && num_groups)

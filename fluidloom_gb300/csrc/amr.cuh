@@ -3,14 +3,12 @@
 #include "common.cuh"
 #include "hash.cuh"
 
-// Unsorted list of new cells produced by a regrid (old-index order).
+// The new cells of a regrid, in key order.
 struct fl_items {
     int32_t* x; int32_t* y; int32_t* z;
     uint8_t* level; uint8_t* state; uint32_t* material; uint16_t* case_id;
     uint32_t* src;   // survivor / parent index (kind 0..8) or group id (kind 9)
     uint8_t* kind;   // 0..7 child index, 8 survivor, 9 merged parent
-    uint64_t* key;
-    uint32_t* pos;
 };
 
 struct fl_mesh_out {

@@ -81,6 +81,24 @@ static __device__ __forceinline__ uint64_t fl_hilbert_encode_cat(const uint8_t* 
     return h;
 }
 
+// Encoder state after the low `level` bits of x, y, z (most significant
+// first): the digit of child (c & 1, c >> 1 & 1, c >> 2) of the cell (x, y, z)
+// is then t1[state * 8 + c] & 7.
+static __device__ __forceinline__ unsigned fl_hilbert_state_cat(const uint8_t* t1, const uint16_t* t3c, uint32_t x,
+                                                                uint32_t y, uint32_t z, int level) {
+    unsigned s = 0;
+    int i = level;
+    for (int k = 0; k < level % 3; ++k) {
+        --i;
+        s = t1[s * 8 + ((((z >> i) & 1u) << 2) | (((y >> i) & 1u) << 1) | ((x >> i) & 1u))] >> 3;
+    }
+    while (i > 0) {
+        i -= 3;
+        s = t3c[s * 512 + ((((x >> i) & 7u) << 6) | (((y >> i) & 7u) << 3) | ((z >> i) & 7u))] >> 9;
+    }
+    return s;
+}
+
 // Interleave up to 21 bits of three coordinates: bit i of x -> 3i, y -> 3i+1, z -> 3i+2.
 static __device__ __forceinline__ uint64_t interleave3(uint32_t x, uint32_t y, uint32_t z) {
     auto sp = [](uint64_t v) {
