@@ -7,8 +7,12 @@
 // MergeEngine::merge (src/adaptation/MergeEngine.cpp:140-334) and the GPU
 // rebuild (AdaptationEngine.cpp:417-656).  The reference moves every
 // intermediate result through the host (about a dozen blocking transfers per
-// call); here the only host reads are the balance counters (one per
-// iteration) and the output cell count.  Semantics (the oracle's):
+// call); here the only host reads are two words of the point locator (the
+// deepest level, whether the cells are in key order), the balance counters
+// (one per iteration) and the output cell count.  Point location goes through
+// the sorted locator of hash.cuh (the hash table only serves FACE6's
+// shadow-level probes), and the new cells are emitted directly in key order,
+// so no sort runs after the split/merge.  Semantics (the oracle's):
 //  * balance FACE6 = the reference kernels (shadow levels, six face probes at
 //    anchor-1 / anchor+size, found at the cell whose shadow level matches,
 //    violation if found level > shadow + 1, at most max_balance_iterations);

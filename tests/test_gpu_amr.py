@@ -64,8 +64,10 @@ def test_reference_kats(ctx):
     assert m.download()["flags"].tolist() == [1, 0]
 
 
-@pytest.mark.parametrize("seed,mode", [(1, 0), (2, 0), (3, 1), (4, 1), (5, 1)])
-def test_adapt_vs_oracle(ctx, seed, mode):
+@pytest.mark.parametrize("seed,mode,shuffled", [(1, 0, False), (2, 0, False), (3, 1, False), (4, 1, False),
+                                                (5, 1, False), (6, 0, True), (7, 1, True), (8, 1, True)])
+def test_adapt_vs_oracle(ctx, seed, mode, shuffled):
+    """Shuffled meshes exercise the locator's own sort and the key-order emission."""
     cols = O.random_octree(seed, ext=(2, 2, 1), rounds=4, max_level=6, frac=0.3, balanced=True)
     rng = np.random.default_rng(seed)
     n = len(cols["x"])
@@ -73,6 +75,10 @@ def test_adapt_vs_oracle(ctx, seed, mode):
     cols["state"] = (rng.random(n) < 0.03).astype(np.uint8)
     C = 5
     f = rng.standard_normal((n, C)).astype(np.float32)
+    if shuffled:
+        perm = rng.permutation(n)
+        cols = {k: np.ascontiguousarray(v[perm]) for k, v in cols.items()}
+        f = np.ascontiguousarray(f[perm])
     kw = dict(max_level=6, min_level=1, balance_mode=mode, max_balance_iterations=10, enforce_balance=1,
               averaging_rule=seed % 2)
     want, wst, wf, *_ = O.adapt(cols, kw, O.domain(ext=(2, 2, 1), max_level=6), f, C)
@@ -88,12 +94,15 @@ def test_adapt_vs_oracle(ctx, seed, mode):
     assert st.balance.total_cells_marked_for_balance == wst.balance.marked
 
 
-@pytest.mark.parametrize("mode", [0, 1])
-def test_balance_vs_oracle(ctx, mode):
+@pytest.mark.parametrize("mode,shuffled", [(0, False), (1, False), (1, True)])
+def test_balance_vs_oracle(ctx, mode, shuffled):
     from fluidloom_gb300.amr import BalanceResult
     cols = O.random_octree(10 + mode, ext=(2, 1, 1), rounds=3, max_level=6, frac=0.3, balanced=False)
     rng = np.random.default_rng(mode)
     cols["flags"] = (rng.random(len(cols["x"])) < 0.2).astype(np.int32)
+    if shuffled:
+        perm = rng.permutation(len(cols["x"]))
+        cols = {k: np.ascontiguousarray(v[perm]) for k, v in cols.items()}
     wf, wst = O.balance(cols, O.domain(ext=(2, 1, 1), max_level=7), mode, 7)
     m = mesh(ctx, cols)
     r = BalanceResult()
