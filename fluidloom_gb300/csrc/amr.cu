@@ -71,16 +71,31 @@ __device__ __forceinline__ uint8_t shadow_of(const fl_mesh_dev& m, size_t i, int
     return (uint8_t)(m.level[i] + (up ? 1 : 0));
 }
 
-__global__ void k_shadow(fl_mesh_dev m, int mode, int max_level, uint8_t* __restrict__ shadow) {
+// Shadow levels; `lowest` (when given) receives their minimum.
+__global__ void k_shadow(fl_mesh_dev m, int mode, int max_level, uint8_t* __restrict__ shadow,
+                         uint32_t* __restrict__ lowest) {
     size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride)
-        shadow[i] = mode == 0 ? m.level[i] : shadow_of(m, i, mode, max_level);
+    unsigned lo = 255u;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
+        const uint8_t v = mode == 0 ? m.level[i] : shadow_of(m, i, mode, max_level);
+        shadow[i] = v;
+        lo = min(lo, (unsigned)v);
+    }
+    lo = __reduce_min_sync(0xFFFFFFFFu, lo);
+    if (lowest && (threadIdx.x & 31) == 0) atomicMin(lowest, lo);
 }
 
-__global__ void k_shadow_update(fl_mesh_dev m, int mode, int max_level, uint8_t* __restrict__ shadow) {
+__global__ void k_shadow_update(fl_mesh_dev m, int mode, int max_level, uint8_t* __restrict__ shadow,
+                                uint32_t* __restrict__ lowest) {
     size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride)
-        shadow[i] = shadow_of(m, i, mode, max_level);
+    unsigned lo = 255u;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
+        const uint8_t v = shadow_of(m, i, mode, max_level);
+        shadow[i] = v;
+        lo = min(lo, (unsigned)v);
+    }
+    lo = __reduce_min_sync(0xFFFFFFFFu, lo);
+    if (lowest && (threadIdx.x & 31) == 0) atomicMin(lowest, lo);
 }
 
 // detect_balance_violations (balance_enforce.cl:57-147), exact lookups.
@@ -117,9 +132,11 @@ __global__ void __launch_bounds__(kT) k_detect_face6(fl_mesh_dev m, fl_domain_de
 
 // Every leaf probes its 26 neighbour points at its own size through the
 // sorted locator (32 cells x 26 directions per block); a leaf found two or
-// more shadow levels coarser is a violation.
+// more shadow levels coarser is a violation.  A leaf less than two shadow
+// levels above the mesh's lowest (*lowest) cannot find one and does not probe.
 __global__ void __launch_bounds__(kProbeThreads, 2) k_detect_full26(fl_mesh_dev m, fl_domain_dev dom, fl_locator L,
                                                                     const uint8_t* __restrict__ shadow,
+                                                                    const uint32_t* __restrict__ lowest,
                                                                     uint8_t* __restrict__ viol,
                                                                     uint32_t* __restrict__ count) {
     __shared__ uint8_t t1[96];
@@ -130,10 +147,11 @@ __global__ void __launch_bounds__(kProbeThreads, 2) k_detect_full26(fl_mesh_dev 
     const int cl = threadIdx.x / 26, k = threadIdx.x - cl * 26;
     const int kk = k < 13 ? k : k + 1;
     const int dv[3] = {kk % 3 - 1, (kk / 3) % 3 - 1, kk / 9 - 1};
+    const int low = (int)*lowest;
     uint32_t local = 0;
     for (size_t base = (size_t)blockIdx.x * 32; base < m.n; base += (size_t)gridDim.x * 32) {
         const size_t i = base + cl;
-        if (i >= m.n) continue;
+        if (i >= m.n || (int)shadow[i] < low + 2) continue;
         const uint16_t cs = m.case_id ? m.case_id[i] : 0;
         const fl_domain_dev::Case& d = dom.c[m.case_id ? cs : 0];
         const int sh = dom.anchor_level - m.level[i];
@@ -492,7 +510,9 @@ int fl_balance_run(fl_ctx* ctx, fl_mesh_dev md, int32_t* flags, const fl_domain_
     if (md.n == 0) { r.converged = 1; if (res) *res = r; return FL_OK; }
     unsigned nb = fl_blocks(md.n, kT, ctx->num_sms * 8);
     int lg = fl_hash_lg(cap);
-    k_shadow<<<nb, kT, 0, ctx->stream>>>(md, mode, max_level, shadow);
+    uint32_t* lowest = counters + 2;  // the lowest shadow level, for FULL26's early out
+    FL_TRY_CUDA(ctx, cudaMemsetAsync(lowest, 0xFF, 4, ctx->stream), "balance lowest");
+    k_shadow<<<nb, kT, 0, ctx->stream>>>(md, mode, max_level, shadow, lowest);
     FL_CHECK_LAUNCH(ctx, "k_shadow");
     int cap_it = mode == 0 ? max_iters : 4096;
     uint32_t it = 0;
@@ -504,7 +524,7 @@ int fl_balance_run(fl_ctx* ctx, fl_mesh_dev md, int32_t* flags, const fl_domain_
         } else {
             k_clear_u8<<<nb, kT, 0, ctx->stream>>>(viol, md.n);
             const unsigned pb = (unsigned)std::min<size_t>((md.n + 31) / 32, (size_t)ctx->num_sms * 2);
-            k_detect_full26<<<pb, kProbeThreads, 0, ctx->stream>>>(md, dom, *L, shadow, viol, counters);
+            k_detect_full26<<<pb, kProbeThreads, 0, ctx->stream>>>(md, dom, *L, shadow, lowest, viol, counters);
         }
         FL_CHECK_LAUNCH(ctx, "k_detect");
         k_mark<<<nb, kT, 0, ctx->stream>>>(md, flags, viol, max_level, counters + 1);
@@ -516,7 +536,8 @@ int fl_balance_run(fl_ctx* ctx, fl_mesh_dev md, int32_t* flags, const fl_domain_
         // k_mark ran after detection regardless; with zero violations it marks nothing
         r.total_cells_marked_for_balance += h[1];
         if (h[1] == 0) { r.converged = 0; r.iterations = it + 1; break; }
-        k_shadow_update<<<nb, kT, 0, ctx->stream>>>(md, mode, max_level, shadow);
+        FL_TRY_CUDA(ctx, cudaMemsetAsync(lowest, 0xFF, 4, ctx->stream), "balance lowest");
+        k_shadow_update<<<nb, kT, 0, ctx->stream>>>(md, mode, max_level, shadow, lowest);
         FL_CHECK_LAUNCH(ctx, "k_shadow_update");
     }
     if (it == (uint32_t)cap_it) { r.converged = 0; r.iterations = it; }
@@ -605,7 +626,7 @@ int fl_adapt_prepare(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cf
         if (rc) return rc;
     }
     unsigned nb = fl_blocks(n, kT, ctx->num_sms * 8);
-    k_shadow_update<<<nb, kT, 0, ctx->stream>>>(md, 1, cfg->max_refinement_level, w.shadow);  // final levels
+    k_shadow_update<<<nb, kT, 0, ctx->stream>>>(md, 1, cfg->max_refinement_level, w.shadow, nullptr);  // final levels
     FL_CHECK_LAUNCH(ctx, "k_shadow_update");
     int check26 = cfg->enforce_2_1_balance && cfg->balance_mode == 1;
     const unsigned wb = fl_blocks((n + 31) / 32 * 32, kT, ctx->num_sms * 8);  // a warp per 32 cells
