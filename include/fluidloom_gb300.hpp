@@ -280,7 +280,7 @@ namespace runtime {
 // (include/fluidloom/runtime/nodes/KernelNode.h:27-73): one level-0 step.
 class BrickPool {
 public:
-    BrickPool(Device& dev, const std::vector<fl_lbm_case>& cases) : dev_(dev) {
+    BrickPool(Device& dev, const std::vector<fl_lbm_case>& cases) : dev_(dev), cases_(cases) {
         check(dev.get(), fl_pool_create(dev.get(), cases.data(), (int)cases.size(), &p_), "fl_pool_create");
     }
     ~BrickPool() { fl_pool_destroy(dev_.get(), p_); }
@@ -293,10 +293,33 @@ public:
         check(dev_.get(), fl_pool_info_get(dev_.get(), p_, &i), "info");
         return i;
     }
+    // Solid voxels of one case at `level` (bit (z * Ny + y) * Nx + x, N = ext * 8 << level),
+    // OR-ed with the case's sphere; an empty vector removes them (fl_pool_set_solid_mask).
+    void setSolidMask(int32_t case_id, int32_t level, const std::vector<uint32_t>& bits) {
+        check(dev_.get(),
+              fl_pool_set_solid_mask(dev_.get(), p_, case_id, level, bits.empty() ? nullptr : bits.data(),
+                                     bits.size()),
+              "fl_pool_set_solid_mask");
+    }
+    // The case's mask level (-1: none) and words.
+    int32_t solidMask(int32_t case_id, std::vector<uint32_t>* bits) const {
+        int32_t level = -1;
+        check(dev_.get(), fl_pool_get_solid_mask(dev_.get(), p_, case_id, &level, nullptr, 0), "fl_pool_get_solid_mask");
+        if (level >= 0 && bits) {
+            const fl_lbm_case& c = cases_.at(case_id);
+            const uint64_t n = ((uint64_t)c.ext[0] * 8 << level) * ((uint64_t)c.ext[1] * 8 << level) *
+                               ((uint64_t)c.ext[2] * 8 << level);
+            bits->assign((size_t)((n + 31) / 32), 0u);
+            check(dev_.get(), fl_pool_get_solid_mask(dev_.get(), p_, case_id, &level, bits->data(), bits->size()),
+                  "fl_pool_get_solid_mask");
+        }
+        return level;
+    }
 
 private:
     Device& dev_;
     fl_pool* p_ = nullptr;
+    std::vector<fl_lbm_case> cases_;
 };
 
 class LbmStepNode {

@@ -108,6 +108,24 @@ int main() {
         step.execute();
         dev.finish();
         EXPECT_TRUE(pool.info().num_bricks >= 8);
+        // a solid block through the mask: fewer fluid updates, the same words back
+        const uint64_t lups = pool.info().fluid_lups_per_step;
+        std::vector<uint32_t> bits(16 * 16 * 16 / 32, 0u);
+        for (int z = 4; z < 8; ++z)
+            for (int y = 4; y < 8; ++y)
+                for (int x = 4; x < 8; ++x) {
+                    const int i = (z * 16 + y) * 16 + x;
+                    bits[i >> 5] |= 1u << (i & 31);
+                }
+        pool.setSolidMask(0, 0, bits);
+        std::vector<uint32_t> back;
+        EXPECT_EQ(pool.solidMask(0, &back), 0);
+        EXPECT_TRUE(back == bits);
+        EXPECT_TRUE(pool.info().fluid_lups_per_step < lups);
+        step.execute();
+        pool.setSolidMask(0, 0, {});
+        EXPECT_EQ(pool.solidMask(0, nullptr), -1);
+        EXPECT_EQ(pool.info().fluid_lups_per_step, lups);
         // the same three operations as an execution graph (test_hazard_analyzer.cpp / 
         // test_topological_scheduler.cpp shapes): hazards chain them, the order is A, B, C
         runtime::BrickPool pool2(dev, {c});
