@@ -177,12 +177,57 @@ def regrid_microbench(ctx, seed=1, L=8):
     stop = timer(ctx)
     ctx.call("fl_sort_pairs_u64_u32", keys.ptr, ids.ptr, n, 0, 63)
     out["sort_ms"] = stop()
+    out["primitives"] = primitives_on(ctx, m, keys, ids, n, out)
     out.update({"leaves_in": int(len(idx)), "leaves_out": int(n), "split": st.num_split, "merged_groups": st.num_groups,
                 "balance_iterations": st.balance.iterations, "balance_marked": st.balance.total_cells_marked_for_balance,
                 "sorted_keys_per_s": n / (out["sort_ms"] * 1e-3),
                 "regrid_ms": out["flags_ms"] + out["adapt_ms"] + out["neighbour_ms"]})
     m.free()
     return out
+
+
+def primitives_on(ctx, m, keys, ids, n, out):
+    """The regrid's primitives alone on the n-leaf result mesh, each against the algorithmic
+    bytes of its unit: encode 24 B per key (12 B coordinates in, 8 B key + 4 B id out); radix
+    sort 8 + 24 B per key and pass (8 passes of 8-bit digits over 63 bits); scan 8 B per
+    element; hash build 24 B per key + 12 B per slot cleared; hash query 12 B per query + one
+    32-byte sector per probe; neighbour rebuild one 32-byte sector per probe (26 per leaf) +
+    104 B of table per leaf.  Times are CUDA-event times of one call each."""
+    import ctypes
+    from fluidloom_gb300 import DeviceArray
+    peak, _ = measured_peak()
+    res = {}
+
+    def put(name, ms, nbytes, units, unit_name):
+        res[name] = {"ms": round(ms, 4), "gbs": round(nbytes / (ms * 1e-3) / 1e9, 1),
+                     "frac_of_measured": round(nbytes / (ms * 1e-3) / 1e9 / peak, 3),
+                     unit_name + "_per_s": round(units / (ms * 1e-3), 1)}
+
+    stop = timer(ctx)
+    N = ctypes.c_size_t(n)
+    ctx.call("fl_hilbert_encode", m.m.x, m.m.y, m.m.z, 21, keys.ptr, ids.ptr, N)
+    put("hilbert_encode", stop(), 24.0 * n, n, "keys")
+    put("radix_sort", out["sort_ms"], (8.0 + 24.0 * 8) * n, n, "keys")
+    a = DeviceArray(ctx, (n,), np.uint32).zero()
+    b = DeviceArray(ctx, (n,), np.uint32)
+    tot = DeviceArray(ctx, (1,), np.uint32)
+    stop = timer(ctx)
+    ctx.call("fl_scan_exclusive_u32", a.ptr, b.ptr, N, tot.ptr)
+    put("scan", stop(), 8.0 * n, n, "elements")
+    ctx.lib.fl_hash_compute_capacity.restype = ctypes.c_uint64
+    cap = int(ctx.lib.fl_hash_compute_capacity(N))
+    tk = DeviceArray(ctx, (cap,), np.uint64)
+    tv = DeviceArray(ctx, (cap,), np.uint32)
+    stop = timer(ctx)
+    ctx.call("fl_hash_build", tk.ptr, tv.ptr, ctypes.c_uint64(cap), keys.ptr, None, N)
+    put("hash_build", stop(), 24.0 * n + 12.0 * cap, n, "keys")
+    stop = timer(ctx)
+    ctx.call("fl_hash_query", tk.ptr, tv.ptr, ctypes.c_uint64(cap), keys.ptr, b.ptr, N)
+    put("hash_query", stop(), (12.0 + 32.0) * n, n, "queries")
+    put("neighbour_rebuild", out["neighbour_ms"], (26 * 32.0 + 104.0) * n, 26 * n, "probes")
+    for d in (a, b, tot, tk, tv):
+        d.free()
+    return res
 
 
 def cpu_sample(steps, threads=None):

@@ -759,17 +759,18 @@ int fl_neighbour_rebuild(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config
         return fl_set_error(ctx, FL_E_INVALID_ARG, "key geometry: need anchor_level <= key_depth <= 21, max level <= anchor_level, ext << anchor_level <= 2^key_depth");
     size_t n = mesh->num_cells;
     if (n == 0) return FL_OK;
-    int rc = fl_scratch_reserve(ctx, 256 + fl_locator_scratch_bytes(n));
+    int rc = fl_scratch_reserve(ctx, 256 + fl_align256(n * 4) + fl_locator_scratch_bytes(n));
     if (rc) return rc;
     Carver cv{(char*)ctx->scratch};
     void* dcase = cv.take<char>(256);
+    uint32_t* marks = cv.take<uint32_t>(n);
     fl_domain_dev dom = fl_domain_from_config(ctx, cfg, dcase);
     dom.max_level = cfg->max_refinement_level;
     fl_mesh_dev md{mesh->x, mesh->y, mesh->z, mesh->level, mesh->state, mesh->flags, mesh->material, mesh->case_id, n};
     fl_locator L;
     rc = fl_locator_build(ctx, md, dom, cv.p, &L);
     if (rc) return rc;
-    rc = fl_neighbours_sorted(ctx, md, dom, L, subslots, nbr);
+    rc = fl_neighbours_sorted(ctx, md, dom, L, subslots, nbr, marks);
     if (rc) return rc;
     return fl_collect_device_status(ctx, "fl_neighbour_rebuild");
 }

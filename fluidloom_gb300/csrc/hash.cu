@@ -148,30 +148,36 @@ __global__ void k_locator_dir(const uint64_t* __restrict__ keys, size_t n, int l
     }
 }
 
-// Blocks of kProbeThreads: 32 / S cells x 26 directions x S sub-slots, so a
-// thread's direction and sub-slot are fixed and a cell's 26 * S probes sit in
-// consecutive threads (one coalesced row of nbr).
-
-template <int S>
+// Neighbour rows in two passes over 13 directions each.  Direction k and
+// 25 - k are opposite, and a same-level neighbour relation is symmetric: when
+// the first pass (k < 13) finds a leaf j of cell i's own level, i is j's
+// neighbour in direction 25 - k on every sub-slot, so it writes that entry of
+// j's row too and marks it (bit 12 - k of marks[j]); the second pass probes
+// only the unmarked directions 13..25.  Blocks of kProbeThreads: 64 / S cells
+// x 13 directions x S sub-slots, a cell's probes in consecutive threads.
+template <int S, bool kFirst>
 __global__ void __launch_bounds__(kProbeThreads, 2) k_neighbours_sorted(fl_mesh_dev m, fl_domain_dev dom,
-                                                                        fl_locator L, uint32_t* __restrict__ nbr) {
-    constexpr int kCells = 32 / S;
+                                                                        fl_locator L, uint32_t* __restrict__ nbr,
+                                                                        uint32_t* __restrict__ marks) {
+    constexpr int kCells = 64 / S;
     __shared__ uint8_t t1[96];
     __shared__ uint16_t t3c[12 * 512];
     fl_keys_fill_tables_cat(t1, t3c);
     __syncthreads();
     const fl_probe P = fl_probe_make(t1, t3c, L, dom);
-    const int cl = threadIdx.x / (26 * S);
-    const int r = threadIdx.x - cl * (26 * S);
-    const int k = r / S, s = r - k * S;
+    const int cl = threadIdx.x / (13 * S);
+    const int r = threadIdx.x - cl * (13 * S);
+    const int k = r / S + (kFirst ? 0 : 13), s = r % S;
     const int kk = k < 13 ? k : k + 1;
     const int dv[3] = {kk % 3 - 1, (kk / 3) % 3 - 1, kk / 9 - 1};
     for (size_t base = (size_t)blockIdx.x * kCells; base < m.n; base += (size_t)gridDim.x * kCells) {
         const size_t i = base + cl;
         if (i >= m.n) continue;
+        if (!kFirst && ((marks[i] >> (k - 13)) & 1u)) continue;
         const uint16_t cs = m.case_id ? m.case_id[i] : 0;
         const fl_domain_dev::Case& d = dom.c[m.case_id ? cs : 0];
-        const int sh = dom.anchor_level - m.level[i];
+        const int lvl = m.level[i];
+        const int sh = dom.anchor_level - lvl;
         const int32_t anc[3] = {m.x[i] << sh, m.y[i] << sh, m.z[i] << sh};
         const int32_t size = 1 << sh;
         int32_t p[3];
@@ -183,9 +189,14 @@ __global__ void __launch_bounds__(kProbeThreads, 2) k_neighbours_sorted(fl_mesh_
             else { p[a] = anc[a] + (((s >> bit) & 1) ? (size >> 1) : 0); ++bit; }
             in = in && fl_fold32(p[a], d.ext[a] << dom.anchor_level, d.periodic[a]);
         }
-        nbr[i * (26 * S) + r] =
+        const uint32_t res =
             in ? fl_probe_point(P, m.case_id != nullptr, cs, (uint32_t)p[0], (uint32_t)p[1], (uint32_t)p[2])
                : FL_INVALID_INDEX;
+        nbr[i * (26 * S) + k * S + s] = res;
+        if (kFirst && res != FL_INVALID_INDEX && m.level[res] == lvl) {
+            nbr[(size_t)res * (26 * S) + (25 - k) * S + s] = (uint32_t)i;
+            if (s == 0) atomicOr(marks + res, 1u << (12 - k));
+        }
     }
 }
 
@@ -236,12 +247,20 @@ int fl_locator_build(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom
 }
 
 int fl_neighbours_sorted(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom, const fl_locator& L,
-                         int subslots, uint32_t* nbr) {
+                         int subslots, uint32_t* nbr, uint32_t* marks) {
     if (m.n == 0) return FL_OK;
-    const size_t cells = (size_t)(32 / subslots);
+    FL_TRY_CUDA(ctx, cudaMemsetAsync(marks, 0, m.n * 4, ctx->stream), "neighbour marks");
+    const size_t cells = (size_t)(64 / subslots);
     const unsigned grid = (unsigned)std::min<size_t>((m.n + cells - 1) / cells, (size_t)ctx->num_sms * 2);
-    if (subslots == 4) k_neighbours_sorted<4><<<grid, kProbeThreads, 0, ctx->stream>>>(m, dom, L, nbr);
-    else k_neighbours_sorted<1><<<grid, kProbeThreads, 0, ctx->stream>>>(m, dom, L, nbr);
+    if (subslots == 4) {
+        k_neighbours_sorted<4, true><<<grid, kProbeThreads, 0, ctx->stream>>>(m, dom, L, nbr, marks);
+        FL_CHECK_LAUNCH(ctx, "k_neighbours_sorted");
+        k_neighbours_sorted<4, false><<<grid, kProbeThreads, 0, ctx->stream>>>(m, dom, L, nbr, marks);
+    } else {
+        k_neighbours_sorted<1, true><<<grid, kProbeThreads, 0, ctx->stream>>>(m, dom, L, nbr, marks);
+        FL_CHECK_LAUNCH(ctx, "k_neighbours_sorted");
+        k_neighbours_sorted<1, false><<<grid, kProbeThreads, 0, ctx->stream>>>(m, dom, L, nbr, marks);
+    }
     FL_CHECK_LAUNCH(ctx, "k_neighbours_sorted");
     return FL_OK;
 }

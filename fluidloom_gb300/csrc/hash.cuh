@@ -221,9 +221,9 @@ size_t fl_locator_scratch_bytes(size_t n);
 // Run starts of the mesh's leaves, sorted (with their cell ids) when the mesh
 // is not already in key order, and the bucket directory; L points into scratch.
 int fl_locator_build(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom, void* scratch, fl_locator* L);
-// nbr[(i*26 + k)*S + s] through the sorted locator.
+// nbr[(i*26 + k)*S + s] through the sorted locator; marks: n words of scratch.
 int fl_neighbours_sorted(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom, const fl_locator& L,
-                         int subslots, uint32_t* nbr);
+                         int subslots, uint32_t* nbr, uint32_t* marks);
 
 int fl_hash_lg(uint64_t cap);
 uint64_t fl_table_capacity(size_t n);

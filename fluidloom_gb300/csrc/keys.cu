@@ -20,12 +20,12 @@ __global__ void __launch_bounds__(kThreads) k_hilbert_encode(const int32_t* __re
                                                              uint64_t* __restrict__ keys,
                                                              uint32_t* __restrict__ ids, size_t n) {
     __shared__ uint8_t t1[96];
-    __shared__ uint16_t t3[12 * 512];
-    fl_keys_fill_tables(t1, t3, false);
+    __shared__ uint16_t t3c[12 * 512];
+    fl_keys_fill_tables_cat(t1, t3c);
     __syncthreads();
     size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        keys[i] = fl_hilbert_encode_dev(t1, t3, (uint32_t)__ldg(x + i), (uint32_t)__ldg(y + i),
+        keys[i] = fl_hilbert_encode_cat(t1, t3c, (uint32_t)__ldg(x + i), (uint32_t)__ldg(y + i),
                                         (uint32_t)__ldg(z + i), level);
         if (ids) ids[i] = (uint32_t)i;
     }
@@ -87,13 +87,13 @@ __global__ void __launch_bounds__(kThreads) k_cell_keys(const int32_t* __restric
                                                         const uint16_t* __restrict__ cs, int depth, int anchor_level,
                                                         uint64_t* __restrict__ keys, size_t n) {
     __shared__ uint8_t t1[96];
-    __shared__ uint16_t t3[12 * 512];
-    fl_keys_fill_tables(t1, t3, false);
+    __shared__ uint16_t t3c[12 * 512];
+    fl_keys_fill_tables_cat(t1, t3c);
     __syncthreads();
     size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         int sh = anchor_level - (int)level[i];
-        uint64_t k = fl_hilbert_encode_dev(t1, t3, (uint32_t)x[i] << sh, (uint32_t)y[i] << sh,
+        uint64_t k = fl_hilbert_encode_cat(t1, t3c, (uint32_t)x[i] << sh, (uint32_t)y[i] << sh,
                                            (uint32_t)z[i] << sh, depth);
         if (cs) k |= (uint64_t)cs[i] << (3 * depth);
         keys[i] = k;

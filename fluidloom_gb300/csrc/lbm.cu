@@ -1320,15 +1320,16 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
     size_t n = P->mesh.num_cells;
     if (P->cap >= (1u << 23))  // descriptors address elements as brick * 512 + site in 32 bits
         return fl_set_error(ctx, FL_E_CAPACITY, "a pool holds fewer than 2^23 bricks");
-    int rc = fl_scratch_reserve(ctx, fl_locator_scratch_bytes(n));
+    int rc = fl_scratch_reserve(ctx, fl_align256(n * 4) + fl_locator_scratch_bytes(n));
     if (rc) return rc;
     fl_domain_dev dom = pool_domain(P);
     fl_mesh_dev md{P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.level, P->mesh.state, P->mesh.flags, P->mesh.material,
                    P->mesh.case_id, n};
     fl_locator L;
-    rc = fl_locator_build(ctx, md, dom, ctx->scratch, &L);
+    uint32_t* marks = (uint32_t*)ctx->scratch;
+    rc = fl_locator_build(ctx, md, dom, (char*)ctx->scratch + fl_align256(n * 4), &L);
     if (rc) return rc;
-    rc = fl_neighbours_sorted(ctx, md, dom, L, 4, P->nbr);
+    rc = fl_neighbours_sorted(ctx, md, dom, L, 4, P->nbr, marks);
     if (rc) return rc;
     const uint8_t* mnear = P->any_mask ? P->mnear : nullptr;
     if (mnear) {
