@@ -71,31 +71,41 @@ __device__ __forceinline__ uint8_t shadow_of(const fl_mesh_dev& m, size_t i, int
     return (uint8_t)(m.level[i] + (up ? 1 : 0));
 }
 
-// Shadow levels; `lowest` (when given) receives their minimum.
+// Shadow levels; lowest[0] / lowest[1] (when given) receive their minimum and maximum.
 __global__ void k_shadow(fl_mesh_dev m, int mode, int max_level, uint8_t* __restrict__ shadow,
                          uint32_t* __restrict__ lowest) {
     size_t stride = (size_t)gridDim.x * blockDim.x;
-    unsigned lo = 255u;
+    unsigned lo = 255u, hi = 0u;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
         const uint8_t v = mode == 0 ? m.level[i] : shadow_of(m, i, mode, max_level);
         shadow[i] = v;
         lo = min(lo, (unsigned)v);
+        hi = max(hi, (unsigned)v);
     }
     lo = __reduce_min_sync(0xFFFFFFFFu, lo);
-    if (lowest && (threadIdx.x & 31) == 0) atomicMin(lowest, lo);
+    hi = __reduce_max_sync(0xFFFFFFFFu, hi);
+    if (lowest && (threadIdx.x & 31) == 0) {
+        atomicMin(lowest, lo);
+        atomicMax(lowest + 1, hi);
+    }
 }
 
 __global__ void k_shadow_update(fl_mesh_dev m, int mode, int max_level, uint8_t* __restrict__ shadow,
                                 uint32_t* __restrict__ lowest) {
     size_t stride = (size_t)gridDim.x * blockDim.x;
-    unsigned lo = 255u;
+    unsigned lo = 255u, hi = 0u;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
         const uint8_t v = shadow_of(m, i, mode, max_level);
         shadow[i] = v;
         lo = min(lo, (unsigned)v);
+        hi = max(hi, (unsigned)v);
     }
     lo = __reduce_min_sync(0xFFFFFFFFu, lo);
-    if (lowest && (threadIdx.x & 31) == 0) atomicMin(lowest, lo);
+    hi = __reduce_max_sync(0xFFFFFFFFu, hi);
+    if (lowest && (threadIdx.x & 31) == 0) {
+        atomicMin(lowest, lo);
+        atomicMax(lowest + 1, hi);
+    }
 }
 
 // detect_balance_violations (balance_enforce.cl:57-147), exact lookups.
@@ -133,7 +143,8 @@ __global__ void __launch_bounds__(kT) k_detect_face6(fl_mesh_dev m, fl_domain_de
 // Every leaf probes its 26 neighbour points at its own size through the
 // sorted locator (32 cells x 26 directions per block); a leaf found two or
 // more shadow levels coarser is a violation.  A leaf less than two shadow
-// levels above the mesh's lowest (*lowest) cannot find one and does not probe.
+// levels above the mesh's lowest (lowest[0]) cannot find one and does not
+// probe; with the highest (lowest[1]) below lowest + 2 no block probes.
 __global__ void __launch_bounds__(kProbeThreads, 2) k_detect_full26(fl_mesh_dev m, fl_domain_dev dom, fl_locator L,
                                                                     const uint8_t* __restrict__ shadow,
                                                                     const uint32_t* __restrict__ lowest,
@@ -147,7 +158,8 @@ __global__ void __launch_bounds__(kProbeThreads, 2) k_detect_full26(fl_mesh_dev 
     const int cl = threadIdx.x / 26, k = threadIdx.x - cl * 26;
     const int kk = k < 13 ? k : k + 1;
     const int dv[3] = {kk % 3 - 1, (kk / 3) % 3 - 1, kk / 9 - 1};
-    const int low = (int)*lowest;
+    const int low = (int)lowest[0];
+    if ((int)lowest[1] < low + 2) return;  // no leaf anywhere is two levels above another
     uint32_t local = 0;
     for (size_t base = (size_t)blockIdx.x * 32; base < m.n; base += (size_t)gridDim.x * 32) {
         const size_t i = base + cl;
@@ -510,8 +522,9 @@ int fl_balance_run(fl_ctx* ctx, fl_mesh_dev md, int32_t* flags, const fl_domain_
     if (md.n == 0) { r.converged = 1; if (res) *res = r; return FL_OK; }
     unsigned nb = fl_blocks(md.n, kT, ctx->num_sms * 8);
     int lg = fl_hash_lg(cap);
-    uint32_t* lowest = counters + 2;  // the lowest shadow level, for FULL26's early out
-    FL_TRY_CUDA(ctx, cudaMemsetAsync(lowest, 0xFF, 4, ctx->stream), "balance lowest");
+    uint32_t* lowest = counters + 2;  // lowest and highest shadow level, for FULL26's early outs
+    const uint32_t extremes[2] = {0xFFFFFFFFu, 0u};
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(lowest, extremes, 8, cudaMemcpyHostToDevice, ctx->stream), "balance extremes");
     k_shadow<<<nb, kT, 0, ctx->stream>>>(md, mode, max_level, shadow, lowest);
     FL_CHECK_LAUNCH(ctx, "k_shadow");
     int cap_it = mode == 0 ? max_iters : 4096;
@@ -536,7 +549,8 @@ int fl_balance_run(fl_ctx* ctx, fl_mesh_dev md, int32_t* flags, const fl_domain_
         // k_mark ran after detection regardless; with zero violations it marks nothing
         r.total_cells_marked_for_balance += h[1];
         if (h[1] == 0) { r.converged = 0; r.iterations = it + 1; break; }
-        FL_TRY_CUDA(ctx, cudaMemsetAsync(lowest, 0xFF, 4, ctx->stream), "balance lowest");
+        FL_TRY_CUDA(ctx, cudaMemcpyAsync(lowest, extremes, 8, cudaMemcpyHostToDevice, ctx->stream),
+                    "balance extremes");
         k_shadow_update<<<nb, kT, 0, ctx->stream>>>(md, mode, max_level, shadow, lowest);
         FL_CHECK_LAUNCH(ctx, "k_shadow_update");
     }

@@ -237,7 +237,9 @@ int fl_locator_build(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(hf, flag, 4, cudaMemcpyDeviceToHost, ctx->stream), "locator");
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "locator");
     if (hf[0]) {  // stable: equal run starts keep mesh order, so the last of them is found
-        int rc = fl_sort_pairs_with(ctx, keys, ids, n, 0, 64, p);
+        // the keys hold 3 (depth - cut) bits, plus 16 for case ids
+        const int end_bit = std::min(64, 3 * (dom.depth - L->cut) + (m.case_id ? 16 : 0));
+        int rc = fl_sort_pairs_with(ctx, keys, ids, n, 0, end_bit, p);
         if (rc) return rc;
         L->ids = ids;
     }
