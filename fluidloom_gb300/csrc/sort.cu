@@ -68,7 +68,7 @@ __global__ void k_bin_offsets(uint32_t* hist) {
 
 __device__ __forceinline__ uint32_t ld_vol(const uint32_t* p) { return *(volatile const uint32_t*)p; }
 
-__global__ void __launch_bounds__(kThreads) k_onesweep(const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+__global__ void __launch_bounds__(kThreads, 4) k_onesweep(const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin,
                                                        uint64_t* __restrict__ kout, uint32_t* __restrict__ vout,
                                                        size_t n, int shift, uint32_t dmask,
                                                        const uint32_t* __restrict__ bin_off,
