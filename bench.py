@@ -230,6 +230,25 @@ def primitives_on(ctx, m, keys, ids, n, out):
     return res
 
 
+def fp64_error(ctx, steps=(1, 10)):
+    """The GPU's FP32 populations against an FP64 run of the same steps (the oracle's
+    arithmetic in double, same mesh) on the half-resolution sphere case: max relative
+    difference over all sites and populations after each step count."""
+    from fluidloom_gb300.lbm import Pool
+    from tests import _oracle as O
+    case = sphere_case(scale=2)
+    op = O.OraclePool([case])
+    out = {"case": "sphere at half resolution per axis (64x32x32 base, 3 levels, r=4)"}
+    for k in steps:
+        ref = op.fp64_steps(k)
+        gp = Pool(ctx, [case])
+        gp.step(k)
+        f = gp.populations().astype(np.float64)
+        gp.close()
+        out["max_rel_after_%d_steps" % k] = float(np.max(np.abs(f - ref) / np.maximum(np.abs(ref), 1e-30)))
+    return out
+
+
 def cpu_sample(steps, threads=None):
     """The oracle (CPU port) on a half-resolution sample of the workload: 64x32x32 base, 3 levels, r=4."""
     from tests import _oracle as O
@@ -353,11 +372,13 @@ def run_gpu(args):
         pool.close()
         micro = regrid_microbench(ctx)
     cpu = None
+    fp64 = None
     if rank == 0 and not args.no_cpu:
         v, th, sl = cpu_sample(1)
         cpu = {"value": round(v, 2), "unit": UNIT, "cores": th, "kind": "port",
                "sample": "CPU oracle (OpenMP, all host threads) on the same case at half resolution per axis "
                          "(64x32x32 base, 3 levels, r=4; %d fluid updates per step), 1 level-0 step" % sl}
+        fp64 = fp64_error(ctx)
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
@@ -370,7 +391,7 @@ def run_gpu(args):
                         "d2h_bytes_per_step": int(d2h)},
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
                 "regrid_ms_per_cycle": round(statistics.mean(regrid_ms), 3), "regrids_in_timed_region": regrids,
-                "regrid_microbench": micro}
+                "regrid_microbench": micro, "fp32_vs_fp64": fp64}
         print(json.dumps(line))
     rep.close()
 

@@ -31,15 +31,20 @@ const int CX[Q] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0}
 const int CY[Q] = {0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -1};
 const int CZ[Q] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1};
 const int OPP[Q] = {0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15, 18, 17};
-const float W0 = 1.0f / 3.0f, W1 = 1.0f / 18.0f, W2 = 1.0f / 36.0f;
-inline float wq(int q) { return q == 0 ? W0 : (q < 7 ? W1 : W2); }
+// The step's arithmetic is written once for the FP32 oracle (T = float, the
+// kernels' operations one by one) and for the FP64 reference run of the same
+// steps (T = double) whose difference states the FP32 rounding error.
+template <typename T>
+inline T wqT(int q) { return q == 0 ? T(1) / T(3) : (q < 7 ? T(1) / T(18) : T(1) / T(36)); }
+inline float wq(int q) { return wqT<float>(q); }
 
 // c_q . u as the sum of its non-zero terms in x, y, z order (c = +-1 is a
 // sign, so no product is formed; c_0 . u = 0).
-inline float cdot(int q, float ux, float uy, float uz) {
-    const float t[3] = {CX[q] > 0 ? ux : -ux, CY[q] > 0 ? uy : -uy, CZ[q] > 0 ? uz : -uz};
+template <typename T>
+inline T cdotT(int q, T ux, T uy, T uz) {
+    const T t[3] = {CX[q] > 0 ? ux : -ux, CY[q] > 0 ? uy : -uy, CZ[q] > 0 ? uz : -uz};
     const int c[3] = {CX[q], CY[q], CZ[q]};
-    float s = 0.0f;
+    T s = T(0);
     bool any = false;
     for (int k = 0; k < 3; ++k) {
         if (!c[k]) continue;
@@ -48,37 +53,46 @@ inline float cdot(int q, float ux, float uy, float uz) {
     }
     return s;
 }
+inline float cdot(int q, float ux, float uy, float uz) { return cdotT<float>(q, ux, uy, uz); }
 
-inline float feq1(int q, float rho, float ux, float uy, float uz, float base) {
-    float cu = cdot(q, ux, uy, uz);
-    float t = 4.5f * cu;
-    t = 3.0f + t;
+template <typename T>
+inline T feqT(int q, T rho, T ux, T uy, T uz, T base) {
+    T cu = cdotT<T>(q, ux, uy, uz);
+    T t = T(4.5) * cu;
+    t = T(3) + t;
     t = cu * t;
     t = base + t;
-    float wr = wq(q) * rho;
+    T wr = wqT<T>(q) * rho;
     return wr * t;
 }
-
-inline float base_of(float ux, float uy, float uz) {
-    float usq = ux * ux;
-    usq = usq + uy * uy;
-    usq = usq + uz * uz;
-    float t = 1.5f * usq;
-    return 1.0f - t;
+inline float feq1(int q, float rho, float ux, float uy, float uz, float base) {
+    return feqT<float>(q, rho, ux, uy, uz, base);
 }
 
+template <typename T>
+inline T base_ofT(T ux, T uy, T uz) {
+    T usq = ux * ux;
+    usq = usq + uy * uy;
+    usq = usq + uz * uz;
+    T t = T(1.5) * usq;
+    return T(1) - t;
+}
+inline float base_of(float ux, float uy, float uz) { return base_ofT<float>(ux, uy, uz); }
+
 // Macroscopic moments in a fixed summation order.
-inline void moments(const float* f, float* rho, float* jx, float* jy, float* jz) {
-    float r = f[0];
+template <typename T>
+inline void momentsT(const T* f, T* rho, T* jx, T* jy, T* jz) {
+    T r = f[0];
     for (int q = 1; q < Q; ++q) r = r + f[q];
-    float a = f[1] - f[2];
+    T a = f[1] - f[2];
     a = a + (f[7] - f[8]); a = a + (f[9] - f[10]); a = a + (f[11] - f[12]); a = a + (f[13] - f[14]);
-    float b = f[3] - f[4];
+    T b = f[3] - f[4];
     b = b + (f[7] - f[8]); b = b + (f[10] - f[9]); b = b + (f[15] - f[16]); b = b + (f[17] - f[18]);
-    float c = f[5] - f[6];
+    T c = f[5] - f[6];
     c = c + (f[11] - f[12]); c = c + (f[14] - f[13]); c = c + (f[15] - f[16]); c = c + (f[18] - f[17]);
     *rho = r; *jx = a; *jy = b; *jz = c;
 }
+inline void moments(const float* f, float* rho, float* jx, float* jy, float* jz) { momentsT<float>(f, rho, jx, jy, jz); }
 
 inline int dir_index(int dx, int dy, int dz) {
     int kk = (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1);
@@ -148,8 +162,10 @@ inline bool solid_at(const or_lbm_case& c, const CaseInfo& ci, int64_t sx, int64
     return !ci.mask.empty() && mask_at(c, ci, sx, sy, sz, l);
 }
 
-// Pull of population q into site G (global level-l coords) of brick b.
-float pull(const Pool& P, size_t b, int q, int l, int sub, const int64_t* G, const float* R) {
+// Pull of population q into site G (global level-l coords) of brick b; F =
+// the two population buffers (of type T), R = level l's current one.
+template <typename T>
+T pullT(const Pool& P, const std::vector<T>* F, size_t b, int q, int l, int sub, const int64_t* G, const T* R) {
     const or_lbm_case& c = P.cases[P.cs[b]];
     const CaseInfo& ci = P.info[P.cs[b]];
     int64_t S[3] = {G[0] - CX[q], G[1] - CY[q], G[2] - CZ[q]};
@@ -174,14 +190,15 @@ float pull(const Pool& P, size_t b, int q, int l, int sub, const int64_t* G, con
             else if (bt == 2 && moving < 0) moving = out_face[a];
         }
         if (inlet) {
-            float base = base_of(c.inlet_u[0], c.inlet_u[1], c.inlet_u[2]);
-            return feq1(q, 1.0f, c.inlet_u[0], c.inlet_u[1], c.inlet_u[2], base);
+            const T iu[3] = {T(c.inlet_u[0]), T(c.inlet_u[1]), T(c.inlet_u[2])};
+            T base = base_ofT<T>(iu[0], iu[1], iu[2]);
+            return feqT<T>(q, T(1), iu[0], iu[1], iu[2], base);
         }
         if (outlet) return R[fidx(P.n, q, b, s_local)];
-        float v = R[fidx(P.n, OPP[q], b, s_local)];
+        T v = R[fidx(P.n, OPP[q], b, s_local)];
         if (moving >= 0) {
-            float cu = cdot(q, c.wall_u[0], c.wall_u[1], c.wall_u[2]);
-            float t = 6.0f * wq(q);
+            T cu = cdotT<T>(q, T(c.wall_u[0]), T(c.wall_u[1]), T(c.wall_u[2]));
+            T t = T(6) * wqT<T>(q);
             t = t * cu;
             v = v + t;
         }
@@ -210,53 +227,55 @@ float pull(const Pool& P, size_t b, int q, int l, int sub, const int64_t* G, con
         int64_t lx = (Sw[0] >> 1) - (int64_t)P.x[nb] * 8, ly = (Sw[1] >> 1) - (int64_t)P.y[nb] * 8,
                 lz = (Sw[2] >> 1) - (int64_t)P.z[nb] * 8;
         size_t i = fidx(P.n, q, nb, (int)(lx + 8 * ly + 64 * lz));
-        const float* oldb = P.f[1 - P.parity[l - 1]].data();
-        const float* newb = P.f[P.parity[l - 1]].data();
+        const T* oldb = F[1 - P.parity[l - 1]].data();
+        const T* newb = F[P.parity[l - 1]].data();
         if (sub == 0) return oldb[i];
-        float t = oldb[i] + newb[i];
-        return t * 0.5f;
+        T t = oldb[i] + newb[i];
+        return t * T(0.5);
     }
     if (ln == l + 1) {
-        const float* fb = P.f[P.parity[l + 1]].data();
-        float s = 0.0f;
+        const T* fb = F[P.parity[l + 1]].data();
+        T s = T(0);
         for (int k = 0; k < 8; ++k) {
             int64_t lx = 2 * Sw[0] + (k & 1) - (int64_t)P.x[nb] * 8;
             int64_t ly = 2 * Sw[1] + ((k >> 1) & 1) - (int64_t)P.y[nb] * 8;
             int64_t lz = 2 * Sw[2] + ((k >> 2) & 1) - (int64_t)P.z[nb] * 8;
             s = s + fb[fidx(P.n, q, nb, (int)(lx + 8 * ly + 64 * lz))];
         }
-        return s * 0.125f;
+        return s * T(0.125);
     }
     return R[fidx(P.n, OPP[q], b, s_local)];
 }
 
-void collide_stream(Pool& P, int l, int sub, int nthreads) {
-    const float* R = P.f[P.parity[l]].data();
-    float* Wt = P.f[1 - P.parity[l]].data();
+// omega(case, l) gives the relaxation rate in T.
+template <typename T, typename Omega>
+void collide_streamT(Pool& P, std::vector<T>* F, Omega omega_of, int l, int sub, int nthreads) {
+    const T* R = F[P.parity[l]].data();
+    T* Wt = F[1 - P.parity[l]].data();
     long long nb = (long long)P.n;
 #pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads)
     for (long long b = 0; b < nb; ++b) {
         if (P.level[b] != l) continue;
         const or_lbm_case& c = P.cases[P.cs[b]];
         const CaseInfo& ci = P.info[P.cs[b]];
-        float omega = ci.omega[l];
+        const T omega = omega_of(P.cs[b], l);
         for (int s = 0; s < 512; ++s) {
             int64_t G[3] = {(int64_t)P.x[b] * 8 + (s & 7), (int64_t)P.y[b] * 8 + ((s >> 3) & 7),
                             (int64_t)P.z[b] * 8 + (s >> 6)};
             if (solid_at(c, ci, G[0], G[1], G[2], l)) {
-                for (int q = 0; q < Q; ++q) Wt[fidx(P.n, q, b, s)] = wq(q);
+                for (int q = 0; q < Q; ++q) Wt[fidx(P.n, q, b, s)] = wqT<T>(q);
                 continue;
             }
-            float fin[Q];
-            for (int q = 0; q < Q; ++q) fin[q] = pull(P, b, q, l, sub, G, R);
-            float rho, jx, jy, jz;
-            moments(fin, &rho, &jx, &jy, &jz);
-            float inv = 1.0f / rho;
-            float ux = jx * inv, uy = jy * inv, uz = jz * inv;
-            float base = base_of(ux, uy, uz);
+            T fin[Q];
+            for (int q = 0; q < Q; ++q) fin[q] = pullT<T>(P, F, b, q, l, sub, G, R);
+            T rho, jx, jy, jz;
+            momentsT<T>(fin, &rho, &jx, &jy, &jz);
+            T inv = T(1) / rho;
+            T ux = jx * inv, uy = jy * inv, uz = jz * inv;
+            T base = base_ofT<T>(ux, uy, uz);
             for (int q = 0; q < Q; ++q) {
-                float fe = feq1(q, rho, ux, uy, uz, base);
-                float d = fe - fin[q];
+                T fe = feqT<T>(q, rho, ux, uy, uz, base);
+                T d = fe - fin[q];
                 d = omega * d;
                 Wt[fidx(P.n, q, b, s)] = fin[q] + d;
             }
@@ -265,9 +284,17 @@ void collide_stream(Pool& P, int l, int sub, int nthreads) {
     P.parity[l] ^= 1;
 }
 
+template <typename T, typename Omega>
+void step_levelT(Pool& P, std::vector<T>* F, Omega omega_of, int l, int sub, int nthreads) {
+    collide_streamT<T>(P, F, omega_of, l, sub, nthreads);
+    if (l < P.maxL) {
+        step_levelT<T>(P, F, omega_of, l + 1, 0, nthreads);
+        step_levelT<T>(P, F, omega_of, l + 1, 1, nthreads);
+    }
+}
+
 void step_level(Pool& P, int l, int sub, int nthreads) {
-    collide_stream(P, l, sub, nthreads);
-    if (l < P.maxL) { step_level(P, l + 1, 0, nthreads); step_level(P, l + 1, 1, nthreads); }
+    step_levelT<float>(P, P.f, [&P](int cs, int lv) { return P.info[cs].omega[lv]; }, l, sub, nthreads);
 }
 
 void derive(Pool& P) {
@@ -584,6 +611,30 @@ void or_pool_set_mask(void* h, int case_id, int level, const uint32_t* bits, siz
 void or_pool_steps(void* h, int nsteps, int nthreads) {
     Pool& P = *(Pool*)h;
     for (int i = 0; i < nsteps; ++i) step_level(P, 0, 0, nthreads);
+}
+
+// The pool's next nsteps level-0 steps in FP64 from its current (FP32) state,
+// on its current mesh; the pool itself is left as it is.  out: the resulting
+// populations as or_pool_populations lays them out, in double.
+void or_pool_fp64_steps(void* h, int nsteps, int nthreads, double* out) {
+    const Pool& P0 = *(const Pool*)h;
+    Pool P = P0;
+    std::vector<double> F[2];
+    for (int k = 0; k < 2; ++k) F[k].assign(P0.f[k].begin(), P0.f[k].end());
+    std::vector<double> omega(P.cases.size() * 20);
+    for (size_t c = 0; c < P.cases.size(); ++c)
+        for (int l = 0; l < 20; ++l) {
+            double t = (double)P.cases[c].tau0 - 0.5;
+            t = (double)(1 << l) * t;
+            t = t + 0.5;
+            omega[c * 20 + l] = 1.0 / t;
+        }
+    auto omega_of = [&omega](int cs, int l) { return omega[(size_t)cs * 20 + l]; };
+    for (int i = 0; i < nsteps; ++i) step_levelT<double>(P, F, omega_of, 0, 0, nthreads);
+    for (size_t b = 0; b < P.n; ++b) {
+        const double* G = F[P.parity[P.level[b]]].data();
+        for (int q = 0; q < Q; ++q) std::memcpy(out + fidx(P.n, q, b, 0), G + fidx(P.n, q, b, 0), 512 * 8);
+    }
 }
 
 void or_pool_regrid(void* h) { regrid(*(Pool*)h, true); }

@@ -115,6 +115,9 @@ size_t or_pool_size(void* h);
 void or_pool_bricks(void* h, int32_t* x, int32_t* y, int32_t* z, uint8_t* level, uint16_t* cs);
 void or_pool_nbr(void* h, uint32_t* out);
 void or_pool_populations(void* h, float* out);
+/* The next nsteps level-0 steps in FP64 from the pool's current state, on its current mesh (the pool is
+ * left unchanged); out as or_pool_populations, in double. */
+void or_pool_fp64_steps(void* h, int nsteps, int nthreads, double* out);
 void or_pool_conservation(void* h, double* out);
 uint64_t or_pool_fluid_lups(void* h);
 /* Solid voxels of one case at `level` (bit (z * Ny + y) * Nx + x); bits == NULL removes them. */

@@ -102,6 +102,7 @@ def load():
         L.or_pool_fluid_lups.restype = ctypes.c_uint64
         L.or_pool_fluid_lups.argtypes = [P]
         L.or_pool_set_mask.argtypes = [P, ctypes.c_int, ctypes.c_int, P, ctypes.c_size_t]
+        L.or_pool_fp64_steps.argtypes = [P, ctypes.c_int, ctypes.c_int, P]
         _lib = L
     return _lib
 
@@ -289,6 +290,13 @@ class OraclePool:
 
     def lups(self):
         return load().or_pool_fluid_lups(self.h)
+
+    def fp64_steps(self, k, threads=0):
+        """Populations after the next k steps run in FP64 from the current state (the pool is unchanged)."""
+        import os
+        out = np.empty((19, self.n(), 512), np.float64)
+        load().or_pool_fp64_steps(self.h, k, threads or (os.cpu_count() or 1), ptr(out))
+        return out
 
     def set_mask(self, case_id, level, words):
         """Solid-mask words (uint32, bit (z*Ny + y)*Nx + x) of one case; None removes them."""

@@ -132,3 +132,14 @@ def test_settled_solid_bricks_skip_equals_always_writing(ctx):
         np.testing.assert_array_equal(a.populations(), b.populations())
         a.regrid()
         b.regrid()
+
+
+def test_gpu_populations_against_fp64(ctx):
+    """The GPU's FP32 populations within 1e-5 relative of an FP64 run of the same steps."""
+    from fluidloom_gb300.lbm import Pool
+    c = cases_small()[1]
+    gp, op = Pool(ctx, [c]), O.OraclePool([c])
+    ref = op.fp64_steps(6)
+    gp.step(6)
+    f = gp.populations().astype(np.float64)
+    assert float(np.max(np.abs(f - ref) / np.maximum(np.abs(ref), 1e-30))) < 1e-5
