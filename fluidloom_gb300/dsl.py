@@ -511,7 +511,7 @@ def _flag_rule(loop, fields):
 
 
 class Scenario:
-    """A parsed script bound to case parameters (BASELINE-like defaults when the
+    """A parsed script bound to case parameters (the benchmark cases' sizes when the
     script does not set them)."""
 
     def __init__(self, tree, ext=None, max_level=None, tau=None, regrid_every=None, base_dir=".", mask_level=None):
