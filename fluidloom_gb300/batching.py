@@ -34,17 +34,26 @@ def cavity_batch(n=256, seed=4):
     return out
 
 
-def autotune(pool, candidates=(2, 3, 4, 6, 8), steps=2):
-    """Pick the CTAs-per-SM of the interior collide-stream kernel by timing each
-    candidate with CUDA events (profile pass, no graphs); returns the choice."""
+def autotune(pool, candidates=(2, 3, 4, 6, 8), streams=(1, 2), steps=4):
+    """Pick the CTAs per SM of the interior collide-stream kernel and the class-stream layout
+    (every launch on one stream, or the per-level dependency graph over two) by timing
+    graph-replayed level-0 steps of each combination with CUDA events (two untimed
+    steps first capture the graphs); returns (ctas_per_sm, streams).  The pool's
+    state advances: tune on a pool that is rebuilt afterwards."""
+    import ctypes
+    ctx = pool.ctx
     best, best_ms = None, None
-    for g in candidates:
-        pool.set_options(graphs=1, grid_mult=g)
-        prof = pool.profile_steps(steps)
-        ms = sum(p[0] for p in prof)
-        if best_ms is None or ms < best_ms:
-            best, best_ms = g, ms
-    pool.set_options(graphs=1, grid_mult=best)
+    for st in streams:
+        for g in candidates:
+            pool.set_options(graphs=1, grid_mult=g, streams=st)
+            pool.step(2)
+            ctx.call("fl_ctx_timer_start")
+            pool.step(steps)
+            ms = ctypes.c_float()
+            ctx.call("fl_ctx_timer_stop", ctypes.byref(ms))
+            if best_ms is None or ms.value < best_ms:
+                best, best_ms = (g, st), ms.value
+    pool.set_options(graphs=1, grid_mult=best[0], streams=best[1])
     return best
 
 
@@ -70,10 +79,10 @@ def main(argv=None):
     cases = cavity_batch(args.cases)
     # batched
     pool = Pool(ctx, cases)
-    tuned = autotune(pool)
+    tuned, tuned_streams = autotune(pool)
     pool.close()
     pool = Pool(ctx, cases)
-    pool.set_options(graphs=1, grid_mult=tuned)
+    pool.set_options(graphs=1, grid_mult=tuned, streams=tuned_streams)
     ctx.sync()
     t0 = time.perf_counter()
     lups_b = run(pool, args.steps, args.regrid_every)
@@ -88,7 +97,7 @@ def main(argv=None):
     mismatched = []
     for i, c in enumerate(cases):
         p = Pool(ctx, [c])
-        p.set_options(graphs=1, grid_mult=tuned)
+        p.set_options(graphs=1, grid_mult=tuned, streams=tuned_streams)
         ctx.sync()
         t0 = time.perf_counter()
         lups_p += run(p, args.steps, args.regrid_every)
@@ -104,6 +113,7 @@ def main(argv=None):
            "batched_mlups": lups_b / tb / 1e6, "plain_mlups": lups_p / tp / 1e6,
            "speedup": (lups_b / tb) / (lups_p / tp), "batched_s": tb, "plain_s": tp,
            "lups_batched": int(lups_b), "lups_plain": int(lups_p), "autotuned_ctas_per_sm": tuned,
+           "autotuned_class_streams": tuned_streams,
            "cases_checked": nchk, "cases_mismatched": mismatched}
     print(json.dumps(res))
     return res
