@@ -612,7 +612,7 @@ __global__ void k_count_kinds(fl_mesh_dev m, int max_level, const uint32_t* __re
 
 // Phase 1: balance, classify, emit the unsorted new cell list; returns its size.
 int fl_adapt_prepare(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, const fl_domain_dev& dom,
-                     bool run_balance, void* scratch, size_t* M_out, fl_adapt_stats* st) {
+                     bool run_balance, void* scratch, size_t* M_out, fl_adapt_stats* st, int level_bound) {
     size_t n = mesh->num_cells;
     fl_adapt_stats s{};
     *M_out = 0;
@@ -623,7 +623,7 @@ int fl_adapt_prepare(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cf
     // the sorted locator serves FULL26 detection and merge grouping; the
     // FACE6 detection (shadow-level probes) keeps the hash table
     fl_locator L;
-    int rc = fl_locator_build(ctx, md, dom, w.locator, &L);
+    int rc = fl_locator_build(ctx, md, dom, w.locator, &L, level_bound);
     if (rc) return rc;
     if (run_balance && cfg->balance_mode == 0) {
         rc = fl_launch_cell_keys(ctx, mesh->x, mesh->y, mesh->z, mesh->level, mesh->case_id, dom.depth,

@@ -213,7 +213,8 @@ size_t fl_locator_scratch_bytes(size_t n) {
     return fl_align256(n * 8) + fl_align256(n * 4) + fl_align256((nb + 1) * 4) + 256 + fl_sort_scratch_bytes(n, 8);
 }
 
-int fl_locator_build(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom, void* scratch, fl_locator* L) {
+int fl_locator_build(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom, void* scratch, fl_locator* L,
+                     int level_bound, bool in_key_order) {
     const size_t n = m.n;
     const int log2nb = locator_log2nb(n);
     char* p = (char*)scratch;
@@ -224,18 +225,23 @@ int fl_locator_build(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom
     *L = fl_locator{keys, nullptr, dir, m.level, n, log2nb, 0};
     if (n == 0) return FL_OK;
     FL_TRY_CUDA(ctx, cudaMemsetAsync(flag, 0, 8, ctx->stream), "locator");
-    k_deepest<<<fl_blocks(n, 256, ctx->num_sms * 4), 256, 0, ctx->stream>>>(m.level, n, flag);
-    FL_CHECK_LAUNCH(ctx, "k_deepest");
-    uint32_t hf[2] = {0, 0};  // unsorted, deepest level
-    FL_TRY_CUDA(ctx, cudaMemcpyAsync(hf, flag, 8, cudaMemcpyDeviceToHost, ctx->stream), "locator");
-    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "locator");
+    uint32_t hf[2] = {0, (uint32_t)std::max(level_bound, 0)};  // unsorted, deepest level
+    if (level_bound < 0) {
+        k_deepest<<<fl_blocks(n, 256, ctx->num_sms * 4), 256, 0, ctx->stream>>>(m.level, n, flag);
+        FL_CHECK_LAUNCH(ctx, "k_deepest");
+        FL_TRY_CUDA(ctx, cudaMemcpyAsync(hf, flag, 8, cudaMemcpyDeviceToHost, ctx->stream), "locator");
+        FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "locator");
+    }
     L->cut = dom.anchor_level > (int)hf[1] ? dom.anchor_level - (int)hf[1] : 0;
     k_run_keys<<<fl_blocks(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(m, dom, L->cut, keys, ids);
     FL_CHECK_LAUNCH(ctx, "k_run_keys");
-    k_check_sorted<<<fl_blocks(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(keys, n, flag);
-    FL_CHECK_LAUNCH(ctx, "k_check_sorted");
-    FL_TRY_CUDA(ctx, cudaMemcpyAsync(hf, flag, 4, cudaMemcpyDeviceToHost, ctx->stream), "locator");
-    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "locator");
+    hf[0] = 0;
+    if (!in_key_order) {
+        k_check_sorted<<<fl_blocks(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(keys, n, flag);
+        FL_CHECK_LAUNCH(ctx, "k_check_sorted");
+        FL_TRY_CUDA(ctx, cudaMemcpyAsync(hf, flag, 4, cudaMemcpyDeviceToHost, ctx->stream), "locator");
+        FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "locator");
+    }
     if (hf[0]) {  // stable: equal run starts keep mesh order, so the last of them is found
         // the keys hold 3 (depth - cut) bits, plus 16 for case ids
         const int end_bit = std::min(64, 3 * (dom.depth - L->cut) + (m.case_id ? 16 : 0));

@@ -220,7 +220,10 @@ static __device__ __forceinline__ bool fl_fold32(int32_t& p, int32_t n, int peri
 size_t fl_locator_scratch_bytes(size_t n);
 // Run starts of the mesh's leaves, sorted (with their cell ids) when the mesh
 // is not already in key order, and the bucket directory; L points into scratch.
-int fl_locator_build(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom, void* scratch, fl_locator* L);
+// level_bound >= 0: no leaf is deeper (saves a host read); in_key_order: the
+// caller knows the mesh is in key order (saves the check and its host read).
+int fl_locator_build(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom, void* scratch, fl_locator* L,
+                     int level_bound = -1, bool in_key_order = false);
 // nbr[(i*26 + k)*S + s] through the sorted locator; marks: n words of scratch.
 int fl_neighbours_sorted(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom, const fl_locator& L,
                          int subslots, uint32_t* nbr, uint32_t* marks);

@@ -1327,7 +1327,9 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
                    P->mesh.case_id, n};
     fl_locator L;
     uint32_t* marks = (uint32_t*)ctx->scratch;
-    rc = fl_locator_build(ctx, md, dom, (char*)ctx->scratch + fl_align256(n * 4), &L);
+    // a pool's bricks are in key order whenever its topology is rebuilt (every
+    // regrid emits them so; removal compacts in order)
+    rc = fl_locator_build(ctx, md, dom, (char*)ctx->scratch + fl_align256(n * 4), &L, P->maxL, true);
     if (rc) return rc;
     rc = fl_neighbours_sorted(ctx, md, dom, L, 4, P->nbr, marks);
     if (rc) return rc;
@@ -1517,7 +1519,7 @@ int pool_regrid(fl_ctx* ctx, fl_pool* P, int use_vorticity, fl_adapt_stats* st, 
     }
     size_t M = 0;
     fl_adapt_stats s{};
-    rc = fl_adapt_prepare(ctx, &P->mesh, &cfg, dom, true, P->adapt_scratch, &M, &s);
+    rc = fl_adapt_prepare(ctx, &P->mesh, &cfg, dom, true, P->adapt_scratch, &M, &s, P->maxL);
     if (rc) return rc;
     size_t new_cap = P->cap;
     if (M > P->cap) new_cap = std::max((size_t)(M * 1.5), M + 64);
