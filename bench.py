@@ -192,7 +192,9 @@ def primitives_on(ctx, m, keys, ids, n, out):
     sort 8 + 24 B per key and pass (8 passes of 8-bit digits over 63 bits); scan 8 B per
     element; hash build 24 B per key + 12 B per slot cleared; hash query 12 B per query + one
     32-byte sector per probe; neighbour rebuild one 32-byte sector per probe (26 per leaf) +
-    104 B of table per leaf.  Times are CUDA-event times of one call each."""
+    104 B of table per leaf; halo pack / unpack of a 19-component field 4 + 2 x 76 B per cell
+    (a random cell order); restriction 32 + 9 x 76 B per sibling group.  Times are
+    CUDA-event times of one call each."""
     import ctypes
     from fluidloom_gb300 import DeviceArray
     peak, _ = measured_peak()
@@ -225,7 +227,26 @@ def primitives_on(ctx, m, keys, ids, n, out):
     ctx.call("fl_hash_query", tk.ptr, tv.ptr, ctypes.c_uint64(cap), keys.ptr, b.ptr, N)
     put("hash_query", stop(), (12.0 + 32.0) * n, n, "queries")
     put("neighbour_rebuild", out["neighbour_ms"], (26 * 32.0 + 104.0) * n, 26 * n, "probes")
-    for d in (a, b, tot, tk, tv):
+    for d in (a, tot, tk, tv):
+        d.free()
+    # ghost fill primitives over a 19-component field (populations-like): gather by index,
+    # scatter back, and restriction of n/8 sibling groups (members in key order)
+    C = 19
+    fld = DeviceArray(ctx, (n * C,), np.float32).zero()
+    pk = DeviceArray(ctx, (n * C,), np.float32)
+    idx = DeviceArray.from_host(ctx, np.random.default_rng(3).permutation(n).astype(np.uint32))
+    stop = timer(ctx)
+    ctx.call("fl_pack_halo", fld.ptr, C, idx.ptr, N, pk.ptr)
+    put("pack_halo", stop(), (4.0 + 2 * 4.0 * C) * n, n, "cells")
+    stop = timer(ctx)
+    ctx.call("fl_unpack_halo", pk.ptr, C, idx.ptr, N, fld.ptr)
+    put("unpack_halo", stop(), (4.0 + 2 * 4.0 * C) * n, n, "cells")
+    g = n // 8
+    mem = DeviceArray.from_host(ctx, np.arange(g * 8, dtype=np.uint32))
+    stop = timer(ctx)
+    ctx.call("fl_restrict_groups", fld.ptr, C, mem.ptr, ctypes.c_size_t(g), 0, pk.ptr)
+    put("restrict_groups", stop(), (32.0 + 9 * 4.0 * C) * g, g, "groups")
+    for d in (b, fld, pk, idx, mem):
         d.free()
     return res
 

@@ -40,25 +40,35 @@ __global__ void k_unpack_fields(const uint8_t* __restrict__ packed, float* __res
     }
 }
 
+// Row kernels: a warp covers 32 / C rows (one row when C > 16), lane j the
+// column j % C of row j / C, so every row is read and written by one warp
+// instruction (its two or three sectors fetched once) and the index math is
+// 32-bit per row.
 __global__ void k_gather_rows(const float* __restrict__ field, uint32_t C, const uint32_t* __restrict__ idx, size_t n,
                               float* __restrict__ out) {
-    size_t total = n * C;
-    size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
-        size_t k = t / C;
-        uint32_t c = (uint32_t)(t - k * C);
-        out[t] = field[(size_t)idx[k] * C + c];
+    const uint32_t lane = threadIdx.x & 31u, rpw = C <= 32u ? 32u / C : 1u;
+    const uint32_t r = lane / C, c = lane - r * C;
+    const size_t nw = ((size_t)gridDim.x * blockDim.x) >> 5;
+    for (size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * rpw < n; w += nw) {
+        const size_t k = w * rpw + r;
+        if (r >= rpw || k >= n) continue;
+        const float* src = field + (size_t)idx[k] * C;
+        float* dst = out + k * C;
+        for (uint32_t j = c; j < C; j += 32u) dst[j] = src[j];
     }
 }
 
 __global__ void k_scatter_rows(const float* __restrict__ in, uint32_t C, const uint32_t* __restrict__ idx, size_t n,
                                float* __restrict__ field) {
-    size_t total = n * C;
-    size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
-        size_t k = t / C;
-        uint32_t c = (uint32_t)(t - k * C);
-        field[(size_t)idx[k] * C + c] = in[t];
+    const uint32_t lane = threadIdx.x & 31u, rpw = C <= 32u ? 32u / C : 1u;
+    const uint32_t r = lane / C, c = lane - r * C;
+    const size_t nw = ((size_t)gridDim.x * blockDim.x) >> 5;
+    for (size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * rpw < n; w += nw) {
+        const size_t k = w * rpw + r;
+        if (r >= rpw || k >= n) continue;
+        const float* src = in + k * C;
+        float* dst = field + (size_t)idx[k] * C;
+        for (uint32_t j = c; j < C; j += 32u) dst[j] = src[j];
     }
 }
 
@@ -92,17 +102,31 @@ __global__ void __launch_bounds__(256) k_interp(fl_mesh_dev m, fl_domain_dev dom
     }
 }
 
+// Restriction, laid out like the row kernels (a warp per 32 / C groups).
 __global__ void k_restrict(const float* __restrict__ field, uint32_t C, const uint32_t* __restrict__ members,
                            size_t G, int rule, float* __restrict__ out) {
-    size_t total = G * C;
-    size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
-        size_t g = t / C;
-        uint32_t c = (uint32_t)(t - g * C);
-        float s = 0.0f;
-        for (int q = 0; q < 8; ++q) s = __fadd_rn(s, field[(size_t)members[g * 8 + q] * C + c]);
-        out[t] = rule == 1 ? s : __fmul_rn(s, 0.125f);
+    const uint32_t lane = threadIdx.x & 31u, rpw = C <= 32u ? 32u / C : 1u;
+    const uint32_t r = lane / C, c = lane - r * C;
+    const size_t nw = ((size_t)gridDim.x * blockDim.x) >> 5;
+    for (size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * rpw < G; w += nw) {
+        const size_t g = w * rpw + r;
+        if (r >= rpw || g >= G) continue;
+        uint32_t mem[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) mem[q] = members[g * 8 + q];
+        for (uint32_t j = c; j < C; j += 32u) {
+            float s = 0.0f;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) s = __fadd_rn(s, field[(size_t)mem[q] * C + j]);
+            out[g * C + j] = rule == 1 ? s : __fmul_rn(s, 0.125f);
+        }
     }
+}
+
+// Blocks for the row kernels: 8 warps a block, a warp per 32 / C rows.
+unsigned row_blocks(fl_ctx* ctx, size_t n, uint32_t C) {
+    const size_t rpw = C <= 32u ? 32u / C : 1u;
+    return fl_blocks((n + rpw - 1) / rpw * 32, 256, ctx->num_sms * 8);
 }
 
 }  // namespace
@@ -135,7 +159,7 @@ int fl_pack_halo(fl_ctx* ctx, const float* field, uint32_t C, const uint32_t* ce
     if (!ctx) return FL_E_INVALID_ARG;
     if (!n || !C) return FL_OK;
     if (!field || !cell_indices || !pack) return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_pack_halo: null pointer");
-    k_gather_rows<<<fl_blocks(n * C, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(field, C, cell_indices, n, pack);
+    k_gather_rows<<<row_blocks(ctx, n, C), 256, 0, ctx->stream>>>(field, C, cell_indices, n, pack);
     FL_CHECK_LAUNCH(ctx, "k_gather_rows");
     return FL_OK;
 }
@@ -144,7 +168,7 @@ int fl_unpack_halo(fl_ctx* ctx, const float* pack, uint32_t C, const uint32_t* c
     if (!ctx) return FL_E_INVALID_ARG;
     if (!n || !C) return FL_OK;
     if (!field || !cell_indices || !pack) return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_unpack_halo: null pointer");
-    k_scatter_rows<<<fl_blocks(n * C, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(pack, C, cell_indices, n, field);
+    k_scatter_rows<<<row_blocks(ctx, n, C), 256, 0, ctx->stream>>>(pack, C, cell_indices, n, field);
     FL_CHECK_LAUNCH(ctx, "k_scatter_rows");
     return FL_OK;
 }
@@ -187,8 +211,7 @@ int fl_restrict_groups(fl_ctx* ctx, const float* field, uint32_t C, const uint32
     if (!ctx) return FL_E_INVALID_ARG;
     if (!ngroups || !C) return FL_OK;
     if (!field || !members || !out) return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_restrict_groups: null pointer");
-    k_restrict<<<fl_blocks(ngroups * C, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(field, C, members, ngroups, rule,
-                                                                                     out);
+    k_restrict<<<row_blocks(ctx, ngroups, C), 256, 0, ctx->stream>>>(field, C, members, ngroups, rule, out);
     FL_CHECK_LAUNCH(ctx, "k_restrict");
     return FL_OK;
 }
