@@ -101,10 +101,12 @@ __global__ void __launch_bounds__(kThreads, 4) k_onesweep(const uint64_t* __rest
         v[i] = ok ? vin[g] : 0u;
         uint32_t d = ok ? (uint32_t)((k[i] >> shift) & dmask) : 256u;
         unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
-        uint32_t base = d < 256u ? s_warp_hist[warp][d] : 0u;
-        __syncwarp();
-        if (d < 256u && (peers & lt) == 0) s_warp_hist[warp][d] = base + __popc(peers);
-        __syncwarp();
+        // the group's first lane adds the group to the warp's digit counter and
+        // hands the old count to its peers (one shared atomic, no warp barrier)
+        const int leader = __ffs(peers) - 1;
+        uint32_t base = 0u;
+        if (d < 256u && lane == leader) base = atomicAdd(&s_warp_hist[warp][d], (uint32_t)__popc(peers));
+        base = __shfl_sync(0xFFFFFFFFu, base, leader);
         rank[i] = base + __popc(peers & lt);
     }
     __syncthreads();
