@@ -328,16 +328,23 @@ __global__ void k_counts(fl_mesh_dev m, int max_level, const uint32_t* __restric
     }
 }
 
-// The new cells in key order, with no sort: the old cells are visited in key
-// order (the locator's order) and every new cell lies inside the run of the
-// old cell that makes it -- a survivor in its own run, the children of a split
-// cell in its run, placed by their Hilbert digit under the cell's curve state,
-// a merged group's parent at its leader's place (the eight members' runs are
-// consecutive and the other seven emit nothing).
+// The new cells in key order, written straight into the output mesh with no
+// sort: the old cells are visited in key order (the locator's order) and every
+// new cell lies inside the run of the old cell that makes it -- a survivor in
+// its own run, the children of a split cell in its run, placed by their
+// Hilbert digit under the cell's curve state, a merged group's parent at its
+// leader's place (the eight members' runs are consecutive and the other seven
+// emit nothing).  Fields (C per cell, AoS) follow the reference: children copy
+// their parent (prolongation), a parent sums its children 0..7 in order, x0.125
+// for the arithmetic rule (restriction).
 __global__ void __launch_bounds__(kT) k_emit(fl_mesh_dev m, fl_domain_dev dom, int max_level,
                                              const uint32_t* __restrict__ order, const uint32_t* __restrict__ off,
                                              const uint32_t* __restrict__ is_leader,
-                                             const uint32_t* __restrict__ group_of, fl_items it) {
+                                             const uint32_t* __restrict__ group_of,
+                                             const uint32_t* __restrict__ members, fl_mesh_out out,
+                                             uint32_t* __restrict__ osrc, uint8_t* __restrict__ okind,
+                                             const float* __restrict__ fin, float* __restrict__ fout, uint32_t C,
+                                             int rule) {
     __shared__ uint8_t t1[96];
     __shared__ uint16_t t3c[12 * 512];
     fl_keys_fill_tables_cat(t1, t3c);
@@ -349,10 +356,25 @@ __global__ void __launch_bounds__(kT) k_emit(fl_mesh_dev m, fl_domain_dev dom, i
         bool split = m.flags[i] > 0 && m.state[i] == 0 && m.level[i] < max_level;
         uint32_t o = off[t];
         auto put = [&](uint32_t j, int32_t x, int32_t y, int32_t z, uint8_t l, uint32_t src, uint8_t kind) {
-            it.x[j] = x; it.y[j] = y; it.z[j] = z; it.level[j] = l;
-            it.state[j] = m.state[i]; it.material[j] = m.material[i];
-            if (it.case_id) it.case_id[j] = cs;
-            it.src[j] = src; it.kind[j] = kind;
+            out.x[j] = x; out.y[j] = y; out.z[j] = z; out.level[j] = l;
+            out.state[j] = m.state[i]; out.flags[j] = 0; out.material[j] = m.material[i];
+            if (out.case_id) out.case_id[j] = cs;
+            if (osrc) osrc[j] = src;
+            if (okind) okind[j] = kind;
+            if (fin && C) {
+                float* fo = fout + (size_t)j * C;
+                if (kind <= 8) {
+                    const float* sp = fin + (size_t)src * C;
+                    for (uint32_t c = 0; c < C; ++c) fo[c] = sp[c];
+                } else {
+                    const uint32_t* mem = members + (size_t)src * 8;
+                    for (uint32_t c = 0; c < C; ++c) {
+                        float sum = 0.0f;
+                        for (int q = 0; q < 8; ++q) sum = __fadd_rn(sum, fin[(size_t)mem[q] * C + c]);
+                        fo[c] = rule == 1 ? sum : __fmul_rn(sum, 0.125f);
+                    }
+                }
+            }
         };
         if (split) {
             const int l = m.level[i];
@@ -366,39 +388,6 @@ __global__ void __launch_bounds__(kT) k_emit(fl_mesh_dev m, fl_domain_dev dom, i
                 put(o, m.x[i] >> 1, m.y[i] >> 1, m.z[i] >> 1, (uint8_t)(m.level[i] - 1), group_of[i], 9);
         } else {
             put(o, m.x[i], m.y[i], m.z[i], m.level[i], (uint32_t)i, 8);
-        }
-    }
-}
-
-// Final gather in key order; fields AoS (C per cell) with the reference's
-// prolongation (copy) and restriction (ordered sum, x0.125 for rule 0).
-__global__ void k_gather(fl_items it, size_t M, fl_mesh_out out,
-                         const float* __restrict__ fin, float* __restrict__ fout, uint32_t C, int rule,
-                         const uint32_t* __restrict__ members, uint32_t* __restrict__ osrc, uint8_t* __restrict__ okind) {
-    size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < M; j += stride) {
-        const size_t p = j;
-        out.x[j] = it.x[p]; out.y[j] = it.y[p]; out.z[j] = it.z[p];
-        out.level[j] = it.level[p]; out.state[j] = it.state[p]; out.material[j] = it.material[p];
-        out.flags[j] = 0;
-        if (out.case_id) out.case_id[j] = it.case_id[p];
-        uint32_t src = it.src[p];
-        uint8_t kind = it.kind[p];
-        if (osrc) osrc[j] = src;
-        if (okind) okind[j] = kind;
-        if (fin && C) {
-            float* o = fout + j * C;
-            if (kind <= 8) {
-                const float* s = fin + (size_t)src * C;
-                for (uint32_t c = 0; c < C; ++c) o[c] = s[c];
-            } else {
-                const uint32_t* mem = members + (size_t)src * 8;
-                for (uint32_t c = 0; c < C; ++c) {
-                    float s = 0.0f;
-                    for (int q = 0; q < 8; ++q) s = __fadd_rn(s, fin[(size_t)mem[q] * C + c]);
-                    o[c] = rule == 1 ? s : __fmul_rn(s, 0.125f);
-                }
-            }
         }
     }
 }
@@ -500,16 +489,13 @@ fl_domain_dev fl_domain_from_config(fl_ctx* ctx, const fl_adapt_config* cfg, voi
 }
 
 size_t fl_adapt_scratch_bytes(size_t n, uint64_t cap) {
-    size_t M = n * 8 + 8;
     size_t b = 0;
-    b += fl_align256(n * 8);                 // old keys
-    b += fl_align256(n * 4);                 // iota
+    b += fl_align256(n * 8);                 // cell keys (FACE6's hash table)
     b += fl_align256(cap * 16) + fl_align256(cap * 4);  // 16-byte-slot table + win
     b += 2 * fl_align256(n);                 // shadow, viol
     b += 4 * fl_align256(n * 4);             // leader, gid, group_of, cnt/off
     b += fl_align256(n * 4);                 // members (n/8 groups * 8)
     b += fl_align256(64);                    // counters
-    b += fl_align256(M * 4) * 5 + fl_align256(M) * 3 + fl_align256(M * 2);  // items
     b += fl_scan_scratch_bytes(n) + fl_align256(fl_locator_scratch_bytes(n)) + 4096;
     return b;
 }
@@ -565,7 +551,6 @@ struct AdaptWork {
     uint64_t* keys; uint64_t* tk; uint32_t* tv; uint32_t* win;
     uint8_t* shadow; uint8_t* viol;
     uint32_t* leader; uint32_t* gid; uint32_t* group_of; uint32_t* cnt; uint32_t* members; uint32_t* counters;
-    fl_items it;
     void* scan_scratch;
     void* locator;  // fl_locator_build scratch
 };
@@ -586,12 +571,6 @@ static AdaptWork carve_adapt(void* scratch, size_t n, bool with_case) {
     w.cnt = cv.take<uint32_t>(n);
     w.members = cv.take<uint32_t>(n + 8);
     w.counters = cv.take<uint32_t>(16);
-    size_t Mcap = n * 8 + 8;
-    w.it.x = cv.take<int32_t>(Mcap); w.it.y = cv.take<int32_t>(Mcap); w.it.z = cv.take<int32_t>(Mcap);
-    w.it.src = cv.take<uint32_t>(Mcap);
-    w.it.level = cv.take<uint8_t>(Mcap); w.it.state = cv.take<uint8_t>(Mcap); w.it.kind = cv.take<uint8_t>(Mcap);
-    w.it.case_id = with_case ? cv.take<uint16_t>(Mcap) : nullptr;
-    w.it.material = cv.take<uint32_t>(Mcap);
     w.scan_scratch = cv.take<char>(fl_scan_scratch_bytes(n));
     w.locator = cv.take<char>(fl_locator_scratch_bytes(n));
     return w;
@@ -658,9 +637,6 @@ int fl_adapt_prepare(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cf
     FL_CHECK_LAUNCH(ctx, "k_count_kinds");
     rc = fl_scan_u32_with(ctx, w.cnt, w.cnt, n, w.counters + 3, w.scan_scratch);
     if (rc) return rc;
-    k_emit<<<nb, kT, 0, ctx->stream>>>(md, dom, cfg->max_refinement_level, L.ids, w.cnt, w.leader, w.group_of,
-                                       w.it);
-    FL_CHECK_LAUNCH(ctx, "k_emit");
     uint32_t hc[6] = {0, 0, 0, 0, 0, 0};
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(hc, w.counters, 24, cudaMemcpyDeviceToHost, ctx->stream), "adapt counts");
     rc = fl_collect_device_status(ctx, "fl_adapt");
@@ -676,18 +652,21 @@ int fl_adapt_prepare(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cf
     return FL_OK;
 }
 
-// Phase 2: sort the emitted list by key and gather into `out` (capacity >= M).
+// Phase 2: the new cells straight into `out` (capacity >= M), in key order.
 int fl_adapt_finish(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, const fl_domain_dev& dom,
                     void* scratch, size_t M, const float* fields, uint32_t C, fl_mesh* out, float* out_fields,
                     uint32_t* osrc, uint8_t* okind, uint32_t* omembers, uint32_t num_groups) {
     size_t n = mesh->num_cells;
     if (n == 0 || M == 0) return FL_OK;
     AdaptWork w = carve_adapt(scratch, n, mesh->case_id != nullptr);
+    fl_mesh_dev md{mesh->x, mesh->y, mesh->z, mesh->level, mesh->state, mesh->flags, mesh->material,
+                   mesh->case_id, n};
     fl_mesh_out o{out->x, out->y, out->z, out->level, out->state, out->flags, out->material,
                   mesh->case_id ? out->case_id : nullptr};
-    k_gather<<<fl_blocks(M, kT, ctx->num_sms * 8), kT, 0, ctx->stream>>>(w.it, M, o, fields, out_fields, C,
-                                                                         cfg->averaging_rule, w.members, osrc, okind);
-    FL_CHECK_LAUNCH(ctx, "k_gather");
+    k_emit<<<fl_blocks(n, kT, ctx->num_sms * 8), kT, 0, ctx->stream>>>(
+        md, dom, cfg->max_refinement_level, fl_locator_ids(w.locator, n), w.cnt, w.leader, w.group_of, w.members, o,
+        osrc, okind, fields, out_fields, C, cfg->averaging_rule);
+    FL_CHECK_LAUNCH(ctx, "k_emit");
     if (omembers && num_groups)
         FL_TRY_CUDA(ctx, cudaMemcpyAsync(omembers, w.members, (size_t)num_groups * 32, cudaMemcpyDeviceToDevice,
                                          ctx->stream), "members copy");

@@ -3,14 +3,6 @@
 #include "common.cuh"
 #include "hash.cuh"
 
-// The new cells of a regrid, in key order.
-struct fl_items {
-    int32_t* x; int32_t* y; int32_t* z;
-    uint8_t* level; uint8_t* state; uint32_t* material; uint16_t* case_id;
-    uint32_t* src;   // survivor / parent index (kind 0..8) or group id (kind 9)
-    uint8_t* kind;   // 0..7 child index, 8 survivor, 9 merged parent
-};
-
 struct fl_mesh_out {
     int32_t* x; int32_t* y; int32_t* z;
     uint8_t* level; uint8_t* state; int32_t* flags; uint32_t* material; uint16_t* case_id;

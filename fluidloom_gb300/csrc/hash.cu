@@ -213,6 +213,8 @@ size_t fl_locator_scratch_bytes(size_t n) {
     return fl_align256(n * 8) + fl_align256(n * 4) + fl_align256((nb + 1) * 4) + 256 + fl_sort_scratch_bytes(n, 8);
 }
 
+uint32_t* fl_locator_ids(void* scratch, size_t n) { return (uint32_t*)((char*)scratch + fl_align256(n * 8)); }
+
 int fl_locator_build(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom, void* scratch, fl_locator* L,
                      int level_bound, bool in_key_order) {
     const size_t n = m.n;

@@ -224,6 +224,10 @@ size_t fl_locator_scratch_bytes(size_t n);
 // caller knows the mesh is in key order (saves the check and its host read).
 int fl_locator_build(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom, void* scratch, fl_locator* L,
                      int level_bound = -1, bool in_key_order = false);
+// The locator's run order (cell of each run in key order) inside the scratch
+// that fl_locator_build carved for n cells: the identity when the mesh was
+// already in key order.
+uint32_t* fl_locator_ids(void* scratch, size_t n);
 // nbr[(i*26 + k)*S + s] through the sorted locator; marks: n words of scratch.
 int fl_neighbours_sorted(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev& dom, const fl_locator& L,
                          int subslots, uint32_t* nbr, uint32_t* marks);
