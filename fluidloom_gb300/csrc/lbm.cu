@@ -685,38 +685,144 @@ __global__ void k_brick_table(size_t n, const uint32_t* __restrict__ nbr, const 
                               const int32_t* __restrict__ bz, const uint16_t* __restrict__ bcase,
                               const LbmCaseDev* __restrict__ cases, const uint8_t* __restrict__ mnear,
                               uint32_t* __restrict__ nb27, uint8_t* __restrict__ bclass) {
-    size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x; b < n; b += stride) {
-        int l = blevel[b];
-        int general = brick_near_sphere(cases[bcase[b]], bx[b], by[b], bz[b], l) | (mnear ? mnear[b] & 1 : 0);
-        for (int d = 0; d < 27; ++d) {
-            uint32_t e = (uint32_t)b;
-            if (d != 13) {
-                int k = d < 13 ? d : d - 1;
-                uint32_t nb = nbr[(b * 26 + k) * 4];
-                e = (nb != FL_INVALID_INDEX && blevel[nb] == l) ? nb : kSlow;
-                int dx = d % 3 - 1, dy = (d / 3) % 3 - 1, dz = d / 9 - 1;
-                bool corner = dx != 0 && dy != 0 && dz != 0;
-                if (!corner && e == kSlow) general = 1;
-            }
-            nb27[b * 28 + d] = e;
+    // one warp per brick: lane d < 27 resolves row entry d (lane 27 writes the
+    // padding word); the all-solid test spreads the 512 sites over the warp
+    const int lane = threadIdx.x & 31;
+    const size_t warps = ((size_t)gridDim.x * blockDim.x) >> 5;
+    for (size_t b = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < n; b += warps) {
+        const int l = blevel[b];
+        const LbmCaseDev& c = cases[bcase[b]];
+        uint32_t e = lane == 27 ? 0u : (uint32_t)b;
+        bool face_slow = false;
+        if (lane < 27 && lane != 13) {
+            const int k = lane < 13 ? lane : lane - 1;
+            const uint32_t nb = nbr[(b * 26 + k) * 4];
+            e = (nb != FL_INVALID_INDEX && blevel[nb] == l) ? nb : kSlow;
+            const int dx = lane % 3 - 1, dy = (lane / 3) % 3 - 1, dz = lane / 9 - 1;
+            face_slow = !(dx != 0 && dy != 0 && dz != 0) && e == kSlow;
         }
-        nb27[b * 28 + 27] = 0;
+        if (lane < 28) nb27[b * 28 + lane] = e;
+        int general = (__any_sync(0xFFFFFFFFu, face_slow) ? 1 : 0) |
+                      brick_near_sphere(c, bx[b], by[b], bz[b], l) | (mnear ? mnear[b] & 1 : 0);
         if (general) {  // all 512 sites solid: the brick only ever holds the rest equilibrium
-            const LbmCaseDev& c = cases[bcase[b]];
             bool all;
             if (c.mask) {
                 all = mnear && ((mnear[b] >> 1) & 1);
             } else {
-                all = c.has_sphere != 0;
-                for (int s = 0; s < 512 && all; ++s)
-                    all = solid_at(c, (int64_t)bx[b] * 8 + (s & 7), (int64_t)by[b] * 8 + ((s >> 3) & 7),
-                                   (int64_t)bz[b] * 8 + (s >> 6), l);
+                bool mine = c.has_sphere != 0;
+                for (int s = lane; s < 512 && mine; s += 32)
+                    mine = solid_at(c, (int64_t)bx[b] * 8 + (s & 7), (int64_t)by[b] * 8 + ((s >> 3) & 7),
+                                    (int64_t)bz[b] * 8 + (s >> 6), l);
+                all = __all_sync(0xFFFFFFFFu, mine);
             }
             if (all) general = 2;
         }
-        bclass[b] = (uint8_t)general;
+        if (lane == 0) bclass[b] = (uint8_t)general;
     }
+}
+
+// Small per-topology results read back by the host: bricks and fluid sites
+// per list bin (bin = level * 3 + class), the descriptor range of each level's
+// general bricks and an error word.
+constexpr int kBins = 3 * kMaxPoolLevels;
+struct TopoCounters {
+    uint32_t count[kBins];
+    uint32_t err;  // bit 0: a level above the pool maximum, bit 1: a case id out of range, bit 2: case ids out of order
+    uint32_t lvl_desc[kMaxPoolLevels + 1];
+    unsigned long long fluid[kBins];
+    unsigned long long desc64;  // descriptors, summed in 64 bits (the offsets are 32-bit)
+};
+
+// Per brick: its list bin as a sort key and its index as the value, the bin
+// counts, and the case ranges (a pool keeps its bricks in case order:
+// case_begin[c] = first brick of case c, case_begin[ncases] = n).
+__global__ void k_topo_bins(size_t n, const uint8_t* __restrict__ blevel, const uint8_t* __restrict__ bclass,
+                            const uint16_t* __restrict__ bcase, int maxL, uint32_t ncases,
+                            uint64_t* __restrict__ keys, uint32_t* __restrict__ ids, TopoCounters* tc,
+                            uint32_t* __restrict__ case_begin) {
+    __shared__ uint32_t h[kBins];
+    for (int i = threadIdx.x; i < kBins; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t rounds = (n + stride - 1) / stride;  // whole warps stay converged for the match below
+    for (size_t r = 0; r < rounds; ++r) {
+        const size_t i = r * stride + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+        uint32_t bin = 0xFFFFFFFFu;
+        if (i < n) {
+            int l = blevel[i], k = bclass[i];
+            k = k > 2 ? 1 : k;
+            if (l > maxL) {
+                atomicOr(&tc->err, 1u);
+                l = maxL;
+            }
+            bin = (uint32_t)(l * 3 + k);
+            keys[i] = bin;
+            ids[i] = (uint32_t)i;
+            const uint32_t c = bcase[i], prev = i ? bcase[i - 1] : 0u;
+            if (c >= ncases) {
+                atomicOr(&tc->err, 2u);
+            } else if (i && c < prev) {
+                atomicOr(&tc->err, 4u);
+            } else {
+                for (uint32_t cc = i ? prev + 1 : 0u; cc <= c; ++cc) case_begin[cc] = (uint32_t)i;
+                if (i == n - 1)
+                    for (uint32_t cc = c + 1; cc <= ncases; ++cc) case_begin[cc] = (uint32_t)n;
+            }
+        }
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, bin);
+        if (bin != 0xFFFFFFFFu && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&h[bin], __popc(peers));
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kBins; i += blockDim.x)
+        if (h[i]) atomicAdd(&tc->count[i], h[i]);
+}
+
+// Positions in the level lists of the general bricks, level by level:
+// general brick j of level l (base[l] <= j < base[l + 1]) sits at start[l] + j - base[l].
+struct GenTable {
+    uint32_t base[kMaxPoolLevels + 1];
+    uint32_t start[kMaxPoolLevels];
+    int levels;
+};
+
+__global__ void k_gen_positions(size_t ng, GenTable t, uint32_t* __restrict__ gen) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < ng; j += stride) {
+        int l = 0;
+        while (l + 1 < t.levels && j >= t.base[l + 1]) ++l;
+        gen[j] = t.start[l] + (uint32_t)(j - t.base[l]);
+    }
+}
+
+// Fluid sites per bin (interior bricks are all fluid, all-solid bricks none,
+// general bricks as counted by k_slow_table), the 64-bit descriptor total and
+// each level's first descriptor (gen_start[l] = first list position of the
+// level's general bricks; off holds n + 1 exclusive offsets).
+__global__ void k_topo_sums(size_t n, const uint8_t* __restrict__ blevel, const uint8_t* __restrict__ bclass,
+                            const uint32_t* __restrict__ fluid, const uint32_t* __restrict__ cnt,
+                            const uint32_t* __restrict__ off, GenTable t, int maxL, TopoCounters* tc) {
+    __shared__ unsigned long long h[kBins];
+    __shared__ unsigned long long dsum;
+    for (int i = threadIdx.x; i < kBins; i += blockDim.x) h[i] = 0ull;
+    if (threadIdx.x == 0) dsum = 0ull;
+    if (blockIdx.x == 0 && threadIdx.x <= maxL + 1)
+        tc->lvl_desc[threadIdx.x] = off[threadIdx.x <= maxL ? t.start[threadIdx.x] : (uint32_t)n];
+    __syncthreads();
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    unsigned long long dmine = 0ull;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        int l = blevel[i], k = bclass[i];
+        k = k > 2 ? 1 : k;
+        l = l > maxL ? maxL : l;
+        const uint32_t f = k == 1 ? fluid[i] : (k == 0 ? 512u : 0u);
+        if (f) atomicAdd(&h[l * 3 + k], (unsigned long long)f);
+        dmine += cnt[i];
+    }
+    if (dmine) atomicAdd(&dsum, dmine);
+    __syncthreads();
+    for (int i = threadIdx.x; i < kBins; i += blockDim.x)
+        if (h[i]) atomicAdd(&tc->fluid[i], h[i]);
+    if (threadIdx.x == 0 && dsum) atomicAdd(&tc->desc64, dsum);
 }
 
 __global__ void k_init_populations(float* f, size_t cap, size_t n, const uint16_t* bcase, const LbmCaseDev* cases) {
@@ -1180,6 +1286,7 @@ struct fl_pool {
     uint64_t num_desc = 0;
     std::vector<uint32_t> case_begin;
     uint32_t* d_case_begin = nullptr;
+    TopoCounters* d_topo = nullptr;       // k_topo_bins / k_topo_sums results
     uint2* d_chunks = nullptr;            // brick ranges of <= 1024 bricks, each within one case
     uint32_t* d_case_chunk = nullptr;     // per case: first chunk; [ncases] = end
     double* chunk_part = nullptr;
@@ -1320,7 +1427,11 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
     size_t n = P->mesh.num_cells;
     if (P->cap >= (1u << 23))  // descriptors address elements as brick * 512 + site in 32 bits
         return fl_set_error(ctx, FL_E_CAPACITY, "a pool holds fewer than 2^23 bricks");
-    int rc = fl_scratch_reserve(ctx, fl_align256(n * 4) + fl_locator_scratch_bytes(n));
+    const size_t ncases = P->cases.size();
+    // scratch: neighbour marks + the point locator, later the list sort keys,
+    // the sort's and the scan's own scratch
+    const size_t lists_bytes = fl_align256(n * 8) + fl_sort_scratch_bytes(n, 1) + fl_scan_scratch_bytes(n);
+    int rc = fl_scratch_reserve(ctx, std::max(fl_align256(n * 4) + fl_locator_scratch_bytes(n), lists_bytes));
     if (rc) return rc;
     fl_domain_dev dom = pool_domain(P);
     fl_mesh_dev md{P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.level, P->mesh.state, P->mesh.flags, P->mesh.material,
@@ -1339,44 +1450,61 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
             n, P->mesh.level, P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.case_id, P->d_cases, P->mnear);
         FL_CHECK_LAUNCH(ctx, "k_mask_near");
     }
-    k_brick_table<<<fl_blocks(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(
+    k_brick_table<<<fl_blocks(n * 32, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(
         n, P->nbr, P->mesh.level, P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.case_id, P->d_cases, mnear, P->nb27,
         P->bclass);
     FL_CHECK_LAUNCH(ctx, "k_brick_table");
-    // host-side lists (levels, classes and case ids are small: four bytes per brick)
-    std::vector<uint8_t> lv(n), cl(n);
-    std::vector<uint16_t> cs(n);
-    FL_TRY_CUDA(ctx, cudaMemcpyAsync(cl.data(), P->bclass, n, cudaMemcpyDeviceToHost, ctx->stream), "classes");
-    FL_TRY_CUDA(ctx, cudaMemcpyAsync(lv.data(), P->mesh.level, n, cudaMemcpyDeviceToHost, ctx->stream), "levels");
-    FL_TRY_CUDA(ctx, cudaMemcpyAsync(cs.data(), P->mesh.case_id, n * 2, cudaMemcpyDeviceToHost, ctx->stream), "cases");
+    // level lists: the bricks stably sorted by bin = level * 3 + class (interior,
+    // general, all-solid), so each level's classes follow one another in brick order
+    uint64_t* bin_keys = (uint64_t*)ctx->scratch;
+    void* sort_scratch = (char*)ctx->scratch + fl_align256(n * 8);
+    void* scan_scratch = (char*)sort_scratch + fl_sort_scratch_bytes(n, 1);
+    TopoCounters* tc = P->d_topo;
+    FL_TRY_CUDA(ctx, cudaMemsetAsync(tc, 0, sizeof(TopoCounters), ctx->stream), "topology counters");
+    k_topo_bins<<<fl_blocks(n, 256, ctx->num_sms * 4), 256, 0, ctx->stream>>>(
+        n, P->mesh.level, P->bclass, P->mesh.case_id, P->maxL, (uint32_t)ncases, bin_keys, P->list, tc,
+        P->d_case_begin);
+    FL_CHECK_LAUNCH(ctx, "k_topo_bins");
+    if (n == 0) FL_TRY_CUDA(ctx, cudaMemsetAsync(P->d_case_begin, 0, (ncases + 1) * 4, ctx->stream), "case ranges");
+    int bits = 1;
+    while ((1 << bits) < 3 * (P->maxL + 1)) ++bits;
+    rc = fl_sort_pairs_with(ctx, bin_keys, P->list, n, 0, bits, sort_scratch);
+    if (rc) return rc;
+    TopoCounters h{};
+    P->case_begin.assign(ncases + 1, 0);
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(&h, tc, sizeof(TopoCounters), cudaMemcpyDeviceToHost, ctx->stream), "counts");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->case_begin.data(), P->d_case_begin, (ncases + 1) * 4, cudaMemcpyDeviceToHost,
+                                     ctx->stream), "case ranges");
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "topology sync");
+    if (h.err & 1u) return fl_set_error(ctx, FL_E_INVALID_ARG, "brick level above the pool maximum");
+    if (h.err & 6u) return fl_set_error(ctx, FL_E_INVALID_ARG, "pool bricks not in case order");
     P->lvl_off.assign(P->maxL + 2, 0);
-    for (size_t i = 0; i < n; ++i) {
-        if (lv[i] > P->maxL) return fl_set_error(ctx, FL_E_INVALID_ARG, "brick level above the pool maximum");
-        P->lvl_off[lv[i] + 1]++;
-    }
-    for (int l = 0; l <= P->maxL; ++l) P->lvl_off[l + 1] += P->lvl_off[l];
-    // within a level: interior bricks, then general ones, then all-solid ones
     for (int k = 0; k < 3; ++k) {
         P->cls_off[k].assign(P->maxL + 1, 0);
         P->cls_cnt[k].assign(P->maxL + 1, 0);
     }
-    for (size_t i = 0; i < n; ++i) P->cls_cnt[cl[i] > 2 ? 1 : cl[i]][lv[i]]++;
+    GenTable gt{};
+    gt.levels = P->maxL + 1;
+    uint32_t run = 0, ng = 0;
     for (int l = 0; l <= P->maxL; ++l) {
-        P->cls_off[0][l] = P->lvl_off[l];
-        P->cls_off[1][l] = P->cls_off[0][l] + P->cls_cnt[0][l];
-        P->cls_off[2][l] = P->cls_off[1][l] + P->cls_cnt[1][l];
+        P->lvl_off[l] = run;
+        for (int k = 0; k < 3; ++k) {
+            P->cls_off[k][l] = run;
+            P->cls_cnt[k][l] = h.count[l * 3 + k];
+            run += h.count[l * 3 + k];
+        }
+        gt.base[l] = ng;
+        gt.start[l] = P->cls_off[1][l];
+        ng += P->cls_cnt[1][l];
     }
-    std::vector<uint32_t> list(n), fill[3] = {P->cls_off[0], P->cls_off[1], P->cls_off[2]};
-    for (size_t i = 0; i < n; ++i) list[fill[cl[i] > 2 ? 1 : cl[i]][lv[i]]++] = (uint32_t)i;
-    // general bricks' list positions (appended after the list in the same upload)
-    std::vector<uint32_t> gen;
-    for (int l = 0; l <= P->maxL; ++l)
-        for (uint32_t k = 0; k < P->cls_cnt[1][l]; ++k) gen.push_back(P->cls_off[1][l] + k);
-    const size_t ng = gen.size();
-    list.insert(list.end(), gen.begin(), gen.end());
-    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->list, list.data(), (n + ng) * 4, cudaMemcpyHostToDevice, ctx->stream), "list");
-    const uint32_t* d_gen = P->list + n;
+    gt.base[P->maxL + 1] = ng;
+    P->lvl_off[P->maxL + 1] = run;
+    if (run != n) return fl_set_error(ctx, FL_E_INVALID_ARG, "brick classes do not cover the pool");
+    uint32_t* d_gen = P->list + n;  // general bricks' list positions
+    if (ng) {
+        k_gen_positions<<<fl_blocks(ng, 256, ctx->num_sms * 4), 256, 0, ctx->stream>>>(ng, gt, d_gen);
+        FL_CHECK_LAUNCH(ctx, "k_gen_positions");
+    }
     FL_TRY_CUDA(ctx, cudaMemsetAsync(P->slow_cnt, 0, n * 4, ctx->stream), "descriptor counts");
     const unsigned tgrid = (unsigned)std::max<size_t>(1, std::min<size_t>(ng, (size_t)ctx->num_sms * 2));
     if (ng) {
@@ -1386,20 +1514,15 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
                                                             P->qmask, nullptr, nullptr, P->fluid, ctx->dev_status);
         FL_CHECK_LAUNCH(ctx, "k_slow_table count");
     }
-    P->case_begin.assign(P->cases.size() + 1, 0);
-    for (size_t i = 0; i < n; ++i) P->case_begin[cs[i] + 1]++;
-    for (size_t c = 0; c < P->cases.size(); ++c) P->case_begin[c + 1] += P->case_begin[c];
-    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->d_case_begin, P->case_begin.data(), P->case_begin.size() * 4,
-                                     cudaMemcpyHostToDevice, ctx->stream), "case ranges");
     {  // conservation-sum chunks
         std::vector<uint2> chunks;
-        std::vector<uint32_t> case_chunk(P->cases.size() + 1, 0);
-        for (size_t c = 0; c < P->cases.size(); ++c) {
+        std::vector<uint32_t> case_chunk(ncases + 1, 0);
+        for (size_t c = 0; c < ncases; ++c) {
             case_chunk[c] = (uint32_t)chunks.size();
             for (uint32_t b = P->case_begin[c]; b < P->case_begin[c + 1]; b += kChunkBricks)
                 chunks.push_back(make_uint2(b, std::min(b + kChunkBricks, P->case_begin[c + 1])));
         }
-        case_chunk[P->cases.size()] = (uint32_t)chunks.size();
+        case_chunk[ncases] = (uint32_t)chunks.size();
         P->nchunks = (uint32_t)chunks.size();
         if (P->nchunks)
             FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->d_chunks, chunks.data(), chunks.size() * sizeof(uint2),
@@ -1407,36 +1530,25 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
         FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->d_case_chunk, case_chunk.data(), case_chunk.size() * 4,
                                          cudaMemcpyHostToDevice, ctx->stream), "case chunks");
     }
-    // fluid sites per brick -> LUPs per level-0 step: interior bricks are all
-    // fluid, all-solid bricks none, general bricks counted by k_slow_table
-    std::vector<uint32_t> fl(n), sc(n + 1);
-    FL_TRY_CUDA(ctx, cudaMemcpyAsync(fl.data(), P->fluid, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "fluid");
-    FL_TRY_CUDA(ctx, cudaMemcpyAsync(sc.data(), P->slow_cnt, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "counts");
+    // stencil descriptors of the general class: offsets by a device scan over
+    // the list positions, words written by the second pass
+    rc = fl_scan_u32_with(ctx, P->slow_cnt, P->slow_off, n, P->slow_off + n, scan_scratch);
+    if (rc) return rc;
+    k_topo_sums<<<fl_blocks(n, 256, ctx->num_sms * 4), 256, 0, ctx->stream>>>(
+        n, P->mesh.level, P->bclass, P->fluid, P->slow_cnt, P->slow_off, gt, P->maxL, tc);
+    FL_CHECK_LAUNCH(ctx, "k_topo_sums");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(&h, tc, sizeof(TopoCounters), cudaMemcpyDeviceToHost, ctx->stream), "sums");
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "topology sync");
-    for (size_t i = 0; i < n; ++i)
-        if (cl[i] != 1) fl[i] = cl[i] == 0 ? 512u : 0u;
-    // stencil descriptors of the general class: offsets on the host, words on the device
-    uint64_t run = 0;
-    for (size_t i = 0; i < n; ++i) {
-        uint32_t c = sc[i];
-        sc[i] = (uint32_t)run;
-        run += c;
-    }
-    if (run >= (1ull << 32)) return fl_set_error(ctx, FL_E_CAPACITY, "more than 2^32 stencil descriptors");
-    sc[n] = (uint32_t)run;
-    P->num_desc = run;
-    P->lvl_desc.assign(P->maxL + 2, 0);
-    for (int l = 0; l <= P->maxL; ++l) P->lvl_desc[l] = sc[P->cls_off[1][l]];
-    P->lvl_desc[P->maxL + 1] = sc[n];
-    if (run > P->desc_cap) {
+    if (h.desc64 >= (1ull << 32)) return fl_set_error(ctx, FL_E_CAPACITY, "more than 2^32 stencil descriptors");
+    P->num_desc = h.desc64;
+    P->lvl_desc.assign(h.lvl_desc, h.lvl_desc + P->maxL + 2);
+    if (P->num_desc > P->desc_cap) {
         if (P->desc) cudaFreeAsync(P->desc, ctx->stream);
         if (P->pv) cudaFreeAsync(P->pv, ctx->stream);
-        P->desc_cap = run + run / 4 + 1024;
+        P->desc_cap = P->num_desc + P->num_desc / 4 + 1024;
         FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->desc, P->desc_cap * 8, ctx->stream), "stencil descriptors");
         FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->pv, P->desc_cap * 4, ctx->stream), "descriptor values");
     }
-    FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->slow_off, sc.data(), (n + 1) * 4, cudaMemcpyHostToDevice, ctx->stream),
-                "descriptor offsets");
     if (ng) {
         k_slow_table<true><<<tgrid, 512, 0, ctx->stream>>>(ng, d_gen, P->list, P->bclass, P->nbr, P->mesh.level,
                                                            P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.case_id,
@@ -1444,14 +1556,14 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
                                                            P->slow_off, P->desc, nullptr, ctx->dev_status);
         FL_CHECK_LAUNCH(ctx, "k_slow_table emit");
     }
-    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "descriptor sync");  // sc is freed on return
     P->lups = 0;
     for (int l = 0; l < 16; ++l) P->fluid_per_level[l] = P->fluid_cls[0][l] = P->fluid_cls[1][l] = P->fluid_cls[2][l] = 0;
-    for (size_t i = 0; i < n; ++i) {
-        P->lups += (uint64_t)fl[i] << lv[i];
-        P->fluid_per_level[lv[i]] += fl[i];
-        P->fluid_cls[cl[i] > 2 ? 1 : cl[i]][lv[i]] += fl[i];
-    }
+    for (int l = 0; l <= P->maxL; ++l)
+        for (int k = 0; k < 3; ++k) {
+            P->fluid_cls[k][l] = h.fluid[l * 3 + k];
+            P->fluid_per_level[l] += h.fluid[l * 3 + k];
+        }
+    for (int l = 0; l <= P->maxL; ++l) P->lups += P->fluid_per_level[l] << l;
     drop_graph(P);
     return fl_collect_device_status(ctx, "pool topology");
 }
@@ -1827,6 +1939,7 @@ int fl_pool_create(fl_ctx* ctx, const fl_lbm_case* cases, int ncases, fl_pool** 
     if (cudaMalloc(&P->d_cases, kMaxCases * sizeof(LbmCaseDev)) != cudaSuccess) return fail(FL_E_OOM);
     if (cudaMalloc(&P->d_dom, kMaxCases * sizeof(fl_domain_dev::Case)) != cudaSuccess) return fail(FL_E_OOM);
     if (cudaMalloc(&P->d_case_begin, (kMaxCases + 1) * 4) != cudaSuccess) return fail(FL_E_OOM);
+    if (cudaMalloc(&P->d_topo, sizeof(TopoCounters)) != cudaSuccess) return fail(FL_E_OOM);
     if (cudaMalloc(&P->d_case_chunk, (kMaxCases + 1) * 4) != cudaSuccess) return fail(FL_E_OOM);
     if (cudaMalloc(&P->case_max, kMaxCases * 4) != cudaSuccess) return fail(FL_E_OOM);
     if (cudaMalloc(&P->cons, kMaxCases * 32) != cudaSuccess) return fail(FL_E_OOM);
@@ -1891,6 +2004,7 @@ int fl_pool_destroy(fl_ctx* ctx, fl_pool* P) {
     if (P->d_cases) cudaFree(P->d_cases);
     if (P->d_dom) cudaFree(P->d_dom);
     if (P->d_case_begin) cudaFree(P->d_case_begin);
+    if (P->d_topo) cudaFree(P->d_topo);
     if (P->d_case_chunk) cudaFree(P->d_case_chunk);
     if (P->case_max) cudaFree(P->case_max);
     if (P->cons) cudaFree(P->cons);
