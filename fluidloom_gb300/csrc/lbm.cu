@@ -395,12 +395,11 @@ __device__ uint64_t resolve_source(const LbmCaseDev& c, const int32_t* bx, const
 }
 
 // Per general brick (one CTA of 512 threads per brick, thread = site; gen
-// lists the bricks' positions p in the level lists): COUNT writes the number
-// of descriptors to cnt[p], the brick's own-site solid mask (16 words), its
-// per-quad masks and its fluid-site count; EMIT writes the descriptors from
-// desc + off[p], quad-major, then q, then site.  Sites inside the sphere get
-// none: their relaxation ignores what they pulled.
-template <bool EMIT>
+// lists the bricks' positions p in the level lists): the number of
+// descriptors to cnt[p], the brick's own-site solid mask (16 words), the
+// solid bits of the brick and its halo (32 words, zero away from solids), its
+// per-quad masks and its fluid-site count.  Sites inside the sphere get no
+// descriptors: their relaxation ignores what they pulled.
 __global__ void __launch_bounds__(512, 2) k_slow_table(size_t ng, const uint32_t* __restrict__ gen,
                                                        const uint32_t* __restrict__ list,
                                                     const uint8_t* __restrict__ bclass, const uint32_t* __restrict__ nbr,
@@ -411,9 +410,7 @@ __global__ void __launch_bounds__(512, 2) k_slow_table(size_t ng, const uint32_t
                                                     const uint32_t* __restrict__ nb27,
                                                     const uint8_t* __restrict__ mnear, uint32_t* __restrict__ cnt,
                                                     uint32_t* __restrict__ smask, uint4* __restrict__ qmask,
-                                                    const uint32_t* __restrict__ off,
-                                                    uint64_t* __restrict__ desc, uint32_t* __restrict__ fluid,
-                                                    uint32_t* dev_status) {
+                                                    uint32_t* __restrict__ hsolid, uint32_t* __restrict__ fluid) {
     __shared__ BrickTopo T;
     __shared__ uint32_t warp_sum[16];
     __shared__ uint32_t solid_count;
@@ -448,6 +445,7 @@ __global__ void __launch_bounds__(512, 2) k_slow_table(size_t ng, const uint32_t
             }
         }
         __syncthreads();
+        if (t < 32) hsolid[(size_t)b * 32 + t] = T.solid[t];
         const int s = t, x = s & 7, y = (s >> 3) & 7, z = s >> 6;
         const bool own_solid = near && solid_bit(T.solid, x, y, z);
         uint32_t slow = 0;  // bit q: element (q, s) needs a descriptor
@@ -483,33 +481,90 @@ __global__ void __launch_bounds__(512, 2) k_slow_table(size_t ng, const uint32_t
 #pragma unroll
         for (int k = 0; k < 4; ++k) m[k] = __shfl_sync(0xFFFFFFFFu, slow, (lane & ~3) + k);
         const uint32_t qbase = __shfl_sync(0xFFFFFFFFu, before + (incl - mine), lane & ~3);
-        if (!EMIT) {
-            if (t == 0) cnt[p] = total;
-            if (lane == 0) {
-                smask[(size_t)b * 16 + wid] = solid_word;
-                atomicAdd(&solid_count, (uint32_t)__popc(solid_word));
-            }
-            if (i == 0) {
-                uint32_t wq[3] = {0u, 0u, 0u};
-                for (int q = 0; q < Q; ++q)
-                    for (int k = 0; k < 4; ++k)
-                        wq[(q * 4 + k) >> 5] |= ((m[k] >> q) & 1u) << ((q * 4 + k) & 31);
-                qmask[(size_t)b * 128 + (t >> 2)] = make_uint4(wq[0], wq[1], wq[2], qbase);
-            }
-        } else {
-            uint64_t* out = desc + off[p] + qbase;
-            while (slow) {
-                const int q = __ffs(slow) - 1;
-                slow &= slow - 1;
-                const uint32_t below = (1u << q) - 1u;
-                uint32_t rank = 0;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) rank += __popc(m[k] & below) + (k < i ? (m[k] >> q) & 1u : 0u);
-                out[rank] = resolve_source(c, bx, by, bz, b, q, l, s, G0, T, dev_status);
-            }
+        if (t == 0) cnt[p] = total;
+        if (lane == 0) {
+            smask[(size_t)b * 16 + wid] = solid_word;
+            atomicAdd(&solid_count, (uint32_t)__popc(solid_word));
+        }
+        if (i == 0) {
+            uint32_t wq[3] = {0u, 0u, 0u};
+            for (int q = 0; q < Q; ++q)
+                for (int k = 0; k < 4; ++k)
+                    wq[(q * 4 + k) >> 5] |= ((m[k] >> q) & 1u) << ((q * 4 + k) & 31);
+            qmask[(size_t)b * 128 + (t >> 2)] = make_uint4(wq[0], wq[1], wq[2], qbase);
         }
         __syncthreads();
-        if (!EMIT && t == 0) fluid[b] = 512u - solid_count;
+        if (t == 0) fluid[b] = 512u - solid_count;
+    }
+}
+
+// The descriptors of the general bricks, from the counting pass's tables: one
+// CTA per brick, one thread per descriptor.  Descriptor k of a brick lies in
+// the x-quad with the largest first offset <= k (qmask .w); inside the quad
+// they run q-major, then site.  Written to desc + off[p] + k.
+__global__ void __launch_bounds__(256, 4) k_slow_emit(size_t ng, const uint32_t* __restrict__ gen,
+                                                      const uint32_t* __restrict__ list,
+                                                      const uint32_t* __restrict__ nbr,
+                                                      const uint8_t* __restrict__ blevel,
+                                                      const int32_t* __restrict__ bx, const int32_t* __restrict__ by,
+                                                      const int32_t* __restrict__ bz,
+                                                      const uint16_t* __restrict__ bcase,
+                                                      const LbmCaseDev* __restrict__ cases,
+                                                      const uint8_t* __restrict__ mnear,
+                                                      const uint32_t* __restrict__ hsolid,
+                                                      const uint4* __restrict__ qmask,
+                                                      const uint32_t* __restrict__ cnt,
+                                                      const uint32_t* __restrict__ off,
+                                                      uint64_t* __restrict__ desc, uint32_t* dev_status) {
+    __shared__ BrickTopo T;
+    __shared__ uint4 Qm[128];
+    const int t = threadIdx.x;
+    for (size_t j = blockIdx.x; j < ng; j += gridDim.x) {
+        const size_t p = gen[j];
+        const uint32_t b = list[p];
+        const int l = blevel[b];
+        const LbmCaseDev& c = cases[bcase[b]];
+        if (t < 104) {
+            uint32_t nb = nbr[(size_t)b * 104 + t];
+            T.nbr[t] = nb;
+            T.nlv[t] = nb == FL_INVALID_INDEX ? 0xFF : blevel[nb];
+        }
+        if (t < 128) Qm[t] = qmask[(size_t)b * 128 + t];
+        if (t >= 128 && t < 160) T.solid[t - 128] = hsolid[(size_t)b * 32 + (t - 128)];
+        if (t == 160) T.near = brick_near_sphere(c, bx[b], by[b], bz[b], l) | (mnear ? mnear[b] & 1 : 0);
+        const uint32_t total = cnt[p];
+        uint64_t* out = desc + off[p];
+        const int64_t G0[3] = {(int64_t)bx[b] * 8, (int64_t)by[b] * 8, (int64_t)bz[b] * 8};
+        __syncthreads();
+        for (uint32_t k = t; k < total; k += blockDim.x) {
+            int lo = 0, hi = 127;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (Qm[mid].w <= k) lo = mid;
+                else hi = mid - 1;
+            }
+            const uint4 w = Qm[lo];
+            uint32_t r = k - w.w;
+            int q = 1, i = 0;
+            for (; q < Q; ++q) {
+                const uint32_t word = (q >> 3) == 0 ? w.x : ((q >> 3) == 1 ? w.y : w.z);
+                const uint32_t nib = (word >> ((q & 7) * 4)) & 0xFu;
+                const uint32_t cq = __popc(nib);
+                if (r < cq) {
+                    uint32_t v = nib;
+                    for (uint32_t skip = 0; skip < r; ++skip) v &= v - 1u;
+                    i = __ffs(v) - 1;
+                    break;
+                }
+                r -= cq;
+            }
+            if (q >= Q) {  // the quad masks do not hold k (not reached when they match cnt)
+                atomicAdd(dev_status + FL_DEVSTAT_BOUNDS, 1u);
+                q = 0;
+            }
+            out[k] = resolve_source(c, bx, by, bz, b, q, l, lo * 4 + i, G0, T, dev_status);
+        }
+        __syncthreads();
     }
 }
 
@@ -785,7 +840,7 @@ struct GenTable {
     int levels;
 };
 
-__global__ void k_gen_positions(size_t ng, GenTable t, uint32_t* __restrict__ gen) {
+__global__ void k_gen_positions(size_t ng, const __grid_constant__ GenTable t, uint32_t* __restrict__ gen) {
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < ng; j += stride) {
         int l = 0;
@@ -800,7 +855,8 @@ __global__ void k_gen_positions(size_t ng, GenTable t, uint32_t* __restrict__ ge
 // level's general bricks; off holds n + 1 exclusive offsets).
 __global__ void k_topo_sums(size_t n, const uint8_t* __restrict__ blevel, const uint8_t* __restrict__ bclass,
                             const uint32_t* __restrict__ fluid, const uint32_t* __restrict__ cnt,
-                            const uint32_t* __restrict__ off, GenTable t, int maxL, TopoCounters* tc) {
+                            const uint32_t* __restrict__ off, const __grid_constant__ GenTable t, int maxL,
+                            TopoCounters* tc) {
     __shared__ unsigned long long h[kBins];
     __shared__ unsigned long long dsum;
     for (int i = threadIdx.x; i < kBins; i += blockDim.x) h[i] = 0ull;
@@ -1279,6 +1335,7 @@ struct fl_pool {
     uint32_t* slow_off = nullptr;   // exclusive prefix of slow_cnt, n + 1 entries
     uint32_t* smask = nullptr;      // [cap][16] own-site solid bits of general bricks
     uint4* qmask = nullptr;         // [cap][128] per x-quad descriptor bits and offsets
+    uint32_t* hsolid = nullptr;     // [cap][32] solid bits of general bricks and their one-site halo
     uint64_t* desc = nullptr;       // stencil descriptors
     float* pv = nullptr;            // their values at the current sub-step
     size_t desc_cap = 0;
@@ -1387,6 +1444,7 @@ int alloc_brick_arrays(fl_ctx* ctx, fl_pool* P, size_t cap) {
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->slow_off, (cap + 1) * 4, ctx->stream), "pool descriptor offsets");
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->smask, cap * 64, ctx->stream), "pool solid masks");
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->qmask, cap * 128 * sizeof(uint4), ctx->stream), "pool quad masks");
+    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->hsolid, cap * 32 * 4, ctx->stream), "pool halo solid bits");
     const size_t max_chunks = cap / kChunkBricks + kMaxCases + 1;  // one partial chunk per case at most
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->d_chunks, max_chunks * sizeof(uint2), ctx->stream), "pool chunks");
     FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->chunk_part, max_chunks * 32, ctx->stream), "pool chunk sums");
@@ -1394,13 +1452,13 @@ int alloc_brick_arrays(fl_ctx* ctx, fl_pool* P, size_t cap) {
 }
 
 void free_brick_arrays(fl_ctx* ctx, fl_pool* P) {
-    void* ps[14] = {P->nbr,      P->list,     P->wmax,  P->part,  P->fluid,    P->nb27,       P->bclass,
-                    P->slow_cnt, P->slow_off, P->smask, P->qmask, P->d_chunks, P->chunk_part, P->mnear};
+    void* ps[15] = {P->nbr,      P->list,     P->wmax,  P->part,  P->fluid,    P->nb27,       P->bclass, P->slow_cnt,
+                    P->slow_off, P->smask, P->qmask, P->d_chunks, P->chunk_part, P->mnear, P->hsolid};
     for (void* p : ps)
         if (p) cudaFreeAsync(p, ctx->stream);
     P->nbr = nullptr; P->list = nullptr; P->wmax = nullptr; P->part = nullptr; P->fluid = nullptr;
     P->nb27 = nullptr; P->bclass = nullptr; P->slow_cnt = nullptr; P->slow_off = nullptr; P->smask = nullptr;
-    P->qmask = nullptr; P->d_chunks = nullptr; P->chunk_part = nullptr; P->mnear = nullptr;
+    P->qmask = nullptr; P->d_chunks = nullptr; P->chunk_part = nullptr; P->mnear = nullptr; P->hsolid = nullptr;
 }
 
 // The captured steps no longer match the pool: mark them stale.  The next
@@ -1508,10 +1566,9 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
     FL_TRY_CUDA(ctx, cudaMemsetAsync(P->slow_cnt, 0, n * 4, ctx->stream), "descriptor counts");
     const unsigned tgrid = (unsigned)std::max<size_t>(1, std::min<size_t>(ng, (size_t)ctx->num_sms * 2));
     if (ng) {
-        k_slow_table<false><<<tgrid, 512, 0, ctx->stream>>>(ng, d_gen, P->list, P->bclass, P->nbr, P->mesh.level,
-                                                            P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.case_id,
-                                                            P->d_cases, P->nb27, mnear, P->slow_cnt, P->smask,
-                                                            P->qmask, nullptr, nullptr, P->fluid, ctx->dev_status);
+        k_slow_table<<<tgrid, 512, 0, ctx->stream>>>(ng, d_gen, P->list, P->bclass, P->nbr, P->mesh.level, P->mesh.x,
+                                                     P->mesh.y, P->mesh.z, P->mesh.case_id, P->d_cases, P->nb27, mnear,
+                                                     P->slow_cnt, P->smask, P->qmask, P->hsolid, P->fluid);
         FL_CHECK_LAUNCH(ctx, "k_slow_table count");
     }
     {  // conservation-sum chunks
@@ -1550,11 +1607,11 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
         FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->pv, P->desc_cap * 4, ctx->stream), "descriptor values");
     }
     if (ng) {
-        k_slow_table<true><<<tgrid, 512, 0, ctx->stream>>>(ng, d_gen, P->list, P->bclass, P->nbr, P->mesh.level,
-                                                           P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.case_id,
-                                                           P->d_cases, P->nb27, mnear, nullptr, nullptr, nullptr,
-                                                           P->slow_off, P->desc, nullptr, ctx->dev_status);
-        FL_CHECK_LAUNCH(ctx, "k_slow_table emit");
+        const unsigned egrid = (unsigned)std::min<size_t>(ng, (size_t)ctx->num_sms * 4);
+        k_slow_emit<<<egrid, 256, 0, ctx->stream>>>(ng, d_gen, P->list, P->nbr, P->mesh.level, P->mesh.x, P->mesh.y,
+                                                    P->mesh.z, P->mesh.case_id, P->d_cases, mnear, P->hsolid, P->qmask,
+                                                    P->slow_cnt, P->slow_off, P->desc, ctx->dev_status);
+        FL_CHECK_LAUNCH(ctx, "k_slow_emit");
     }
     P->lups = 0;
     for (int l = 0; l < 16; ++l) P->fluid_per_level[l] = P->fluid_cls[0][l] = P->fluid_cls[1][l] = P->fluid_cls[2][l] = 0;
