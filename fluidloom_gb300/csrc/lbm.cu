@@ -166,7 +166,7 @@ struct StepArgs {
     const uint32_t* nbr;  // [n][26][4]
     const LbmCaseDev* cases;
     uint32_t* dev_status;
-    const uint64_t* desc;      // stencil descriptors of the general class (k_slow_table)
+    const uint64_t* desc;      // stencil descriptors of the general class (k_slow_emit)
     const uint32_t* desc_off;  // per list position: first descriptor; [count] = end
     const uint32_t* smask;     // [n][16]: own sites inside the sphere
     const uint4* qmask;        // [n][128]: per x-quad descriptor bits (4q + i) and first descriptor
@@ -394,111 +394,7 @@ __device__ uint64_t resolve_source(const LbmCaseDev& c, const int32_t* bx, const
     return make_desc(kSrcBounce, q, s, own);
 }
 
-// Per general brick (one CTA of 512 threads per brick, thread = site; gen
-// lists the bricks' positions p in the level lists): the number of
-// descriptors to cnt[p], the brick's own-site solid mask (16 words), the
-// solid bits of the brick and its halo (32 words, zero away from solids), its
-// per-quad masks and its fluid-site count.  Sites inside the sphere get no
-// descriptors: their relaxation ignores what they pulled.
-__global__ void __launch_bounds__(512, 2) k_slow_table(size_t ng, const uint32_t* __restrict__ gen,
-                                                       const uint32_t* __restrict__ list,
-                                                    const uint8_t* __restrict__ bclass, const uint32_t* __restrict__ nbr,
-                                                    const uint8_t* __restrict__ blevel, const int32_t* __restrict__ bx,
-                                                    const int32_t* __restrict__ by, const int32_t* __restrict__ bz,
-                                                    const uint16_t* __restrict__ bcase,
-                                                    const LbmCaseDev* __restrict__ cases,
-                                                    const uint32_t* __restrict__ nb27,
-                                                    const uint8_t* __restrict__ mnear, uint32_t* __restrict__ cnt,
-                                                    uint32_t* __restrict__ smask, uint4* __restrict__ qmask,
-                                                    uint32_t* __restrict__ hsolid, uint32_t* __restrict__ fluid) {
-    __shared__ BrickTopo T;
-    __shared__ uint32_t warp_sum[16];
-    __shared__ uint32_t solid_count;
-    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-    (void)bclass;
-    for (size_t j = blockIdx.x; j < ng; j += gridDim.x) {
-        const size_t p = gen[j];
-        const uint32_t b = list[p];
-        const int l = blevel[b];
-        const LbmCaseDev& c = cases[bcase[b]];
-        if (t < 104) {
-            uint32_t nb = nbr[(size_t)b * 104 + t];
-            T.nbr[t] = nb;
-            T.nlv[t] = nb == FL_INVALID_INDEX ? 0xFF : blevel[nb];
-        }
-        if (t < 27) T.nb27[t] = nb27[(size_t)b * 28 + t];
-        if (t < 32) T.solid[t] = 0u;
-        if (t == 32) T.near = brick_near_sphere(c, bx[b], by[b], bz[b], l) | (mnear ? mnear[b] & 1 : 0);
-        if (t == 0) solid_count = 0;  // thread 0 also reads it last, after the final barrier
-        __syncthreads();
-        const int near = T.near;
-        const int64_t G0[3] = {(int64_t)bx[b] * 8, (int64_t)by[b] * 8, (int64_t)bz[b] * 8};
-        if (near) {
-            for (int i = t; i < 1000; i += 512) {
-                int64_t G[3] = {G0[0] + i % 10 - 1, G0[1] + (i / 10) % 10 - 1, G0[2] + i / 100 - 1};
-                for (int ax = 0; ax < 3; ++ax) {
-                    if (!c.periodic[ax]) continue;
-                    int64_t N = ((int64_t)c.ext[ax] * 8) << l;
-                    G[ax] = G[ax] < 0 ? G[ax] + N : (G[ax] >= N ? G[ax] - N : G[ax]);
-                }
-                if (solid_at(c, G[0], G[1], G[2], l)) atomicOr(&T.solid[i >> 5], 1u << (i & 31));
-            }
-        }
-        __syncthreads();
-        if (t < 32) hsolid[(size_t)b * 32 + t] = T.solid[t];
-        const int s = t, x = s & 7, y = (s >> 3) & 7, z = s >> 6;
-        const bool own_solid = near && solid_bit(T.solid, x, y, z);
-        uint32_t slow = 0;  // bit q: element (q, s) needs a descriptor
-        if (!own_solid) {
-#pragma unroll
-            for (int q = 1; q < Q; ++q) {
-                const int xi = x - CXq(q), yi = y - CYq(q), zi = z - CZq(q);
-                const bool sl = T.nb27[((zi >> 3) + 1) * 9 + ((yi >> 3) + 1) * 3 + ((xi >> 3) + 1)] == kSlow ||
-                                (near && solid_bit(T.solid, xi, yi, zi));
-                slow |= (uint32_t)sl << q;
-            }
-        }
-        const uint32_t mine = __popc(slow);
-        // block exclusive scan of the per-site counts
-        uint32_t incl = mine;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if (lane >= o) incl += v;
-        }
-        if (lane == 31) warp_sum[wid] = incl;
-        const uint32_t solid_word = __ballot_sync(0xFFFFFFFFu, own_solid);
-        __syncthreads();
-        uint32_t before = 0, total = 0;
-        for (int k = 0; k < 16; ++k) {
-            uint32_t v = warp_sum[k];
-            before += k < wid ? v : 0u;
-            total += v;
-        }
-        // x-quads are threads 4u .. 4u + 3; a quad's elements are numbered q-major, then site
-        const int i = lane & 3;
-        uint32_t m[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) m[k] = __shfl_sync(0xFFFFFFFFu, slow, (lane & ~3) + k);
-        const uint32_t qbase = __shfl_sync(0xFFFFFFFFu, before + (incl - mine), lane & ~3);
-        if (t == 0) cnt[p] = total;
-        if (lane == 0) {
-            smask[(size_t)b * 16 + wid] = solid_word;
-            atomicAdd(&solid_count, (uint32_t)__popc(solid_word));
-        }
-        if (i == 0) {
-            uint32_t wq[3] = {0u, 0u, 0u};
-            for (int q = 0; q < Q; ++q)
-                for (int k = 0; k < 4; ++k)
-                    wq[(q * 4 + k) >> 5] |= ((m[k] >> q) & 1u) << ((q * 4 + k) & 31);
-            qmask[(size_t)b * 128 + (t >> 2)] = make_uint4(wq[0], wq[1], wq[2], qbase);
-        }
-        __syncthreads();
-        if (t == 0) fluid[b] = 512u - solid_count;
-    }
-}
-
-// The descriptors of the general bricks, from the counting pass's tables: one
+// The descriptors of the general bricks, from k_brick_table's tables: one
 // CTA per brick, one thread per descriptor.  Descriptor k of a brick lies in
 // the x-quad with the largest first offset <= k (qmask .w); inside the quad
 // they run q-major, then site.  Written to desc + off[p] + k.
@@ -732,17 +628,32 @@ __global__ void k_mask_near(size_t n, const uint8_t* __restrict__ blevel, const 
     }
 }
 
-// Per brick: the 27-entry same-level neighbour row (centre = the brick,
-// kSlow where the neighbour is missing or at another level) and the class
-// (1 = needs the general kernel).
-__global__ void k_brick_table(size_t n, const uint32_t* __restrict__ nbr, const uint8_t* __restrict__ blevel,
-                              const int32_t* __restrict__ bx, const int32_t* __restrict__ by,
-                              const int32_t* __restrict__ bz, const uint16_t* __restrict__ bcase,
-                              const LbmCaseDev* __restrict__ cases, const uint8_t* __restrict__ mnear,
-                              uint32_t* __restrict__ nb27, uint8_t* __restrict__ bclass) {
-    // one warp per brick: lane d < 27 resolves row entry d (lane 27 writes the
-    // padding word); the all-solid test spreads the 512 sites over the warp
+// One warp per brick.  Lane d < 27 resolves entry d of the brick's 27-entry
+// same-level neighbour row (centre = the brick, kSlow where the neighbour is
+// missing or at another level; lane 27 writes the padding word).  A brick
+// with a slow face or edge neighbour, or near a solid, is general (class 1);
+// a general brick whose 512 sites are all solid is class 2; the rest are
+// interior (class 0).  For each class-1 brick the warp then builds its
+// stencil-descriptor tables: the solid bits of the brick and its one-site
+// halo (hsolid, 32 words; zero away from solids), the own-site solid words
+// (smask, 16), per x-quad the 76 bits "element (q, site) needs a descriptor"
+// (bit 4q + i) with the quad's first descriptor (qmask, 128 entries, in site
+// order), the descriptor count (cnt, by brick) and the fluid sites.  Lane L
+// owns sites 16L .. 16L + 15, i.e. the quads 4L .. 4L + 3.  Own sites inside
+// a solid get no descriptors: their relaxation ignores what they pulled.
+__global__ void __launch_bounds__(256) k_brick_table(size_t n, const uint32_t* __restrict__ nbr,
+                                                     const uint8_t* __restrict__ blevel,
+                                                     const int32_t* __restrict__ bx, const int32_t* __restrict__ by,
+                                                     const int32_t* __restrict__ bz, const uint16_t* __restrict__ bcase,
+                                                     const LbmCaseDev* __restrict__ cases,
+                                                     const uint8_t* __restrict__ mnear, uint32_t* __restrict__ nb27,
+                                                     uint8_t* __restrict__ bclass, uint32_t* __restrict__ cnt,
+                                                     uint32_t* __restrict__ smask, uint4* __restrict__ qmask,
+                                                     uint32_t* __restrict__ hsolid, uint32_t* __restrict__ fluid) {
+    __shared__ uint32_t s_solid[8][32];
+    __shared__ uint32_t s_wq[8][32 * 12];
     const int lane = threadIdx.x & 31;
+    uint32_t* S = s_solid[(threadIdx.x >> 5) & 7];
     const size_t warps = ((size_t)gridDim.x * blockDim.x) >> 5;
     for (size_t b = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < n; b += warps) {
         const int l = blevel[b];
@@ -757,8 +668,9 @@ __global__ void k_brick_table(size_t n, const uint32_t* __restrict__ nbr, const 
             face_slow = !(dx != 0 && dy != 0 && dz != 0) && e == kSlow;
         }
         if (lane < 28) nb27[b * 28 + lane] = e;
-        int general = (__any_sync(0xFFFFFFFFu, face_slow) ? 1 : 0) |
-                      brick_near_sphere(c, bx[b], by[b], bz[b], l) | (mnear ? mnear[b] & 1 : 0);
+        const uint32_t slow_dirs = __ballot_sync(0xFFFFFFFFu, lane < 27 && e == kSlow);
+        const int near = brick_near_sphere(c, bx[b], by[b], bz[b], l) | (mnear ? mnear[b] & 1 : 0);
+        int general = (__any_sync(0xFFFFFFFFu, face_slow) ? 1 : 0) | near;
         if (general) {  // all 512 sites solid: the brick only ever holds the rest equilibrium
             bool all;
             if (c.mask) {
@@ -773,6 +685,78 @@ __global__ void k_brick_table(size_t n, const uint32_t* __restrict__ nbr, const 
             if (all) general = 2;
         }
         if (lane == 0) bclass[b] = (uint8_t)general;
+        if (general != 1) continue;  // uniform over the warp
+        const int64_t G0[3] = {(int64_t)bx[b] * 8, (int64_t)by[b] * 8, (int64_t)bz[b] * 8};
+        uint32_t word = 0;  // word `lane` of the 10^3 halo bits
+        if (near) {
+            for (int k = 0; k < 32; ++k) {
+                const int i = 32 * k + lane;
+                bool sd = false;
+                if (i < 1000) {
+                    int64_t G[3] = {G0[0] + i % 10 - 1, G0[1] + (i / 10) % 10 - 1, G0[2] + i / 100 - 1};
+                    for (int ax = 0; ax < 3; ++ax) {
+                        if (!c.periodic[ax]) continue;
+                        const int64_t N = ((int64_t)c.ext[ax] * 8) << l;
+                        G[ax] = G[ax] < 0 ? G[ax] + N : (G[ax] >= N ? G[ax] - N : G[ax]);
+                    }
+                    sd = solid_at(c, G[0], G[1], G[2], l);
+                }
+                const uint32_t wd = __ballot_sync(0xFFFFFFFFu, sd);
+                if (lane == k) word = wd;
+            }
+        }
+        S[lane] = word;
+        hsolid[b * 32 + lane] = word;
+        __syncwarp();
+        const int z = lane >> 2, y0 = 2 * (lane & 3);
+        uint32_t* W = s_wq[(threadIdx.x >> 5) & 7] + lane * 12;  // this lane's 4 quads x 3 mask words
+        uint32_t mine = 0, own16 = 0, qcs = 0;                    // qcs: per-quad counts (<= 72), a byte each
+#pragma unroll 1
+        for (int u = 0; u < 4; ++u) {  // quad 4L + u: row y0 + (u >> 1), x = 4 (u & 1) .. + 3
+            const int y = y0 + (u >> 1);
+            uint32_t w0 = 0u, w1 = 0u, w2 = 0u, qc = 0u;
+#pragma unroll 1
+            for (int k = 0; k < 4; ++k) {
+                const int x = 4 * (u & 1) + k;
+                const bool own_solid = near && solid_bit(S, x, y, z);
+                own16 |= (uint32_t)own_solid << (4 * u + k);
+                if (own_solid) continue;
+#pragma unroll
+                for (int q = 1; q < Q; ++q) {
+                    const int xi = x - CXq(q), yi = y - CYq(q), zi = z - CZq(q);
+                    const int dir = ((zi >> 3) + 1) * 9 + ((yi >> 3) + 1) * 3 + ((xi >> 3) + 1);
+                    const bool sl = ((slow_dirs >> dir) & 1u) || (near && solid_bit(S, xi, yi, zi));
+                    const uint32_t bit = (uint32_t)sl << ((q & 7) * 4 + k);  // bit 4q + k of the 96
+                    if ((q >> 3) == 0) w0 |= bit;
+                    else if ((q >> 3) == 1) w1 |= bit;
+                    else w2 |= bit;
+                    qc += sl ? 1u : 0u;
+                }
+            }
+            W[3 * u] = w0;
+            W[3 * u + 1] = w1;
+            W[3 * u + 2] = w2;
+            qcs |= qc << (8 * u);
+            mine += qc;
+        }
+        uint32_t incl = mine;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        uint32_t base = incl - mine;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            qmask[b * 128 + 4 * lane + u] = make_uint4(W[3 * u], W[3 * u + 1], W[3 * u + 2], base);
+            base += (qcs >> (8 * u)) & 0xFFu;
+        }
+        const uint32_t partner = __shfl_xor_sync(0xFFFFFFFFu, own16, 1);
+        if (!(lane & 1)) smask[b * 16 + (lane >> 1)] = own16 | (partner << 16);
+        const uint32_t nsolid = __reduce_add_sync(0xFFFFFFFFu, (uint32_t)__popc(own16));
+        if (lane == 31) cnt[b] = incl;
+        if (lane == 0) fluid[b] = 512u - nsolid;
+        __syncwarp();  // S is rewritten for the next brick
     }
 }
 
@@ -833,24 +817,30 @@ __global__ void k_topo_bins(size_t n, const uint8_t* __restrict__ blevel, const 
 }
 
 // Positions in the level lists of the general bricks, level by level:
-// general brick j of level l (base[l] <= j < base[l + 1]) sits at start[l] + j - base[l].
+// general brick j of level l (base[l] <= j < base[l + 1]) sits at
+// start[l] + j - base[l].  Its descriptor count moves from brick order (cnt_b)
+// to list order (cnt, zero elsewhere).
 struct GenTable {
     uint32_t base[kMaxPoolLevels + 1];
     uint32_t start[kMaxPoolLevels];
     int levels;
 };
 
-__global__ void k_gen_positions(size_t ng, const __grid_constant__ GenTable t, uint32_t* __restrict__ gen) {
+__global__ void k_gen_positions(size_t ng, const __grid_constant__ GenTable t, const uint32_t* __restrict__ list,
+                                const uint32_t* __restrict__ cnt_b, uint32_t* __restrict__ gen,
+                                uint32_t* __restrict__ cnt) {
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < ng; j += stride) {
         int l = 0;
         while (l + 1 < t.levels && j >= t.base[l + 1]) ++l;
-        gen[j] = t.start[l] + (uint32_t)(j - t.base[l]);
+        const uint32_t p = t.start[l] + (uint32_t)(j - t.base[l]);
+        gen[j] = p;
+        cnt[p] = cnt_b[list[p]];
     }
 }
 
 // Fluid sites per bin (interior bricks are all fluid, all-solid bricks none,
-// general bricks as counted by k_slow_table), the 64-bit descriptor total and
+// general bricks as counted by k_brick_table), the 64-bit descriptor total and
 // each level's first descriptor (gen_start[l] = first list position of the
 // level's general bricks; off holds n + 1 exclusive offsets).
 __global__ void k_topo_sums(size_t n, const uint8_t* __restrict__ blevel, const uint8_t* __restrict__ bclass,
@@ -1489,7 +1479,8 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
     // scratch: neighbour marks + the point locator, later the list sort keys,
     // the sort's and the scan's own scratch
     const size_t lists_bytes = fl_align256(n * 8) + fl_sort_scratch_bytes(n, 1) + fl_scan_scratch_bytes(n);
-    int rc = fl_scratch_reserve(ctx, std::max(fl_align256(n * 4) + fl_locator_scratch_bytes(n), lists_bytes));
+    int rc = fl_scratch_reserve(ctx, std::max(fl_align256(n * 4) + fl_locator_scratch_bytes(n),
+                                              lists_bytes + fl_align256(n * 4)));
     if (rc) return rc;
     fl_domain_dev dom = pool_domain(P);
     fl_mesh_dev md{P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.level, P->mesh.state, P->mesh.flags, P->mesh.material,
@@ -1508,15 +1499,18 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
             n, P->mesh.level, P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.case_id, P->d_cases, P->mnear);
         FL_CHECK_LAUNCH(ctx, "k_mask_near");
     }
-    k_brick_table<<<fl_blocks(n * 32, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(
-        n, P->nbr, P->mesh.level, P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.case_id, P->d_cases, mnear, P->nb27,
-        P->bclass);
-    FL_CHECK_LAUNCH(ctx, "k_brick_table");
-    // level lists: the bricks stably sorted by bin = level * 3 + class (interior,
-    // general, all-solid), so each level's classes follow one another in brick order
+    // classes and descriptor tables (the locator's scratch is free again: the
+    // per-brick descriptor counts go behind the list-building scratch)
     uint64_t* bin_keys = (uint64_t*)ctx->scratch;
     void* sort_scratch = (char*)ctx->scratch + fl_align256(n * 8);
     void* scan_scratch = (char*)sort_scratch + fl_sort_scratch_bytes(n, 1);
+    uint32_t* cnt_b = (uint32_t*)((char*)ctx->scratch + lists_bytes);
+    k_brick_table<<<fl_blocks(n * 32, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(
+        n, P->nbr, P->mesh.level, P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.case_id, P->d_cases, mnear, P->nb27,
+        P->bclass, cnt_b, P->smask, P->qmask, P->hsolid, P->fluid);
+    FL_CHECK_LAUNCH(ctx, "k_brick_table");
+    // level lists: the bricks stably sorted by bin = level * 3 + class (interior,
+    // general, all-solid), so each level's classes follow one another in brick order
     TopoCounters* tc = P->d_topo;
     FL_TRY_CUDA(ctx, cudaMemsetAsync(tc, 0, sizeof(TopoCounters), ctx->stream), "topology counters");
     k_topo_bins<<<fl_blocks(n, 256, ctx->num_sms * 4), 256, 0, ctx->stream>>>(
@@ -1559,17 +1553,11 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
     P->lvl_off[P->maxL + 1] = run;
     if (run != n) return fl_set_error(ctx, FL_E_INVALID_ARG, "brick classes do not cover the pool");
     uint32_t* d_gen = P->list + n;  // general bricks' list positions
-    if (ng) {
-        k_gen_positions<<<fl_blocks(ng, 256, ctx->num_sms * 4), 256, 0, ctx->stream>>>(ng, gt, d_gen);
-        FL_CHECK_LAUNCH(ctx, "k_gen_positions");
-    }
     FL_TRY_CUDA(ctx, cudaMemsetAsync(P->slow_cnt, 0, n * 4, ctx->stream), "descriptor counts");
-    const unsigned tgrid = (unsigned)std::max<size_t>(1, std::min<size_t>(ng, (size_t)ctx->num_sms * 2));
     if (ng) {
-        k_slow_table<<<tgrid, 512, 0, ctx->stream>>>(ng, d_gen, P->list, P->bclass, P->nbr, P->mesh.level, P->mesh.x,
-                                                     P->mesh.y, P->mesh.z, P->mesh.case_id, P->d_cases, P->nb27, mnear,
-                                                     P->slow_cnt, P->smask, P->qmask, P->hsolid, P->fluid);
-        FL_CHECK_LAUNCH(ctx, "k_slow_table count");
+        k_gen_positions<<<fl_blocks(ng, 256, ctx->num_sms * 4), 256, 0, ctx->stream>>>(ng, gt, P->list, cnt_b, d_gen,
+                                                                                     P->slow_cnt);
+        FL_CHECK_LAUNCH(ctx, "k_gen_positions");
     }
     {  // conservation-sum chunks
         std::vector<uint2> chunks;
