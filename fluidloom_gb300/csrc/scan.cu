@@ -28,8 +28,9 @@ constexpr unsigned long long kFlagMask = 3ull << 62;
 __device__ __forceinline__ unsigned long long ld_status(const unsigned long long* p) {
     return *(volatile const unsigned long long*)p;
 }
+// A status word carries its flag and its value together, so publishing it
+// needs no fence against other stores.
 __device__ __forceinline__ void st_status(unsigned long long* p, unsigned long long v) {
-    __threadfence();
     *(volatile unsigned long long*)p = v;
 }
 

@@ -122,11 +122,10 @@ __global__ void __launch_bounds__(kThreads, 4) k_onesweep(const uint64_t* __rest
         // publish aggregate, look back, publish inclusive
         uint32_t* st = status + (size_t)tile * kRadix + d;
         uint32_t prefix = 0;
+        // a status word carries its own value: no fence orders it after other data
         if (tile == 0) {
-            __threadfence();
             *(volatile uint32_t*)st = kFlagInc | run;
         } else {
-            __threadfence();
             *(volatile uint32_t*)st = kFlagAgg | run;
             int t = tile - 1;
             unsigned spins = 0;
@@ -144,7 +143,6 @@ __global__ void __launch_bounds__(kThreads, 4) k_onesweep(const uint64_t* __rest
                 if ((s & kFlagMask) == kFlagInc) break;
                 --t;
             }
-            __threadfence();
             *(volatile uint32_t*)st = kFlagInc | ((prefix + run) & kValMask);
         }
         s_glob[d] = bin_off[d] + prefix;
