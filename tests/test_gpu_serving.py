@@ -73,6 +73,29 @@ def test_add_remove_and_per_case_regrid_match_solo(ctx):
     assert info.num_active_cases == 3
 
 
+def test_pool_emptied_and_refilled(ctx):
+    """Every case leaves (a pool of no bricks: empty level lists, case ranges and
+    descriptor tables), the pool steps and regrids empty, then a new case joins
+    and runs as it does alone."""
+    from fluidloom_gb300.lbm import Pool
+    a, b, c = _cases()
+    mix = Pool(ctx, [a, b])
+    mix.step(2)
+    mix.remove_cases([0, 1])
+    info = mix.info()
+    assert info.num_bricks == 0 and info.fluid_lups_per_step == 0 and info.num_active_cases == 0
+    mix.step(2)
+    mix.regrid()
+    ids = mix.add_cases([c])
+    solo = Pool(ctx, [c])
+    for p in (mix, solo):
+        p.step(3)
+        p.regrid()
+        p.step(1)
+    _same(mix, ids[0], solo, 0)
+    assert mix.info().fluid_lups_per_step == solo.info().fluid_lups_per_step
+
+
 def test_served_loop_matches_solo_runs(ctx):
     """The serving loop (admission at regrid boundaries, shared regrids, removal at
     completion) leaves every job with the state of its solo run."""
