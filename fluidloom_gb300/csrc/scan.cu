@@ -76,9 +76,11 @@ __global__ void k_lookback_probe(unsigned long long* status, uint32_t* dev_statu
     lookback_limited(status, 1, dev_status, limit);
 }
 
-template <typename Load>
+// VEC: `in` and `out` are 16-byte aligned plain arrays; full tiles then move
+// each thread's 16 items as four 128-bit loads and stores.
+template <bool VEC = false, typename Load>
 __device__ void scan_tile(Load load, uint32_t* __restrict__ out, size_t n, unsigned long long* status,
-                          unsigned* ticket, uint32_t* total, uint32_t* dev_status) {
+                          unsigned* ticket, uint32_t* total, uint32_t* dev_status, const uint32_t* in = nullptr) {
     __shared__ int s_tile;
     __shared__ uint32_t s_warp[kThreads / 32];
     __shared__ uint32_t s_prefix;
@@ -89,11 +91,23 @@ __device__ void scan_tile(Load load, uint32_t* __restrict__ out, size_t n, unsig
     // blocked arrangement: thread t owns items [t*kItems, t*kItems+kItems)
     uint32_t v[kItems];
     uint32_t sum = 0;
+    const bool full = VEC && base + kTile <= n;
+    if (full) {
+        const uint4* p4 = (const uint4*)(in + base + (size_t)threadIdx.x * kItems);
 #pragma unroll
-    for (int i = 0; i < kItems; ++i) {
-        size_t g = base + (size_t)threadIdx.x * kItems + i;
-        v[i] = g < n ? load(g) : 0u;
-        sum += v[i];
+        for (int j = 0; j < kItems / 4; ++j) {
+            const uint4 a = __ldg(p4 + j);
+            v[4 * j] = a.x; v[4 * j + 1] = a.y; v[4 * j + 2] = a.z; v[4 * j + 3] = a.w;
+        }
+#pragma unroll
+        for (int i = 0; i < kItems; ++i) sum += v[i];
+    } else {
+#pragma unroll
+        for (int i = 0; i < kItems; ++i) {
+            size_t g = base + (size_t)threadIdx.x * kItems + i;
+            v[i] = g < n ? load(g) : 0u;
+            sum += v[i];
+        }
     }
     // block exclusive scan of per-thread sums
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -128,11 +142,24 @@ __device__ void scan_tile(Load load, uint32_t* __restrict__ out, size_t n, unsig
     }
     __syncthreads();
     uint32_t run = s_prefix + s_warp[warp] + (incl - sum);
+    if (full) {
+        uint4* o4 = (uint4*)(out + base + (size_t)threadIdx.x * kItems);
 #pragma unroll
-    for (int i = 0; i < kItems; ++i) {
-        size_t g = base + (size_t)threadIdx.x * kItems + i;
-        if (g < n) out[g] = run;
-        run += v[i];
+        for (int j = 0; j < kItems / 4; ++j) {
+            uint4 a;
+            a.x = run; run += v[4 * j];
+            a.y = run; run += v[4 * j + 1];
+            a.z = run; run += v[4 * j + 2];
+            a.w = run; run += v[4 * j + 3];
+            o4[j] = a;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < kItems; ++i) {
+            size_t g = base + (size_t)threadIdx.x * kItems + i;
+            if (g < n) out[g] = run;
+            run += v[i];
+        }
     }
 }
 
@@ -141,10 +168,11 @@ struct LoadU32 {
     __device__ uint32_t operator()(size_t i) const { return __ldg(p + i); }
 };
 
+template <bool VEC>
 __global__ void __launch_bounds__(kThreads) k_scan(const uint32_t* in, uint32_t* out, size_t n,
                                                    unsigned long long* status, unsigned* ticket, uint32_t* total,
                                                    uint32_t* dev_status) {
-    scan_tile(LoadU32{in}, out, n, status, ticket, total, dev_status);
+    scan_tile<VEC>(LoadU32{in}, out, n, status, ticket, total, dev_status, in);
 }
 
 // CompactionEngine::compactAndPermute predicate (CompactionEngine.cpp:51-56).
@@ -222,7 +250,11 @@ int fl_scan_u32_with(fl_ctx* ctx, const uint32_t* in, uint32_t* out, size_t n, u
     unsigned long long* status = (unsigned long long*)scratch;
     unsigned* ticket = (unsigned*)((char*)scratch + fl_align256(tiles * 8 + 8));
     FL_TRY_CUDA(ctx, cudaMemsetAsync(scratch, 0, fl_scan_scratch_bytes(n), ctx->stream), "scan status clear");
-    k_scan<<<(unsigned)tiles, kThreads, 0, ctx->stream>>>(in, out, n, status, ticket, total, ctx->dev_status);
+    // in == out (an in-place scan) is fine: each thread reads its items before writing them
+    if ((((uintptr_t)in | (uintptr_t)out) & 15u) == 0)
+        k_scan<true><<<(unsigned)tiles, kThreads, 0, ctx->stream>>>(in, out, n, status, ticket, total, ctx->dev_status);
+    else
+        k_scan<false><<<(unsigned)tiles, kThreads, 0, ctx->stream>>>(in, out, n, status, ticket, total, ctx->dev_status);
     FL_CHECK_LAUNCH(ctx, "k_scan");
     return FL_OK;
 }
@@ -378,7 +410,10 @@ extern "C" int fl_scan_exclusive_u32_noalloc(const uint32_t* in, uint32_t* out, 
     // the array keeps the previous call's contents: clear the words this call reads as zero
     if (cudaMemsetAsync(status, 0, tiles * 8, st) != cudaSuccess) return FL_E_CUDA;
     if (cudaMemsetAsync(ticket, 0, 256 + FL_DEVSTAT_WORDS * 4, st) != cudaSuccess) return FL_E_CUDA;
-    k_scan<<<(unsigned)tiles, kThreads, 0, st>>>(in, out, n, status, ticket, total, timeout);
+    if ((((uintptr_t)in | (uintptr_t)out) & 15u) == 0)
+        k_scan<true><<<(unsigned)tiles, kThreads, 0, st>>>(in, out, n, status, ticket, total, timeout);
+    else
+        k_scan<false><<<(unsigned)tiles, kThreads, 0, st>>>(in, out, n, status, ticket, total, timeout);
     if (cudaGetLastError() != cudaSuccess) return FL_E_CUDA;
     uint32_t expired = 0;  // a pageable destination makes this copy wait for the scan
     if (cudaMemcpyAsync(&expired, timeout + FL_DEVSTAT_TIMEOUT, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess)

@@ -43,6 +43,22 @@ def test_scan_in_place_wraps(ctx):
     np.testing.assert_array_equal(da.to_host(), want)
 
 
+def test_scan_unaligned_pointers(ctx):
+    """Input and output not 16-byte aligned: the per-item path of every tile."""
+    n = 100_003
+    a = np.random.default_rng(5).integers(0, 1000, n + 1).astype(np.uint32)
+    da = D(ctx, a)
+    do = E(ctx, (n + 2,), np.uint32)
+    tot = E(ctx, (1,), np.uint32)
+    ctx.call("fl_scan_exclusive_u32", ctypes.c_void_p(da.ptr.value + 4), ctypes.c_void_p(do.ptr.value + 8), n,
+             tot.ptr)
+    src = np.ascontiguousarray(a[1:])
+    want = np.empty(n, np.uint32)
+    t = O.load().or_scan_exclusive_u32(O.ptr(src), O.ptr(want), n)
+    np.testing.assert_array_equal(do.to_host()[2:], want)
+    assert int(tot.to_host()[0]) == t
+
+
 def _sort(ctx, k, v, b0=0, b1=64):
     dk, dv = D(ctx, k), D(ctx, v)
     ctx.call("fl_sort_pairs_u64_u32", dk.ptr, dv.ptr, len(k), b0, b1)
