@@ -841,7 +841,7 @@ __global__ void k_gen_positions(size_t ng, const __grid_constant__ GenTable t, c
 
 // Fluid sites per bin (interior bricks are all fluid, all-solid bricks none,
 // general bricks as counted by k_brick_table), the 64-bit descriptor total and
-// each level's first descriptor (gen_start[l] = first list position of the
+// each level's first descriptor (t.start[l] = first list position of the
 // level's general bricks; off holds n + 1 exclusive offsets).
 __global__ void k_topo_sums(size_t n, const uint8_t* __restrict__ blevel, const uint8_t* __restrict__ bclass,
                             const uint32_t* __restrict__ fluid, const uint32_t* __restrict__ cnt,
@@ -1576,7 +1576,7 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
                                          cudaMemcpyHostToDevice, ctx->stream), "case chunks");
     }
     // stencil descriptors of the general class: offsets by a device scan over
-    // the list positions, words written by the second pass
+    // the list positions, words written by k_slow_emit
     rc = fl_scan_u32_with(ctx, P->slow_cnt, P->slow_off, n, P->slow_off + n, scan_scratch);
     if (rc) return rc;
     k_topo_sums<<<fl_blocks(n, 256, ctx->num_sms * 4), 256, 0, ctx->stream>>>(
