@@ -217,55 +217,88 @@ __device__ __forceinline__ uint32_t sibling_of(const fl_probe& P, const fl_mesh_
     return j;
 }
 
-// Leaders, one warp per candidate: 32 cells are screened a lane each, then
-// each candidate is checked by the whole warp -- lanes 0-7 locate its eight
-// siblings (all must be mergeable leaves of its level) and, for the FULL26
-// merge condition, the 98 probe points around the octet are spread over the
-// lanes: no leaf touching the octet from outside may end above its level.
-// The probe points take, per axis, only five coordinates -- the last fine
-// point below the octet, the first and last of its lower cell, the first of
-// its upper cell, the first point above -- so the 98 combinations with at
-// least one outside coordinate are exactly the distinct probes outside the
-// octet (the 27 others lie inside it).
+// Leaders: a warp screens 32 cells, a lane each, then checks the chunk's
+// candidates four at a time -- lanes 8s .. 8s + 7 locate the eight siblings of
+// the s-th (all must be mergeable leaves of its level) -- and, for the FULL26
+// merge condition, spreads the 98 probe points around each surviving octet
+// over the lanes, the candidates' points one after another: no leaf touching
+// an octet from outside may end above its level.  The probe points take, per
+// axis, only five coordinates -- the last fine point below the octet, the
+// first and last of its lower cell, the first of its upper cell, the first
+// point above -- so the 98 combinations with at least one outside coordinate
+// are exactly the distinct probes outside the octet (the 27 others lie inside
+// it).
 __global__ void __launch_bounds__(kT) k_leaders(fl_mesh_dev m, fl_domain_dev dom, fl_locator L, int min_level,
                                                 int check26, const uint8_t* __restrict__ shadow,
                                                 uint32_t* __restrict__ is_leader) {
     __shared__ uint8_t t1[96];
     __shared__ uint16_t t3c[12 * 512];
+    __shared__ uint8_t surf[98];  // the outside points k = ix + 5 iy + 25 iz of the 5^3 grid
     fl_keys_fill_tables_cat(t1, t3c);
+    if (threadIdx.x == 0) {
+        int e = 0;
+        for (int k = 0; k < 125; ++k) {
+            const int ix = k % 5, iy = (k / 5) % 5, iz = k / 25;
+            if (ix == 0 || ix == 4 || iy == 0 || iy == 4 || iz == 0 || iz == 4) surf[e++] = (uint8_t)k;
+        }
+    }
     __syncthreads();
     const fl_probe P = fl_probe_make(t1, t3c, L, dom);
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, grp = lane >> 3;
     const size_t warps = (size_t)gridDim.x * (blockDim.x >> 5);
     for (size_t base = ((size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; base < m.n;
          base += warps * 32) {
         const size_t mine = base + lane;
         const bool cand = mine < m.n && merge_candidate(m, mine, min_level);
         if (mine < m.n && !cand) is_leader[mine] = 0u;
-        for (unsigned cm = __ballot_sync(0xFFFFFFFFu, cand); cm; cm &= cm - 1) {
-            const size_t i = base + (__ffs(cm) - 1);
+        unsigned cm = __ballot_sync(0xFFFFFFFFu, cand);
+        while (cm) {
+            const int n4 = min(__popc(cm), 4);  // candidates of this round
+            unsigned pick = cm;
+            for (int s = 0; s < grp && pick; ++s) pick &= pick - 1;
+            for (int s = 0; s < 4 && cm; ++s) cm &= cm - 1;
+            const bool have = grp < n4;
+            const size_t i = have ? base + (__ffs(pick) - 1) : 0;
             bool ok = true;
             uint32_t j = FL_INVALID_INDEX;
-            if (lane < 8) j = sibling_of(P, m, dom, i, lane, &ok);
-            bool leader = __all_sync(0xFFFFFFFFu, ok);
-            if (leader && check26) {
-                uint32_t mem[8];
-                for (int c = 0; c < 8; ++c) mem[c] = __shfl_sync(0xFFFFFFFFu, j, c);
-                const uint16_t cs = m.case_id ? m.case_id[i] : 0;
-                const fl_domain_dev::Case& d = dom.c[m.case_id ? cs : 0];
-                const int l = m.level[i];
-                const int sh = dom.anchor_level - l;
-                const int32_t size = 1 << sh;
-                const int32_t b[3] = {m.x[i] << sh, m.y[i] << sh, m.z[i] << sh};
-                bool bad = false;
-                for (int k = lane; k < 125; k += 32) {
-                    const int ix = k % 5, iy = (k / 5) % 5, iz = k / 25;
-                    if (!(ix == 0 || ix == 4 || iy == 0 || iy == 4 || iz == 0 || iz == 4)) continue;
-                    const int id[3] = {ix, iy, iz};
+            if (have) j = sibling_of(P, m, dom, i, lane & 7, &ok);
+            const unsigned okm = __ballot_sync(0xFFFFFFFFu, ok);
+            unsigned lead4 = 0;  // bit s: candidate s has eight mergeable siblings
+            for (int s = 0; s < n4; ++s)
+                if (((okm >> (8 * s)) & 0xFFu) == 0xFFu) lead4 |= 1u << s;
+            unsigned bad4 = 0;  // bit s: a probe of candidate s found a leaf ending above its level
+            if (lead4 && check26) {
+                // per-candidate values, held by every lane of its group
+                const uint16_t cs_m = have && m.case_id ? m.case_id[i] : 0;
+                const int l_m = have ? m.level[i] : 0;
+                const int sh_m = dom.anchor_level - l_m;
+                const int32_t b_m[3] = {have ? m.x[i] << sh_m : 0, have ? m.y[i] << sh_m : 0,
+                                        have ? m.z[i] << sh_m : 0};
+                const int nc = __popc(lead4);
+                for (int e0 = 0; e0 < nc * 98; e0 += 32) {
+                    const int e = e0 + lane;
+                    const bool act = e < nc * 98;
+                    int t = act ? e / 98 : 0;  // t-th surviving candidate ...
+                    unsigned lm = lead4;
+                    for (int k = 0; k < t; ++k) lm &= lm - 1;
+                    const int s = __ffs(lm) - 1;  // ... is candidate s
+                    const int src = 8 * s;
+                    const uint16_t cs = (uint16_t)__shfl_sync(0xFFFFFFFFu, (int)cs_m, src);
+                    const int l = __shfl_sync(0xFFFFFFFFu, l_m, src);
+                    const int32_t b3[3] = {__shfl_sync(0xFFFFFFFFu, b_m[0], src), __shfl_sync(0xFFFFFFFFu, b_m[1], src),
+                                           __shfl_sync(0xFFFFFFFFu, b_m[2], src)};
+                    uint32_t mem[8];
+                    for (int c = 0; c < 8; ++c) mem[c] = __shfl_sync(0xFFFFFFFFu, j, src + c);
+                    if (!act) continue;
+                    const fl_domain_dev::Case& d = dom.c[m.case_id ? cs : 0];
+                    const int32_t size = 1 << (dom.anchor_level - l);
+                    const int k = surf[e - t * 98];
+                    const int id[3] = {k % 5, (k / 5) % 5, k / 25};
                     int32_t p[3];
                     for (int a = 0; a < 3; ++a) {
-                        const int t = id[a];
-                        p[a] = t == 0 ? b[a] - 1 : (t == 1 ? b[a] : (t == 2 ? b[a] + size - 1 : (t == 3 ? b[a] + size : b[a] + 2 * size)));
+                        const int u = id[a];
+                        p[a] = u == 0 ? b3[a] - 1
+                                      : (u == 1 ? b3[a] : (u == 2 ? b3[a] + size - 1 : (u == 3 ? b3[a] + size : b3[a] + 2 * size)));
                     }
                     if (!fold3_32(p, d, dom.anchor_level)) continue;
                     const uint32_t r =
@@ -273,16 +306,17 @@ __global__ void __launch_bounds__(kT) k_leaders(fl_mesh_dev m, fl_domain_dev dom
                     if (r == FL_INVALID_INDEX) continue;
                     bool inside = false;  // only on a periodic axis of one octet's extent
                     for (int q = 0; q < 8; ++q) inside |= (mem[q] == r);
-                    if (!inside && (int)shadow[r] > l) bad = true;
+                    if (!inside && (int)shadow[r] > l) bad4 |= 1u << s;
                 }
-                leader = !__any_sync(0xFFFFFFFFu, bad);
+                bad4 = __reduce_or_sync(0xFFFFFFFFu, bad4);
             }
-            if (lane == 0) is_leader[i] = leader ? 1u : 0u;
+            if (have && (lane & 7) == 0) is_leader[i] = ((lead4 >> grp) & 1u) && !((bad4 >> grp) & 1u) ? 1u : 0u;
         }
     }
 }
 
-// Members of each leader's group, one warp per leader (lane c < 8: sibling c).
+// Members of each leader's group: a warp locates the siblings of four leaders
+// at a time (lane 8s + c: sibling c of the s-th).
 __global__ void __launch_bounds__(kT) k_members(fl_mesh_dev m, fl_domain_dev dom, fl_locator L,
                                                 const uint32_t* __restrict__ is_leader,
                                                 const uint32_t* __restrict__ gid, uint32_t* __restrict__ members,
@@ -298,13 +332,19 @@ __global__ void __launch_bounds__(kT) k_members(fl_mesh_dev m, fl_domain_dev dom
          base += warps * 32) {
         const size_t mine = base + lane;
         const bool lead = mine < m.n && is_leader[mine];
-        for (unsigned cm = __ballot_sync(0xFFFFFFFFu, lead); cm; cm &= cm - 1) {
-            const size_t i = base + (__ffs(cm) - 1);
-            if (lane < 8) {
+        unsigned cm = __ballot_sync(0xFFFFFFFFu, lead);
+        while (cm) {
+            // up to four leaders per round: lanes 8s .. 8s + 7 take the s-th next one
+            unsigned pick = cm;
+            for (int s = 0; s < (lane >> 3) && pick; ++s) pick &= pick - 1;
+            for (int s = 0; s < 4 && cm; ++s) cm &= cm - 1;
+            if (pick) {
+                const size_t i = base + (__ffs(pick) - 1);
+                const int c = lane & 7;
                 bool ok;
-                const uint32_t j = sibling_of(P, m, dom, i, lane, &ok);
+                const uint32_t j = sibling_of(P, m, dom, i, c, &ok);
                 const uint32_t g = gid[i];
-                members[(size_t)g * 8 + lane] = j;
+                members[(size_t)g * 8 + c] = j;
                 group_of[j] = g;
             }
         }
