@@ -43,32 +43,52 @@ __global__ void k_unpack_fields(const uint8_t* __restrict__ packed, float* __res
 // Row kernels: a warp covers 32 / C rows (one row when C > 16), lane j the
 // column j % C of row j / C, so every row is read and written by one warp
 // instruction (its two or three sectors fetched once) and the index math is
-// 32-bit per row.
-__global__ void k_gather_rows(const float* __restrict__ field, uint32_t C, const uint32_t* __restrict__ idx, size_t n,
-                              float* __restrict__ out) {
-    const uint32_t lane = threadIdx.x & 31u, rpw = C <= 32u ? 32u / C : 1u;
-    const uint32_t r = lane / C, c = lane - r * C;
-    const size_t nw = ((size_t)gridDim.x * blockDim.x) >> 5;
-    for (size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * rpw < n; w += nw) {
-        const size_t k = w * rpw + r;
-        if (r >= rpw || k >= n) continue;
-        const float* src = field + (size_t)idx[k] * C;
-        float* dst = out + k * C;
-        for (uint32_t j = c; j < C; j += 32u) dst[j] = src[j];
-    }
-}
+// 32-bit per row.  Rows of up to 32 columns move kRowUnroll row groups per
+// warp round, their index and value loads issued together (random rows need
+// many bytes in flight); wider rows one group at a time.
+constexpr int kRowUnroll = 8;
 
-__global__ void k_scatter_rows(const float* __restrict__ in, uint32_t C, const uint32_t* __restrict__ idx, size_t n,
-                               float* __restrict__ field) {
+template <bool SCATTER>
+__global__ void k_move_rows(const float* __restrict__ src, uint32_t C, const uint32_t* __restrict__ idx, size_t n,
+                            float* __restrict__ dst) {
     const uint32_t lane = threadIdx.x & 31u, rpw = C <= 32u ? 32u / C : 1u;
-    const uint32_t r = lane / C, c = lane - r * C;
+    const uint32_t r = C <= 32u ? lane / C : 0u, c = lane - r * C;
+    const bool on = r < rpw;
     const size_t nw = ((size_t)gridDim.x * blockDim.x) >> 5;
-    for (size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * rpw < n; w += nw) {
-        const size_t k = w * rpw + r;
-        if (r >= rpw || k >= n) continue;
-        const float* src = in + k * C;
-        float* dst = field + (size_t)idx[k] * C;
-        for (uint32_t j = c; j < C; j += 32u) dst[j] = src[j];
+    const size_t per_round = (size_t)rpw * kRowUnroll;
+    for (size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * per_round < n; w += nw) {
+        const size_t k0 = w * per_round + r;
+        if (C <= 32u) {
+            uint32_t id[kRowUnroll];
+            float v[kRowUnroll];
+#pragma unroll
+            for (int u = 0; u < kRowUnroll; ++u) {
+                const size_t k = k0 + (size_t)u * rpw;
+                id[u] = on && k < n ? idx[k] : 0u;
+            }
+#pragma unroll
+            for (int u = 0; u < kRowUnroll; ++u) {
+                const size_t k = k0 + (size_t)u * rpw;
+                v[u] = on && k < n ? (SCATTER ? src[k * C + c] : src[(size_t)id[u] * C + c]) : 0.0f;
+            }
+#pragma unroll
+            for (int u = 0; u < kRowUnroll; ++u) {
+                const size_t k = k0 + (size_t)u * rpw;
+                if (on && k < n) {
+                    if (SCATTER) dst[(size_t)id[u] * C + c] = v[u];
+                    else dst[k * C + c] = v[u];
+                }
+            }
+        } else {
+            for (int u = 0; u < kRowUnroll; ++u) {
+                const size_t k = k0 + (size_t)u;
+                if (k >= n) break;
+                const size_t row = idx[k];
+                const float* s = SCATTER ? src + k * C : src + row * C;
+                float* d = SCATTER ? dst + row * C : dst + k * C;
+                for (uint32_t j = lane; j < C; j += 32u) d[j] = s[j];
+            }
+        }
     }
 }
 
@@ -159,8 +179,8 @@ int fl_pack_halo(fl_ctx* ctx, const float* field, uint32_t C, const uint32_t* ce
     if (!ctx) return FL_E_INVALID_ARG;
     if (!n || !C) return FL_OK;
     if (!field || !cell_indices || !pack) return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_pack_halo: null pointer");
-    k_gather_rows<<<row_blocks(ctx, n, C), 256, 0, ctx->stream>>>(field, C, cell_indices, n, pack);
-    FL_CHECK_LAUNCH(ctx, "k_gather_rows");
+    k_move_rows<false><<<row_blocks(ctx, n, C), 256, 0, ctx->stream>>>(field, C, cell_indices, n, pack);
+    FL_CHECK_LAUNCH(ctx, "k_move_rows gather");
     return FL_OK;
 }
 
@@ -168,8 +188,8 @@ int fl_unpack_halo(fl_ctx* ctx, const float* pack, uint32_t C, const uint32_t* c
     if (!ctx) return FL_E_INVALID_ARG;
     if (!n || !C) return FL_OK;
     if (!field || !cell_indices || !pack) return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_unpack_halo: null pointer");
-    k_scatter_rows<<<row_blocks(ctx, n, C), 256, 0, ctx->stream>>>(pack, C, cell_indices, n, field);
-    FL_CHECK_LAUNCH(ctx, "k_scatter_rows");
+    k_move_rows<true><<<row_blocks(ctx, n, C), 256, 0, ctx->stream>>>(pack, C, cell_indices, n, field);
+    FL_CHECK_LAUNCH(ctx, "k_move_rows scatter");
     return FL_OK;
 }
 

@@ -31,17 +31,20 @@ def test_pack_unpack_fields_roundtrip(ctx):
     np.testing.assert_array_equal(buf.to_host()[64:].view(np.float32), f)
 
 
-def test_pack_unpack_halo(ctx):
-    rng = np.random.default_rng(1)
-    C, n = 19, 5000
+@pytest.mark.parametrize("C,m", [(19, 700), (1, 1001), (7, 333), (32, 9), (33, 77), (70, 130)])
+def test_pack_unpack_halo(ctx, C, m):
+    """Rows narrower than a warp (several per warp), exactly a warp, and wider;
+    row counts that leave partial rounds."""
+    rng = np.random.default_rng(C)
+    n = 5000
     f = rng.standard_normal((n, C)).astype(np.float32)
-    idx = rng.choice(n, 700, replace=False).astype(np.uint32)
-    df, di, pk = D(ctx, f), D(ctx, idx), E(ctx, (700, C), np.float32)
-    ctx.call("fl_pack_halo", df.ptr, C, di.ptr, 700, pk.ptr)
+    idx = rng.choice(n, m, replace=False).astype(np.uint32)
+    df, di, pk = D(ctx, f), D(ctx, idx), E(ctx, (m, C), np.float32)
+    ctx.call("fl_pack_halo", df.ptr, C, di.ptr, m, pk.ptr)
     np.testing.assert_array_equal(pk.to_host(), f[idx])
     g = np.zeros_like(f)
     dg = D(ctx, g)
-    ctx.call("fl_unpack_halo", pk.ptr, C, di.ptr, 700, dg.ptr)
+    ctx.call("fl_unpack_halo", pk.ptr, C, di.ptr, m, dg.ptr)
     g[idx] = f[idx]
     np.testing.assert_array_equal(dg.to_host(), g)
 
