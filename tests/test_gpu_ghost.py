@@ -75,9 +75,11 @@ def test_interp_trilinear_vs_oracle(ctx):
     assert np.abs(want).sum() > 0
 
 
-def test_restrict_groups_vs_oracle(ctx):
-    rng = np.random.default_rng(3)
-    n, C, G = 4096, 5, 300
+@pytest.mark.parametrize("C,G", [(5, 300), (19, 301), (1, 257), (32, 33), (40, 97)])
+def test_restrict_groups_vs_oracle(ctx, C, G):
+    """Rows narrower than a warp, exactly a warp and wider; odd group counts."""
+    rng = np.random.default_rng(3 + C)
+    n = 8 * G + 100
     f = rng.standard_normal((n, C)).astype(np.float32)
     mem = rng.choice(n, G * 8, replace=False).astype(np.uint32)
     for rule in (0, 1):
