@@ -24,13 +24,17 @@ static __constant__ uint8_t c_dec[12][8] = {
 
 // Fill the shared tables: t1[s*8+q] (single level) and t3[s*512+w] where w
 // packs three levels of input (MSB level first, 3 bits each).
+// Both fills are called by every thread of the block at kernel start: the
+// one-level table goes to shared memory first (scattered reads of constant
+// memory serialise across a warp), then the three-level table is built from it.
 static __device__ __forceinline__ void fl_keys_fill_tables(uint8_t* t1, uint16_t* t3, bool decode) {
     for (int i = threadIdx.x; i < 96; i += blockDim.x) t1[i] = decode ? c_dec[i >> 3][i & 7] : c_enc[i >> 3][i & 7];
+    __syncthreads();
     for (int i = threadIdx.x; i < 12 * 512; i += blockDim.x) {
         unsigned s = i >> 9, w = i & 511, out = 0;
         for (int k = 2; k >= 0; --k) {
             unsigned q = (w >> (3 * k)) & 7u;
-            unsigned v = decode ? c_dec[s][q] : c_enc[s][q];
+            unsigned v = t1[s * 8 + q];
             out = (out << 3) | (v & 7u);
             s = v >> 3;
         }
@@ -44,12 +48,13 @@ static __device__ __forceinline__ void fl_keys_fill_tables(uint8_t* t1, uint16_t
 // from the coordinates without interleaving them first.
 static __device__ __forceinline__ void fl_keys_fill_tables_cat(uint8_t* t1, uint16_t* t3c) {
     for (int i = threadIdx.x; i < 96; i += blockDim.x) t1[i] = c_enc[i >> 3][i & 7];
+    __syncthreads();
     for (int i = threadIdx.x; i < 12 * 512; i += blockDim.x) {
         unsigned s = i >> 9, out = 0;
         const unsigned x3 = (i >> 6) & 7u, y3 = (i >> 3) & 7u, z3 = i & 7u;
         for (int k = 2; k >= 0; --k) {
             unsigned q = (((z3 >> k) & 1u) << 2) | (((y3 >> k) & 1u) << 1) | ((x3 >> k) & 1u);
-            unsigned v = c_enc[s][q];
+            unsigned v = t1[s * 8 + q];
             out = (out << 3) | (v & 7u);
             s = v >> 3;
         }
