@@ -387,47 +387,111 @@ __global__ void __launch_bounds__(kT) k_emit(fl_mesh_dev m, fl_domain_dev dom, i
                                              int rule) {
     __shared__ uint8_t t1[96];
     __shared__ uint16_t t3c[12 * 512];
+    __shared__ uint32_t stage[kT / 32][256];  // one column of a warp's (at most 256) new cells
     fl_keys_fill_tables_cat(t1, t3c);
     __syncthreads();
-    size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < m.n; t += stride) {
-        const size_t i = order ? order[t] : t;
-        uint16_t cs = m.case_id ? m.case_id[i] : 0;
-        bool split = m.flags[i] > 0 && m.state[i] == 0 && m.level[i] < max_level;
-        uint32_t o = off[t];
-        auto put = [&](uint32_t j, int32_t x, int32_t y, int32_t z, uint8_t l, uint32_t src, uint8_t kind) {
-            out.x[j] = x; out.y[j] = y; out.z[j] = z; out.level[j] = l;
-            out.state[j] = m.state[i]; out.flags[j] = 0; out.material[j] = m.material[i];
-            if (out.case_id) out.case_id[j] = cs;
-            if (osrc) osrc[j] = src;
-            if (okind) okind[j] = kind;
-            if (fin && C) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t* S = stage[threadIdx.x >> 5];
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t rounds = (m.n + stride - 1) / stride;  // whole warps stay in the loop
+    for (size_t rr = 0; rr < rounds; ++rr) {
+        const size_t t = rr * stride + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+        // kind: 0 nothing (a merged non-leader or past the end), 1 split, 2 group leader, 3 kept
+        int kind = 0, l = 0;
+        size_t i = 0;
+        uint32_t o = 0, cnt = 0, g = FL_INVALID_INDEX;
+        unsigned st = 0;
+        if (t < m.n) {
+            i = order ? order[t] : t;
+            o = off[t];
+            l = m.level[i];
+            if (m.flags[i] > 0 && m.state[i] == 0 && l < max_level) {
+                kind = 1;
+                cnt = 8;
+                st = fl_hilbert_state_cat(t1, t3c, (uint32_t)m.x[i], (uint32_t)m.y[i], (uint32_t)m.z[i],
+                                          dom.depth - dom.anchor_level + l);
+            } else if ((g = group_of[i]) != FL_INVALID_INDEX) {
+                if (is_leader[i]) { kind = 2; cnt = 1; }
+            } else {
+                kind = 3;
+                cnt = 1;
+            }
+        }
+        // a warp's new cells are one contiguous range (off is the exclusive scan of
+        // the counts in visiting order, and lane 0 visits first): each column is
+        // staged in shared memory, then stored coalesced
+        const uint32_t total = __reduce_add_sync(0xFFFFFFFFu, cnt);
+        if (total == 0) continue;
+        const uint32_t base = __shfl_sync(0xFFFFFFFFu, o, 0), rel = o - base;
+        const int32_t mx = kind ? m.x[i] : 0, my = kind ? m.y[i] : 0, mz = kind ? m.z[i] : 0;
+        auto stage_col = [&](auto value_of) {
+            if (kind == 1) {
+                for (int c = 0; c < 8; ++c) S[rel + (t1[st * 8 + c] & 7u)] = value_of(c);
+            } else if (kind >= 2) {
+                S[rel] = value_of(-1);
+            }
+            __syncwarp();
+        };
+        auto axis = [&](int32_t v, int bit) {
+            return [=](int c) -> uint32_t {
+                return (uint32_t)(c >= 0 ? (v << 1) | ((c >> bit) & 1) : (kind == 2 ? v >> 1 : v));
+            };
+        };
+        stage_col(axis(mx, 0));
+        for (uint32_t e = lane; e < total; e += 32u) out.x[base + e] = (int32_t)S[e];
+        __syncwarp();
+        stage_col(axis(my, 1));
+        for (uint32_t e = lane; e < total; e += 32u) out.y[base + e] = (int32_t)S[e];
+        __syncwarp();
+        stage_col(axis(mz, 2));
+        for (uint32_t e = lane; e < total; e += 32u) out.z[base + e] = (int32_t)S[e];
+        __syncwarp();
+        stage_col([&](int c) -> uint32_t { return (uint32_t)(c >= 0 ? l + 1 : (kind == 2 ? l - 1 : l)); });
+        for (uint32_t e = lane; e < total; e += 32u) out.level[base + e] = (uint8_t)S[e];
+        __syncwarp();
+        const uint32_t mstate = kind ? m.state[i] : 0u, mmat = kind ? m.material[i] : 0u;
+        stage_col([&](int) -> uint32_t { return mstate; });
+        for (uint32_t e = lane; e < total; e += 32u) out.state[base + e] = (uint8_t)S[e];
+        __syncwarp();
+        stage_col([&](int) -> uint32_t { return mmat; });
+        for (uint32_t e = lane; e < total; e += 32u) out.material[base + e] = S[e];
+        __syncwarp();
+        for (uint32_t e = lane; e < total; e += 32u) out.flags[base + e] = 0;
+        if (out.case_id) {
+            const uint32_t cs = kind && m.case_id ? m.case_id[i] : 0u;
+            stage_col([&](int) -> uint32_t { return cs; });
+            for (uint32_t e = lane; e < total; e += 32u) out.case_id[base + e] = (uint16_t)S[e];
+            __syncwarp();
+        }
+        if (osrc) {
+            stage_col([&](int) -> uint32_t { return kind == 2 ? g : (uint32_t)i; });
+            for (uint32_t e = lane; e < total; e += 32u) osrc[base + e] = S[e];
+            __syncwarp();
+        }
+        if (okind) {
+            stage_col([&](int c) -> uint32_t { return c >= 0 ? (uint32_t)c : (kind == 2 ? 9u : 8u); });
+            for (uint32_t e = lane; e < total; e += 32u) okind[base + e] = (uint8_t)S[e];
+            __syncwarp();
+        }
+        if (fin && C && kind) {  // fields: copied from the source cell, or the mean of a group's members
+            auto copy_row = [&](uint32_t j) {
+                const float* sp = fin + i * C;
                 float* fo = fout + (size_t)j * C;
-                if (kind <= 8) {
-                    const float* sp = fin + (size_t)src * C;
-                    for (uint32_t c = 0; c < C; ++c) fo[c] = sp[c];
-                } else {
-                    const uint32_t* mem = members + (size_t)src * 8;
-                    for (uint32_t c = 0; c < C; ++c) {
-                        float sum = 0.0f;
-                        for (int q = 0; q < 8; ++q) sum = __fadd_rn(sum, fin[(size_t)mem[q] * C + c]);
-                        fo[c] = rule == 1 ? sum : __fmul_rn(sum, 0.125f);
-                    }
+                for (uint32_t c = 0; c < C; ++c) fo[c] = sp[c];
+            };
+            if (kind == 1) {
+                for (int c = 0; c < 8; ++c) copy_row(o + (t1[st * 8 + c] & 7u));
+            } else if (kind == 3) {
+                copy_row(o);
+            } else {
+                const uint32_t* mem = members + (size_t)g * 8;
+                float* fo = fout + (size_t)o * C;
+                for (uint32_t c = 0; c < C; ++c) {
+                    float sum = 0.0f;
+                    for (int q = 0; q < 8; ++q) sum = __fadd_rn(sum, fin[(size_t)mem[q] * C + c]);
+                    fo[c] = rule == 1 ? sum : __fmul_rn(sum, 0.125f);
                 }
             }
-        };
-        if (split) {
-            const int l = m.level[i];
-            const unsigned st = fl_hilbert_state_cat(t1, t3c, (uint32_t)m.x[i], (uint32_t)m.y[i], (uint32_t)m.z[i],
-                                                     dom.depth - dom.anchor_level + l);
-            for (int c = 0; c < 8; ++c)
-                put(o + (t1[st * 8 + c] & 7u), (m.x[i] << 1) | (c & 1), (m.y[i] << 1) | ((c >> 1) & 1),
-                    (m.z[i] << 1) | ((c >> 2) & 1), (uint8_t)(l + 1), (uint32_t)i, (uint8_t)c);
-        } else if (group_of[i] != FL_INVALID_INDEX) {
-            if (is_leader[i])
-                put(o, m.x[i] >> 1, m.y[i] >> 1, m.z[i] >> 1, (uint8_t)(m.level[i] - 1), group_of[i], 9);
-        } else {
-            put(o, m.x[i], m.y[i], m.z[i], m.level[i], (uint32_t)i, 8);
         }
     }
 }
