@@ -26,13 +26,21 @@ def build(force=False):
     return LIB
 
 
-def build_reference(ref_root="/root/reference"):
-    """Compile the reference's key codecs in place (only where the tree exists)."""
+# The reference tree, read only by the in-place compile recipe (Makefile.ref) and
+# the tests that parse its scripts; absent on hosts without it.
+REF_ROOT = os.environ.get("FLUIDLOOM_REF_ROOT", "/root/reference")
+REF_DIR = os.path.join(HERE, "_ref")
+
+
+def build_reference(ref_root=None):
+    """Compile parts of the reference in place (only where the tree exists):
+    its key codecs, geometry placement and regrid/hash kernels."""
+    ref_root = ref_root or REF_ROOT
     if not os.path.isdir(ref_root):
         return None
     subprocess.run(["make", "-s", "-f", os.path.join(HERE, "Makefile.ref"), "REF=" + ref_root],
                    check=True)
-    return os.path.join(HERE, "_ref")
+    return REF_DIR
 
 
 if __name__ == "__main__":

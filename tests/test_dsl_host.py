@@ -7,9 +7,10 @@ import os
 import pytest
 
 from fluidloom_gb300 import dsl
+from oracle.build import REF_ROOT
 
 SCEN = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "fluidloom_gb300", "scenarios")
-REF_BENCH = "/root/reference/benchmarks"
+REF_BENCH = os.path.join(REF_ROOT, "benchmarks")
 
 
 def ev(src, **names):
