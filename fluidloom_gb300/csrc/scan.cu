@@ -13,6 +13,8 @@
 #include "common.cuh"
 #include "scan.cuh"
 
+#include <cuda.h>
+
 #include <mutex>
 
 namespace {
@@ -350,15 +352,16 @@ int fl_apply_permutation(fl_ctx* ctx, const void* src, void* dst, size_t elem_si
 // ---------------------------------------------------------------------------
 // Exclusive scan for callers that cannot allocate device memory.
 //
-// Some callers cannot call cudaMalloc: code running while a CUDA graph is
-// being captured on another thread, host callbacks and FFI hosts that must not
-// allocate on their hot path, and embedders that own every device allocation
-// through their own pool.  For them this entry point takes no context and
-// allocates nothing: the scan's only scratch (one status word per 4,096-element
-// tile, a tile ticket and a timeout word) lives in the file-scope array below,
-// sized for at most kNoAllocMaxN elements (128 KiB + 512 B); every GPU that
-// loads this library keeps that array until the process exits.  The caller
-// passes the input, the output and (optionally) the total.
+// Some callers cannot call cudaMalloc: embedders that own every device
+// allocation through their own pool or arena sized at start-up, hosts running
+// under a fixed device-memory budget that must not grow, and FFI hosts that
+// must not allocate on their hot path (cudaMalloc and cudaFree can synchronize
+// the whole device).  For them this entry point takes no context and allocates
+// nothing: the scan's only scratch (one status word per 4,096-element tile, a
+// tile ticket and a timeout word) lives in the file-scope array below, sized
+// for at most kNoAllocMaxN elements (128 KiB + 512 B); every GPU that loads
+// this library keeps that array until the process exits.  The caller passes
+// the input, the output and (optionally) the total.
 namespace {
 
 constexpr size_t kNoAllocMaxN = (size_t)1 << 26;                 // 67,108,864 elements
@@ -368,24 +371,61 @@ constexpr size_t kNoAllocBytes = kNoAllocStatusBytes + 512;      // + ticket and
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
-// Device address of g_noalloc_scratch per device: the array's name is only a
-// host-side stand-in, so host code must ask the runtime for the address, once
-// per device, with that device current.
+// Device address of g_noalloc_scratch: the array's name is only a host-side
+// stand-in, so host code asks the runtime for the address with the device
+// current.  The address belongs to one context instance; it is cached with
+// that context's unique id (cuCtxGetId, which allocates nothing) and looked up
+// again when a call finds another context current on the device -- after a
+// cudaDeviceReset or a primary-context reset by the embedding host.
+struct NoAllocSlot {
+    unsigned long long ctx_id;
+    void* ptr;
+};
 std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[64] = {nullptr};
+NoAllocSlot g_noalloc_slot[64] = {};
+
+// The two driver calls come through the runtime's entry-point query, so the
+// library does not link libcuda itself (it loads on hosts without a driver).
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+int current_ctx_id(unsigned long long* id) {
+    if (!g_ctx_get_current || !g_ctx_get_id) {
+        void* a = nullptr;
+        void* b = nullptr;
+        cudaDriverEntryPointQueryResult qa, qb;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 4000, cudaEnableDefault, &qa) != cudaSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) != cudaSuccess ||
+            qa != cudaDriverEntryPointSuccess || qb != cudaDriverEntryPointSuccess || !a || !b)
+            return FL_E_CUDA;
+        g_ctx_get_current = (CtxGetCurrentFn)a;
+        g_ctx_get_id = (CtxGetIdFn)b;
+    }
+    CUcontext c = nullptr;
+    if (g_ctx_get_current(&c) != CUDA_SUCCESS) return FL_E_CUDA;
+    if (!c) { *id = 0; return FL_OK; }
+    return g_ctx_get_id(c, id) == CUDA_SUCCESS ? FL_OK : FL_E_CUDA;
+}
 
 int noalloc_scratch(void** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return FL_E_CUDA;
     if (dev < 0 || dev >= 64) return FL_E_INVALID_ARG;
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
-        void* p = nullptr;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);  // also guards the driver entry points' first lookup
+    unsigned long long id = 0;
+    if (current_ctx_id(&id)) return FL_E_CUDA;
+    NoAllocSlot& s = g_noalloc_slot[dev];
+    if (!s.ptr || id == 0 || s.ctx_id != id) {
+        void* p = nullptr;  // the lookup makes the device's primary context current if none was
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) return FL_E_CUDA;
-        g_noalloc_ptr[dev] = p;
+        if (current_ctx_id(&id) || id == 0) return FL_E_CUDA;
+        s.ptr = p;
+        s.ctx_id = id;
     }
-    *out = g_noalloc_ptr[dev];
+    *out = s.ptr;
     return FL_OK;
 }
 
@@ -401,7 +441,7 @@ extern "C" int fl_scan_exclusive_u32_noalloc(const uint32_t* in, uint32_t* out, 
     if (rc) return rc;
     if (n == 0) {
         if (total && cudaMemsetAsync(total, 0, 4, st) != cudaSuccess) return FL_E_CUDA;
-        return FL_OK;
+        return cudaStreamSynchronize(st) == cudaSuccess ? FL_OK : FL_E_CUDA;
     }
     size_t tiles = (n + kTile - 1) / kTile;
     unsigned long long* status = (unsigned long long*)base;
@@ -410,11 +450,17 @@ extern "C" int fl_scan_exclusive_u32_noalloc(const uint32_t* in, uint32_t* out, 
     // the array keeps the previous call's contents: clear the words this call reads as zero
     if (cudaMemsetAsync(status, 0, tiles * 8, st) != cudaSuccess) return FL_E_CUDA;
     if (cudaMemsetAsync(ticket, 0, 256 + FL_DEVSTAT_WORDS * 4, st) != cudaSuccess) return FL_E_CUDA;
+    // An error the embedding host left pending is its own: only an error that
+    // appears with this launch is reported (and cleared) as this call's failure.
+    const cudaError_t pending = cudaPeekAtLastError();
     if ((((uintptr_t)in | (uintptr_t)out) & 15u) == 0)
         k_scan<true><<<(unsigned)tiles, kThreads, 0, st>>>(in, out, n, status, ticket, total, timeout);
     else
         k_scan<false><<<(unsigned)tiles, kThreads, 0, st>>>(in, out, n, status, ticket, total, timeout);
-    if (cudaGetLastError() != cudaSuccess) return FL_E_CUDA;
+    if (pending == cudaSuccess && cudaPeekAtLastError() != cudaSuccess) {
+        cudaGetLastError();
+        return FL_E_CUDA;
+    }
     uint32_t expired = 0;  // a pageable destination makes this copy wait for the scan
     if (cudaMemcpyAsync(&expired, timeout + FL_DEVSTAT_TIMEOUT, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess)
         return FL_E_CUDA;
