@@ -136,49 +136,79 @@ def timer(ctx):
     return stop
 
 
-def regrid_microbench(ctx, seed=1, L=8):
-    """16.7M-leaf regrid (a uniform level-L mesh, 8^L leaves): blob flags, FULL26
-    balance to a fixed point, split/merge, key sort, rebuild; neighbour table; and
-    a 63-bit key sort of the result alone."""
+def blob_table(seed, n=64):
+    """Seeded Gaussian blobs over the unit cube: {cx, cy, cz, 1/(2 sigma^2), amplitude},
+    centres uniform, sigma uniform in [0.02, 0.1] of the domain."""
+    rng = np.random.default_rng(seed)
+    c = rng.random((n, 3))
+    s = rng.uniform(0.02, 0.1, n)
+    return np.ascontiguousarray(np.concatenate([c, (1 / (2 * s * s))[:, None], np.ones((n, 1))], 1), np.float32)
+
+
+def microbench_mesh(L=8):
+    """The regrid microbenchmark's synthetic octree: a uniform level-L mesh (8^L leaves)
+    regridded once by thresholding blob field 1 (refine above 0.7 to level L+1, coarsen
+    below 0.4) -- about 0.98 x 8^L leaves over three levels -- then the benchmark's
+    regrid by an independent blob field 2 (same thresholds, up to level L+2), whose
+    refinement crosses the first round's level boundaries so FULL26 balance iterates."""
+    n1 = 1 << L
+    idx = np.arange(n1 ** 3, dtype=np.int64)
+    N = len(idx)
+    start = {"x": (idx % n1).astype(np.int32), "y": ((idx // n1) % n1).astype(np.int32),
+             "z": (idx // (n1 * n1)).astype(np.int32), "level": np.full(N, L, np.uint8),
+             "state": np.zeros(N, np.uint8), "flags": np.zeros(N, np.int32), "material": np.zeros(N, np.uint32)}
+    return {"start": start, "rounds": [(blob_table(1), 0.4, 0.7, L + 1), (blob_table(2), 0.4, 0.7, L + 2)]}
+
+
+def regrid_microbench(ctx, L=8):
+    """The regrid of the microbenchmark octree (microbench_mesh; round 1 untimed):
+    blob flags, FULL26 balance to a fixed point, split/merge, key-order rebuild, the
+    neighbour table; then a 63-bit key sort of the result alone and the primitives."""
     import ctypes
     from fluidloom_gb300 import DeviceArray
     from fluidloom_gb300.amr import AdaptConfig, AdaptStats, Mesh
-    n1 = 1 << L
-    idx = np.arange(n1 ** 3, dtype=np.int64)
-    cols = {"x": (idx % n1).astype(np.int32), "y": ((idx // n1) % n1).astype(np.int32),
-            "z": (idx // (n1 * n1)).astype(np.int32), "level": np.full(len(idx), L, np.uint8)}
-    rng = np.random.default_rng(seed)
-    c = rng.random((64, 3))
-    s = rng.uniform(0.02, 0.1, 64)
-    blobs = np.ascontiguousarray(np.concatenate([c, (1 / (2 * s * s))[:, None], np.ones((64, 1))], 1), np.float32)
-    m = Mesh(ctx, cols)
-    cfg = AdaptConfig.make(max_level=L + 1, min_level=0, balance_mode=1)
+    mb = microbench_mesh(L)
+    m = Mesh(ctx, mb["start"], capacity=1 << (3 * L))
     out = {}
-    stop = timer(ctx)
-    ctx.call("fl_flags_from_blobs", ctypes.byref(m.m), blobs.ctypes.data_as(ctypes.c_void_p), 64,
-             ctypes.c_float(0.05), ctypes.c_float(0.5), L + 1)
-    out["flags_ms"] = stop()
-    st = AdaptStats()
-    fp = ctypes.c_void_p(0)
-    stop = timer(ctx)
-    ctx.call("fl_adapt", ctypes.byref(m.m), ctypes.byref(cfg), ctypes.byref(fp), 0, ctypes.byref(st))
-    out["adapt_ms"] = stop()
+    for r, (blobs, lo, hi, ml) in enumerate(mb["rounds"]):
+        cfg = AdaptConfig.make(max_level=ml, min_level=0, balance_mode=1)
+        leaves_in = m.n
+        stop = timer(ctx)
+        ctx.call("fl_flags_from_blobs", ctypes.byref(m.m), blobs.ctypes.data_as(ctypes.c_void_p), len(blobs),
+                 ctypes.c_float(lo), ctypes.c_float(hi), ml)
+        flags_ms = stop()
+        st = AdaptStats()
+        fp = ctypes.c_void_p(0)
+        stop = timer(ctx)
+        ctx.call("fl_adapt", ctypes.byref(m.m), ctypes.byref(cfg), ctypes.byref(fp), 0, ctypes.byref(st))
+        adapt_ms = stop()
+    out["flags_ms"], out["adapt_ms"] = flags_ms, adapt_ms
     n = m.n
     nbr = DeviceArray(ctx, (n * 26,), np.uint32)
     stop = timer(ctx)
     ctx.call("fl_neighbour_rebuild", ctypes.byref(m.m), ctypes.byref(cfg), 1, nbr.ptr)
     out["neighbour_ms"] = stop()
     nbr.free()
+    # the leaves' 63-bit keys: the 21-level Hilbert key of each leaf's anchor (unique per leaf),
+    # with uint32 leaf ids, shuffled so the sort has work to do
     keys = DeviceArray(ctx, (n,), np.uint64)
-    ids = DeviceArray(ctx, (n,), np.uint32)
     ctx.call("fl_cell_keys", m.m.x, m.m.y, m.m.z, m.m.level, None, 21, 21, keys.ptr, n)
-    ctx.call("fl_hilbert_encode", m.m.x, m.m.y, m.m.z, 21, keys.ptr, ids.ptr, n)
+    perm = np.random.default_rng(5).permutation(n).astype(np.uint32)
+    hk = keys.to_host()[perm]
+    keys.free()
+    keys = DeviceArray.from_host(ctx, hk)
+    ids = DeviceArray.from_host(ctx, perm)
+    del hk
     ctx.sync()
     stop = timer(ctx)
     ctx.call("fl_sort_pairs_u64_u32", keys.ptr, ids.ptr, n, 0, 63)
     out["sort_ms"] = stop()
     out["primitives"] = primitives_on(ctx, m, keys, ids, n, out)
-    out.update({"leaves_in": int(len(idx)), "leaves_out": int(n), "split": st.num_split, "merged_groups": st.num_groups,
+    lv = np.bincount(m.download()["level"], minlength=L + 3)[L - 2:].tolist()
+    out.update({"octree": "uniform level %d (%d leaves), regridded once by blob field 1; timed: the regrid by "
+                          "blob field 2 (refine > 0.7 to level %d, coarsen < 0.4)" % (L, 8 ** L, L + 2),
+                "leaves_in": int(leaves_in), "leaves_out": int(n), "levels_out_from_%d" % (L - 2): lv,
+                "split": st.num_split, "merged_groups": st.num_groups,
                 "balance_iterations": st.balance.iterations, "balance_marked": st.balance.total_cells_marked_for_balance,
                 "sorted_keys_per_s": n / (out["sort_ms"] * 1e-3),
                 "regrid_ms": out["flags_ms"] + out["adapt_ms"] + out["neighbour_ms"]})
@@ -191,8 +221,8 @@ def primitives_on(ctx, m, keys, ids, n, out):
     bytes of its unit: encode 24 B per key (12 B coordinates in, 8 B key + 4 B id out); radix
     sort 8 + 24 B per key and pass (8 passes of 8-bit digits over 63 bits); scan 8 B per
     element; hash build 24 B per key + 12 B per slot cleared; hash query 12 B per query + one
-    32-byte sector per probe; neighbour rebuild one 32-byte sector per probe (26 per leaf) +
-    104 B of table per leaf; halo pack / unpack of a 19-component field 4 + 2 x 76 B per cell
+    32-byte sector per probe; neighbour rebuild 104 B of table written + 23 B read per leaf
+    (coordinates, level, locator key, directory share); halo pack / unpack of a 19-component field 4 + 2 x 76 B per cell
     (a random cell order); restriction 32 + 9 x 76 B per sibling group.  Times are
     CUDA-event times of one call each."""
     import ctypes
@@ -205,10 +235,14 @@ def primitives_on(ctx, m, keys, ids, n, out):
                      "frac_of_measured": round(nbytes / (ms * 1e-3) / 1e9 / peak, 3),
                      unit_name + "_per_s": round(units / (ms * 1e-3), 1)}
 
-    stop = timer(ctx)
     N = ctypes.c_size_t(n)
-    ctx.call("fl_hilbert_encode", m.m.x, m.m.y, m.m.z, 21, keys.ptr, ids.ptr, N)
+    ek = DeviceArray(ctx, (n,), np.uint64)
+    ei = DeviceArray(ctx, (n,), np.uint32)
+    stop = timer(ctx)
+    ctx.call("fl_hilbert_encode", m.m.x, m.m.y, m.m.z, 21, ek.ptr, ei.ptr, N)
     put("hilbert_encode", stop(), 24.0 * n, n, "keys")
+    ek.free()
+    ei.free()
     put("radix_sort", out["sort_ms"], (8.0 + 24.0 * 8) * n, n, "keys")
     a = DeviceArray(ctx, (n,), np.uint32).zero()
     b = DeviceArray(ctx, (n,), np.uint32)
@@ -226,7 +260,9 @@ def primitives_on(ctx, m, keys, ids, n, out):
     stop = timer(ctx)
     ctx.call("fl_hash_query", tk.ptr, tv.ptr, ctypes.c_uint64(cap), keys.ptr, b.ptr, N)
     put("hash_query", stop(), (12.0 + 32.0) * n, n, "queries")
-    put("neighbour_rebuild", out["neighbour_ms"], (26 * 32.0 + 104.0) * n, 26 * n, "probes")
+    # algorithmic bytes: the 26-entry row written (104 B) and per leaf its coordinates and level
+    # (13 B), its locator key (8 B) and its share of the bucket directory (2 B) read
+    put("neighbour_rebuild", out["neighbour_ms"], (104.0 + 13.0 + 8.0 + 2.0) * n, 26 * n, "probes")
     for d in (a, tot, tk, tv):
         d.free()
     # ghost fill primitives over a 19-component field (populations-like): gather by index,
@@ -270,10 +306,37 @@ def fp64_error(ctx, steps=(1, 10)):
     return out
 
 
+def full_run(ctx, steps=1000):
+    """The sphere case as its configuration runs it: 1000 level-0 steps with a vorticity
+    regrid every 25, from a fresh pool; wall time from the first step to the last
+    (synchronised), every regrid included, and the mesh as the flow develops."""
+    from fluidloom_gb300.lbm import Pool
+    pool = Pool(ctx, [sphere_case()])
+    ctx.sync()
+    lups, peak_sites, trace = 0, 0, []
+    t0 = time.perf_counter()
+    for s in range(1, steps + 1):
+        inf = pool.info()
+        lups += inf.fluid_lups_per_step
+        peak_sites = max(peak_sites, sum(int(inf.fluid_sites_per_level[l]) for l in range(4)))
+        pool.step(1)
+        if s % REGRID_EVERY == 0:
+            pool.regrid()
+        if s % 250 == 0:
+            inf = pool.info()
+            trace.append({"step": s, "bricks": int(inf.num_bricks),
+                          "fluid_sites": sum(int(inf.fluid_sites_per_level[l]) for l in range(4))})
+    ctx.sync()
+    dt = time.perf_counter() - t0
+    pool.close()
+    return {"steps": steps, "regrids": steps // REGRID_EVERY, "wall_s": round(dt, 3),
+            "mlups": round(lups / dt / 1e6, 1), "peak_fluid_sites": peak_sites, "mesh": trace}
+
+
 def cpu_sample(steps, threads=None):
-    """The oracle (CPU port) on a half-resolution sample of the workload: 64x32x32 base, 3 levels, r=4."""
+    """The oracle (CPU port) on the workload itself (128x64x64 base, 3 levels, r=8): `steps` level-0 steps."""
     from tests import _oracle as O
-    case = sphere_case(scale=2)
+    case = sphere_case()
     p = O.OraclePool([case])
     lups = p.lups()
     threads = threads or os.cpu_count() or 1
@@ -294,12 +357,18 @@ def run_gpu(args):
     ws, rank, local = rep.world, rep.rank, rep.local
     ctx = fl.Context(local)
     pool = Pool(ctx, [sphere_case()])
+    info0 = pool.info()
+    # spin-up: the flow develops (and the vorticity regrids refine its wake) before anything is timed
+    step_no = 0
+    for _ in range(args.spinup + args.warmup):
+        pool.step(1)
+        step_no += 1
+        if step_no % REGRID_EVERY == 0:
+            pool.regrid()
+    ctx.sync()
     info = pool.info()
     bricks0 = info.num_bricks
     lups0 = info.fluid_lups_per_step
-    for _ in range(args.warmup):
-        pool.step(1)
-    ctx.sync()
     rep.barrier()
     clocks = ClockSampler(local)
     clocks.start()
@@ -310,7 +379,7 @@ def run_gpu(args):
     launches0 = ctx.launch_count()
     stop = timer(ctx)
     for k in range(args.steps):
-        step_no = args.warmup + k + 1
+        step_no += 1
         inf = pool.info()
         total_lups += inf.fluid_lups_per_step
         pool.step(1)
@@ -342,12 +411,25 @@ def run_gpu(args):
             per_kernel[name] = {"launches": la, "avg_launch_ms": round(m / la, 4), "fluid_sites": int(st_),
                                 "achieved_gbs": round(BYTES_PER_LUP * st_ / (m * 1e-3) / 1e9, 1),
                                 "time_share": round(m / kms, 3)}
+    nprof = max(2, min(args.steps, 6))
+    lms, lla, lst = pool.profile_levels(nprof)
+    per_level = []
+    for l in range(16):
+        for kk, name in enumerate(("interior", "general", "all-solid")):
+            if lla[l, kk]:
+                per_level.append({"level": l, "kernel": name, "ms_per_step": round(lms[l, kk] / nprof, 4),
+                                  "launches_per_step": int(lla[l, kk]) // nprof,
+                                  "achieved_gbs": round(BYTES_PER_LUP * lst[l, kk] / (lms[l, kk] * 1e-3) / 1e9, 1)})
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": (round(tr * sites / nla) if tr else None),
+                "traffic_source": ("not measured in this run: DRAM bytes per fluid site update from the committed "
+                                   "ncu capture (profiles/collide_stream_sphere_ncu.md, dram__bytes_read.sum + "
+                                   "dram__bytes_write.sum of one level-3 sub-step / its fluid sites) x the fluid "
+                                   "sites per profiled launch" if tr else None),
                 "kernel": "collide-stream (k_collide_fast + k_interface + k_collide_general + k_collide_solid)",
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                 "algorithmic_bytes_per_launch": round(BYTES_PER_LUP * sites / nla), "launches_profiled": nla,
-                "avg_launch_ms": round(kms / nla, 4), "per_kernel": per_kernel,
+                "avg_launch_ms": round(kms / nla, 4), "per_kernel": per_kernel, "per_level": per_level,
                 # the timed steps themselves (dependency graph, regrids included): algorithmic
                 # collide-stream bytes over the timed region
                 "timed_region_achieved": round(value * 1e6 * BYTES_PER_LUP / 1e9, 1),
@@ -388,58 +470,91 @@ def run_gpu(args):
     d2h = (fbytes + args.steps * 32) / args.steps
     ctx.call("fl_host_free_pinned", hp)
     ctx.call("fl_host_free_pinned", vp)
+    pool.close()
+    full = None
+    if rank == 0 and not args.no_full_run:
+        full = full_run(ctx)
     micro = None
     if rank == 0 and not args.no_microbench:
-        pool.close()
         micro = regrid_microbench(ctx)
+    batch = None
+    if rank == 0 and not args.no_batching:
+        from fluidloom_gb300 import batching
+        batch = batching.benchmark(ctx, batching.cavity_batch(256), 500, 20)
+    serve = None
+    if rank == 0 and not args.no_serving:
+        from fluidloom_gb300 import serving
+        serve = serving.benchmark(ctx, rate=50.0, duration=args.serving_seconds, steps_range=(200, 2000),
+                                  budget_gb=150.0, check=8)
     cpu = None
     fp64 = None
     if rank == 0 and not args.no_cpu:
-        v, th, sl = cpu_sample(1)
+        v, th, sl = cpu_sample(2)
         cpu = {"value": round(v, 2), "unit": UNIT, "cores": th, "kind": "port",
-               "sample": "CPU oracle (OpenMP, all host threads) on the same case at half resolution per axis "
-                         "(64x32x32 base, 3 levels, r=4; %d fluid updates per step), 1 level-0 step" % sl}
+               "sample": "CPU oracle (OpenMP, all host threads) on the same case (128x64x64 base, 3 levels, r=8; "
+                         "%d fluid updates per step on its initial mesh), 2 level-0 steps" % sl}
         fp64 = fp64_error(ctx)
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": workload_config({"bricks": int(bricks0), "fluid_lups_per_step": int(lups0),
+                "config": workload_config({"timed_from_step": args.spinup + args.warmup + 1,
+                                           "bricks": int(bricks0), "fluid_lups_per_step": int(lups0),
                                            "bricks_per_level": [int(info.bricks_per_level[l]) for l in range(4)],
                                            "fluid_sites_per_level": [int(info.fluid_sites_per_level[l]) for l in range(4)],
+                                           "initial_mesh": {"bricks": int(info0.num_bricks),
+                                                            "fluid_lups_per_step": int(info0.fluid_lups_per_step)},
                                            "parallelism": "replicas" if ws > 1 else "single"}),
                 "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h)},
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
                 "regrid_ms_per_cycle": round(statistics.mean(regrid_ms), 3), "regrids_in_timed_region": regrids,
-                "regrid_microbench": micro, "fp32_vs_fp64": fp64}
+                "config2_full_run": full, "regrid_microbench": micro, "batching": batch, "serving": serve,
+                "fp32_vs_fp64": fp64}
         print(json.dumps(line))
     rep.close()
 
 
 def run_reference(args):
+    """The reference arm: the CPU implementation of the path (the oracle port; the reference's
+    own OpenCL kernels cannot run on this host and it has no lattice-Boltzmann code) on the
+    same workload as the GPU arm -- the full 128x64x64, 3-level sphere, a regrid every 25
+    steps -- over all host threads.  K timed steps after W warm-up steps, at most 40 timed
+    (about 1.2 s each on 16 host cores) so the run stays within minutes."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     from tests import _oracle as O
-    case = sphere_case(scale=2)
-    p = O.OraclePool([case])
-    lups = p.lups()
+    p = O.OraclePool([sphere_case()])
     threads = os.cpu_count() or 1
+    step_no = 0
     for _ in range(args.warmup):
         p.step(1, threads)
+        step_no += 1
+        if step_no % REGRID_EVERY == 0:
+            p.regrid()
+    k = min(args.steps, 40)
+    lups = 0
+    regrids = 0
     t0 = time.perf_counter()
-    p.step(args.steps, threads)
+    for _ in range(k):
+        lups += p.lups()
+        p.step(1, threads)
+        step_no += 1
+        if step_no % REGRID_EVERY == 0:
+            p.regrid()
+            regrids += 1
     dt = time.perf_counter() - t0
-    value = lups * args.steps / dt / 1e6
+    value = lups / dt / 1e6
     sample = ("CPU restatement of the path (oracle/, OpenMP over all host threads; the reference has no "
-              "lattice-Boltzmann code and its OpenCL kernels cannot run on this host) on the workload at half "
-              "resolution per axis (64x32x32 base, 3 levels, r=4), %d fluid updates per step" % lups)
-    line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 3), "higher_is_better": True,
+              "lattice-Boltzmann code and its OpenCL kernels cannot run on this host) on the same workload: "
+              "%d timed level-0 steps (of the %d asked) after %d warm-up steps, %d regrid(s) inside"
+              % (k, args.steps, args.warmup, regrids))
+    line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": ws, "steps": k,
+            "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / k, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-            "config": workload_config({"sample_scale": 0.5}),
+            "config": workload_config({"same_config": True}),
             "cpu_baseline": {"value": round(value, 2), "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(value, 2), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -454,6 +569,14 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-microbench", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--spinup", type=int, default=500,
+                    help="untimed level-0 steps (with regrids) before the warm-up, so the timed steps see the "
+                         "developed flow")
+    ap.add_argument("--no-full-run", action="store_true")
+    ap.add_argument("--no-batching", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serving-seconds", type=float, default=2.0,
+                    help="length of the Poisson arrival stream of the serving figure (the configuration's is 60 s)")
     ap.add_argument("--microbench-only", action="store_true",
                     help="run only the 2^24-leaf regrid microbench (one warm-up pass, one timed) and print it")
     ap.add_argument("--microbench-level", type=int, default=8,

@@ -68,16 +68,9 @@ def run(pool, steps, regrid_every):
     return lups
 
 
-def main(argv=None):
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--cases", type=int, default=256)
-    ap.add_argument("--steps", type=int, default=500)
-    ap.add_argument("--regrid-every", type=int, default=20)
-    ap.add_argument("--check", type=int, default=-1, help="cases compared bitwise with their solo run (-1 = all)")
-    args = ap.parse_args(argv)
-    ctx = Context(0)
-    cases = cavity_batch(args.cases)
-    # batched
+def benchmark(ctx, cases, steps=500, regrid_every=20, check=-1):
+    """The batched pool against the same cases one at a time (both with the autotuned options);
+    returns throughput, speed-up and the cases whose batched populations differ from their solo run."""
     pool = Pool(ctx, cases)
     tuned, tuned_streams = autotune(pool)
     pool.close()
@@ -85,13 +78,14 @@ def main(argv=None):
     pool.set_options(graphs=1, grid_mult=tuned, streams=tuned_streams)
     ctx.sync()
     t0 = time.perf_counter()
-    lups_b = run(pool, args.steps, args.regrid_every)
+    lups_b = run(pool, steps, regrid_every)
     ctx.sync()
     tb = time.perf_counter() - t0
     bricks = pool.bricks()
     fb = pool.populations()
+    pool.close()
     # plain: one case at a time on the same GPU
-    nchk = args.cases if args.check < 0 else min(args.check, args.cases)
+    nchk = len(cases) if check < 0 else min(check, len(cases))
     tp = 0.0
     lups_p = 0
     mismatched = []
@@ -100,7 +94,7 @@ def main(argv=None):
         p.set_options(graphs=1, grid_mult=tuned, streams=tuned_streams)
         ctx.sync()
         t0 = time.perf_counter()
-        lups_p += run(p, args.steps, args.regrid_every)
+        lups_p += run(p, steps, regrid_every)
         ctx.sync()
         tp += time.perf_counter() - t0
         if i < nchk:
@@ -108,13 +102,22 @@ def main(argv=None):
             if not np.array_equal(fb[:, m, :], p.populations()):
                 mismatched.append(i)
         p.close()
-    res = {"workload": "%d lid-driven cavities, %d steps, regrid every %d" % (args.cases, args.steps,
-                                                                              args.regrid_every),
-           "batched_mlups": lups_b / tb / 1e6, "plain_mlups": lups_p / tp / 1e6,
-           "speedup": (lups_b / tb) / (lups_p / tp), "batched_s": tb, "plain_s": tp,
-           "lups_batched": int(lups_b), "lups_plain": int(lups_p), "autotuned_ctas_per_sm": tuned,
-           "autotuned_class_streams": tuned_streams,
-           "cases_checked": nchk, "cases_mismatched": mismatched}
+    return {"workload": "%d lid-driven cavities, %d steps, regrid every %d" % (len(cases), steps, regrid_every),
+            "batched_mlups": round(lups_b / tb / 1e6, 1), "plain_mlups": round(lups_p / tp / 1e6, 1),
+            "speedup": round((lups_b / tb) / (lups_p / tp), 3), "batched_s": round(tb, 3), "plain_s": round(tp, 3),
+            "lups_batched": int(lups_b), "lups_plain": int(lups_p), "autotuned_ctas_per_sm": tuned,
+            "autotuned_class_streams": tuned_streams, "cases_checked": nchk, "cases_mismatched": mismatched}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--cases", type=int, default=256)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--regrid-every", type=int, default=20)
+    ap.add_argument("--check", type=int, default=-1, help="cases compared bitwise with their solo run (-1 = all)")
+    args = ap.parse_args(argv)
+    ctx = Context(0)
+    res = benchmark(ctx, cavity_batch(args.cases), args.steps, args.regrid_every, args.check)
     print(json.dumps(res))
     return res
 

@@ -783,14 +783,17 @@ int fl_mesh_alloc(fl_ctx* ctx, size_t capacity, int with_case_id, fl_mesh* m) {
     if (!ctx || !m) return FL_E_INVALID_ARG;
     *m = fl_mesh{};
     if (capacity == 0) capacity = 1;
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&m->x, capacity * 4, ctx->stream), "mesh alloc");
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&m->y, capacity * 4, ctx->stream), "mesh alloc");
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&m->z, capacity * 4, ctx->stream), "mesh alloc");
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&m->level, capacity, ctx->stream), "mesh alloc");
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&m->state, capacity, ctx->stream), "mesh alloc");
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&m->flags, capacity * 4, ctx->stream), "mesh alloc");
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&m->material, capacity * 4, ctx->stream), "mesh alloc");
-    if (with_case_id) FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&m->case_id, capacity * 2, ctx->stream), "mesh alloc");
+    void** col[8] = {(void**)&m->x, (void**)&m->y, (void**)&m->z, (void**)&m->level, (void**)&m->state,
+                     (void**)&m->flags, (void**)&m->material, (void**)&m->case_id};
+    const size_t width[8] = {4, 4, 4, 1, 1, 4, 4, 2};
+    for (int k = 0; k < (with_case_id ? 8 : 7); ++k) {
+        cudaError_t e = fl_dev_malloc_async(ctx, col[k], capacity * width[k], ctx->stream);
+        if (e != cudaSuccess) {  // nothing half-allocated is left behind
+            for (int j = 0; j < k; ++j) cudaFreeAsync(*col[j], ctx->stream);
+            *m = fl_mesh{};
+            return fl_check_cuda(ctx, e, "mesh alloc");
+        }
+    }
     m->capacity = capacity;
     m->num_cells = 0;
     return FL_OK;
@@ -904,10 +907,20 @@ int fl_adapt(fl_ctx* ctx, fl_mesh* mesh, const fl_adapt_config* cfg, float** fie
     rc = fl_mesh_alloc(ctx, cap_out, mesh->case_id != nullptr, &out);
     if (rc) return rc;
     float* nf = nullptr;
-    if (C) FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&nf, cap_out * C * 4, ctx->stream), "fields alloc");
+    if (C) {
+        cudaError_t e = fl_dev_malloc_async(ctx, (void**)&nf, cap_out * C * 4, ctx->stream);
+        if (e != cudaSuccess) {  // the input mesh and fields stay as they were
+            fl_mesh_free(ctx, &out);
+            return fl_check_cuda(ctx, e, "fields alloc");
+        }
+    }
     rc = fl_adapt_finish(ctx, mesh, cfg, dom, scratch, M, C ? *fields : nullptr, C, &out, nf, nullptr, nullptr,
                          nullptr, s.num_groups);
-    if (rc) return rc;
+    if (rc) {
+        fl_mesh_free(ctx, &out);
+        if (nf) cudaFreeAsync(nf, ctx->stream);
+        return rc;
+    }
     fl_mesh old = *mesh;
     fl_mesh_free(ctx, &old);
     if (C) {

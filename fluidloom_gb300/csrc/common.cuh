@@ -28,9 +28,19 @@ struct fl_ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // fl_ctx_timer_start / stop
     void* soa = nullptr;                       // structure-of-arrays field manager (fields.cu)
     uint64_t launches = 0;                     // kernels launched on behalf of this context
+    int64_t alloc_fail_countdown = -1;         // fault injection: allocations left before they fail (-1 off)
 };
 
+// Every device allocation the library makes goes through these two: cudaMalloc
+// or cudaMallocAsync on st, unless the context's fault-injection countdown
+// (fl_ctx_inject_alloc_failure) has run out, in which case nothing is
+// allocated and cudaErrorMemoryAllocation is returned as CUDA would.
+cudaError_t fl_dev_malloc(fl_ctx* ctx, void** p, size_t bytes);
+cudaError_t fl_dev_malloc_async(fl_ctx* ctx, void** p, size_t bytes, cudaStream_t st);
+
 void fl_soa_release_all(fl_ctx* ctx);
+int fl_soa_bind_external(fl_ctx* ctx, const fl_field_desc* d, size_t num_cells, size_t pitch, void* base,
+                         uint64_t* handle);
 
 // Device status words written by kernels instead of trapping.
 enum {
@@ -38,6 +48,7 @@ enum {
     FL_DEVSTAT_HASH_OVERFLOW = 1,
     FL_DEVSTAT_LEVEL_JUMP = 2,  // a neighbour more than one level away
     FL_DEVSTAT_BOUNDS = 3,      // an index failed a bounds check and the access was skipped
+    FL_DEVSTAT_HASH_DUPS = 4,   // the current hash build met a repeated key (not an error)
     FL_DEVSTAT_WORDS = 8
 };
 

@@ -16,6 +16,31 @@ int fl_check_cuda(fl_ctx* ctx, cudaError_t e, const char* what) {
     return fl_set_error(ctx, FL_E_CUDA, m);
 }
 
+static bool injected_alloc_failure(fl_ctx* ctx) {
+    if (!ctx || ctx->alloc_fail_countdown < 0) return false;
+    if (ctx->alloc_fail_countdown == 0) return true;
+    --ctx->alloc_fail_countdown;
+    return false;
+}
+
+// A failed allocation always leaves *p null, so cleanup paths never free a
+// stale pointer.
+cudaError_t fl_dev_malloc(fl_ctx* ctx, void** p, size_t bytes) {
+    *p = nullptr;
+    if (injected_alloc_failure(ctx)) return cudaErrorMemoryAllocation;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) *p = nullptr;
+    return e;
+}
+
+cudaError_t fl_dev_malloc_async(fl_ctx* ctx, void** p, size_t bytes, cudaStream_t st) {
+    *p = nullptr;
+    if (injected_alloc_failure(ctx)) return cudaErrorMemoryAllocation;
+    cudaError_t e = cudaMallocAsync(p, bytes, st);
+    if (e != cudaSuccess) *p = nullptr;
+    return e;
+}
+
 int fl_scratch_reserve(fl_ctx* ctx, size_t bytes) {
     if (bytes <= ctx->scratch_bytes) return FL_OK;
     size_t want = bytes + bytes / 4 + (1 << 20);
@@ -26,7 +51,7 @@ int fl_scratch_reserve(fl_ctx* ctx, size_t bytes) {
         ctx->scratch = nullptr;
         ctx->scratch_bytes = 0;
     }
-    FL_TRY_CUDA(ctx, cudaMalloc(&ctx->scratch, want), "scratch allocation");
+    FL_TRY_CUDA(ctx, fl_dev_malloc(ctx, &ctx->scratch, want), "scratch allocation");
     ctx->scratch_bytes = want;
     return FL_OK;
 }
@@ -138,13 +163,19 @@ int fl_ctx_synchronize(fl_ctx* ctx) {
     return FL_OK;
 }
 
+int fl_ctx_inject_alloc_failure(fl_ctx* ctx, int64_t after) {
+    if (!ctx) return FL_E_INVALID_ARG;
+    ctx->alloc_fail_countdown = after < 0 ? -1 : after;
+    return FL_OK;
+}
+
 const char* fl_last_error(fl_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "no context"; }
 
 int fl_device_alloc(fl_ctx* ctx, size_t bytes, void** out) {
     if (!ctx || !out) return FL_E_INVALID_ARG;
     *out = nullptr;
     if (bytes == 0) return FL_OK;
-    FL_TRY_CUDA(ctx, cudaMalloc(out, bytes), "fl_device_alloc");
+    FL_TRY_CUDA(ctx, fl_dev_malloc(ctx, out, bytes), "fl_device_alloc");
     return FL_OK;
 }
 

@@ -57,6 +57,7 @@ struct FieldState {
     size_t pitch = 0;  // bytes between components
     void* base = nullptr;
     uint64_t version = 1;
+    bool external = false;  // storage owned elsewhere (a pool's populations): never freed or resized here
 };
 
 struct SoaManager {
@@ -85,7 +86,7 @@ void fl_soa_release_all(fl_ctx* ctx) {
     if (!ctx || !ctx->soa) return;
     SoaManager* m = (SoaManager*)ctx->soa;
     for (auto& kv : m->fields)
-        if (kv.second.base) cudaFree(kv.second.base);
+        if (kv.second.base && !kv.second.external) cudaFree(kv.second.base);
     delete m;
     ctx->soa = nullptr;
 }
@@ -177,7 +178,7 @@ int fl_soa_allocate(fl_ctx* ctx, const fl_field_desc* d, size_t num_cells, uint6
     st.num_cells = num_cells;
     st.pitch = pitch_of(*d, num_cells);
     size_t bytes = st.pitch * d->num_components;
-    if (bytes) FL_TRY_CUDA(ctx, cudaMalloc(&st.base, bytes), "fl_soa_allocate");
+    if (bytes) FL_TRY_CUDA(ctx, fl_dev_malloc(ctx, (void**)&st.base, bytes), "fl_soa_allocate");
     if (bytes) FL_TRY_CUDA(ctx, cudaMemsetAsync(st.base, 0, bytes, ctx->stream), "fl_soa_allocate zero");
     m->fields[id] = st;
     *handle = id;
@@ -191,12 +192,13 @@ int fl_soa_resize(fl_ctx* ctx, uint64_t handle, size_t new_num_cells) {
     auto it = m->fields.find(handle);
     if (it == m->fields.end()) return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_soa_resize: unknown field");
     FieldState& st = it->second;
+    if (st.external) return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_soa_resize: the field's storage belongs to a pool");
     if (new_num_cells == st.num_cells) return FL_OK;
     size_t np = pitch_of(st.desc, new_num_cells);
     void* nb = nullptr;
     size_t bytes = np * st.desc.num_components;
     if (bytes) {
-        FL_TRY_CUDA(ctx, cudaMalloc(&nb, bytes), "fl_soa_resize");
+        FL_TRY_CUDA(ctx, fl_dev_malloc(ctx, (void**)&nb, bytes), "fl_soa_resize");
         FL_TRY_CUDA(ctx, cudaMemsetAsync(nb, 0, bytes, ctx->stream), "fl_soa_resize zero");
     }
     size_t keep = type_size(st.desc.type) * (new_num_cells < st.num_cells ? new_num_cells : st.num_cells);
@@ -219,7 +221,7 @@ int fl_soa_deallocate(fl_ctx* ctx, uint64_t handle) {
     auto it = m->fields.find(handle);
     if (it == m->fields.end()) return FL_OK;  // the reference only warns
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "fl_soa_deallocate");
-    if (it->second.base) cudaFree(it->second.base);
+    if (it->second.base && !it->second.external) cudaFree(it->second.base);
     m->fields.erase(it);
     return FL_OK;
 }
@@ -258,3 +260,31 @@ size_t fl_soa_total_bytes(fl_ctx* ctx) {
 }
 
 }  // extern "C"
+
+// A field of the context's manager over storage owned elsewhere (component c at
+// base + c * pitch bytes, num_cells cells); binding the same name again points
+// it at the new storage and bumps its version when anything changed.
+int fl_soa_bind_external(fl_ctx* ctx, const fl_field_desc* d, size_t num_cells, size_t pitch, void* base,
+                         uint64_t* handle) {
+    if (!ctx || !d || !handle) return FL_E_INVALID_ARG;
+    int rc = validate(d, ctx);
+    if (rc) return rc;
+    if (!ctx->soa) ctx->soa = new SoaManager();
+    SoaManager* m = (SoaManager*)ctx->soa;
+    std::lock_guard<std::mutex> lock(m->mu);
+    const uint64_t id = fnv1a_64(d->name);
+    auto it = m->fields.find(id);
+    if (it != m->fields.end() && !it->second.external)
+        return fl_set_error(ctx, FL_E_INVALID_ARG, "a field of that name is allocated by the manager");
+    FieldState& st = m->fields[id];
+    const bool changed = st.base != base || st.pitch != pitch || st.num_cells != num_cells;
+    st.desc = *d;
+    st.desc.id = id;
+    st.num_cells = num_cells;
+    st.pitch = pitch;
+    st.base = base;
+    st.external = true;
+    if (changed && it != m->fields.end()) st.version++;
+    *handle = id;
+    return FL_OK;
+}

@@ -184,7 +184,7 @@ int compact_grid(fl_ctx* ctx, uint32_t* flag, size_t nv, int x0, int y0, int z0,
                  int32_t* ox, int32_t* oy, int32_t* oz, size_t* count) {
     uint32_t* off = nullptr;
     uint32_t* dtot = nullptr;
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&off, nv * 4 + 256, ctx->stream), "geometry offsets");
+    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&off, nv * 4 + 256, ctx->stream), "geometry offsets");
     dtot = off + ((nv + 63) / 64) * 64;
     int rc = fl_scan_exclusive_u32(ctx, flag, off, nv, dtot);
     if (rc) { cudaFreeAsync(off, ctx->stream); return rc; }
@@ -293,8 +293,8 @@ int fl_stl_voxelize(fl_ctx* ctx, const float* tris, size_t ntri, const fl_geomet
     if (rc || !nv) return rc;
     float* dt = nullptr;
     uint32_t* flag = nullptr;
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&dt, t.size() * 4 + 32, ctx->stream), "triangles");
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&flag, nv * 4, ctx->stream), "voxel flags");
+    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&dt, t.size() * 4 + 32, ctx->stream), "triangles");
+    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&flag, nv * 4, ctx->stream), "voxel flags");
     float* dmb = dt + t.size();
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(dt, t.data(), t.size() * 4, cudaMemcpyHostToDevice, ctx->stream), "triangles");
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(dmb, mb, 24, cudaMemcpyHostToDevice, ctx->stream), "mesh bounds");
@@ -330,7 +330,7 @@ int fl_geometry_process(fl_ctx* ctx, const fl_geometry_desc* d, const float* tri
     int rc = grid_range(ctx, lo, hi, cell_size, false, o, e, &nv);
     if (rc || !nv) return rc;
     uint32_t* flag = nullptr;
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&flag, nv * 4, ctx->stream), "candidate flags");
+    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&flag, nv * 4, ctx->stream), "candidate flags");
     k_implicit_candidates<<<fl_blocks(nv, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(to_dev(*d), o[0], o[1], o[2],
                                                                                         e[0], e[1], nv, flag);
     FL_CHECK_LAUNCH(ctx, "k_implicit_candidates");

@@ -5,9 +5,9 @@
 // which launch nothing) with the kernels they name (kernels/hashmap/hash_build.cl:19-82,
 // kernels/hashmap/hash_query.cl:22-98): EMPTY key = ~0, INVALID value = ~0,
 // power-of-two capacity, linear probing, a repeated key keeps the value of
-// the LAST input carrying it (the order sequential insertion gives; resolved
-// here with an atomicMax on the input index so the result does not depend
-// on thread timing).  The slot is the high bits of key * 0x9e3779b97f4a7c15
+// the LAST input carrying it (the order sequential insertion gives; resolved,
+// only when a build meets repeated keys, with an atomicMax on the input index
+// so the result does not depend on thread timing).  The slot is the high bits of key * 0x9e3779b97f4a7c15
 // (Fibonacci hashing); the reference masks the low bits, which for 12-state
 // keys of coarse anchors fall on a handful of slots.
 #include "common.cuh"
@@ -19,8 +19,7 @@ namespace {
 
 constexpr int kProbeLimit = 256;
 
-__global__ void k_hash_clear(uint64_t* __restrict__ tk, uint32_t* __restrict__ tv, uint32_t* __restrict__ win,
-                             uint64_t cap) {
+__global__ void k_hash_clear(uint64_t* __restrict__ tk, uint32_t* __restrict__ tv, uint64_t cap) {
     size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += stride) {
         if (tv) {
@@ -29,43 +28,98 @@ __global__ void k_hash_clear(uint64_t* __restrict__ tk, uint32_t* __restrict__ t
         } else {
             reinterpret_cast<ulonglong2*>(tk)[i] = make_ulonglong2(FL_EMPTY_KEY, FL_INVALID_INDEX);
         }
-        if (win) win[i] = 0u;
     }
 }
 
-__global__ void k_hash_insert(uint64_t* __restrict__ tk, int slot_words, uint32_t* __restrict__ win, int lg,
-                              const uint64_t* __restrict__ keys, size_t n, uint32_t* dev_status) {
+// The value input i stores: vals[i], or (level << kPackedIdxBits) | i, or i.
+__device__ __forceinline__ uint32_t hash_value_of(size_t i, const uint32_t* __restrict__ vals,
+                                                  const uint8_t* __restrict__ levels) {
+    if (vals) return vals[i];
+    if (levels) return ((uint32_t)levels[i] << kPackedIdxBits) | (uint32_t)i;
+    return (uint32_t)i;
+}
+
+__device__ __forceinline__ void hash_store_value(uint64_t* tk, uint32_t* tv, uint64_t s, uint32_t v) {
+    if (tv) tv[s] = v;
+    else tk[2 * s + 1] = v;
+}
+
+// Insertion: the thread whose CAS claims an empty slot stores its value with a
+// plain store; a thread that finds its key already there flags the build
+// (FL_DEVSTAT_HASH_DUPS) and stores nothing.  Without repeated keys that is
+// the table; with them the three passes below give each repeated key the
+// value of its last input.
+__global__ void k_hash_insert(uint64_t* __restrict__ tk, uint32_t* __restrict__ tv, int lg,
+                              const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals,
+                              const uint8_t* __restrict__ levels, size_t n, uint32_t* dev_status) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const uint64_t mask = (1ull << lg) - 1;
+    const int sw = tv ? 1 : 2;
+    for (size_t base = (size_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+        const size_t i = base + threadIdx.x;
+        bool dup = false;
+        if (i < n) {
+            const uint64_t k = keys[i];
+            if (k != FL_EMPTY_KEY) {
+                uint64_t s = fl_hash_slot(k, lg);
+                int p = 0;
+                for (; p < kProbeLimit; ++p) {
+                    unsigned long long prev = atomicCAS((unsigned long long*)(tk + s * sw), FL_EMPTY_KEY, k);
+                    if (prev == FL_EMPTY_KEY) {
+                        hash_store_value(tk, tv, s, hash_value_of(i, vals, levels));
+                        break;
+                    }
+                    if (prev == k) {
+                        dup = true;
+                        break;
+                    }
+                    s = (s + 1) & mask;
+                }
+                if (p == kProbeLimit) atomicAdd(dev_status + FL_DEVSTAT_HASH_OVERFLOW, 1u);
+            }
+        }
+        if (__any_sync(0xFFFFFFFFu, dup) && (threadIdx.x & 31) == 0) atomicOr(dev_status + FL_DEVSTAT_HASH_DUPS, 1u);
+    }
+}
+
+// Repeated keys only (each kernel returns at once when the build met none):
+// clear the winner words, let every input take the maximum of its slot's
+// winner (input index + 1), then store each claimed slot's winning value.
+__global__ void k_hash_dup_clear(uint32_t* __restrict__ win, uint64_t cap, const uint32_t* dev_status) {
+    if (!*(volatile const uint32_t*)(dev_status + FL_DEVSTAT_HASH_DUPS)) return;
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += stride) win[i] = 0u;
+}
+
+__global__ void k_hash_dup_winners(const uint64_t* __restrict__ tk, int sw, uint32_t* __restrict__ win, int lg,
+                                   const uint64_t* __restrict__ keys, size_t n, const uint32_t* dev_status) {
+    if (!*(volatile const uint32_t*)(dev_status + FL_DEVSTAT_HASH_DUPS)) return;
     size_t stride = (size_t)gridDim.x * blockDim.x;
     const uint64_t mask = (1ull << lg) - 1;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        uint64_t k = keys[i];
+        const uint64_t k = keys[i];
         if (k == FL_EMPTY_KEY) continue;
         uint64_t s = fl_hash_slot(k, lg);
-        int p = 0;
-        for (; p < kProbeLimit; ++p) {
-            unsigned long long prev = atomicCAS((unsigned long long*)(tk + s * slot_words), FL_EMPTY_KEY, k);
-            if (prev == FL_EMPTY_KEY || prev == k) {
+        for (int p = 0; p < kProbeLimit; ++p) {
+            const uint64_t cur = tk[s * sw];
+            if (cur == k) {
                 atomicMax(win + s, (uint32_t)(i + 1));
                 break;
             }
+            if (cur == FL_EMPTY_KEY) break;  // not inserted (probe overflow, reported by the insertion)
             s = (s + 1) & mask;
         }
-        if (p == kProbeLimit) atomicAdd(dev_status + FL_DEVSTAT_HASH_OVERFLOW, 1u);
     }
 }
 
-__global__ void k_hash_values(uint64_t* __restrict__ tk, uint32_t* __restrict__ tv, const uint32_t* __restrict__ win,
-                              const uint32_t* __restrict__ vals, const uint8_t* __restrict__ levels, uint64_t cap) {
+__global__ void k_hash_dup_values(uint64_t* __restrict__ tk, uint32_t* __restrict__ tv,
+                                  const uint32_t* __restrict__ win, const uint32_t* __restrict__ vals,
+                                  const uint8_t* __restrict__ levels, uint64_t cap, const uint32_t* dev_status) {
+    if (!*(volatile const uint32_t*)(dev_status + FL_DEVSTAT_HASH_DUPS)) return;
     size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += stride) {
-        uint32_t w = win[i];
-        if (!w) continue;
-        uint32_t v;
-        if (vals) v = vals[w - 1];
-        else if (levels) v = ((uint32_t)levels[w - 1] << kPackedIdxBits) | (w - 1);
-        else v = w - 1;
-        if (tv) tv[i] = v;
-        else tk[2 * i + 1] = v;
+        const uint32_t w = win[i];
+        if (w) hash_store_value(tk, tv, i, hash_value_of(w - 1, vals, levels));
     }
 }
 
@@ -289,15 +343,21 @@ int fl_hash_build_with(fl_ctx* ctx, uint64_t* tk, uint32_t* tv, uint64_t cap, co
     if (levels && !vals && n >= ((size_t)1 << kPackedIdxBits))
         return fl_set_error(ctx, FL_E_CAPACITY, "a mesh of 2^27 or more cells");
     unsigned cb = fl_blocks(cap, 256, ctx->num_sms * 8);
-    k_hash_clear<<<cb, 256, 0, ctx->stream>>>(tk, tv, win, cap);
+    k_hash_clear<<<cb, 256, 0, ctx->stream>>>(tk, tv, cap);
     FL_CHECK_LAUNCH(ctx, "k_hash_clear");
     if (n == 0) return FL_OK;
+    const uint8_t* lv = vals ? nullptr : levels;
+    FL_TRY_CUDA(ctx, cudaMemsetAsync(ctx->dev_status + FL_DEVSTAT_HASH_DUPS, 0, 4, ctx->stream), "hash flag");
     int lg = fl_hash_lg(cap);
-    k_hash_insert<<<fl_blocks(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(tk, tv ? 1 : 2, win, lg, keys, n,
-                                                                                 ctx->dev_status);
+    unsigned nb = fl_blocks(n, 256, ctx->num_sms * 8);
+    k_hash_insert<<<nb, 256, 0, ctx->stream>>>(tk, tv, lg, keys, vals, lv, n, ctx->dev_status);
     FL_CHECK_LAUNCH(ctx, "k_hash_insert");
-    k_hash_values<<<cb, 256, 0, ctx->stream>>>(tk, tv, win, vals, vals ? nullptr : levels, cap);
-    FL_CHECK_LAUNCH(ctx, "k_hash_values");
+    k_hash_dup_clear<<<cb, 256, 0, ctx->stream>>>(win, cap, ctx->dev_status);
+    FL_CHECK_LAUNCH(ctx, "k_hash_dup_clear");
+    k_hash_dup_winners<<<nb, 256, 0, ctx->stream>>>(tk, tv ? 1 : 2, win, lg, keys, n, ctx->dev_status);
+    FL_CHECK_LAUNCH(ctx, "k_hash_dup_winners");
+    k_hash_dup_values<<<cb, 256, 0, ctx->stream>>>(tk, tv, win, vals, lv, cap, ctx->dev_status);
+    FL_CHECK_LAUNCH(ctx, "k_hash_dup_values");
     return FL_OK;
 }
 

@@ -50,6 +50,13 @@ __device__ __forceinline__ float Wq(int q) {
 }
 
 constexpr uint32_t kSlow = 0xFFFFFFFEu;
+
+#define FL_POOL_USABLE(ctx, P)                                                                              \
+    do {                                                                                                    \
+        if ((P)->unusable)                                                                                  \
+            return fl_set_error((ctx), FL_E_INVALID_ARG,                                                    \
+                                "pool unusable: an earlier call on it failed part-way (destroy it)");       \
+    } while (0)
 constexpr int kMaxPoolLevels = 14;  // case max_level is 0..13
 
 }  // namespace
@@ -575,6 +582,20 @@ __global__ void __launch_bounds__(128, 4) k_collide_general(StepArgs a, const ui
             *(float4*)(a.W + fidx(a.cap, q, b, own)) = make_float4(f[q][0], f[q][1], f[q][2], f[q][3]);
         __syncthreads();
         b = bn;
+    }
+}
+
+// The populations of the listed bricks from one buffer to the other, a float4
+// per thread.
+__global__ void k_copy_bricks(const float* __restrict__ src, float* __restrict__ dst, size_t cap,
+                              const uint32_t* __restrict__ list, uint32_t count) {
+    const size_t total = (size_t)count * Q * 128;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
+        const size_t w = t / (Q * 128);
+        const int r = (int)(t - w * (Q * 128));
+        const size_t off = ((size_t)(r >> 7) * cap + list[w]) * 512 + (size_t)(r & 127) * 4;
+        *(float4*)(dst + off) = *(const float4*)(src + off);
     }
 }
 
@@ -1299,6 +1320,11 @@ __global__ void k_compact_bricks(fl_mesh_dev m, const uint32_t* __restrict__ kee
 constexpr int kMaxCases = 4096;  // case ids live in 12 key bits
 
 struct fl_pool {
+    // Set while a call that replaces the pool's bricks or tables is past its
+    // point of no return; left set when such a call fails there, after which
+    // every entry point refuses the pool (FL_POOL_USABLE) instead of launching
+    // on tables that no longer match its bricks.  Destroying it stays allowed.
+    bool unusable = false;
     std::vector<fl_lbm_case> cases;   // one entry per slot (case id)
     std::vector<uint8_t> active;      // slot in use
     uint8_t* d_mask = nullptr;        // per-slot byte mask on the device (regrid / removal)
@@ -1422,33 +1448,75 @@ int pool_reserve_bricks(fl_ctx* ctx, fl_pool* P, size_t need) {
 }
 
 int alloc_brick_arrays(fl_ctx* ctx, fl_pool* P, size_t cap) {
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->nbr, cap * 26 * 4 * 4, ctx->stream), "pool nbr");
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->list, cap * 8, ctx->stream), "pool list");  // list + general positions
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->wmax, cap * 4, ctx->stream), "pool wmax");
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->part, cap * 32, ctx->stream), "pool partials");
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->fluid, cap * 4, ctx->stream), "pool fluid");
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->nb27, cap * 28 * 4, ctx->stream), "pool nb27");
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->bclass, cap, ctx->stream), "pool classes");
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->mnear, cap, ctx->stream), "pool mask bits");
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->slow_cnt, cap * 4, ctx->stream), "pool descriptor counts");
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->slow_off, (cap + 1) * 4, ctx->stream), "pool descriptor offsets");
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->smask, cap * 64, ctx->stream), "pool solid masks");
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->qmask, cap * 128 * sizeof(uint4), ctx->stream), "pool quad masks");
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->hsolid, cap * 32 * 4, ctx->stream), "pool halo solid bits");
+    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->nbr, cap * 26 * 4 * 4, ctx->stream), "pool nbr");
+    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->list, cap * 8, ctx->stream), "pool list");  // list + general positions
+    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->wmax, cap * 4, ctx->stream), "pool wmax");
+    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->part, cap * 32, ctx->stream), "pool partials");
+    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->fluid, cap * 4, ctx->stream), "pool fluid");
+    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->nb27, cap * 28 * 4, ctx->stream), "pool nb27");
+    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->bclass, cap, ctx->stream), "pool classes");
+    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->mnear, cap, ctx->stream), "pool mask bits");
+    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->slow_cnt, cap * 4, ctx->stream), "pool descriptor counts");
+    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->slow_off, (cap + 1) * 4, ctx->stream), "pool descriptor offsets");
+    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->smask, cap * 64, ctx->stream), "pool solid masks");
+    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->qmask, cap * 128 * sizeof(uint4), ctx->stream), "pool quad masks");
+    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->hsolid, cap * 32 * 4, ctx->stream), "pool halo solid bits");
     const size_t max_chunks = cap / kChunkBricks + kMaxCases + 1;  // one partial chunk per case at most
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->d_chunks, max_chunks * sizeof(uint2), ctx->stream), "pool chunks");
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->chunk_part, max_chunks * 32, ctx->stream), "pool chunk sums");
+    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->d_chunks, max_chunks * sizeof(uint2), ctx->stream), "pool chunks");
+    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->chunk_part, max_chunks * 32, ctx->stream), "pool chunk sums");
     return FL_OK;
 }
 
-void free_brick_arrays(fl_ctx* ctx, fl_pool* P) {
-    void* ps[15] = {P->nbr,      P->list,     P->wmax,  P->part,  P->fluid,    P->nb27,       P->bclass, P->slow_cnt,
-                    P->slow_off, P->smask, P->qmask, P->d_chunks, P->chunk_part, P->mnear, P->hsolid};
-    for (void* p : ps)
+// The pool's 15 per-brick arrays as one set of pointers, so that a grown set can
+// be allocated beside the current one and swapped in only when complete.
+struct BrickArrays {
+    void* p[15];
+};
+
+void brick_slots(fl_pool* P, void** s[15]) {
+    s[0] = (void**)&P->nbr; s[1] = (void**)&P->list; s[2] = (void**)&P->wmax; s[3] = (void**)&P->part;
+    s[4] = (void**)&P->fluid; s[5] = (void**)&P->nb27; s[6] = (void**)&P->bclass; s[7] = (void**)&P->slow_cnt;
+    s[8] = (void**)&P->slow_off; s[9] = (void**)&P->smask; s[10] = (void**)&P->qmask; s[11] = (void**)&P->d_chunks;
+    s[12] = (void**)&P->chunk_part; s[13] = (void**)&P->mnear; s[14] = (void**)&P->hsolid;
+}
+
+BrickArrays get_brick_arrays(fl_pool* P) {
+    void** s[15];
+    brick_slots(P, s);
+    BrickArrays b;
+    for (int k = 0; k < 15; ++k) b.p[k] = *s[k];
+    return b;
+}
+
+void put_brick_arrays(fl_pool* P, const BrickArrays& b) {
+    void** s[15];
+    brick_slots(P, s);
+    for (int k = 0; k < 15; ++k) *s[k] = b.p[k];
+}
+
+void release_brick_arrays(fl_ctx* ctx, const BrickArrays& b) {
+    for (void* p : b.p)
         if (p) cudaFreeAsync(p, ctx->stream);
-    P->nbr = nullptr; P->list = nullptr; P->wmax = nullptr; P->part = nullptr; P->fluid = nullptr;
-    P->nb27 = nullptr; P->bclass = nullptr; P->slow_cnt = nullptr; P->slow_off = nullptr; P->smask = nullptr;
-    P->qmask = nullptr; P->d_chunks = nullptr; P->chunk_part = nullptr; P->mnear = nullptr; P->hsolid = nullptr;
+}
+
+void free_brick_arrays(fl_ctx* ctx, fl_pool* P) {
+    release_brick_arrays(ctx, get_brick_arrays(P));
+    put_brick_arrays(P, BrickArrays{});
+}
+
+// A new set of per-brick arrays for cap bricks in *fresh, leaving the pool's own
+// set in place; nothing stays allocated on failure.
+int alloc_brick_arrays_beside(fl_ctx* ctx, fl_pool* P, size_t cap, BrickArrays* fresh) {
+    const BrickArrays cur = get_brick_arrays(P);
+    put_brick_arrays(P, BrickArrays{});
+    int rc = alloc_brick_arrays(ctx, P, cap);
+    *fresh = get_brick_arrays(P);
+    put_brick_arrays(P, cur);
+    if (rc) {
+        release_brick_arrays(ctx, *fresh);
+        *fresh = BrickArrays{};
+    }
+    return rc;
 }
 
 // The captured steps no longer match the pool: mark them stale.  The next
@@ -1471,7 +1539,18 @@ void free_graphs(fl_pool* P) {
 }
 
 // Neighbour table, per-level lists, case ranges and fluid count for the current mesh.
+int pool_topology_build(fl_ctx* ctx, fl_pool* P);
+
+// Rebuild the tables of the pool's current bricks; the pool is unusable until
+// this succeeds.
 int pool_topology(fl_ctx* ctx, fl_pool* P) {
+    P->unusable = true;
+    int rc = pool_topology_build(ctx, P);
+    if (rc == FL_OK) P->unusable = false;
+    return rc;
+}
+
+int pool_topology_build(fl_ctx* ctx, fl_pool* P) {
     size_t n = P->mesh.num_cells;
     if (P->cap >= (1u << 23))  // descriptors address elements as brick * 512 + site in 32 bits
         return fl_set_error(ctx, FL_E_CAPACITY, "a pool holds fewer than 2^23 bricks");
@@ -1588,11 +1667,16 @@ int pool_topology(fl_ctx* ctx, fl_pool* P) {
     P->num_desc = h.desc64;
     P->lvl_desc.assign(h.lvl_desc, h.lvl_desc + P->maxL + 2);
     if (P->num_desc > P->desc_cap) {
+        // no pointer is left naming freed memory if an allocation fails
         if (P->desc) cudaFreeAsync(P->desc, ctx->stream);
         if (P->pv) cudaFreeAsync(P->pv, ctx->stream);
-        P->desc_cap = P->num_desc + P->num_desc / 4 + 1024;
-        FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->desc, P->desc_cap * 8, ctx->stream), "stencil descriptors");
-        FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->pv, P->desc_cap * 4, ctx->stream), "descriptor values");
+        P->desc = nullptr;
+        P->pv = nullptr;
+        P->desc_cap = 0;
+        const size_t want = P->num_desc + P->num_desc / 4 + 1024;
+        FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->desc, want * 8, ctx->stream), "stencil descriptors");
+        FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->pv, want * 4, ctx->stream), "descriptor values");
+        P->desc_cap = want;
     }
     if (ng) {
         const unsigned egrid = (unsigned)std::min<size_t>(ng, (size_t)ctx->num_sms * 4);
@@ -1670,33 +1754,67 @@ int pool_regrid(fl_ctx* ctx, fl_pool* P, int use_vorticity, fl_adapt_stats* st, 
     fl_domain_dev dom = pool_domain(P);
     size_t sb = fl_adapt_scratch_bytes(n, fl_table_capacity(n));
     if (sb > P->adapt_scratch_bytes) {
+        void* ns = nullptr;
+        const size_t want = sb + sb / 4;
+        FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, &ns, want, ctx->stream), "adapt scratch");
         if (P->adapt_scratch) cudaFreeAsync(P->adapt_scratch, ctx->stream);
-        P->adapt_scratch_bytes = sb + sb / 4;
-        FL_TRY_CUDA(ctx, cudaMallocAsync(&P->adapt_scratch, P->adapt_scratch_bytes, ctx->stream), "adapt scratch");
+        P->adapt_scratch = ns;
+        P->adapt_scratch_bytes = want;
     }
     size_t M = 0;
     fl_adapt_stats s{};
     rc = fl_adapt_prepare(ctx, &P->mesh, &cfg, dom, true, P->adapt_scratch, &M, &s, P->maxL);
     if (rc) return rc;
+    // Nothing splits and nothing merges: the bricks, their key order, the tables
+    // and the populations all stay as they are (AdaptationEngine.cpp:72-78 returns
+    // early the same way); only the flags are reset.  The sort-only regrid after
+    // cases were appended (use_vorticity < 0) must still reorder.
+    if (use_vorticity >= 0 && s.num_split == 0 && s.num_groups == 0) {
+        FL_TRY_CUDA(ctx, cudaMemsetAsync(P->mesh.flags, 0, n * 4, ctx->stream), "flags reset");
+        if (st) *st = s;
+        return FL_OK;
+    }
     size_t new_cap = P->cap;
     if (M > P->cap) new_cap = std::max((size_t)(M * 1.5), M + 64);
+    const bool grew = new_cap != P->cap;
+    // Everything the new mesh needs is allocated before the pool is touched: a
+    // failure up to the remap returns with the pool as it was.
     fl_mesh out{};
-    rc = fl_mesh_alloc(ctx, new_cap, 1, &out);
-    if (rc) return rc;
     uint32_t *osrc = nullptr, *members = nullptr;
     uint8_t* okind = nullptr;
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&osrc, (M + 1) * 4, ctx->stream), "remap src");
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&okind, M + 1, ctx->stream), "remap kind");
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&members, (size_t)s.num_groups * 32 + 32, ctx->stream), "members");
+    float* nf[3] = {nullptr, nullptr, nullptr};
+    BrickArrays fresh{};
+    auto undo = [&](int code) {
+        if (out.x) fl_mesh_free(ctx, &out);
+        void* tmp[6] = {osrc, okind, members, nf[0], nf[1], nf[2]};
+        for (void* p : tmp)
+            if (p) cudaFreeAsync(p, ctx->stream);
+        release_brick_arrays(ctx, fresh);
+        return code;
+    };
+    rc = fl_mesh_alloc(ctx, new_cap, 1, &out);
+    if (rc) return rc;
+    cudaError_t e = fl_dev_malloc_async(ctx, (void**)&osrc, (M + 1) * 4, ctx->stream);
+    if (e == cudaSuccess) e = fl_dev_malloc_async(ctx, (void**)&okind, M + 1, ctx->stream);
+    if (e == cudaSuccess) e = fl_dev_malloc_async(ctx, (void**)&members, (size_t)s.num_groups * 32 + 32, ctx->stream);
+    for (int k = 0; grew && k < 3 && e == cudaSuccess; ++k)
+        e = fl_dev_malloc_async(ctx, (void**)&nf[k], new_cap * 512 * Q * 4, ctx->stream);
+    if (e != cudaSuccess) return undo(fl_check_cuda(ctx, e, "regrid buffers"));
+    if (grew) {
+        rc = alloc_brick_arrays_beside(ctx, P, new_cap, &fresh);
+        if (rc) return undo(rc);
+    }
     rc = fl_adapt_finish(ctx, &P->mesh, &cfg, dom, P->adapt_scratch, M, nullptr, 0, &out, nullptr, osrc, okind, members,
                          s.num_groups);
-    if (rc) return rc;
-    float* target = P->f[2];
-    bool grew = new_cap != P->cap;
-    if (grew) FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&target, new_cap * 512 * Q * 4, ctx->stream), "populations");
+    if (rc) return undo(rc);
+    float* target = grew ? nf[0] : P->f[2];
     k_remap<<<fl_blocks(M * 512, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(view(P), M, osrc, okind, members,
                                                                                 target, new_cap);
-    FL_CHECK_LAUNCH(ctx, "k_remap");
+    ++ctx->launches;
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return undo(fl_check_cuda(ctx, e, "k_remap"));
+    // From here the pool is being replaced: nothing below allocates until the
+    // topology rebuild, whose failure leaves the pool unusable.
     cudaFreeAsync(osrc, ctx->stream);
     cudaFreeAsync(okind, ctx->stream);
     cudaFreeAsync(members, ctx->stream);
@@ -1706,13 +1824,12 @@ int pool_regrid(fl_ctx* ctx, fl_pool* P, int use_vorticity, fl_adapt_stats* st, 
     out.capacity = new_cap;
     P->mesh = out;
     if (grew) {
-        for (int k = 0; k < 3; ++k) cudaFreeAsync(P->f[k], ctx->stream);
-        P->f[0] = target;
-        FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->f[1], new_cap * 512 * Q * 4, ctx->stream), "populations");
-        FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&P->f[2], new_cap * 512 * Q * 4, ctx->stream), "populations");
-        free_brick_arrays(ctx, P);
-        rc = alloc_brick_arrays(ctx, P, new_cap);
-        if (rc) return rc;
+        for (int k = 0; k < 3; ++k) {
+            cudaFreeAsync(P->f[k], ctx->stream);
+            P->f[k] = nf[k];
+        }
+        release_brick_arrays(ctx, get_brick_arrays(P));
+        put_brick_arrays(P, fresh);
         P->cap = new_cap;
     } else {
         // spare <- remapped; old A/B become free
@@ -1728,12 +1845,29 @@ int pool_regrid(fl_ctx* ctx, fl_pool* P, int use_vorticity, fl_adapt_stats* st, 
 
 // Grow every per-brick array to new_cap, keeping the first n bricks (both
 // population buffers A and B are copied, so each level's parity stays valid).
+// Grow the pool's per-brick storage to new_cap bricks.  Everything new is
+// allocated before anything is copied or freed, so an allocation failure
+// returns with the pool exactly as it was.
 int pool_grow(fl_ctx* ctx, fl_pool* P, size_t new_cap) {
     if (new_cap <= P->cap) return FL_OK;
     size_t n = P->mesh.num_cells;
     fl_mesh m2{};
     int rc = fl_mesh_alloc(ctx, new_cap, 1, &m2);
     if (rc) return rc;
+    float* nf[3] = {nullptr, nullptr, nullptr};
+    auto undo = [&](int code) {
+        for (float* p : nf)
+            if (p) cudaFreeAsync(p, ctx->stream);
+        fl_mesh_free(ctx, &m2);
+        return code;
+    };
+    for (int k = 0; k < 3; ++k) {
+        cudaError_t e = fl_dev_malloc_async(ctx, (void**)&nf[k], new_cap * 512 * Q * 4, ctx->stream);
+        if (e != cudaSuccess) return undo(fl_check_cuda(ctx, e, "grow populations"));
+    }
+    BrickArrays fresh;
+    rc = alloc_brick_arrays_beside(ctx, P, new_cap, &fresh);
+    if (rc) return undo(rc);
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(m2.x, P->mesh.x, n * 4, cudaMemcpyDeviceToDevice, ctx->stream), "grow");
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(m2.y, P->mesh.y, n * 4, cudaMemcpyDeviceToDevice, ctx->stream), "grow");
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(m2.z, P->mesh.z, n * 4, cudaMemcpyDeviceToDevice, ctx->stream), "grow");
@@ -1747,18 +1881,15 @@ int pool_grow(fl_ctx* ctx, fl_pool* P, size_t new_cap) {
     fl_mesh_free(ctx, &old);
     P->mesh = m2;
     for (int k = 0; k < 3; ++k) {
-        float* nf = nullptr;
-        FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&nf, new_cap * 512 * Q * 4, ctx->stream), "grow populations");
         if (k < 2)
             for (int q = 0; q < Q; ++q)
-                FL_TRY_CUDA(ctx, cudaMemcpyAsync(nf + (size_t)q * new_cap * 512, P->f[k] + (size_t)q * P->cap * 512,
+                FL_TRY_CUDA(ctx, cudaMemcpyAsync(nf[k] + (size_t)q * new_cap * 512, P->f[k] + (size_t)q * P->cap * 512,
                                                  n * 512 * 4, cudaMemcpyDeviceToDevice, ctx->stream), "grow");
         cudaFreeAsync(P->f[k], ctx->stream);
-        P->f[k] = nf;
+        P->f[k] = nf[k];
     }
-    free_brick_arrays(ctx, P);
-    rc = alloc_brick_arrays(ctx, P, new_cap);
-    if (rc) return rc;
+    release_brick_arrays(ctx, get_brick_arrays(P));
+    put_brick_arrays(P, fresh);
     P->cap = new_cap;
     drop_graph(P);
     return FL_OK;
@@ -1768,6 +1899,7 @@ struct LaunchTimer {
     std::vector<cudaEvent_t> ev;  // start/stop pairs
     std::vector<uint64_t> sites;  // fluid sites processed by each launch
     std::vector<int> kind;        // 0 interior kernel, 1 general kernel, 2 all-solid bricks
+    std::vector<int> level;       // the level of each launch
 };
 
 StepArgs level_args(fl_ctx* ctx, fl_pool* P, int l, int sub) {
@@ -1822,6 +1954,7 @@ void launch_class(fl_ctx* ctx, fl_pool* P, StepArgs a, int l, int kind, cudaStre
         tm->ev.push_back(e1);
         tm->sites.push_back(P->fluid_cls[kind][l]);
         tm->kind.push_back(kind);
+        tm->level.push_back(l);
     }
 }
 
@@ -1981,14 +2114,14 @@ int fl_pool_create(fl_ctx* ctx, const fl_lbm_case* cases, int ncases, fl_pool** 
     }
     if (!sok) return fail(fl_set_error(ctx, FL_E_CUDA, "fl_pool_create: stream or event creation failed"));
     // case tables sized for every slot a pool can hold (cases may be added later)
-    if (cudaMalloc(&P->d_cases, kMaxCases * sizeof(LbmCaseDev)) != cudaSuccess) return fail(FL_E_OOM);
-    if (cudaMalloc(&P->d_dom, kMaxCases * sizeof(fl_domain_dev::Case)) != cudaSuccess) return fail(FL_E_OOM);
-    if (cudaMalloc(&P->d_case_begin, (kMaxCases + 1) * 4) != cudaSuccess) return fail(FL_E_OOM);
-    if (cudaMalloc(&P->d_topo, sizeof(TopoCounters)) != cudaSuccess) return fail(FL_E_OOM);
-    if (cudaMalloc(&P->d_case_chunk, (kMaxCases + 1) * 4) != cudaSuccess) return fail(FL_E_OOM);
-    if (cudaMalloc(&P->case_max, kMaxCases * 4) != cudaSuccess) return fail(FL_E_OOM);
-    if (cudaMalloc(&P->cons, kMaxCases * 32) != cudaSuccess) return fail(FL_E_OOM);
-    if (cudaMalloc(&P->d_mask, kMaxCases) != cudaSuccess) return fail(FL_E_OOM);
+    if (fl_dev_malloc(ctx, (void**)&P->d_cases, kMaxCases * sizeof(LbmCaseDev)) != cudaSuccess) return fail(FL_E_OOM);
+    if (fl_dev_malloc(ctx, (void**)&P->d_dom, kMaxCases * sizeof(fl_domain_dev::Case)) != cudaSuccess) return fail(FL_E_OOM);
+    if (fl_dev_malloc(ctx, (void**)&P->d_case_begin, (kMaxCases + 1) * 4) != cudaSuccess) return fail(FL_E_OOM);
+    if (fl_dev_malloc(ctx, (void**)&P->d_topo, sizeof(TopoCounters)) != cudaSuccess) return fail(FL_E_OOM);
+    if (fl_dev_malloc(ctx, (void**)&P->d_case_chunk, (kMaxCases + 1) * 4) != cudaSuccess) return fail(FL_E_OOM);
+    if (fl_dev_malloc(ctx, (void**)&P->case_max, kMaxCases * 4) != cudaSuccess) return fail(FL_E_OOM);
+    if (fl_dev_malloc(ctx, (void**)&P->cons, kMaxCases * 32) != cudaSuccess) return fail(FL_E_OOM);
+    if (fl_dev_malloc(ctx, (void**)&P->d_mask, kMaxCases) != cudaSuccess) return fail(FL_E_OOM);
     P->active.assign(ncases, 1);
     cudaMemcpy(P->d_cases, P->hcases.data(), ncases * sizeof(LbmCaseDev), cudaMemcpyHostToDevice);
     cudaMemcpy(P->d_dom, dom.data(), ncases * sizeof(fl_domain_dev::Case), cudaMemcpyHostToDevice);
@@ -2015,7 +2148,7 @@ int fl_pool_create(fl_ctx* ctx, const fl_lbm_case* cases, int ncases, fl_pool** 
     cudaStreamSynchronize(ctx->stream);
     P->mesh.num_cells = n0;
     for (int k = 0; k < 3; ++k)
-        if (cudaMallocAsync((void**)&P->f[k], P->cap * 512 * Q * 4, ctx->stream) != cudaSuccess) return fail(FL_E_OOM);
+        if (fl_dev_malloc_async(ctx, (void**)&P->f[k], P->cap * 512 * Q * 4, ctx->stream) != cudaSuccess) return fail(FL_E_OOM);
     rc = alloc_brick_arrays(ctx, P, P->cap);
     if (rc) return fail(rc);
     // an adapt with all flags 0 only sorts: bricks into key order
@@ -2071,6 +2204,7 @@ int fl_pool_destroy(fl_ctx* ctx, fl_pool* P) {
 
 int fl_pool_step(fl_ctx* ctx, fl_pool* P, int nsteps) {
     if (!ctx || !P || nsteps < 0) return FL_E_INVALID_ARG;
+    FL_POOL_USABLE(ctx, P);
     cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
     FL_TRY_CUDA(ctx, cudaStreamIsCapturing(ctx->stream, &capturing), "capture status");
     P->emit_solid = capturing != cudaStreamCaptureStatusNone;
@@ -2124,6 +2258,7 @@ int fl_pool_step(fl_ctx* ctx, fl_pool* P, int nsteps) {
 
 int fl_pool_regrid(fl_ctx* ctx, fl_pool* P, fl_adapt_stats* st) {
     if (!ctx || !P) return FL_E_INVALID_ARG;
+    FL_POOL_USABLE(ctx, P);
     int rc = pool_regrid(ctx, P, 1, st);
     if (rc) return rc;
     return fl_collect_device_status(ctx, "fl_pool_regrid");
@@ -2141,12 +2276,14 @@ int fl_pool_info_get(fl_ctx* ctx, fl_pool* P, fl_pool_info* info) {
     info->fluid_lups_per_step = P->lups;
     for (int l = 0; l < 16; ++l) info->fluid_sites_per_level[l] = P->fluid_per_level[l];
     info->population_bytes = (uint64_t)P->cap * 512 * Q * 4 * 3;
+    info->usable = P->unusable ? 0 : 1;
     return FL_OK;
 }
 
 int fl_pool_download(fl_ctx* ctx, fl_pool* P, int32_t* x, int32_t* y, int32_t* z, uint8_t* level, uint16_t* case_id,
                      float* f) {
     if (!ctx || !P) return FL_E_INVALID_ARG;
+    FL_POOL_USABLE(ctx, P);
     size_t n = P->mesh.num_cells;
     if (x) FL_TRY_CUDA(ctx, cudaMemcpyAsync(x, P->mesh.x, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "dl");
     if (y) FL_TRY_CUDA(ctx, cudaMemcpyAsync(y, P->mesh.y, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "dl");
@@ -2176,6 +2313,7 @@ int fl_pool_download(fl_ctx* ctx, fl_pool* P, int32_t* x, int32_t* y, int32_t* z
 
 int fl_pool_nbr(fl_ctx* ctx, fl_pool* P, uint32_t* nbr) {
     if (!ctx || !P || !nbr) return FL_E_INVALID_ARG;
+    FL_POOL_USABLE(ctx, P);
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(nbr, P->nbr, P->mesh.num_cells * 26 * 4 * 4, cudaMemcpyDeviceToHost, ctx->stream), "nbr");
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "nbr");
     return FL_OK;
@@ -2183,6 +2321,7 @@ int fl_pool_nbr(fl_ctx* ctx, fl_pool* P, uint32_t* nbr) {
 
 int fl_pool_flags(fl_ctx* ctx, fl_pool* P, int32_t* flags, float* wmax) {
     if (!ctx || !P) return FL_E_INVALID_ARG;
+    FL_POOL_USABLE(ctx, P);
     int rc = pool_flags(ctx, P, 1);
     if (rc) return rc;
     size_t n = P->mesh.num_cells;
@@ -2194,6 +2333,7 @@ int fl_pool_flags(fl_ctx* ctx, fl_pool* P, int32_t* flags, float* wmax) {
 
 int fl_pool_conservation(fl_ctx* ctx, fl_pool* P, double* out) {
     if (!ctx || !P || !out) return FL_E_INVALID_ARG;
+    FL_POOL_USABLE(ctx, P);
     size_t n = P->mesh.num_cells;
     k_brick_sums<<<fl_blocks(n, 1, ctx->num_sms * 16), 128, 0, ctx->stream>>>(view(P), n, P->part, P->fluid);
     FL_CHECK_LAUNCH(ctx, "k_brick_sums");
@@ -2210,37 +2350,61 @@ int fl_pool_conservation(fl_ctx* ctx, fl_pool* P, double* out) {
     return fl_collect_device_status(ctx, "fl_pool_conservation");
 }
 
-int fl_pool_profile_steps(fl_ctx* ctx, fl_pool* P, int nsteps, double* kernel_ms, uint32_t* launches,
-                          uint64_t* fluid_sites) {
-    if (!ctx || !P || nsteps < 0) return FL_E_INVALID_ARG;
+// Per-launch timing pass shared by the two profile entry points: totals per
+// [level][class] (16 x 3 each).
+int profile_levels(fl_ctx* ctx, fl_pool* P, int nsteps, double* ms, uint32_t* cnt, uint64_t* sites) {
     LaunchTimer tm;
     for (int i = 0; i < nsteps; ++i) level0_step(ctx, P, &tm);
     FL_CHECK_ERRORS(ctx, "collide-stream");
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "profile sync");
-    double ms[3] = {0.0, 0.0, 0.0};
-    uint64_t sites[3] = {0, 0, 0};
-    uint32_t cnt[3] = {0, 0, 0};
+    for (int k = 0; k < 48; ++k) { ms[k] = 0.0; cnt[k] = 0; sites[k] = 0; }
     for (size_t k = 0; k < tm.ev.size(); k += 2) {
         float t = 0.0f;
         cudaEventElapsedTime(&t, tm.ev[k], tm.ev[k + 1]);
-        int kind = tm.kind[k / 2];
-        ms[kind] += t;
-        sites[kind] += tm.sites[k / 2];
-        cnt[kind] += 1;
+        const int slot = tm.level[k / 2] * 3 + tm.kind[k / 2];
+        ms[slot] += t;
+        sites[slot] += tm.sites[k / 2];
+        cnt[slot] += 1;
         cudaEventDestroy(tm.ev[k]);
         cudaEventDestroy(tm.ev[k + 1]);
     }
-    for (int k = 0; k < 3; ++k) {
-        if (kernel_ms) kernel_ms[k] = ms[k];
-        if (launches) launches[k] = cnt[k];
-        if (fluid_sites) fluid_sites[k] = sites[k];
-    }
     drop_graph(P);
+    return FL_OK;
+}
+
+int fl_pool_profile_steps(fl_ctx* ctx, fl_pool* P, int nsteps, double* kernel_ms, uint32_t* launches,
+                          uint64_t* fluid_sites) {
+    if (!ctx || !P || nsteps < 0) return FL_E_INVALID_ARG;
+    FL_POOL_USABLE(ctx, P);
+    double ms[48];
+    uint32_t cnt[48];
+    uint64_t sites[48];
+    int rc = profile_levels(ctx, P, nsteps, ms, cnt, sites);
+    if (rc) return rc;
+    for (int k = 0; k < 3; ++k) {
+        double m = 0.0;
+        uint32_t c = 0;
+        uint64_t st = 0;
+        for (int l = 0; l < 16; ++l) { m += ms[l * 3 + k]; c += cnt[l * 3 + k]; st += sites[l * 3 + k]; }
+        if (kernel_ms) kernel_ms[k] = m;
+        if (launches) launches[k] = c;
+        if (fluid_sites) fluid_sites[k] = st;
+    }
     return fl_collect_device_status(ctx, "fl_pool_profile_steps");
+}
+
+int fl_pool_profile_levels(fl_ctx* ctx, fl_pool* P, int nsteps, double* kernel_ms, uint32_t* launches,
+                           uint64_t* fluid_sites) {
+    if (!ctx || !P || nsteps < 0 || !kernel_ms || !launches || !fluid_sites) return FL_E_INVALID_ARG;
+    FL_POOL_USABLE(ctx, P);
+    int rc = profile_levels(ctx, P, nsteps, kernel_ms, launches, fluid_sites);
+    if (rc) return rc;
+    return fl_collect_device_status(ctx, "fl_pool_profile_levels");
 }
 
 int fl_pool_upload(fl_ctx* ctx, fl_pool* P, const float* f) {
     if (!ctx || !P || !f) return FL_E_INVALID_ARG;
+    FL_POOL_USABLE(ctx, P);
     size_t n = P->mesh.num_cells;
     for (int q = 0; q < Q; ++q)
         FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->f[0] + (size_t)q * P->cap * 512, f + (size_t)q * n * 512, n * 512 * 4,
@@ -2252,10 +2416,11 @@ int fl_pool_upload(fl_ctx* ctx, fl_pool* P, const float* f) {
 
 int fl_pool_macroscopic(fl_ctx* ctx, fl_pool* P, float* rho, float* ux, float* uy, float* uz) {
     if (!ctx || !P || !rho || !ux || !uy || !uz) return FL_E_INVALID_ARG;
+    FL_POOL_USABLE(ctx, P);
     const size_t n = P->mesh.num_cells, sites = n * 512;
     if (!n) return FL_OK;
     float* d = nullptr;
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&d, sites * 16, ctx->stream), "macroscopic buffer");
+    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&d, sites * 16, ctx->stream), "macroscopic buffer");
     k_macroscopic<<<fl_blocks(n, 1, ctx->num_sms * 16), 128, 0, ctx->stream>>>(view(P), n, d, d + sites,
                                                                                d + 2 * sites, d + 3 * sites);
     FL_CHECK_LAUNCH(ctx, "k_macroscopic");
@@ -2271,6 +2436,7 @@ int fl_pool_macroscopic(fl_ctx* ctx, fl_pool* P, float* rho, float* ux, float* u
 int fl_pool_load(fl_ctx* ctx, fl_pool* P, size_t n, const int32_t* x, const int32_t* y, const int32_t* z,
                  const uint8_t* level, const uint16_t* case_id, const float* f) {
     if (!ctx || !P || !n || !x || !y || !z || !level || !case_id || !f) return FL_E_INVALID_ARG;
+    FL_POOL_USABLE(ctx, P);
     for (size_t i = 0; i < n; ++i) {
         const int cs = case_id[i], l = level[i];
         if (cs >= (int)P->cases.size() || !P->active[cs] || l > P->maxL)
@@ -2285,6 +2451,7 @@ int fl_pool_load(fl_ctx* ctx, fl_pool* P, size_t n, const int32_t* x, const int3
         int rc = pool_grow(ctx, P, std::max((size_t)(n * 1.5), n + 64));
         if (rc) return rc;
     }
+    P->unusable = true;  // until the loaded bricks' tables are rebuilt
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->mesh.x, x, n * 4, cudaMemcpyHostToDevice, ctx->stream), "load");
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->mesh.y, y, n * 4, cudaMemcpyHostToDevice, ctx->stream), "load");
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->mesh.z, z, n * 4, cudaMemcpyHostToDevice, ctx->stream), "load");
@@ -2307,6 +2474,7 @@ int fl_pool_load(fl_ctx* ctx, fl_pool* P, size_t n, const int32_t* x, const int3
 
 int fl_pool_set_velocities(fl_ctx* ctx, fl_pool* P, const float* wall_u, const float* inlet_u) {
     if (!ctx || !P) return FL_E_INVALID_ARG;
+    FL_POOL_USABLE(ctx, P);
     // per case 3 floats each; a host->device copy ordered on the stream, read by the next step
     for (size_t c = 0; c < P->cases.size(); ++c) {
         char* base = (char*)P->d_cases + c * sizeof(LbmCaseDev);
@@ -2328,7 +2496,7 @@ int fl_pool_set_solid_mask(fl_ctx* ctx, fl_pool* P, int32_t id, int32_t level, c
     const uint64_t words = (N[0] * N[1] * N[2] + 31) / 32;
     if (nwords != words) return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_pool_set_solid_mask: nwords != ceil(Nx*Ny*Nz/32)");
     uint32_t* d = nullptr;
-    if (cudaMalloc(&d, words * 4) != cudaSuccess) return fl_set_error(ctx, FL_E_OOM, "solid mask");
+    if (fl_dev_malloc(ctx, (void**)&d, words * 4) != cudaSuccess) return fl_set_error(ctx, FL_E_OOM, "solid mask");
     if (cudaMemcpyAsync(d, bits, words * 4, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess) {
         cudaFree(d);
         return fl_set_error(ctx, FL_E_CUDA, "solid mask upload");
@@ -2344,7 +2512,7 @@ int fl_pool_set_solid_cells(fl_ctx* ctx, fl_pool* P, int32_t id, int32_t level, 
     if (n && (!x || !y || !z)) return FL_E_INVALID_ARG;
     const uint64_t words = (N[0] * N[1] * N[2] + 31) / 32;
     uint32_t* d = nullptr;
-    if (cudaMalloc(&d, words * 4) != cudaSuccess) return fl_set_error(ctx, FL_E_OOM, "solid mask");
+    if (fl_dev_malloc(ctx, (void**)&d, words * 4) != cudaSuccess) return fl_set_error(ctx, FL_E_OOM, "solid mask");
     cudaMemsetAsync(d, 0, words * 4, ctx->stream);
     if (n) {
         k_mask_cells<<<fl_blocks(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(x, y, z, n, (int64_t)N[0],
@@ -2361,6 +2529,9 @@ int fl_pool_set_solid_cells(fl_ctx* ctx, fl_pool* P, int32_t id, int32_t level, 
 int fl_pool_get_solid_mask(fl_ctx* ctx, fl_pool* P, int32_t id, int32_t* level, uint32_t* bits, size_t nwords) {
     if (!ctx || !P || !level || id < 0 || id >= (int)P->active.size() || !P->active[id])
         return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_pool_get_solid_mask: not an active case");
+    FL_POOL_USABLE(ctx, P);
+    FL_POOL_USABLE(ctx, P);
+    FL_POOL_USABLE(ctx, P);
     const bool has = id < (int)P->dmask.size() && P->dmask[id];
     *level = has ? P->hcases[id].mask_level : -1;
     if (!has || !bits) return FL_OK;
@@ -2376,6 +2547,7 @@ int fl_pool_get_solid_mask(fl_ctx* ctx, fl_pool* P, int32_t id, int32_t* level, 
 
 int fl_pool_regrid_flags(fl_ctx* ctx, fl_pool* P, const int32_t* flags, fl_adapt_stats* st) {
     if (!ctx || !P || !flags) return FL_E_INVALID_ARG;
+    FL_POOL_USABLE(ctx, P);
     int rc = pool_regrid(ctx, P, 0, st, nullptr, flags);
     if (rc) return rc;
     return fl_collect_device_status(ctx, "fl_pool_regrid_flags");
@@ -2383,6 +2555,7 @@ int fl_pool_regrid_flags(fl_ctx* ctx, fl_pool* P, const int32_t* flags, fl_adapt
 
 int fl_pool_regrid_cases(fl_ctx* ctx, fl_pool* P, const uint8_t* due, fl_adapt_stats* st) {
     if (!ctx || !P || !due) return FL_E_INVALID_ARG;
+    FL_POOL_USABLE(ctx, P);
     int rc = pool_regrid(ctx, P, 1, st, due);
     if (rc) return rc;
     return fl_collect_device_status(ctx, "fl_pool_regrid_cases");
@@ -2390,6 +2563,7 @@ int fl_pool_regrid_cases(fl_ctx* ctx, fl_pool* P, const uint8_t* due, fl_adapt_s
 
 int fl_pool_add_cases(fl_ctx* ctx, fl_pool* P, const fl_lbm_case* cases, int ncases, int32_t* ids) {
     if (!ctx || !P || !cases || ncases <= 0 || !ids) return FL_E_INVALID_ARG;
+    FL_POOL_USABLE(ctx, P);
     // slots: freed ids first, then ids past the last one used
     std::vector<int> slot;
     for (int i = 0; i < (int)P->active.size() && (int)slot.size() < ncases; ++i)
@@ -2405,7 +2579,9 @@ int fl_pool_add_cases(fl_ctx* ctx, fl_pool* P, const fl_lbm_case* cases, int nca
         rc = pool_grow(ctx, P, std::max((size_t)((n + nt) * 1.5), n + nt + 64));
         if (rc) { fl_pool_destroy(ctx, T); return rc; }
     }
-    // append columns (case ids mapped to the slots) and populations (into A and B)
+    // append columns (case ids mapped to the slots) and populations (into A and B);
+    // the pool is unusable until the regrid below has rebuilt its tables
+    P->unusable = true;
     std::vector<uint16_t> tc(nt);
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(tc.data(), T->mesh.case_id, nt * 2, cudaMemcpyDeviceToHost, ctx->stream), "add");
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "add");
@@ -2453,10 +2629,12 @@ int fl_pool_add_cases(fl_ctx* ctx, fl_pool* P, const fl_lbm_case* cases, int nca
 
 int fl_pool_remove_cases(fl_ctx* ctx, fl_pool* P, const int32_t* ids, int nids) {
     if (!ctx || !P || (nids && !ids)) return FL_E_INVALID_ARG;
+    FL_POOL_USABLE(ctx, P);
     for (int i = 0; i < nids; ++i) {
         if (ids[i] < 0 || ids[i] >= (int)P->active.size() || !P->active[ids[i]])
             return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_pool_remove_cases: not an active case");
     }
+    P->unusable = true;  // until the compacted pool's tables are rebuilt
     for (int i = 0; i < nids; ++i) P->active[ids[i]] = 0;
     release_masks(ctx, P);
     size_t n = P->mesh.num_cells;
@@ -2483,8 +2661,8 @@ int fl_pool_remove_cases(fl_ctx* ctx, fl_pool* P, const int32_t* ids, int nids) 
     if (rc) return rc;
     uint32_t* osrc = nullptr;
     uint8_t* okind = nullptr;
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&osrc, (M + 1) * 4, ctx->stream), "remove src");
-    FL_TRY_CUDA(ctx, cudaMallocAsync((void**)&okind, M + 1, ctx->stream), "remove kind");
+    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&osrc, (M + 1) * 4, ctx->stream), "remove src");
+    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&okind, M + 1, ctx->stream), "remove kind");
     fl_mesh_dev md{P->mesh.x, P->mesh.y, P->mesh.z, P->mesh.level, P->mesh.state, P->mesh.flags, P->mesh.material,
                    P->mesh.case_id, n};
     fl_mesh_out o{out.x, out.y, out.z, out.level, out.state, out.flags, out.material, out.case_id};
@@ -2514,6 +2692,7 @@ int fl_pool_remove_cases(fl_ctx* ctx, fl_pool* P, const int32_t* ids, int nids) 
 int fl_pool_download_case(fl_ctx* ctx, fl_pool* P, int32_t id, int32_t* x, int32_t* y, int32_t* z, uint8_t* level,
                           float* f, size_t* nbricks) {
     if (!ctx || !P || !nbricks || id < 0 || id >= (int)P->active.size() || !P->active[id]) return FL_E_INVALID_ARG;
+    FL_POOL_USABLE(ctx, P);
     uint32_t b0 = P->case_begin[id], b1 = P->case_begin[id + 1];
     size_t n = b1 - b0;
     *nbricks = n;
@@ -2543,8 +2722,34 @@ int fl_pool_download_case(fl_ctx* ctx, fl_pool* P, int32_t id, int32_t* x, int32
     return FL_OK;
 }
 
+int fl_pool_populations_field(fl_ctx* ctx, fl_pool* P, const char* name, uint64_t* handle) {
+    if (!ctx || !P || !name || !handle) return FL_E_INVALID_ARG;
+    FL_POOL_USABLE(ctx, P);
+    // Gather the current populations into buffer A: a level whose parity is odd
+    // (between level-0 steps only level 0 can be) has them in B; copying them
+    // makes both buffers current for it, so its next step reads A consistently.
+    for (int l = 0; l <= P->maxL && l < 16; ++l) {
+        if (!P->parity[l]) continue;
+        const uint32_t b0 = P->lvl_off[l], cnt = P->lvl_off[l + 1] - b0;
+        if (cnt) {
+            k_copy_bricks<<<fl_blocks((size_t)cnt * Q * 128, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(
+                P->f[1], P->f[0], P->cap, P->list + b0, cnt);
+            FL_CHECK_LAUNCH(ctx, "k_copy_bricks");
+        }
+        P->parity[l] = 0;
+    }
+    fl_field_desc d;
+    if (fl_field_make(name, 0, Q, 1, 0, 0, &d) != FL_OK)
+        return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_pool_populations_field: bad field name");
+    int rc = fl_soa_bind_external(ctx, &d, P->mesh.num_cells * 512, P->cap * 512 * sizeof(float), P->f[0], handle);
+    if (rc) return rc;
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "fl_pool_populations_field");
+    return FL_OK;
+}
+
 int fl_pool_set_options(fl_ctx* ctx, fl_pool* P, int use_graphs, int grid_mult) {
     if (!ctx || !P) return FL_E_INVALID_ARG;
+    FL_POOL_USABLE(ctx, P);
     P->graphs = use_graphs;
     if (grid_mult > 0) P->grid_mult = grid_mult;
     drop_graph(P);
@@ -2553,6 +2758,7 @@ int fl_pool_set_options(fl_ctx* ctx, fl_pool* P, int use_graphs, int grid_mult) 
 
 int fl_pool_set_class_streams(fl_ctx* ctx, fl_pool* P, int streams) {
     if (!ctx || !P || streams < 1 || streams > 2) return FL_E_INVALID_ARG;
+    FL_POOL_USABLE(ctx, P);
     cudaStreamSynchronize(ctx->stream);
     P->streams = streams;
     drop_graph(P);

@@ -35,7 +35,8 @@ class PoolInfo(ctypes.Structure):
     _fields_ = [("num_bricks", ctypes.c_size_t), ("capacity", ctypes.c_size_t), ("num_cases", ctypes.c_int32),
                 ("max_level", ctypes.c_int32), ("bricks_per_level", ctypes.c_uint32 * 16),
                 ("fluid_lups_per_step", ctypes.c_uint64), ("population_bytes", ctypes.c_uint64),
-                ("fluid_sites_per_level", ctypes.c_uint64 * 16), ("num_active_cases", ctypes.c_int32)]
+                ("fluid_sites_per_level", ctypes.c_uint64 * 16), ("num_active_cases", ctypes.c_int32),
+                ("usable", ctypes.c_int32)]
 
 
 WALL, MOVING, INLET, OUTLET, PERIODIC = 1, 2, 3, 4, 0
@@ -70,6 +71,69 @@ def sphere_channel(nx=128, ny=64, nz=64, max_level=3, radius=8.0, centre=(32.0, 
     c.band = band
     c.refine_frac, c.coarsen_frac = 0.5, 0.1
     return c
+
+
+def periodic_box(nx=64, ny=64, nz=8, max_level=0, tau=0.8):
+    """A box periodic on all six faces (no walls, no sphere): the Taylor-Green
+    vortex case.  Sizes are in level-0 sites (multiples of 8)."""
+    c = LbmCase()
+    c.ext[:] = [nx // 8, ny // 8, nz // 8]
+    c.bc[:] = [PERIODIC] * 6
+    c.tau0 = tau
+    c.max_level = max_level
+    c.refine_frac, c.coarsen_frac = 2.0, -1.0  # no vorticity-driven regrid: refinement by explicit flags only
+    return c
+
+
+# D3Q19 velocities in the kernels' order: rest, +-x, +-y, +-z, then the twelve
+# edge directions in opposite pairs; weights 1/3, 1/18, 1/36.
+CX = (0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0)
+CY = (0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -1)
+CZ = (0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1)
+WQ = (1 / 3,) + (1 / 18,) * 6 + (1 / 36,) * 12
+
+
+def site_centres(bricks):
+    """Centre of every site, (n, 512, 3) in level-0 site units: site s = i + 8 j + 64 k of
+    a level-l brick at native (x, y, z) sits at ((8 x + i + 1/2) / 2^l, ...)."""
+    s = np.arange(512)
+    ijk = np.stack([s & 7, (s >> 3) & 7, s >> 6], -1).astype(np.float64)
+    b = np.stack([bricks["x"], bricks["y"], bricks["z"]], -1).astype(np.float64)[:, None, :]
+    scale = (0.5 ** bricks["level"].astype(np.float64))[:, None, None]
+    return (8.0 * b + ijk[None] + 0.5) * scale
+
+
+def equilibrium(rho, u):
+    """D3Q19 BGK equilibrium populations (19, ...) in FP32 of density rho (...) and
+    velocity u (..., 3), evaluated in FP64."""
+    rho = np.asarray(rho, np.float64)
+    u = np.asarray(u, np.float64)
+    usq = (u * u).sum(-1)
+    out = np.empty((Q,) + rho.shape, np.float32)
+    for q in range(Q):
+        cu = CX[q] * u[..., 0] + CY[q] * u[..., 1] + CZ[q] * u[..., 2]
+        out[q] = WQ[q] * rho * (1.0 + 3.0 * cu + 4.5 * cu * cu - 1.5 * usq)
+    return out
+
+
+def taylor_green(bricks, nx, ny, u0=0.01):
+    """Populations (19, n, 512) of the z-invariant Taylor-Green vortex on an nx x ny periodic
+    box: u = u0 sin(kx x) cos(ky y), v = -u0 cos(kx x) sin(ky y), w = 0, with its pressure
+    p = rho0 u0^2 / 4 (cos 2 kx x + cos 2 ky y) as density 1 + 3 p (c_s^2 = 1/3)."""
+    r = site_centres(bricks)
+    kx, ky = 2 * np.pi / nx, 2 * np.pi / ny
+    X, Y = kx * r[..., 0], ky * r[..., 1]
+    u = np.stack([u0 * np.sin(X) * np.cos(Y), -u0 * np.cos(X) * np.sin(Y), np.zeros_like(X)], -1)
+    rho = 1.0 + 3.0 * (u0 * u0 / 4.0) * (np.cos(2 * X) + np.cos(2 * Y))
+    return equilibrium(rho, u)
+
+
+def moments(f):
+    """Density (n, 512) and velocity (n, 512, 3) of populations (19, n, 512), in FP64."""
+    f = np.asarray(f, np.float64)
+    rho = f.sum(0)
+    j = np.stack([np.tensordot(np.asarray(c, np.float64), f, 1) for c in (CX, CY, CZ)], -1)
+    return rho, j / rho[..., None]
 
 
 class Pool:
@@ -137,6 +201,12 @@ class Pool:
         ms, la, st = (ctypes.c_double * 3)(), (ctypes.c_uint32 * 3)(), (ctypes.c_uint64 * 3)()
         self.ctx.call("fl_pool_profile_steps", self.h, n, ms, la, st)
         return [(ms[k], la[k], st[k]) for k in range(3)]
+
+    def profile_levels(self, n):
+        """Per level and kernel: (kernel ms, launches, fluid sites updated), arrays (16, 3)."""
+        ms, la, st = (ctypes.c_double * 48)(), (ctypes.c_uint32 * 48)(), (ctypes.c_uint64 * 48)()
+        self.ctx.call("fl_pool_profile_levels", self.h, n, ms, la, st)
+        return (np.array(ms[:]).reshape(16, 3), np.array(la[:]).reshape(16, 3), np.array(st[:]).reshape(16, 3))
 
     def upload(self, f):
         f = np.ascontiguousarray(f, np.float32)

@@ -31,8 +31,8 @@ BRICK_BYTES = 3 * 19 * 512 * 4  # three population buffers per brick
 
 
 class Job:
-    __slots__ = ("jid", "arrival", "case", "steps", "regrid_every", "done", "cid", "start", "end", "est_bytes",
-                 "result")
+    __slots__ = ("jid", "arrival", "case", "steps", "regrid_every", "done", "cid", "start", "end", "result",
+                 "refused")
 
     def __init__(self, jid, arrival, case, steps, regrid_every=20):
         self.jid, self.arrival, self.case, self.steps, self.regrid_every = jid, arrival, case, steps, regrid_every
@@ -40,9 +40,13 @@ class Job:
         self.cid = None
         self.start = self.end = None
         self.result = None
-        e = case.ext
-        # footprint estimate: level-0 bricks refined into an eighth of the volume per extra level
-        self.est_bytes = int(e[0] * e[1] * e[2] * (1 + 0.125 * 8 ** max(case.max_level, 0) / 2) * BRICK_BYTES)
+        self.refused = None  # the reason, when admission refused the job for good
+
+    def start_bytes(self):
+        """Population bytes of the job's level-0 bricks: the least it holds from its first step,
+        so a job whose bound exceeds the whole budget can never run."""
+        e = self.case.ext
+        return int(e[0] * e[1] * e[2]) * BRICK_BYTES
 
 
 def make_jobs(rate, duration, steps_range, seed=5):
@@ -68,45 +72,59 @@ def make_jobs(rate, duration, steps_range, seed=5):
     return jobs
 
 
-def run_served(ctx, jobs, budget_bytes, check_ids=(), regrid_every=20, resident_bytes=None):
+def reserved_bytes(pool):
+    """The pool's device footprint as the library reports it: its three population buffers
+    at their current capacity (fl_pool_info population_bytes)."""
+    return 0 if pool is None else int(pool.info().population_bytes)
+
+
+def run_served(ctx, jobs, budget_bytes, check_ids=(), regrid_every=20, resident_bytes=None, admit_every=None):
     """Continuous batching; returns the LUPs done, the makespan and the pool steps run.
 
-    Jobs are admitted in arrival order while the resident population footprint
-    stays within min(budget_bytes, resident_bytes): enough resident bricks to
-    keep HBM busy, and no more, so queued jobs start in order instead of all
-    sharing the GPU at once."""
+    Jobs are admitted in arrival order at pool steps that are multiples of
+    admit_every (default: the regrid interval, so that resident jobs share their
+    regrids).  Admission is gated by the pool's actual reserved bytes: a queued job
+    is added, and if the pool's footprint then exceeds min(budget_bytes,
+    resident_bytes) it is removed again and waits for jobs to finish (deferred); a
+    job whose level-0 bricks alone exceed the whole budget (start_bytes) is refused.
+    resident_bytes is the throughput knob: enough resident bricks to keep HBM busy,
+    and no more, so queued jobs start in order instead of all sharing the GPU."""
     cap = budget_bytes if resident_bytes is None else min(budget_bytes, resident_bytes)
+    admit_every = admit_every or regrid_every
     pending = collections.deque(sorted(jobs, key=lambda j: j.arrival))
     queue, active = collections.deque(), {}
     pool = None
-    used = 0
     lups = 0
     steps_run = 0
-    phase = 0  # pool steps since the last regrid boundary (restarts whenever the pool empties)
+    phase = 0  # pool steps since the last admission boundary (restarts whenever the pool empties)
+    deferrals = 0
     t0 = time.perf_counter()
     while pending or queue or active:
         now = time.perf_counter() - t0
         while pending and pending[0].arrival <= now:
-            queue.append(pending.popleft())
-        admit = []
+            j = pending.popleft()
+            if j.start_bytes() > budget_bytes:
+                j.refused = "level-0 footprint %.3f GB above the %.3f GB budget" % (j.start_bytes() / 1e9,
+                                                                                   budget_bytes / 1e9)
+                j.start = j.end = now
+                continue
+            queue.append(j)
         if not active:
             phase = 0
-        boundary = phase % regrid_every == 0
-        while boundary and queue and (used + queue[0].est_bytes <= cap or not active and not admit):
-            j = queue.popleft()
-            used += j.est_bytes
-            admit.append(j)
-        if admit:
-            cases = [j.case for j in admit]
+        while phase % admit_every == 0 and queue:
+            j = queue[0]
             if pool is None:
-                pool = Pool(ctx, cases)
-                ids = list(range(len(cases)))
+                pool = Pool(ctx, [j.case])
+                cid = 0
             else:
-                ids = pool.add_cases(cases)
-            now = time.perf_counter() - t0
-            for j, cid in zip(admit, ids):
-                j.cid, j.start = cid, now
-                active[cid] = j
+                cid = pool.add_cases([j.case])[0]
+            if active and reserved_bytes(pool) > cap:  # over the cap: back to the queue until jobs finish
+                pool.remove_cases([cid])
+                deferrals += 1
+                break
+            queue.popleft()
+            j.cid, j.start = cid, time.perf_counter() - t0
+            active[cid] = j
         if not active:
             if pending:
                 time.sleep(max(0.0, min(0.05, pending[0].arrival - (time.perf_counter() - t0))))
@@ -132,7 +150,6 @@ def run_served(ctx, jobs, budget_bytes, check_ids=(), regrid_every=20, resident_
             for cid in fin:
                 j = active.pop(cid)
                 j.end = now
-                used -= j.est_bytes
                 if j.jid in check_ids:
                     j.result = pool.case_state(cid)
             pool.remove_cases(fin)
@@ -140,6 +157,7 @@ def run_served(ctx, jobs, budget_bytes, check_ids=(), regrid_every=20, resident_
     makespan = time.perf_counter() - t0
     if pool is not None:
         pool.close()
+    run_served.deferrals = deferrals
     return lups, makespan, steps_run
 
 
@@ -165,22 +183,16 @@ def percentile(v, q):
     return float(np.percentile(np.asarray(v), q)) if len(v) else None
 
 
-def main(argv=None):
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--rate", type=float, default=50.0)
-    ap.add_argument("--duration", type=float, default=60.0)
-    ap.add_argument("--steps", type=int, nargs=2, default=[200, 2000])
-    ap.add_argument("--budget-gb", type=float, default=150.0)
-    ap.add_argument("--resident-gb", type=float, default=6.0,
-                    help="admission stops while the resident population footprint exceeds this")
-    ap.add_argument("--check", type=int, default=8, help="jobs whose result is compared with their solo run")
-    ap.add_argument("--seed", type=int, default=5)
-    args = ap.parse_args(argv)
-    ctx = Context(0)
-    jobs = make_jobs(args.rate, args.duration, args.steps, args.seed)
-    check_ids = set(range(min(args.check, len(jobs))))
-    lups, makespan, steps_run = run_served(ctx, jobs, args.budget_gb * 1e9, check_ids,
-                                           resident_bytes=args.resident_gb * 1e9)
+def benchmark(ctx, rate=50.0, duration=60.0, steps_range=(200, 2000), budget_gb=150.0, resident_gb=6.0, check=8,
+              seed=5):
+    """Serve the arrival stream, then run the same jobs one at a time in arrival order;
+    returns throughput and p50/p99 time to completion of both, and the checked jobs whose
+    served result differs from their solo run."""
+    jobs = make_jobs(rate, duration, list(steps_range), seed)
+    check_ids = set(range(min(check, len(jobs))))
+    lups, makespan, steps_run = run_served(ctx, jobs, budget_gb * 1e9, check_ids, resident_bytes=resident_gb * 1e9)
+    refused = [j for j in jobs if j.refused]
+    jobs = [j for j in jobs if not j.refused]
     lat = [j.end - j.arrival for j in jobs]
     # plain sequential: each job alone, one after another in arrival order
     end_prev, lat_plain, solo_s, solo_lups, mismatched = 0.0, [], 0.0, 0, []
@@ -197,14 +209,30 @@ def main(argv=None):
             same = all(np.array_equal(g1[k], g2[k]) for k in ("x", "y", "z", "level")) and np.array_equal(f1, f2)
             if not same:
                 mismatched.append(j.jid)
-    res = {"jobs": len(jobs), "rate_per_s": args.rate, "duration_s": args.duration, "steps_range": args.steps,
-           "admission": "arrival order, resident footprint <= %.1f GB of a %.0f GB budget" % (
-               args.resident_gb, args.budget_gb),
-           "served_makespan_s": makespan, "served_mlups": lups / makespan / 1e6,
-           "served_p50_s": percentile(lat, 50), "served_p99_s": percentile(lat, 99),
-           "plain_mlups": solo_lups / solo_s / 1e6, "plain_makespan_s": end_prev,
-           "plain_p50_s": percentile(lat_plain, 50), "plain_p99_s": percentile(lat_plain, 99),
-           "pool_steps": steps_run, "checked": sorted(check_ids), "mismatched": mismatched}
+    return {"jobs": len(jobs), "rate_per_s": rate, "duration_s": duration, "steps_range": list(steps_range),
+            "admission": "arrival order, resident footprint <= %.1f GB of a %.0f GB budget" % (resident_gb, budget_gb),
+            "served_makespan_s": round(makespan, 3), "served_mlups": round(lups / makespan / 1e6, 1),
+            "served_p50_s": percentile(lat, 50), "served_p99_s": percentile(lat, 99),
+            "plain_mlups": round(solo_lups / solo_s / 1e6, 1), "plain_makespan_s": round(end_prev, 3),
+            "plain_p50_s": percentile(lat_plain, 50), "plain_p99_s": percentile(lat_plain, 99),
+            "pool_steps": steps_run, "checked": sorted(check_ids), "mismatched": mismatched,
+            "refused": len(refused), "deferrals": run_served.deferrals}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--rate", type=float, default=50.0)
+    ap.add_argument("--duration", type=float, default=60.0)
+    ap.add_argument("--steps", type=int, nargs=2, default=[200, 2000])
+    ap.add_argument("--budget-gb", type=float, default=150.0)
+    ap.add_argument("--resident-gb", type=float, default=6.0,
+                    help="admission stops while the resident population footprint exceeds this")
+    ap.add_argument("--check", type=int, default=8, help="jobs whose result is compared with their solo run")
+    ap.add_argument("--seed", type=int, default=5)
+    args = ap.parse_args(argv)
+    ctx = Context(0)
+    res = benchmark(ctx, args.rate, args.duration, args.steps, args.budget_gb, args.resident_gb, args.check,
+                    args.seed)
     print(json.dumps(res))
     return res
 

@@ -45,6 +45,12 @@ int fl_ctx_destroy(fl_ctx* ctx);
 int fl_ctx_set_stream(fl_ctx* ctx, void* cuda_stream);
 void* fl_ctx_stream(fl_ctx* ctx);
 int fl_ctx_synchronize(fl_ctx* ctx);
+/* Host-side fault injection for failure tests (no reference counterpart; the reference's device
+ * allocations throw from OpenCL wrappers, include/fluidloom/common/FluidLoomError.h:77-81): after
+ * `after` more device allocations made by the library for this context, every allocation fails as
+ * out of memory (the call returns FL_E_OOM) until it is switched off with after < 0.  Nothing is
+ * allocated by a failed allocation; the context stays usable. */
+int fl_ctx_inject_alloc_failure(fl_ctx* ctx, int64_t after);
 const char* fl_last_error(fl_ctx* ctx);
 const char* fl_status_string(int status);
 int fl_version(void);
@@ -97,12 +103,18 @@ int fl_hilbert_is_valid(uint64_t key, uint8_t level);
  * total (device pointer, may be NULL) receives the sum.  in == out is allowed. */
 int fl_scan_exclusive_u32(fl_ctx* ctx, const uint32_t* in, uint32_t* out, size_t n, uint32_t* total);
 /* The same scan for callers that cannot allocate device memory (no counterpart in the reference):
- * no context, no cudaMalloc/cudaFree or allocating library call; its scratch is a fixed array inside
- * the library (128 KiB + 512 B per GPU, held until exit), so n is limited to 2^26 (67,108,864)
- * elements and larger n returns FL_E_CAPACITY.  Runs on cuda_stream (a cudaStream_t, NULL = the
- * default stream) and returns after the scan finished.  The first call on a device looks up the
+ * embedders that own every device allocation through their own pool, hosts under a fixed device
+ * memory budget, FFI hosts that must not allocate on their hot path.  No context, no
+ * cudaMalloc/cudaFree or allocating library call; its scratch is a fixed array inside the library
+ * (128 KiB + 512 B per GPU, held until exit), so n is limited to 2^26 (67,108,864) elements and
+ * larger n returns FL_E_CAPACITY.  Runs on cuda_stream (a cudaStream_t the caller owns; NULL is
+ * the legacy default stream, which orders against every blocking stream of the device) and
+ * synchronizes that stream before it returns (it reads the look-back timeout word back).  The
+ * first call on a device, and the first after the device's context was reset, looks up the
  * array's device address: make that first call before any stream capture.  All calls share the
- * array, so calls that overlap on the GPU (other threads or streams) race. */
+ * array and each clears the words it uses, so calls that overlap on the GPU (other threads or
+ * streams) race.  n == 0 sets *total (if given) to 0.  A CUDA error pending from the caller's
+ * own earlier calls is left pending and not reported. */
 int fl_scan_exclusive_u32_noalloc(const uint32_t* in, uint32_t* out, size_t n, uint32_t* total, void* cuda_stream);
 /* Failure-detection check of the bounded device waits (no reference counterpart: the reference
  * has no device-side wait limits): one warp polls a look-back word that nothing publishes; after
@@ -307,6 +319,9 @@ typedef struct fl_pool_info {
     uint64_t population_bytes;
     uint64_t fluid_sites_per_level[16];
     int32_t num_active_cases;       /* num_cases counts slots, including freed ones */
+    int32_t usable;                 /* 0 after a call failed part-way through replacing the pool's bricks or
+                                       tables: every call but fl_pool_destroy and this one then returns
+                                       FL_E_INVALID_ARG without touching the device */
 } fl_pool_info;
 
 /* Build the cases: level-0 bricks, max_level rounds of sphere-band refinement, equilibrium start. */
@@ -332,6 +347,11 @@ int fl_pool_conservation(fl_ctx* ctx, fl_pool* pool, double* out);
  * an array of 3). */
 int fl_pool_profile_steps(fl_ctx* ctx, fl_pool* pool, int nsteps, double* kernel_ms, uint32_t* launches,
                           uint64_t* fluid_sites);
+/* The same timing pass, totals per level and kernel: kernel_ms, launches and fluid_sites are arrays
+ * of 16 x 3 ([level][kernel], kernels as above).  A launch of kernel 1 covers the level's
+ * descriptor values (k_interface) and its general bricks. */
+int fl_pool_profile_levels(fl_ctx* ctx, fl_pool* pool, int nsteps, double* kernel_ms, uint32_t* launches,
+                           uint64_t* fluid_sites);
 /* Replace the populations with a host array [19][n][512] (the layout fl_pool_download gives). */
 int fl_pool_upload(fl_ctx* ctx, fl_pool* pool, const float* f);
 /* Density and velocity of every site ([nbricks][512] host arrays each, bricks in pool order),
@@ -381,6 +401,15 @@ int fl_pool_remove_cases(fl_ctx* ctx, fl_pool* pool, const int32_t* ids, int nid
 int fl_pool_download_case(fl_ctx* ctx, fl_pool* pool, int32_t id, int32_t* x, int32_t* y, int32_t* z,
                           uint8_t* level, float* f, size_t* nbricks);
 /* use_graphs: replay captured CUDA graphs per level-0 step; grid_mult: CTAs per SM (0 keeps). */
+/* The pool's populations as a 19-component FP32 field of this context's structure-of-arrays manager,
+ * as the reference allocates them (SOAFieldManager::allocate, src/core/fields/SOAFieldManager.cpp:17-131)
+ * and binds them to its LBM kernel nodes (KernelNode::bindField, src/runtime/nodes/KernelNode.cpp:27-29):
+ * cell = brick * 512 + site over the pool's bricks in order, component q = population q;
+ * fl_soa_device_ptr(handle, q) gives its device pointer and fl_soa_info its pitch (capacity * 512
+ * floats).  The field is a view of the pool's current population buffer, not a copy: writes through
+ * it change the pool.  It stays valid until the next call that steps, regrids, loads, adds or removes
+ * cases; call again to refresh it (the handle stays, its version grows when the storage moved). */
+int fl_pool_populations_field(fl_ctx* ctx, fl_pool* pool, const char* name, uint64_t* handle);
 int fl_pool_set_options(fl_ctx* ctx, fl_pool* pool, int use_graphs, int grid_mult);
 /* streams = 2 (default): each level-0 step runs as a dependency graph over two streams per
  * level -- general, interface and all-solid bricks on one, interior bricks on the other --

@@ -273,6 +273,42 @@ private:
 
 }  // namespace hashmap
 
+namespace fields {
+
+// SOAFieldManager (include/fluidloom/core/fields/SOAFieldManager.h:26-51) over one context:
+// FieldHandle is the field id; device pointers are per component (component-major storage).
+using FieldHandle = uint64_t;
+class SOAFieldManager {
+public:
+    explicit SOAFieldManager(Device& dev) : dev_(dev) {}
+    FieldHandle allocate(const fl_field_desc& desc, size_t num_cells) {
+        FieldHandle h = 0;
+        check(dev_.get(), fl_soa_allocate(dev_.get(), &desc, num_cells, &h), "SOAFieldManager::allocate");
+        return h;
+    }
+    void deallocate(FieldHandle h) { check(dev_.get(), fl_soa_deallocate(dev_.get(), h), "SOAFieldManager::deallocate"); }
+    void* getDevicePtr(FieldHandle h, uint16_t component = 0) const {
+        void* p = nullptr;
+        check(dev_.get(), fl_soa_device_ptr(dev_.get(), h, component, &p), "SOAFieldManager::getDevicePtr");
+        return p;
+    }
+    size_t numCells(FieldHandle h) const {
+        size_t n = 0;
+        check(dev_.get(), fl_soa_info(dev_.get(), h, &n, nullptr, nullptr), "SOAFieldManager::numCells");
+        return n;
+    }
+    uint64_t getVersion(FieldHandle h) const {
+        uint64_t v = 0;
+        check(dev_.get(), fl_soa_info(dev_.get(), h, nullptr, nullptr, &v), "SOAFieldManager::getVersion");
+        return v;
+    }
+
+private:
+    Device& dev_;
+};
+
+}  // namespace fields
+
 namespace runtime {
 
 // AdaptMeshNode (include/fluidloom/runtime/nodes/AdaptMeshNode.h:18-70): one regrid of a brick pool.
@@ -300,6 +336,13 @@ public:
               fl_pool_set_solid_mask(dev_.get(), p_, case_id, level, bits.empty() ? nullptr : bits.data(),
                                      bits.size()),
               "fl_pool_set_solid_mask");
+    }
+    // The populations as a 19-component field of the device's SOAFieldManager (a view of the pool's
+    // current buffer, valid until the pool is stepped or regridded; fl_pool_populations_field).
+    fields::FieldHandle populationsField(const std::string& name = "f") {
+        fields::FieldHandle h = 0;
+        check(dev_.get(), fl_pool_populations_field(dev_.get(), p_, name.c_str(), &h), "fl_pool_populations_field");
+        return h;
     }
     // The case's mask level (-1: none) and words.
     int32_t solidMask(int32_t case_id, std::vector<uint32_t>* bits) const {

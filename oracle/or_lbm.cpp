@@ -440,8 +440,14 @@ void compute_flags(Pool& P, bool use_vorticity, float* out_wmax) {
 // One regrid of the pool: adapt with FULL26 balance, then remap populations:
 // survivors copied, children take the parent site covering them (copy),
 // parents take the mean of the 2x2x2 child sites (children 0..7 in bit order).
+void regrid_with_flags(Pool& P);
+
 void regrid(Pool& P, bool use_vorticity) {
     compute_flags(P, use_vorticity, nullptr);
+    regrid_with_flags(P);
+}
+
+void regrid_with_flags(Pool& P) {
     or_mesh m = P.mesh();
     or_adapt_cfg cfg{P.maxL, 0, 1, 10, 1, 0};
     size_t cap = P.n * 8 + 8;
@@ -638,6 +644,22 @@ void or_pool_fp64_steps(void* h, int nsteps, int nthreads, double* out) {
 }
 
 void or_pool_regrid(void* h) { regrid(*(Pool*)h, true); }
+
+// A regrid with the caller's flags (one per brick, pool order: > 0 split,
+// -1 merge, 0 keep), as fl_pool_regrid_flags.
+void or_pool_regrid_flags(void* h, const int32_t* flags) {
+    Pool& P = *(Pool*)h;
+    std::memcpy(P.flags.data(), flags, P.n * 4);
+    regrid_with_flags(P);
+}
+
+// Replace the populations of every brick ([19][n][512], pool order), all
+// levels at parity 0, as fl_pool_upload.
+void or_pool_upload(void* h, const float* f) {
+    Pool& P = *(Pool*)h;
+    std::memcpy(P.f[0].data(), f, sizeof(float) * (size_t)Q * P.n * 512);
+    for (int l = 0; l < 20; ++l) P.parity[l] = 0;
+}
 
 void or_pool_flags(void* h, int32_t* flags, float* wmax) {
     Pool& P = *(Pool*)h;

@@ -110,6 +110,8 @@ void* or_pool_new(const or_lbm_case* cases, int ncases);
 void or_pool_free(void* h);
 void or_pool_steps(void* h, int nsteps, int nthreads);
 void or_pool_regrid(void* h);
+void or_pool_regrid_flags(void* h, const int32_t* flags);
+void or_pool_upload(void* h, const float* f);
 void or_pool_flags(void* h, int32_t* flags, float* wmax);
 size_t or_pool_size(void* h);
 void or_pool_bricks(void* h, int32_t* x, int32_t* y, int32_t* z, uint8_t* level, uint16_t* cs);

@@ -92,6 +92,8 @@ def load():
         L.or_pool_free.argtypes = [P]
         L.or_pool_steps.argtypes = [P, ctypes.c_int, ctypes.c_int]
         L.or_pool_regrid.argtypes = [P]
+        L.or_pool_regrid_flags.argtypes = [P, P]
+        L.or_pool_upload.argtypes = [P, P]
         L.or_pool_flags.argtypes = [P, P, P]
         L.or_pool_size.restype = ctypes.c_size_t
         L.or_pool_size.argtypes = [P]
@@ -258,6 +260,14 @@ class OraclePool:
 
     def regrid(self):
         load().or_pool_regrid(self.h)
+
+    def regrid_flags(self, flags):
+        fl = np.ascontiguousarray(flags, np.int32)
+        load().or_pool_regrid_flags(self.h, ptr(fl))
+
+    def upload(self, f):
+        f = np.ascontiguousarray(f, np.float32)
+        load().or_pool_upload(self.h, ptr(f))
 
     def bricks(self):
         n = self.n()

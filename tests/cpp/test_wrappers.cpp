@@ -126,6 +126,32 @@ int main() {
         pool.setSolidMask(0, 0, {});
         EXPECT_EQ(pool.solidMask(0, nullptr), -1);
         EXPECT_EQ(pool.info().fluid_lups_per_step, lups);
+        // the populations bound the reference's way: a 19-component field of the SOA manager
+        // whose component pointers a kernel node binds (KernelNode::bindField); equal to the
+        // downloaded populations, and writes through the field reach the pool
+        {
+            // one more level-0 step: an odd count, so level 0's current populations sit in buffer B
+            check(dev.get(), fl_pool_step(dev.get(), pool.get(), 1), "step");
+            fields::SOAFieldManager soa(dev);
+            fields::FieldHandle h = pool.populationsField("f");
+            const size_t n = pool.info().num_bricks;
+            EXPECT_EQ(soa.numCells(h), n * 512);
+            std::vector<float> all(19 * n * 512), comp(n * 512);
+            check(dev.get(), fl_pool_download(dev.get(), pool.get(), nullptr, nullptr, nullptr, nullptr, nullptr,
+                                              all.data()), "download");
+            bool same = true;
+            for (int q = 0; q < 19; ++q) {
+                check(dev.get(), fl_memcpy_d2h(dev.get(), comp.data(), soa.getDevicePtr(h, (uint16_t)q),
+                                               comp.size() * 4), "field read");
+                for (size_t i = 0; i < comp.size(); ++i) same = same && comp[i] == all[q * n * 512 + i];
+            }
+            EXPECT_TRUE(same);
+            const float v = 0.25f;
+            check(dev.get(), fl_memcpy_h2d(dev.get(), soa.getDevicePtr(h, 3), &v, 4), "field write");
+            check(dev.get(), fl_pool_download(dev.get(), pool.get(), nullptr, nullptr, nullptr, nullptr, nullptr,
+                                              all.data()), "download");
+            EXPECT_EQ(all[3 * n * 512], v);
+        }
         // the same three operations as an execution graph (test_hazard_analyzer.cpp / 
         // test_topological_scheduler.cpp shapes): hazards chain them, the order is A, B, C
         runtime::BrickPool pool2(dev, {c});
