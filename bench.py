@@ -356,7 +356,7 @@ def run_gpu(args):
     rep = Replicas()
     ws, rank, local = rep.world, rep.rank, rep.local
     ctx = fl.Context(local)
-    pool = Pool(ctx, [sphere_case()])
+    pool = Pool(ctx, [sphere_case(args.scale)])
     info0 = pool.info()
     # spin-up: the flow develops (and the vorticity regrids refine its wake) before anything is timed
     step_no = 0
@@ -455,14 +455,19 @@ def run_gpu(args):
     t0 = time.perf_counter()
     stop = timer(ctx)
     ctx.call("fl_pool_upload", pool.h, hp)
+    ctx.sync()
+    t_up = time.perf_counter()
     for k in range(args.steps):
         ctx.call("fl_pool_set_velocities", pool.h, vp, ctypes.c_void_p(vp.value + 12))
         e2e_lups += inf.fluid_lups_per_step
         pool.step(1)
         ctx.call("fl_pool_conservation", pool.h, cons.ctypes.data_as(ctypes.c_void_p))
+    t_steps = time.perf_counter()
     ctx.call("fl_pool_download", pool.h, None, None, None, None, None, hp)
     e2e_ms = stop()
     e2e_wall = time.perf_counter() - t0
+    e2e_phases = {"upload_ms": round((t_up - t0) * 1e3, 2), "steps_ms": round((t_steps - t_up) * 1e3, 2),
+                  "download_ms": round((time.perf_counter() - t_steps) * 1e3, 2)}
     e2e_ms = max(e2e_ms, e2e_wall * 1e3)
     e2e_ms = rep.max(e2e_ms)
     e2e_value = rep.sum(float(e2e_lups)) / (e2e_ms * 1e-3) / 1e6
@@ -499,6 +504,7 @@ def run_gpu(args):
                 "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": workload_config({"timed_from_step": args.spinup + args.warmup + 1,
+                                           "scale": args.scale,
                                            "bricks": int(bricks0), "fluid_lups_per_step": int(lups0),
                                            "bricks_per_level": [int(info.bricks_per_level[l]) for l in range(4)],
                                            "fluid_sites_per_level": [int(info.fluid_sites_per_level[l]) for l in range(4)],
@@ -506,7 +512,7 @@ def run_gpu(args):
                                                             "fluid_lups_per_step": int(info0.fluid_lups_per_step)},
                                            "parallelism": "replicas" if ws > 1 else "single"}),
                 "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                        "d2h_bytes_per_step": int(d2h)},
+                        "d2h_bytes_per_step": int(d2h), "phases_wall": e2e_phases},
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
                 "regrid_ms_per_cycle": round(statistics.mean(regrid_ms), 3), "regrids_in_timed_region": regrids,
                 "config2_full_run": full, "regrid_microbench": micro, "batching": batch, "serving": serve,
@@ -573,6 +579,9 @@ def main():
                     help="untimed level-0 steps (with regrids) before the warm-up, so the timed steps see the "
                          "developed flow")
     ap.add_argument("--no-full-run", action="store_true")
+    ap.add_argument("--scale", type=int, default=1, choices=[1, 2],
+                    help="2 runs the sphere at half resolution per axis (profiling captures only; the "
+                         "reported workload is scale 1)")
     ap.add_argument("--no-batching", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serving-seconds", type=float, default=2.0,

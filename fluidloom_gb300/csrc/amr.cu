@@ -148,6 +148,8 @@ __global__ void __launch_bounds__(kT) k_detect_face6(fl_mesh_dev m, fl_domain_de
 __global__ void __launch_bounds__(kProbeThreads, 2) k_detect_full26(fl_mesh_dev m, fl_domain_dev dom, fl_locator L,
                                                                     const uint8_t* __restrict__ shadow,
                                                                     const uint32_t* __restrict__ lowest,
+                                                                    const uint8_t* __restrict__ act,
+                                                                    uint8_t* __restrict__ nxt,
                                                                     uint8_t* __restrict__ viol,
                                                                     uint32_t* __restrict__ count) {
     __shared__ uint8_t t1[96];
@@ -163,7 +165,7 @@ __global__ void __launch_bounds__(kProbeThreads, 2) k_detect_full26(fl_mesh_dev 
     uint32_t local = 0;
     for (size_t base = (size_t)blockIdx.x * 32; base < m.n; base += (size_t)gridDim.x * 32) {
         const size_t i = base + cl;
-        if (i >= m.n || (int)shadow[i] < low + 2) continue;
+        if (i >= m.n || (int)shadow[i] < low + 2 || (act && !act[i])) continue;
         const uint16_t cs = m.case_id ? m.case_id[i] : 0;
         const fl_domain_dev::Case& d = dom.c[m.case_id ? cs : 0];
         const int sh = dom.anchor_level - m.level[i];
@@ -173,19 +175,27 @@ __global__ void __launch_bounds__(kProbeThreads, 2) k_detect_full26(fl_mesh_dev 
         if (!fold3_32(p, d, dom.anchor_level)) continue;
         const uint32_t r = fl_probe_point(P, m.case_id != nullptr, cs, (uint32_t)p[0], (uint32_t)p[1], (uint32_t)p[2]);
         if (r == FL_INVALID_INDEX) continue;
-        if ((int)shadow[i] >= (int)shadow[r] + 2) { viol[r] = 1; ++local; }
+        if ((int)shadow[i] >= (int)shadow[r] + 2) {
+            viol[r] = 1;
+            if (nxt) nxt[i] = 1;
+            ++local;
+        }
     }
     if (local) atomicAdd(count, local);
 }
 
 // mark_cascading_refinement (balance_enforce.cl:150-172).
 __global__ void k_mark(fl_mesh_dev m, int32_t* __restrict__ flags, const uint8_t* __restrict__ viol, int max_level,
-                       uint32_t* __restrict__ count) {
+                       uint8_t* __restrict__ nxt, uint32_t* __restrict__ count) {
     size_t stride = (size_t)gridDim.x * blockDim.x;
     uint32_t local = 0;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
         if (!viol[i] || m.state[i] != 0 || m.level[i] >= max_level) continue;
-        if (flags[i] <= 0) { flags[i] = 1; ++local; }
+        if (flags[i] <= 0) {
+            flags[i] = 1;
+            if (nxt) nxt[i] = 1;
+            ++local;
+        }
     }
     if (local) atomicAdd(count, local);
 }
@@ -596,7 +606,7 @@ size_t fl_adapt_scratch_bytes(size_t n, uint64_t cap) {
     size_t b = 0;
     b += fl_align256(n * 8);                 // cell keys (FACE6's hash table)
     b += fl_align256(cap * 16) + fl_align256(cap * 4);  // 16-byte-slot table + win
-    b += 2 * fl_align256(n);                 // shadow, viol
+    b += 4 * fl_align256(n);                 // shadow, viol, two rounds of probing leaves
     b += 4 * fl_align256(n * 4);             // leader, gid, group_of, cnt/off
     b += fl_align256(n * 4);                 // members (n/8 groups * 8)
     b += fl_align256(64);                    // counters
@@ -605,9 +615,16 @@ size_t fl_adapt_scratch_bytes(size_t n, uint64_t cap) {
 }
 
 // Balance over a mesh with an already-built table (shared by fl_balance_enforce and fl_adapt).
+// FULL26 probes from every leaf in the first round only.  A pair (i, r)
+// violates when shadow(i) >= shadow(r) + 2, and a round changes shadow levels
+// only by raising those of the leaves it marks; so a pair can violate in round
+// k + 1 only if i was marked in round k or i already found a violation in
+// round k.  Those leaves (act: two buffers of one byte per leaf, stride
+// fl_align256(n), or nullptr to probe from every leaf each round) are the only
+// ones that probe afterwards, which gives the same violations, marks and counts.
 int fl_balance_run(fl_ctx* ctx, fl_mesh_dev md, int32_t* flags, const fl_domain_dev& dom, const uint64_t* tk,
                    const uint32_t* tv, uint64_t cap, const fl_locator* L, int mode, int max_level, int max_iters,
-                   uint8_t* shadow, uint8_t* viol, uint32_t* counters, fl_balance_result* res) {
+                   uint8_t* shadow, uint8_t* viol, uint8_t* act, uint32_t* counters, fl_balance_result* res) {
     fl_balance_result r{};
     if (md.n == 0) { r.converged = 1; if (res) *res = r; return FL_OK; }
     unsigned nb = fl_blocks(md.n, kT, ctx->num_sms * 8);
@@ -622,15 +639,20 @@ int fl_balance_run(fl_ctx* ctx, fl_mesh_dev md, int32_t* flags, const fl_domain_
     uint32_t h[2];
     for (; it < (uint32_t)cap_it; ++it) {
         FL_TRY_CUDA(ctx, cudaMemsetAsync(counters, 0, 8, ctx->stream), "balance counters");
+        // this round's probing leaves (all of them in the first round) and the next round's
+        uint8_t* cur = (act && mode == 1 && it > 0) ? act + (size_t)((it - 1) & 1) * fl_align256(md.n) : nullptr;
+        uint8_t* nxt = (act && mode == 1) ? act + (size_t)(it & 1) * fl_align256(md.n) : nullptr;
         if (mode == 0) {
             k_detect_face6<<<nb, kT, 0, ctx->stream>>>(md, dom, tk, tv, lg, shadow, viol, counters);
         } else {
             k_clear_u8<<<nb, kT, 0, ctx->stream>>>(viol, md.n);
+            if (nxt) k_clear_u8<<<nb, kT, 0, ctx->stream>>>(nxt, md.n);
             const unsigned pb = (unsigned)std::min<size_t>((md.n + 31) / 32, (size_t)ctx->num_sms * 2);
-            k_detect_full26<<<pb, kProbeThreads, 0, ctx->stream>>>(md, dom, *L, shadow, lowest, viol, counters);
+            k_detect_full26<<<pb, kProbeThreads, 0, ctx->stream>>>(md, dom, *L, shadow, lowest, cur, nxt, viol,
+                                                                   counters);
         }
         FL_CHECK_LAUNCH(ctx, "k_detect");
-        k_mark<<<nb, kT, 0, ctx->stream>>>(md, flags, viol, max_level, counters + 1);
+        k_mark<<<nb, kT, 0, ctx->stream>>>(md, flags, viol, max_level, nxt, counters + 1);
         FL_CHECK_LAUNCH(ctx, "k_mark");
         FL_TRY_CUDA(ctx, cudaMemcpyAsync(h, counters, 8, cudaMemcpyDeviceToHost, ctx->stream), "balance read");
         FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "balance sync");
@@ -653,7 +675,7 @@ int fl_balance_run(fl_ctx* ctx, fl_mesh_dev md, int32_t* flags, const fl_domain_
 struct AdaptWork {
     uint64_t cap;
     uint64_t* keys; uint64_t* tk; uint32_t* tv; uint32_t* win;
-    uint8_t* shadow; uint8_t* viol;
+    uint8_t* shadow; uint8_t* viol; uint8_t* act;
     uint32_t* leader; uint32_t* gid; uint32_t* group_of; uint32_t* cnt; uint32_t* members; uint32_t* counters;
     void* scan_scratch;
     void* locator;  // fl_locator_build scratch
@@ -669,6 +691,7 @@ static AdaptWork carve_adapt(void* scratch, size_t n, bool with_case) {
     w.win = cv.take<uint32_t>(w.cap);
     w.shadow = cv.take<uint8_t>(n);
     w.viol = cv.take<uint8_t>(n);
+    w.act = cv.take<uint8_t>(2 * fl_align256(n));
     w.leader = cv.take<uint32_t>(n);
     w.gid = cv.take<uint32_t>(n);
     w.group_of = cv.take<uint32_t>(n);
@@ -718,7 +741,7 @@ int fl_adapt_prepare(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cf
     FL_TRY_CUDA(ctx, cudaMemsetAsync(w.counters, 0, 64, ctx->stream), "adapt counters");
     if (run_balance) {
         rc = fl_balance_run(ctx, md, mesh->flags, dom, w.tk, w.tv, w.cap, &L, cfg->balance_mode,
-                            cfg->max_refinement_level, (int)cfg->max_balance_iterations, w.shadow, w.viol,
+                            cfg->max_refinement_level, (int)cfg->max_balance_iterations, w.shadow, w.viol, w.act,
                             w.counters + 8, &s.balance);
         if (rc) return rc;
     }
@@ -818,7 +841,7 @@ int fl_balance_enforce(fl_ctx* ctx, fl_mesh* mesh, const fl_adapt_config* cfg, f
     if (n == 0) { if (res) res->converged = 1; return FL_OK; }
     const bool face6 = cfg->balance_mode == 0;  // FACE6 probes shadow levels through the hash table
     uint64_t cap = face6 ? fl_table_capacity(n) : 0;
-    size_t need = fl_align256(n * 8) + fl_align256(cap * 16) + fl_align256(cap * 4) + 2 * fl_align256(n) + 512 + 256 +
+    size_t need = fl_align256(n * 8) + fl_align256(cap * 16) + fl_align256(cap * 4) + 4 * fl_align256(n) + 512 + 256 +
                   (face6 ? 0 : fl_locator_scratch_bytes(n));
     int rc = fl_scratch_reserve(ctx, need);
     if (rc) return rc;
@@ -830,6 +853,7 @@ int fl_balance_enforce(fl_ctx* ctx, fl_mesh* mesh, const fl_adapt_config* cfg, f
     uint32_t* win = cv.take<uint32_t>(cap);
     uint8_t* shadow = cv.take<uint8_t>(n);
     uint8_t* viol = cv.take<uint8_t>(n);
+    uint8_t* act = cv.take<uint8_t>(2 * fl_align256(n));
     uint32_t* counters = cv.take<uint32_t>(16);
     fl_domain_dev dom = fl_domain_from_config(ctx, cfg, dcase);
     fl_mesh_dev md{mesh->x, mesh->y, mesh->z, mesh->level, mesh->state, mesh->flags, mesh->material, mesh->case_id, n};
@@ -845,7 +869,7 @@ int fl_balance_enforce(fl_ctx* ctx, fl_mesh* mesh, const fl_adapt_config* cfg, f
     if (rc) return rc;
     fl_balance_result r;
     rc = fl_balance_run(ctx, md, mesh->flags, dom, tk, tv, cap, &L, cfg->balance_mode, cfg->max_refinement_level,
-                        (int)cfg->max_balance_iterations, shadow, viol, counters, &r);
+                        (int)cfg->max_balance_iterations, shadow, viol, act, counters, &r);
     if (rc) return rc;
     rc = fl_collect_device_status(ctx, "fl_balance_enforce");
     if (rc) return rc;

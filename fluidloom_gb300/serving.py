@@ -72,6 +72,11 @@ def make_jobs(rate, duration, steps_range, seed=5):
     return jobs
 
 
+def used_bytes(pool):
+    """Population bytes the pool's resident bricks hold (three buffers per brick)."""
+    return 0 if pool is None else int(pool.info().num_bricks) * BRICK_BYTES
+
+
 def reserved_bytes(pool):
     """The pool's device footprint as the library reports it: its three population buffers
     at their current capacity (fl_pool_info population_bytes)."""
@@ -83,16 +88,19 @@ def run_served(ctx, jobs, budget_bytes, check_ids=(), regrid_every=20, resident_
 
     Jobs are admitted in arrival order at pool steps that are multiples of
     admit_every (default: the regrid interval, so that resident jobs share their
-    regrids).  Admission is gated by the pool's actual reserved bytes: a queued job
-    is added, and if the pool's footprint then exceeds min(budget_bytes,
-    resident_bytes) it is removed again and waits for jobs to finish (deferred); a
-    job whose level-0 bricks alone exceed the whole budget (start_bytes) is refused.
-    resident_bytes is the throughput knob: enough resident bricks to keep HBM busy,
-    and no more, so queued jobs start in order instead of all sharing the GPU."""
+    regrids), gated by measured bytes: a queued job is added, and if the bricks
+    then resident hold more than min(budget_bytes, resident_bytes), or the pool's
+    reserved buffers exceed budget_bytes, it is taken out again and waits
+    (deferred) -- it keeps the footprint it was measured at, so it is only tried
+    again once that fits.  A job whose level-0 bricks alone exceed the whole
+    budget (start_bytes) is refused.  resident_bytes is the throughput knob:
+    enough resident bricks to keep HBM busy, and no more, so queued jobs start in
+    order instead of all sharing the GPU."""
     cap = budget_bytes if resident_bytes is None else min(budget_bytes, resident_bytes)
     admit_every = admit_every or regrid_every
     pending = collections.deque(sorted(jobs, key=lambda j: j.arrival))
     queue, active = collections.deque(), {}
+    need = {}  # job id -> bytes its bricks took when it was last added
     pool = None
     lups = 0
     steps_run = 0
@@ -111,20 +119,27 @@ def run_served(ctx, jobs, budget_bytes, check_ids=(), regrid_every=20, resident_
             queue.append(j)
         if not active:
             phase = 0
-        while phase % admit_every == 0 and queue:
-            j = queue[0]
-            if pool is None:
-                pool = Pool(ctx, [j.case])
-                cid = 0
-            else:
-                cid = pool.add_cases([j.case])[0]
-            if active and reserved_bytes(pool) > cap:  # over the cap: back to the queue until jobs finish
-                pool.remove_cases([cid])
-                deferrals += 1
-                break
-            queue.popleft()
-            j.cid, j.start = cid, time.perf_counter() - t0
-            active[cid] = j
+        if phase % admit_every == 0 and queue:
+            used = used_bytes(pool)
+            while queue:
+                j = queue[0]
+                if active and j.jid in need and used + need[j.jid] > cap:
+                    break  # known not to fit until jobs finish
+                if pool is None:
+                    pool = Pool(ctx, [j.case])
+                    cid = 0
+                else:
+                    cid = pool.add_cases([j.case])[0]
+                now_used = used_bytes(pool)
+                need[j.jid] = now_used - used
+                if active and (now_used > cap or reserved_bytes(pool) > budget_bytes):
+                    pool.remove_cases([cid])  # over the budget: back to the queue until jobs finish
+                    deferrals += 1
+                    break
+                used = now_used
+                queue.popleft()
+                j.cid, j.start = cid, time.perf_counter() - t0
+                active[cid] = j
         if not active:
             if pending:
                 time.sleep(max(0.0, min(0.05, pending[0].arrival - (time.perf_counter() - t0))))
@@ -210,7 +225,8 @@ def benchmark(ctx, rate=50.0, duration=60.0, steps_range=(200, 2000), budget_gb=
             if not same:
                 mismatched.append(j.jid)
     return {"jobs": len(jobs), "rate_per_s": rate, "duration_s": duration, "steps_range": list(steps_range),
-            "admission": "arrival order, resident footprint <= %.1f GB of a %.0f GB budget" % (resident_gb, budget_gb),
+            "admission": "arrival order, resident bricks' bytes <= %.1f GB, reserved buffers <= the %.0f GB budget"
+                         % (resident_gb, budget_gb),
             "served_makespan_s": round(makespan, 3), "served_mlups": round(lups / makespan / 1e6, 1),
             "served_p50_s": percentile(lat, 50), "served_p99_s": percentile(lat, 99),
             "plain_mlups": round(solo_lups / solo_s / 1e6, 1), "plain_makespan_s": round(end_prev, 3),

@@ -115,28 +115,25 @@ def test_served_loop_matches_solo_runs(ctx):
 
 
 def test_admission_defers_and_refuses_under_a_small_budget(ctx):
-    """A budget of 1.5 pools of the first job: the second job (a 32^3 cavity) makes the
-    pool grow past it, so it is taken out again and admitted once the first has
-    finished (deferred, not lost), and the third waits for the second the same way;
-    a job whose level-0 bricks alone exceed the budget is refused.  Every admitted
-    job still ends in its solo state."""
+    """A budget of 100 level-0 bricks' worth of populations: the first 32^3 cavity
+    (64 bricks) is admitted, the second would bring the resident bricks to 128, so
+    it is taken out again and admitted once the first has finished (deferred, not
+    lost), and the small third job waits behind it in arrival order; a job whose
+    level-0 bricks alone exceed the budget is refused.  Every admitted job still
+    ends in its solo state."""
     from fluidloom_gb300 import lbm, serving
-    from fluidloom_gb300.lbm import Pool
-    a, b, c = _cases()
-    probe = Pool(ctx, [a])
-    one = probe.info().population_bytes  # the footprint of a pool holding job a alone
-    probe.close()
-    mid = lbm.cavity(32, 1, u_lid=0.04, tau=0.6)
+    mid1 = lbm.cavity(32, 1, u_lid=0.04, tau=0.6)
+    mid2 = lbm.cavity(32, 1, u_lid=0.03, tau=0.58)
+    a = _cases()[0]
     big = lbm.sphere_channel(128, 64, 64, 1, radius=8.0, centre=(32.0, 32.0, 32.0), u_in=0.04, band=6.0)
-    jobs = [serving.Job(0, 0.0, a, 25), serving.Job(1, 0.0, mid, 25), serving.Job(2, 0.0, a, 25),
+    jobs = [serving.Job(0, 0.0, mid1, 25), serving.Job(1, 0.0, mid2, 25), serving.Job(2, 0.0, a, 25),
             serving.Job(3, 0.0, big, 25)]
-    budget = 1.5 * one
+    budget = 100 * serving.BRICK_BYTES
     assert jobs[3].start_bytes() > budget and all(j.start_bytes() <= budget for j in jobs[:3])
     lups, makespan, steps_run = serving.run_served(ctx, jobs, budget_bytes=budget, check_ids={0, 1, 2})
     assert jobs[3].refused and jobs[3].cid is None
     assert run_deferrals() > 0
-    starts = sorted(j.start for j in jobs[:3])
-    assert starts[-1] > starts[0]  # not all three ran at once
+    assert jobs[1].start >= jobs[0].end  # the second waited for the first
     for j in jobs[:3]:
         assert j.end is not None and j.refused is None
         _, _, solo = serving.run_solo(ctx, j)
