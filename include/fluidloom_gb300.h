@@ -400,7 +400,6 @@ int fl_pool_remove_cases(fl_ctx* ctx, fl_pool* pool, const int32_t* ids, int nid
  * except nbricks.  Call with f == NULL first to learn nbricks. */
 int fl_pool_download_case(fl_ctx* ctx, fl_pool* pool, int32_t id, int32_t* x, int32_t* y, int32_t* z,
                           uint8_t* level, float* f, size_t* nbricks);
-/* use_graphs: replay captured CUDA graphs per level-0 step; grid_mult: CTAs per SM (0 keeps). */
 /* The pool's populations as a 19-component FP32 field of this context's structure-of-arrays manager,
  * as the reference allocates them (SOAFieldManager::allocate, src/core/fields/SOAFieldManager.cpp:17-131)
  * and binds them to its LBM kernel nodes (KernelNode::bindField, src/runtime/nodes/KernelNode.cpp:27-29):
@@ -410,6 +409,7 @@ int fl_pool_download_case(fl_ctx* ctx, fl_pool* pool, int32_t id, int32_t* x, in
  * it change the pool.  It stays valid until the next call that steps, regrids, loads, adds or removes
  * cases; call again to refresh it (the handle stays, its version grows when the storage moved). */
 int fl_pool_populations_field(fl_ctx* ctx, fl_pool* pool, const char* name, uint64_t* handle);
+/* use_graphs: replay captured CUDA graphs per level-0 step; grid_mult: CTAs per SM (0 keeps). */
 int fl_pool_set_options(fl_ctx* ctx, fl_pool* pool, int use_graphs, int grid_mult);
 /* streams = 2 (default): each level-0 step runs as a dependency graph over two streams per
  * level -- general, interface and all-solid bricks on one, interior bricks on the other --
