@@ -357,6 +357,8 @@ def run_gpu(args):
     ws, rank, local = rep.world, rep.rank, rep.local
     ctx = fl.Context(local)
     pool = Pool(ctx, [sphere_case(args.scale)])
+    if args.staging:
+        pool.set_options(staging=args.staging)
     info0 = pool.info()
     # spin-up: the flow develops (and the vorticity regrids refine its wake) before anything is timed
     step_no = 0
@@ -504,10 +506,14 @@ def run_gpu(args):
                 "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": workload_config({"timed_from_step": args.spinup + args.warmup + 1,
-                                           "scale": args.scale,
+                                           "scale": args.scale, "staging": args.staging,
                                            "bricks": int(bricks0), "fluid_lups_per_step": int(lups0),
                                            "bricks_per_level": [int(info.bricks_per_level[l]) for l in range(4)],
                                            "fluid_sites_per_level": [int(info.fluid_sites_per_level[l]) for l in range(4)],
+                                           "general_bricks_per_level": [int(info.general_bricks_per_level[l])
+                                                                        for l in range(4)],
+                                           "stencil_descriptors_per_level": [
+                                               int(info.stencil_descriptors_per_level[l]) for l in range(4)],
                                            "initial_mesh": {"bricks": int(info0.num_bricks),
                                                             "fluid_lups_per_step": int(info0.fluid_lups_per_step)},
                                            "parallelism": "replicas" if ws > 1 else "single"}),
@@ -582,6 +588,9 @@ def main():
     ap.add_argument("--scale", type=int, default=1, choices=[1, 2],
                     help="2 runs the sphere at half resolution per axis (profiling captures only; the "
                          "reported workload is scale 1)")
+    ap.add_argument("--staging", type=int, default=0, choices=[0, 1, 2],
+                    help="collide kernels' reads of a brick's own populations: 0 registers, 1 bulk copies into "
+                         "shared memory, 2 also the general bricks' descriptor values (fl_pool_set_staging)")
     ap.add_argument("--no-batching", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serving-seconds", type=float, default=2.0,

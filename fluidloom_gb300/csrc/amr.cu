@@ -140,48 +140,93 @@ __global__ void __launch_bounds__(kT) k_detect_face6(fl_mesh_dev m, fl_domain_de
     if (local) atomicAdd(count, local);
 }
 
-// Every leaf probes its 26 neighbour points at its own size through the
-// sorted locator (32 cells x 26 directions per block); a leaf found two or
-// more shadow levels coarser is a violation.  A leaf less than two shadow
-// levels above the mesh's lowest (lowest[0]) cannot find one and does not
-// probe; with the highest (lowest[1]) below lowest + 2 no block probes.
-__global__ void __launch_bounds__(kProbeThreads, 2) k_detect_full26(fl_mesh_dev m, fl_domain_dev dom, fl_locator L,
-                                                                    const uint8_t* __restrict__ shadow,
-                                                                    const uint32_t* __restrict__ lowest,
-                                                                    const uint8_t* __restrict__ act,
-                                                                    uint8_t* __restrict__ nxt,
-                                                                    uint8_t* __restrict__ viol,
-                                                                    uint32_t* __restrict__ count) {
+// Every leaf probes, through the sorted locator, its neighbour points at its
+// own size in the 19 directions that leave its parent cell (32 leaves x 19
+// directions per block); a leaf found two or more shadow levels coarser is a
+// violation.  The 7 directions that stay inside the parent (towards the
+// leaf's siblings' places) cannot find one: a leaf there coarser than this
+// one would contain the parent and so overlap this leaf.  A leaf less than
+// two shadow levels above the mesh's lowest (lowest[0]) cannot find one either
+// and does not probe; with the highest (lowest[1]) below lowest + 2 no block
+// probes.  list (with its length at *list_n) restricts the probing leaves, in
+// any order: violations and counts do not depend on it.
+constexpr int kDetectThreads = 32 * 19;
+__global__ void __launch_bounds__(kDetectThreads, 3) k_detect_full26(fl_mesh_dev m, fl_domain_dev dom, fl_locator L,
+                                                                     const uint8_t* __restrict__ shadow,
+                                                                     const uint32_t* __restrict__ lowest,
+                                                                     const uint32_t* __restrict__ list,
+                                                                     const uint32_t* __restrict__ list_n,
+                                                                     uint8_t* __restrict__ nxt,
+                                                                     uint8_t* __restrict__ viol,
+                                                                     uint32_t* __restrict__ count) {
     __shared__ uint8_t t1[96];
     __shared__ uint16_t t3c[12 * 512];
+    __shared__ uint8_t s_dir[8][19];  // per child position (x&1 | (y&1)<<1 | (z&1)<<2): outward directions
     fl_keys_fill_tables_cat(t1, t3c);
+    if (threadIdx.x < 8) {
+        const int c = threadIdx.x;
+        int e = 0;
+        for (int kk = 0; kk < 27; ++kk) {
+            if (kk == 13) continue;
+            const int d[3] = {kk % 3 - 1, (kk / 3) % 3 - 1, kk / 9 - 1};
+            bool out = false;
+            for (int a = 0; a < 3; ++a) out |= d[a] == (((c >> a) & 1) ? 1 : -1);
+            if (out) s_dir[c][e++] = (uint8_t)kk;
+        }
+    }
     __syncthreads();
     const fl_probe P = fl_probe_make(t1, t3c, L, dom);
-    const int cl = threadIdx.x / 26, k = threadIdx.x - cl * 26;
-    const int kk = k < 13 ? k : k + 1;
-    const int dv[3] = {kk % 3 - 1, (kk / 3) % 3 - 1, kk / 9 - 1};
+    const int cl = threadIdx.x / 19, k = threadIdx.x - cl * 19;
     const int low = (int)lowest[0];
     if ((int)lowest[1] < low + 2) return;  // no leaf anywhere is two levels above another
+    const size_t n = list ? (size_t)*list_n : m.n;
     uint32_t local = 0;
-    for (size_t base = (size_t)blockIdx.x * 32; base < m.n; base += (size_t)gridDim.x * 32) {
-        const size_t i = base + cl;
-        if (i >= m.n || (int)shadow[i] < low + 2 || (act && !act[i])) continue;
+    for (size_t base = (size_t)blockIdx.x * 32; base < n; base += (size_t)gridDim.x * 32) {
+        const size_t j = base + cl;
+        if (j >= n) continue;
+        const size_t i = list ? (size_t)list[j] : j;
+        const int si = shadow[i];
+        if (si < low + 2) continue;
         const uint16_t cs = m.case_id ? m.case_id[i] : 0;
         const fl_domain_dev::Case& d = dom.c[m.case_id ? cs : 0];
         const int sh = dom.anchor_level - m.level[i];
         const int32_t size = 1 << sh;
-        int32_t p[3] = {m.x[i] << sh, m.y[i] << sh, m.z[i] << sh};
+        const int32_t cx = m.x[i], cy = m.y[i], cz = m.z[i];
+        const int kk = s_dir[(cx & 1) | ((cy & 1) << 1) | ((cz & 1) << 2)][k];
+        const int dv[3] = {kk % 3 - 1, (kk / 3) % 3 - 1, kk / 9 - 1};
+        int32_t p[3] = {cx << sh, cy << sh, cz << sh};
         for (int a = 0; a < 3; ++a) p[a] += dv[a] < 0 ? -1 : (dv[a] > 0 ? size : 0);
         if (!fold3_32(p, d, dom.anchor_level)) continue;
         const uint32_t r = fl_probe_point(P, m.case_id != nullptr, cs, (uint32_t)p[0], (uint32_t)p[1], (uint32_t)p[2]);
         if (r == FL_INVALID_INDEX) continue;
-        if ((int)shadow[i] >= (int)shadow[r] + 2) {
+        if (si >= (int)shadow[r] + 2) {
             viol[r] = 1;
             if (nxt) nxt[i] = 1;
             ++local;
         }
     }
     if (local) atomicAdd(count, local);
+}
+
+// The leaves whose byte is set, into list (in any order; their number added
+// to *list_n), and the bytes cleared.
+__global__ void k_compact_active(uint8_t* __restrict__ flags, size_t n, uint32_t* __restrict__ list,
+                                 uint32_t* __restrict__ list_n) {
+    const int lane = threadIdx.x & 31;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x - lane; i0 < n; i0 += stride) {
+        const size_t i = i0 + lane;
+        const bool on = i < n && flags[i];
+        const unsigned bal = __ballot_sync(0xFFFFFFFFu, on);
+        if (!bal) continue;
+        uint32_t first = 0;
+        if (lane == 0) first = atomicAdd(list_n, (uint32_t)__popc(bal));
+        first = __shfl_sync(0xFFFFFFFFu, first, 0);
+        if (on) {
+            flags[i] = 0;
+            list[first + __popc(bal & ((1u << lane) - 1u))] = (uint32_t)i;
+        }
+    }
 }
 
 // mark_cascading_refinement (balance_enforce.cl:150-172).
@@ -230,26 +275,32 @@ __device__ __forceinline__ uint32_t sibling_of(const fl_probe& P, const fl_mesh_
 // Leaders: a warp screens 32 cells, a lane each, then checks the chunk's
 // candidates four at a time -- lanes 8s .. 8s + 7 locate the eight siblings of
 // the s-th (all must be mergeable leaves of its level) -- and, for the FULL26
-// merge condition, spreads the 98 probe points around each surviving octet
-// over the lanes, the candidates' points one after another: no leaf touching
-// an octet from outside may end above its level.  The probe points take, per
-// axis, only five coordinates -- the last fine point below the octet, the
-// first and last of its lower cell, the first of its upper cell, the first
-// point above -- so the 98 combinations with at least one outside coordinate
-// are exactly the distinct probes outside the octet (the 27 others lie inside
-// it).
+// merge condition, spreads the probes around each surviving octet over the
+// lanes, the candidates' probes one after another: no leaf touching an octet
+// from outside may end above its level.  The reference's probes are each
+// child's 26 neighbour points at the child's size; per axis they take five
+// coordinates -- the last fine point below the octet, the first and last of
+// its lower cell, the first of its upper cell, the first point above -- and
+// the 98 combinations with at least one outside coordinate are the distinct
+// probes outside the octet.  They fall into the 56 cells of the children's
+// size around the octet (4 per axis: below, lower, upper, above).  One point
+// per cell decides the cell whenever it finds a leaf: a leaf of the octet's
+// level or coarser holding it holds the whole cell, and a finer one is above
+// the octet's level wherever in the cell it lies; only when that point is
+// not covered (a mesh that does not fill its domain) are the cell's other
+// probe points tried.  Same answer as the 98 probes, from 56 on a filled mesh.
 __global__ void __launch_bounds__(kT) k_leaders(fl_mesh_dev m, fl_domain_dev dom, fl_locator L, int min_level,
                                                 int check26, const uint8_t* __restrict__ shadow,
                                                 uint32_t* __restrict__ is_leader) {
     __shared__ uint8_t t1[96];
     __shared__ uint16_t t3c[12 * 512];
-    __shared__ uint8_t surf[98];  // the outside points k = ix + 5 iy + 25 iz of the 5^3 grid
+    __shared__ uint8_t surf[56];  // the outside cells k = ux + 4 uy + 16 uz of the 4^3 grid of child-sized cells
     fl_keys_fill_tables_cat(t1, t3c);
     if (threadIdx.x == 0) {
         int e = 0;
-        for (int k = 0; k < 125; ++k) {
-            const int ix = k % 5, iy = (k / 5) % 5, iz = k / 25;
-            if (ix == 0 || ix == 4 || iy == 0 || iy == 4 || iz == 0 || iz == 4) surf[e++] = (uint8_t)k;
+        for (int k = 0; k < 64; ++k) {
+            const int ux = k & 3, uy = (k >> 2) & 3, uz = k >> 4;
+            if (ux == 0 || ux == 3 || uy == 0 || uy == 3 || uz == 0 || uz == 3) surf[e++] = (uint8_t)k;
         }
     }
     __syncthreads();
@@ -285,10 +336,10 @@ __global__ void __launch_bounds__(kT) k_leaders(fl_mesh_dev m, fl_domain_dev dom
                 const int32_t b_m[3] = {have ? m.x[i] << sh_m : 0, have ? m.y[i] << sh_m : 0,
                                         have ? m.z[i] << sh_m : 0};
                 const int nc = __popc(lead4);
-                for (int e0 = 0; e0 < nc * 98; e0 += 32) {
+                for (int e0 = 0; e0 < nc * 56; e0 += 32) {
                     const int e = e0 + lane;
-                    const bool act = e < nc * 98;
-                    int t = act ? e / 98 : 0;  // t-th surviving candidate ...
+                    const bool act = e < nc * 56;
+                    int t = act ? e / 56 : 0;  // t-th surviving candidate ...
                     unsigned lm = lead4;
                     for (int k = 0; k < t; ++k) lm &= lm - 1;
                     const int s = __ffs(lm) - 1;  // ... is candidate s
@@ -302,21 +353,39 @@ __global__ void __launch_bounds__(kT) k_leaders(fl_mesh_dev m, fl_domain_dev dom
                     if (!act) continue;
                     const fl_domain_dev::Case& d = dom.c[m.case_id ? cs : 0];
                     const int32_t size = 1 << (dom.anchor_level - l);
-                    const int k = surf[e - t * 98];
-                    const int id[3] = {k % 5, (k / 5) % 5, k / 25};
+                    const int k = surf[e - t * 56];
+                    const int uc[3] = {k & 3, (k >> 2) & 3, k >> 4};
+                    // the cell's probe point with alt set on the axes where the cell is the lower child's
+                    // span: its last point there instead of its first
+                    auto point = [&](int alt, int32_t (&p)[3]) {
+                        for (int a = 0; a < 3; ++a) {
+                            const int u = uc[a];
+                            p[a] = u == 0 ? b3[a] - 1
+                                          : (u == 1 ? b3[a] + (((alt >> a) & 1) ? size - 1 : 0)
+                                                    : (u == 2 ? b3[a] + size : b3[a] + 2 * size));
+                        }
+                        return fold3_32(p, d, dom.anchor_level);
+                    };
+                    auto found = [&](uint32_t r) {
+                        bool inside = false;  // only on a periodic axis of one octet's extent
+                        for (int q = 0; q < 8; ++q) inside |= (mem[q] == r);
+                        if (!inside && (int)shadow[r] > l) bad4 |= 1u << s;
+                    };
                     int32_t p[3];
-                    for (int a = 0; a < 3; ++a) {
-                        const int u = id[a];
-                        p[a] = u == 0 ? b3[a] - 1
-                                      : (u == 1 ? b3[a] : (u == 2 ? b3[a] + size - 1 : (u == 3 ? b3[a] + size : b3[a] + 2 * size)));
-                    }
-                    if (!fold3_32(p, d, dom.anchor_level)) continue;
+                    if (!point(0, p)) continue;
                     const uint32_t r =
                         fl_probe_point(P, m.case_id != nullptr, cs, (uint32_t)p[0], (uint32_t)p[1], (uint32_t)p[2]);
-                    if (r == FL_INVALID_INDEX) continue;
-                    bool inside = false;  // only on a periodic axis of one octet's extent
-                    for (int q = 0; q < 8; ++q) inside |= (mem[q] == r);
-                    if (!inside && (int)shadow[r] > l) bad4 |= 1u << s;
+                    if (r != FL_INVALID_INDEX) {
+                        found(r);
+                        continue;
+                    }
+                    const int multi = (uc[0] == 1) | ((uc[1] == 1) << 1) | ((uc[2] == 1) << 2);
+                    for (int v = multi; v; v = (v - 1) & multi) {  // the cell's other probe points
+                        if (!point(v, p)) continue;
+                        const uint32_t r2 =
+                            fl_probe_point(P, m.case_id != nullptr, cs, (uint32_t)p[0], (uint32_t)p[1], (uint32_t)p[2]);
+                        if (r2 != FL_INVALID_INDEX) found(r2);
+                    }
                 }
                 bad4 = __reduce_or_sync(0xFFFFFFFFu, bad4);
             }
@@ -602,11 +671,14 @@ fl_domain_dev fl_domain_from_config(fl_ctx* ctx, const fl_adapt_config* cfg, voi
     return d;
 }
 
+// FULL26 balance's probing-leaf state for n leaves: a byte per leaf, then a list of leaf ids.
+static size_t fl_balance_act_bytes(size_t n) { return fl_align256(n) + fl_align256(n * 4); }
+
 size_t fl_adapt_scratch_bytes(size_t n, uint64_t cap) {
     size_t b = 0;
     b += fl_align256(n * 8);                 // cell keys (FACE6's hash table)
     b += fl_align256(cap * 16) + fl_align256(cap * 4);  // 16-byte-slot table + win
-    b += 4 * fl_align256(n);                 // shadow, viol, two rounds of probing leaves
+    b += 2 * fl_align256(n) + fl_balance_act_bytes(n);  // shadow, viol, probing leaves
     b += 4 * fl_align256(n * 4);             // leader, gid, group_of, cnt/off
     b += fl_align256(n * 4);                 // members (n/8 groups * 8)
     b += fl_align256(64);                    // counters
@@ -619,9 +691,11 @@ size_t fl_adapt_scratch_bytes(size_t n, uint64_t cap) {
 // violates when shadow(i) >= shadow(r) + 2, and a round changes shadow levels
 // only by raising those of the leaves it marks; so a pair can violate in round
 // k + 1 only if i was marked in round k or i already found a violation in
-// round k.  Those leaves (act: two buffers of one byte per leaf, stride
-// fl_align256(n), or nullptr to probe from every leaf each round) are the only
-// ones that probe afterwards, which gives the same violations, marks and counts.
+// round k.  Those leaves are the only ones that probe afterwards, which gives
+// the same violations, marks and counts.  act (fl_balance_act_bytes(n), or
+// nullptr to probe from every leaf each round) holds one byte per leaf, set
+// for the next round's probing leaves, then at offset fl_align256(n) the list
+// they are gathered into before that round.
 int fl_balance_run(fl_ctx* ctx, fl_mesh_dev md, int32_t* flags, const fl_domain_dev& dom, const uint64_t* tk,
                    const uint32_t* tv, uint64_t cap, const fl_locator* L, int mode, int max_level, int max_iters,
                    uint8_t* shadow, uint8_t* viol, uint8_t* act, uint32_t* counters, fl_balance_result* res) {
@@ -640,16 +714,23 @@ int fl_balance_run(fl_ctx* ctx, fl_mesh_dev md, int32_t* flags, const fl_domain_
     for (; it < (uint32_t)cap_it; ++it) {
         FL_TRY_CUDA(ctx, cudaMemsetAsync(counters, 0, 8, ctx->stream), "balance counters");
         // this round's probing leaves (all of them in the first round) and the next round's
-        uint8_t* cur = (act && mode == 1 && it > 0) ? act + (size_t)((it - 1) & 1) * fl_align256(md.n) : nullptr;
-        uint8_t* nxt = (act && mode == 1) ? act + (size_t)(it & 1) * fl_align256(md.n) : nullptr;
+        uint8_t* nxt = (act && mode == 1) ? act : nullptr;
+        uint32_t* list = (act && mode == 1 && it > 0) ? (uint32_t*)(act + fl_align256(md.n)) : nullptr;
+        uint32_t* list_n = counters + 4;  // free until the merge grouping after balance
         if (mode == 0) {
             k_detect_face6<<<nb, kT, 0, ctx->stream>>>(md, dom, tk, tv, lg, shadow, viol, counters);
         } else {
             k_clear_u8<<<nb, kT, 0, ctx->stream>>>(viol, md.n);
-            if (nxt) k_clear_u8<<<nb, kT, 0, ctx->stream>>>(nxt, md.n);
-            const unsigned pb = (unsigned)std::min<size_t>((md.n + 31) / 32, (size_t)ctx->num_sms * 2);
-            k_detect_full26<<<pb, kProbeThreads, 0, ctx->stream>>>(md, dom, *L, shadow, lowest, cur, nxt, viol,
-                                                                   counters);
+            if (list) {
+                // this round's probing leaves: those flagged in the last round (the flags are cleared)
+                FL_TRY_CUDA(ctx, cudaMemsetAsync(list_n, 0, 4, ctx->stream), "balance list");
+                k_compact_active<<<nb, kT, 0, ctx->stream>>>(nxt, md.n, list, list_n);
+            } else if (nxt) {
+                k_clear_u8<<<nb, kT, 0, ctx->stream>>>(nxt, md.n);
+            }
+            const unsigned pb = (unsigned)std::min<size_t>((md.n + 31) / 32, (size_t)ctx->num_sms * 3);
+            k_detect_full26<<<pb, kDetectThreads, 0, ctx->stream>>>(md, dom, *L, shadow, lowest, list, list_n, nxt,
+                                                                    viol, counters);
         }
         FL_CHECK_LAUNCH(ctx, "k_detect");
         k_mark<<<nb, kT, 0, ctx->stream>>>(md, flags, viol, max_level, nxt, counters + 1);
@@ -691,7 +772,7 @@ static AdaptWork carve_adapt(void* scratch, size_t n, bool with_case) {
     w.win = cv.take<uint32_t>(w.cap);
     w.shadow = cv.take<uint8_t>(n);
     w.viol = cv.take<uint8_t>(n);
-    w.act = cv.take<uint8_t>(2 * fl_align256(n));
+    w.act = cv.take<uint8_t>(fl_balance_act_bytes(n));
     w.leader = cv.take<uint32_t>(n);
     w.gid = cv.take<uint32_t>(n);
     w.group_of = cv.take<uint32_t>(n);
@@ -841,7 +922,8 @@ int fl_balance_enforce(fl_ctx* ctx, fl_mesh* mesh, const fl_adapt_config* cfg, f
     if (n == 0) { if (res) res->converged = 1; return FL_OK; }
     const bool face6 = cfg->balance_mode == 0;  // FACE6 probes shadow levels through the hash table
     uint64_t cap = face6 ? fl_table_capacity(n) : 0;
-    size_t need = fl_align256(n * 8) + fl_align256(cap * 16) + fl_align256(cap * 4) + 4 * fl_align256(n) + 512 + 256 +
+    size_t need = fl_align256(n * 8) + fl_align256(cap * 16) + fl_align256(cap * 4) + 2 * fl_align256(n) +
+                  fl_balance_act_bytes(n) + 512 + 256 +
                   (face6 ? 0 : fl_locator_scratch_bytes(n));
     int rc = fl_scratch_reserve(ctx, need);
     if (rc) return rc;
@@ -853,7 +935,7 @@ int fl_balance_enforce(fl_ctx* ctx, fl_mesh* mesh, const fl_adapt_config* cfg, f
     uint32_t* win = cv.take<uint32_t>(cap);
     uint8_t* shadow = cv.take<uint8_t>(n);
     uint8_t* viol = cv.take<uint8_t>(n);
-    uint8_t* act = cv.take<uint8_t>(2 * fl_align256(n));
+    uint8_t* act = cv.take<uint8_t>(fl_balance_act_bytes(n));
     uint32_t* counters = cv.take<uint32_t>(16);
     fl_domain_dev dom = fl_domain_from_config(ctx, cfg, dcase);
     fl_mesh_dev md{mesh->x, mesh->y, mesh->z, mesh->level, mesh->state, mesh->flags, mesh->material, mesh->case_id, n};

@@ -26,6 +26,7 @@
 // restatement it is tested against.
 #include "common.cuh"
 #include "amr.cuh"
+#include "bulk.cuh"
 #include "hash.cuh"
 #include "keys.cuh"
 #include "scan.cuh"
@@ -581,6 +582,208 @@ __global__ void __launch_bounds__(128, 4) k_collide_general(StepArgs a, const ui
         for (int q = 0; q < Q; ++q)
             *(float4*)(a.W + fidx(a.cap, q, b, own)) = make_float4(f[q][0], f[q][1], f[q][2], f[q][3]);
         __syncthreads();
+        b = bn;
+    }
+}
+
+// Staged variant of both collide kernels (fl_pool_set_staging): the brick's
+// own 19 population planes (2 KB each, contiguous in f[q][brick][site]) --
+// and, for general bricks with kDesc, its 128 quad masks and the values of its
+// stencil descriptors -- arrive in shared memory by bulk copies (the TMA
+// engine's linear mode) on an mbarrier, issued one brick ahead by thread 0
+// while the block relaxes and stores the current brick.  Rows of the brick's
+// own planes are then read from shared memory; halo rows and x-face columns
+// of neighbours stay global loads, as in gather_quad.  Same arithmetic in the
+// same order: the results equal the register kernels' bit for bit.
+constexpr uint32_t kStagePlaneBytes = Q * 2048;
+constexpr uint32_t kStagePv = 2048;  // descriptor values staged per brick (more: read from global)
+
+__host__ __device__ constexpr uint32_t stage_bytes(bool general, bool desc) {
+    return kStagePlaneBytes + (general && desc ? 2048 + kStagePv * 4 : 0);
+}
+
+template <int Q0, int Q1>
+__device__ __forceinline__ void gather_quad_staged(const StepArgs& a, const uint32_t* s_nb, const float* s_f, int x0,
+                                                   int y, int z, float (&f)[Q][4]) {
+    const int lane_odd = x0 != 0;
+#pragma unroll
+    for (int q = Q0; q < Q1; ++q) {
+        const int cx = CXq(q), cy = CYq(q), cz = CZq(q);
+        const int sy = y - cy, sz = z - cz;
+        const int dy = sy >> 3, dz = sz >> 3;
+        const int rowoff = (sy & 7) * 8 + (sz & 7) * 64;
+        const uint32_t erow = s_nb[(dz + 1) * 9 + (dy + 1) * 3 + 1];
+        float4 A;
+        if (dy == 0 && dz == 0) A = *(const float4*)(s_f + q * 512 + rowoff + x0);
+        else A = __ldg((const float4*)(a.R + fidx(a.cap, q, erow, rowoff + x0)));
+        if (cx == 0) {
+            f[q][0] = A.x; f[q][1] = A.y; f[q][2] = A.z; f[q][3] = A.w;
+        } else if (cx == 1) {
+            float h = __shfl_xor_sync(0xFFFFFFFFu, A.w, 1);
+            if (!lane_odd) h = __ldg(a.R + fidx(a.cap, q, s_nb[(dz + 1) * 9 + (dy + 1) * 3 + 0], rowoff + 7));
+            f[q][0] = h; f[q][1] = A.x; f[q][2] = A.y; f[q][3] = A.z;
+        } else {
+            float h = __shfl_xor_sync(0xFFFFFFFFu, A.x, 1);
+            if (lane_odd) h = __ldg(a.R + fidx(a.cap, q, s_nb[(dz + 1) * 9 + (dy + 1) * 3 + 2], rowoff + 0));
+            f[q][0] = A.y; f[q][1] = A.z; f[q][2] = A.w; f[q][3] = h;
+        }
+    }
+}
+
+// The elements of an x-quad flagged in its quad mask qm (bit 4q + i, ordered
+// like the descriptors, from the quad's first descriptor qm.w on) replaced by
+// their descriptor values vals[qm.w ...]: from shared memory, or from global
+// memory through the read-only path.
+__device__ __forceinline__ void replace_described(const uint4 qm, const float* vals, float (&f)[Q][4]) {
+    uint32_t r = qm.w;
+    if (qm.x) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if ((qm.x >> (q * 4 + i)) & 1u) f[q][i] = vals[r++];
+    }
+    if (qm.y) {
+#pragma unroll
+        for (int q = 8; q < 16; ++q)
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if ((qm.y >> (q * 4 + i - 32)) & 1u) f[q][i] = vals[r++];
+    }
+    if (qm.z) {
+#pragma unroll
+        for (int q = 16; q < Q; ++q)
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if ((qm.z >> (q * 4 + i - 64)) & 1u) f[q][i] = vals[r++];
+    }
+}
+
+__device__ __forceinline__ void replace_described_global(const uint4 qm, const float* __restrict__ vals,
+                                                         float (&f)[Q][4]) {
+    uint32_t r = qm.w;
+    if (qm.x) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if ((qm.x >> (q * 4 + i)) & 1u) f[q][i] = __ldg(vals + r++);
+    }
+    if (qm.y) {
+#pragma unroll
+        for (int q = 8; q < 16; ++q)
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if ((qm.y >> (q * 4 + i - 32)) & 1u) f[q][i] = __ldg(vals + r++);
+    }
+    if (qm.z) {
+#pragma unroll
+        for (int q = 16; q < Q; ++q)
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if ((qm.z >> (q * 4 + i - 64)) & 1u) f[q][i] = __ldg(vals + r++);
+    }
+}
+
+struct StageState {
+    uint64_t bar;
+    uint32_t pv_off;  // the brick's first descriptor within the staged values
+    uint32_t pv_n;    // staged values (0: read them from global)
+};
+
+// Thread 0: arm the barrier and issue the copies of list position w (brick b).
+template <bool kGeneral, bool kDesc>
+__device__ __forceinline__ void stage_issue(const StepArgs& a, uint32_t w, uint32_t b, unsigned char* s_dyn,
+                                            StageState* st) {
+    uint32_t bytes = kStagePlaneBytes, pv0 = 0, pvn = 0;
+    if (kGeneral && kDesc) {
+        bytes += 2048;
+        const uint32_t d0 = a.desc_off[w], d1 = a.desc_off[w + 1];
+        const uint32_t s0 = d0 & ~3u, n = (d1 - s0 + 3u) & ~3u;  // 16-byte aligned superset (the buffer has slack)
+        if (d1 > d0 && n <= kStagePv) {
+            pv0 = s0;
+            pvn = n;
+            bytes += n * 4;
+        }
+        st->pv_off = d0 - s0;
+        st->pv_n = pvn;
+    }
+    flbulk::mbar_arrive_expect_tx(&st->bar, bytes);
+#pragma unroll 1
+    for (int q = 0; q < Q; ++q)
+        flbulk::copy_g2s(s_dyn + q * 2048, a.R + fidx(a.cap, q, b, 0), 2048, &st->bar);
+    if (kGeneral && kDesc) {
+        flbulk::copy_g2s(s_dyn + kStagePlaneBytes, a.qmask + (size_t)b * 128, 2048, &st->bar);
+        if (pvn) flbulk::copy_g2s(s_dyn + kStagePlaneBytes + 2048, a.pv + pv0, pvn * 4, &st->bar);
+    }
+}
+
+template <bool kGeneral, bool kDesc>
+__global__ void __launch_bounds__(128, 4) k_collide_staged(StepArgs a, const uint32_t* __restrict__ nb27) {
+    extern __shared__ __align__(128) unsigned char s_dyn[];
+    __shared__ uint32_t s_nb[27];
+    __shared__ StageState st;
+    const float* s_f = (const float*)s_dyn;
+    const uint4* s_qm = (const uint4*)(s_dyn + kStagePlaneBytes);
+    const float* s_pv = (const float*)(s_dyn + kStagePlaneBytes + 2048);
+    const int l = a.level;
+    const int t = threadIdx.x;
+    const int x0 = (t & 1) * 4, y = (t >> 1) & 7, z = t >> 4;
+    const int own = x0 + 8 * y + 64 * z;
+    if (t == 0) flbulk::mbar_init(&st.bar, 1);
+    __syncthreads();
+    uint32_t w = blockIdx.x;
+    uint32_t b = w < a.count ? a.list[w] : 0u;
+    if (t == 0 && w < a.count) stage_issue<kGeneral, kDesc>(a, w, b, s_dyn, &st);
+    uint32_t row = (w < a.count && t < 27) ? nb27[(size_t)b * 28 + t] : 0u;
+    uint32_t phase = 0;
+    for (; w < a.count; w += gridDim.x) {
+        if (t < 27) s_nb[t] = (kGeneral && row == kSlow) ? b : row;
+        __syncthreads();
+        const uint32_t wn = w + gridDim.x;
+        const uint32_t bn = wn < a.count ? a.list[wn] : 0u;
+        if (wn < a.count && t < 27) row = nb27[(size_t)bn * 28 + t];
+        const float omega = a.cases[a.bcase[b]].omega[l];
+        const uint32_t sw = kGeneral ? a.smask[(size_t)b * 16 + (own >> 5)] : 0u;
+        const uint4 qm_g = (kGeneral && !kDesc) ? a.qmask[(size_t)b * 128 + t] : make_uint4(0, 0, 0, 0);
+        const bool ok = flbulk::mbar_wait(&st.bar, phase, FL_SPIN_LIMIT);
+        if (__syncthreads_or(!ok)) {
+            // a copy never landed: report it, give the copies one more bounded
+            // wait, and leave without touching the output
+            if (t == 0) {
+                atomicAdd(a.dev_status + FL_DEVSTAT_TIMEOUT, 1u);
+                flbulk::mbar_wait(&st.bar, phase, FL_SPIN_LIMIT);
+            }
+            return;
+        }
+        phase ^= 1u;
+        float f[Q][4];
+        gather_quad_staged<0, Q>(a, s_nb, s_f, x0, y, z, f);
+        if (kGeneral) {
+            const uint4 qm = kDesc ? s_qm[t] : qm_g;
+            if (kDesc && st.pv_n != 0)
+                replace_described(qm, s_pv + st.pv_off, f);  // shared-memory reads
+            else
+                replace_described_global(qm, a.pv + a.desc_off[w], f);
+        }
+        __syncthreads();  // every read of the staged brick and of s_nb is done
+        if (t == 0 && wn < a.count) {
+            // order the block's shared-memory reads above before the copies that overwrite the stage
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            stage_issue<kGeneral, kDesc>(a, wn, bn, s_dyn, &st);
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            float g[Q];
+#pragma unroll
+            for (int q = 0; q < Q; ++q) g[q] = f[q][i];
+            relax_site(g, omega, kGeneral && ((sw >> ((own + i) & 31)) & 1u));
+#pragma unroll
+            for (int q = 0; q < Q; ++q) f[q][i] = g[q];
+        }
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+            *(float4*)(a.W + fidx(a.cap, q, b, own)) = make_float4(f[q][0], f[q][1], f[q][2], f[q][3]);
         b = bn;
     }
 }
@@ -1379,6 +1582,11 @@ struct fl_pool {
     void* adapt_scratch = nullptr;
     size_t adapt_scratch_bytes = 0;
     int grid_mult = 4;
+    // 0: collide kernels load straight into registers; 1: the brick's own
+    // population planes bulk-copied into shared memory one brick ahead
+    // (k_collide_staged); 2: as 1, with the general bricks' quad masks and
+    // descriptor values staged too
+    int staging = 0;
     // All-solid bricks only ever hold the rest equilibrium: once both
     // population buffers of a level hold it (two sub-steps after any change of
     // the bricks or populations), rewriting it changes nothing and its launch
@@ -1666,7 +1874,7 @@ int pool_topology_build(fl_ctx* ctx, fl_pool* P) {
     if (h.desc64 >= (1ull << 32)) return fl_set_error(ctx, FL_E_CAPACITY, "more than 2^32 stencil descriptors");
     P->num_desc = h.desc64;
     P->lvl_desc.assign(h.lvl_desc, h.lvl_desc + P->maxL + 2);
-    if (P->num_desc > P->desc_cap) {
+    if (P->num_desc + 4 > P->desc_cap) {  // k_collide_staged reads up to 3 values past the last
         // no pointer is left naming freed memory if an allocation fails
         if (P->desc) cudaFreeAsync(P->desc, ctx->stream);
         if (P->pv) cudaFreeAsync(P->pv, ctx->stream);
@@ -1939,12 +2147,21 @@ void launch_class(fl_ctx* ctx, fl_pool* P, StepArgs a, int l, int kind, cudaStre
     ctx->launches += (kind == 1 && P->lvl_desc[l + 1] > P->lvl_desc[l]) ? 2 : 1;
     if (kind == 0) {
         unsigned grid = std::min<unsigned>(cnt, (unsigned)ctx->num_sms * P->grid_mult);
-        k_collide_fast<<<grid, 128, 0, st>>>(a, P->nb27);
+        if (P->staging)
+            k_collide_staged<false, false><<<grid, 128, stage_bytes(false, false), st>>>(a, P->nb27);
+        else
+            k_collide_fast<<<grid, 128, 0, st>>>(a, P->nb27);
     } else if (kind == 1) {
         a.desc_off = P->slow_off + off;
         const uint32_t dd0 = P->lvl_desc[l], dd1 = P->lvl_desc[l + 1];
         if (dd1 > dd0) k_interface<<<fl_blocks(dd1 - dd0, 256, ctx->num_sms * 8), 256, 0, st>>>(a, dd0, dd1, P->pv);
-        k_collide_general<<<std::min<unsigned>(cnt, (unsigned)ctx->num_sms * 4), 128, 0, st>>>(a, P->nb27);
+        const unsigned grid = std::min<unsigned>(cnt, (unsigned)ctx->num_sms * 4);
+        if (P->staging == 2)
+            k_collide_staged<true, true><<<grid, 128, stage_bytes(true, true), st>>>(a, P->nb27);
+        else if (P->staging == 1)
+            k_collide_staged<true, false><<<grid, 128, stage_bytes(true, false), st>>>(a, P->nb27);
+        else
+            k_collide_general<<<grid, 128, 0, st>>>(a, P->nb27);
     } else {
         k_collide_solid<<<fl_blocks((size_t)cnt * 512, 256, ctx->num_sms * 8), 256, 0, st>>>(a);
     }
@@ -2277,6 +2494,11 @@ int fl_pool_info_get(fl_ctx* ctx, fl_pool* P, fl_pool_info* info) {
     for (int l = 0; l < 16; ++l) info->fluid_sites_per_level[l] = P->fluid_per_level[l];
     info->population_bytes = (uint64_t)P->cap * 512 * Q * 4 * 3;
     info->usable = P->unusable ? 0 : 1;
+    for (int l = 0; l <= P->maxL && l < 16; ++l) {
+        info->general_bricks_per_level[l] = P->cls_cnt[1].size() > (size_t)l ? P->cls_cnt[1][l] : 0;
+        info->stencil_descriptors_per_level[l] =
+            P->lvl_desc.size() > (size_t)l + 1 ? (uint64_t)(P->lvl_desc[l + 1] - P->lvl_desc[l]) : 0;
+    }
     return FL_OK;
 }
 
@@ -2752,6 +2974,21 @@ int fl_pool_set_options(fl_ctx* ctx, fl_pool* P, int use_graphs, int grid_mult) 
     FL_POOL_USABLE(ctx, P);
     P->graphs = use_graphs;
     if (grid_mult > 0) P->grid_mult = grid_mult;
+    drop_graph(P);
+    return FL_OK;
+}
+
+int fl_pool_set_staging(fl_ctx* ctx, fl_pool* P, int mode) {
+    if (!ctx || !P || mode < 0 || mode > 2) return FL_E_INVALID_ARG;
+    FL_POOL_USABLE(ctx, P);
+    if (mode) {
+        // above the default 48 KB of dynamic shared memory per block
+        FL_TRY_CUDA(ctx, cudaFuncSetAttribute(k_collide_staged<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)stage_bytes(true, true)),
+                    "staged kernel shared memory");
+    }
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "fl_pool_set_staging");
+    P->staging = mode;
     drop_graph(P);
     return FL_OK;
 }

@@ -36,7 +36,8 @@ class PoolInfo(ctypes.Structure):
                 ("max_level", ctypes.c_int32), ("bricks_per_level", ctypes.c_uint32 * 16),
                 ("fluid_lups_per_step", ctypes.c_uint64), ("population_bytes", ctypes.c_uint64),
                 ("fluid_sites_per_level", ctypes.c_uint64 * 16), ("num_active_cases", ctypes.c_int32),
-                ("usable", ctypes.c_int32)]
+                ("usable", ctypes.c_int32), ("general_bricks_per_level", ctypes.c_uint32 * 16),
+                ("stencil_descriptors_per_level", ctypes.c_uint64 * 16)]
 
 
 WALL, MOVING, INLET, OUTLET, PERIODIC = 1, 2, 3, 4, 0
@@ -161,10 +162,12 @@ class Pool:
         self.ctx.call("fl_pool_info_get", self.h, ctypes.byref(i))
         return i
 
-    def set_options(self, graphs=1, grid_mult=0, streams=None):
+    def set_options(self, graphs=1, grid_mult=0, streams=None, staging=None):
         self.ctx.call("fl_pool_set_options", self.h, graphs, grid_mult)
         if streams is not None:
             self.ctx.call("fl_pool_set_class_streams", self.h, streams)
+        if staging is not None:
+            self.ctx.call("fl_pool_set_staging", self.h, staging)
 
     def bricks(self):
         n = self.info().num_bricks

@@ -322,6 +322,9 @@ typedef struct fl_pool_info {
     int32_t usable;                 /* 0 after a call failed part-way through replacing the pool's bricks or
                                        tables: every call but fl_pool_destroy and this one then returns
                                        FL_E_INVALID_ARG without touching the device */
+    uint32_t general_bricks_per_level[16];         /* bricks with stencil descriptors (interface, boundary,
+                                                      near the sphere) */
+    uint64_t stencil_descriptors_per_level[16];    /* elements whose source is not a plain same-level load */
 } fl_pool_info;
 
 /* Build the cases: level-0 bricks, max_level rounds of sphere-band refinement, equilibrium start. */
@@ -411,6 +414,12 @@ int fl_pool_download_case(fl_ctx* ctx, fl_pool* pool, int32_t id, int32_t* x, in
 int fl_pool_populations_field(fl_ctx* ctx, fl_pool* pool, const char* name, uint64_t* handle);
 /* use_graphs: replay captured CUDA graphs per level-0 step; grid_mult: CTAs per SM (0 keeps). */
 int fl_pool_set_options(fl_ctx* ctx, fl_pool* pool, int use_graphs, int grid_mult);
+/* How the collide-stream kernels read a brick's own populations: 0 (default) straight into
+ * registers with 128-bit loads; 1 its 19 population planes bulk-copied into shared memory by the
+ * TMA engine (cp.async.bulk on an mbarrier), one brick ahead of the one being relaxed; 2 as 1,
+ * with the general bricks' quad masks and stencil-descriptor values staged the same way.
+ * Results are identical in every mode. */
+int fl_pool_set_staging(fl_ctx* ctx, fl_pool* pool, int mode);
 /* streams = 2 (default): each level-0 step runs as a dependency graph over two streams per
  * level -- general, interface and all-solid bricks on one, interior bricks on the other --
  * joined by events (coarse and fine sources are always interface bricks, so only the

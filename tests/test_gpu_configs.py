@@ -78,6 +78,23 @@ def test_config2_sphere_full_size(ctx):
     gp.close()
 
 
+def test_config2_sphere_bulk_staged_equals_register_kernels(ctx):
+    """Full-size sphere: the bulk-staged collide kernels (both staging modes) equal the
+    register kernels bit for bit over 6 level-0 steps (48 level-3 sub-steps)."""
+    from bench import sphere_case
+    case = sphere_case()
+    ref = Pool(ctx, [case])
+    ref.step(6)
+    f0 = ref.populations()
+    ref.close()
+    for mode in (1, 2):
+        p = Pool(ctx, [case])
+        p.set_options(staging=mode)
+        p.step(6)
+        assert np.array_equal(p.populations(), f0), mode
+        p.close()
+
+
 # ----------------------------------------------------------------- config 3
 
 

@@ -29,11 +29,13 @@ def assert_pool_equal(gp, op, check_f=True):
     return 0.0
 
 
+@pytest.mark.parametrize("staging", [0, 2])
 @pytest.mark.parametrize("which", [0, 1])
-def test_pool_steps_and_regrid_vs_oracle(ctx, which):
+def test_pool_steps_and_regrid_vs_oracle(ctx, which, staging):
     from fluidloom_gb300.lbm import Pool
     c = cases_small()[which]
     gp, op = Pool(ctx, [c]), O.OraclePool([c])
+    gp.set_options(staging=staging)
     assert gp.info().fluid_lups_per_step == op.lups()
     assert_pool_equal(gp, op)
     for rnd in range(2):
@@ -74,6 +76,28 @@ def test_concurrent_class_streams_match_one_stream(ctx, graphs):
         p.step(4)
         p.regrid()
         p.step(3)
+    np.testing.assert_array_equal(a.populations(), b.populations())
+
+
+@pytest.mark.parametrize("staging", [1, 2])
+@pytest.mark.parametrize("graphs", [0, 1])
+def test_bulk_staged_kernels_match_register_kernels(ctx, staging, graphs):
+    """The collide kernels with each brick's planes (and, in mode 2, the general bricks'
+    quad masks and descriptor values) bulk-copied into shared memory give the register
+    kernels' populations bit for bit, both cases in one pool, across a regrid."""
+    from fluidloom_gb300.lbm import Pool
+    cs = list(cases_small())
+    a, b = Pool(ctx, cs), Pool(ctx, cs)
+    a.set_options(graphs=graphs, staging=staging)
+    b.set_options(graphs=graphs, staging=0)
+    for p in (a, b):
+        p.step(4)
+        p.regrid()
+        p.step(3)
+    np.testing.assert_array_equal(a.populations(), b.populations())
+    a.set_options(graphs=graphs, staging=0)  # and back: the pool keeps stepping in either mode
+    for p in (a, b):
+        p.step(2)
     np.testing.assert_array_equal(a.populations(), b.populations())
 
 
