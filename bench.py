@@ -40,15 +40,27 @@ METRIC = "AMR-LBM MLUPS (D3Q19, flow past a sphere)"
 UNIT = "MLUPS"
 
 
+RUN_STEPS = 1000  # the configuration's run length
+# Vorticity thresholds of the sphere case, as fractions of the case's maximum |vorticity|: the
+# configuration names "a threshold" and "about 20 M leaf cells at peak"; over its 1000 steps
+# the peak fluid sites are 8.5 M at 0.5 (only the band refines), 11.7 M at 0.1, 14.9 M at
+# 0.07, 18.2 M at 0.05 and 24.3 M at 0.03, so 0.04 (coarsen below 0.015) gives about 20 M.
+SPHERE_REFINE_FRAC, SPHERE_COARSEN_FRAC = 0.04, 0.015
+
+
 def sphere_case(scale=1):
     from fluidloom_gb300 import lbm
-    return lbm.sphere_channel(128 // scale, 64 // scale, 64 // scale, 3, radius=8.0 / scale,
-                              centre=(32.0 / scale,) * 3, u_in=0.04, tau=0.56, band=6.0 / scale)
+    c = lbm.sphere_channel(128 // scale, 64 // scale, 64 // scale, 3, radius=8.0 / scale,
+                           centre=(32.0 / scale,) * 3, u_in=0.04, tau=0.56, band=6.0 / scale)
+    c.refine_frac, c.coarsen_frac = SPHERE_REFINE_FRAC, SPHERE_COARSEN_FRAC
+    return c
 
 
 def workload_config(extra=None):
     c = {"workload": "flow past a sphere, D3Q19 BGK FP32, 128x64x64 base, 3 levels, r=8, u=0.04, tau0=0.56",
          "base_grid": [128, 64, 64], "levels": 3, "brick": "8^3 sites", "regrid_every": REGRID_EVERY,
+         "refine": "6-cell band around the sphere, plus bricks with |vorticity| > %g of the case's maximum "
+                   "(coarsen below %g)" % (SPHERE_REFINE_FRAC, SPHERE_COARSEN_FRAC),
          "l2": "inputs larger than L2 (populations > 129 MB), no flush", "graphs": True}
     if extra:
         c.update(extra)
@@ -375,6 +387,8 @@ def run_gpu(args):
     info0 = pool.info()
     # spin-up: the flow develops (and the vorticity regrids refine its wake) before anything is timed
     step_no = 0
+    if args.spinup is None:  # the timed steps are the last of the configuration's 1000-step run
+        args.spinup = max(0, RUN_STEPS - args.steps - args.warmup)
     for _ in range(args.spinup + args.warmup):
         pool.step(1)
         step_no += 1
@@ -594,9 +608,9 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-microbench", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--spinup", type=int, default=500,
-                    help="untimed level-0 steps (with regrids) before the warm-up, so the timed steps see the "
-                         "developed flow")
+    ap.add_argument("--spinup", type=int, default=None,
+                    help="untimed level-0 steps (with regrids) before the warm-up; default: so that the timed "
+                         "steps end at step 1000, the end of the configuration's run, where its mesh peaks")
     ap.add_argument("--no-full-run", action="store_true")
     ap.add_argument("--scale", type=int, default=1, choices=[1, 2],
                     help="2 runs the sphere at half resolution per axis (profiling captures only; the "

@@ -788,6 +788,21 @@ __global__ void __launch_bounds__(128, 4) k_collide_staged(StepArgs a, const uin
     }
 }
 
+// Every brick's populations, from the buffer its level's parity names (bit l
+// of odd: level l's current populations are in f1), into dst, a float4 per
+// thread: the current state in one buffer for a single device-to-host copy.
+__global__ void k_gather_current(const float* __restrict__ f0, const float* __restrict__ f1, float* __restrict__ dst,
+                                 size_t cap, size_t n, const uint8_t* __restrict__ level, uint32_t odd) {
+    const size_t total = (size_t)Q * n * 128;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
+        const size_t qb = t >> 7, q = qb / n, b = qb - q * n;
+        const size_t off = (q * cap + b) * 512 + (t & 127) * 4;
+        const float* src = ((odd >> level[b]) & 1u) ? f1 : f0;
+        *(float4*)(dst + off) = *(const float4*)(src + off);
+    }
+}
+
 // The populations of the listed bricks from one buffer to the other, a float4
 // per thread.
 __global__ void k_copy_bricks(const float* __restrict__ src, float* __restrict__ dst, size_t cap,
@@ -1649,12 +1664,6 @@ PoolView view(fl_pool* P) {
     return v;
 }
 
-int pool_reserve_bricks(fl_ctx* ctx, fl_pool* P, size_t need) {
-    // grows nbr / flags scratch / partials; population buffers are handled by the regrid
-    if (need <= P->cap) return FL_OK;
-    return FL_E_CAPACITY;
-}
-
 int alloc_brick_arrays(fl_ctx* ctx, fl_pool* P, size_t cap) {
     FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->nbr, cap * 26 * 4 * 4, ctx->stream), "pool nbr");
     FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->list, cap * 8, ctx->stream), "pool list");  // list + general positions
@@ -2512,22 +2521,26 @@ int fl_pool_download(fl_ctx* ctx, fl_pool* P, int32_t* x, int32_t* y, int32_t* z
     if (z) FL_TRY_CUDA(ctx, cudaMemcpyAsync(z, P->mesh.z, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "dl");
     if (level) FL_TRY_CUDA(ctx, cudaMemcpyAsync(level, P->mesh.level, n, cudaMemcpyDeviceToHost, ctx->stream), "dl");
     if (case_id) FL_TRY_CUDA(ctx, cudaMemcpyAsync(case_id, P->mesh.case_id, n * 2, cudaMemcpyDeviceToHost, ctx->stream), "dl");
-    if (f) {
-        std::vector<uint8_t> lv(n);
-        FL_TRY_CUDA(ctx, cudaMemcpyAsync(lv.data(), P->mesh.level, n, cudaMemcpyDeviceToHost, ctx->stream), "dl");
-        FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "dl");
-        // bricks of one level are contiguous runs only by chance; copy per brick run of equal parity
-        for (int q = 0; q < Q; ++q) {
-            size_t b = 0;
-            while (b < n) {
-                int par = P->parity[lv[b]];
-                size_t e = b + 1;
-                while (e < n && P->parity[lv[e]] == par) ++e;
-                FL_TRY_CUDA(ctx, cudaMemcpyAsync(f + ((size_t)q * n + b) * 512, P->f[par] + ((size_t)q * P->cap + b) * 512,
-                                                 (e - b) * 512 * 4, cudaMemcpyDeviceToHost, ctx->stream), "dl f");
-                b = e;
-            }
+    if (f && n) {
+        // the levels' current buffers: one of the two for all of them (one copy per population), or
+        // mixed -- level 0 has flipped once more than the others after an odd number of level-0 steps --
+        // and then gathered on the device into the spare buffer first
+        uint32_t odd = 0, present = 0;
+        for (int l = 0; l <= P->maxL; ++l) {
+            if (P->lvl_off[l + 1] == P->lvl_off[l]) continue;
+            present |= 1u << l;
+            if (P->parity[l]) odd |= 1u << l;
         }
+        const float* src = P->f[odd ? 1 : 0];
+        if (odd && odd != present) {
+            k_gather_current<<<fl_blocks((size_t)Q * n * 128, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(
+                P->f[0], P->f[1], P->f[2], P->cap, n, P->mesh.level, odd);
+            FL_CHECK_LAUNCH(ctx, "k_gather_current");
+            src = P->f[2];
+        }
+        for (int q = 0; q < Q; ++q)
+            FL_TRY_CUDA(ctx, cudaMemcpyAsync(f + (size_t)q * n * 512, src + (size_t)q * P->cap * 512, n * 512 * 4,
+                                             cudaMemcpyDeviceToHost, ctx->stream), "dl f");
     }
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "download");
     return FL_OK;
