@@ -399,6 +399,10 @@ def run_gpu(args):
     bricks0 = info.num_bricks
     lups0 = info.fluid_lups_per_step
     rep.barrier()
+    if args.profile_region:  # a profiler started with --profile-from-start off records from here on
+        import torch
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
@@ -463,6 +467,10 @@ def run_gpu(args):
                 # collide-stream bytes over the timed region
                 "timed_region_achieved": round(value * 1e6 * BYTES_PER_LUP / 1e9, 1),
                 "timed_region_frac": round(value * 1e6 * BYTES_PER_LUP / 1e9 / peak, 4)}
+    if args.profile_region:
+        import torch
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
     # e2e through the C ABI with pinned host buffers
     inf = pool.info()
     n = inf.num_bricks
@@ -618,6 +626,9 @@ def main():
     ap.add_argument("--staging", type=int, default=0, choices=[0, 1, 2],
                     help="collide kernels' reads of a brick's own populations: 0 registers, 1 bulk copies into "
                          "shared memory, 2 also the general bricks' descriptor values (fl_pool_set_staging)")
+    ap.add_argument("--profile-region", action="store_true",
+                    help="bracket the timed steps, the regrid and the per-kernel profile passes with "
+                         "cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     ap.add_argument("--no-batching", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serving-seconds", type=float, default=2.0,

@@ -34,26 +34,41 @@ def cavity_batch(n=256, seed=4):
     return out
 
 
-def autotune(pool, candidates=(2, 3, 4, 6, 8), streams=(1, 2), steps=4):
-    """Pick the CTAs per SM of the interior collide-stream kernel and the class-stream layout
-    (every launch on one stream, or the per-level dependency graph over two) by timing
-    graph-replayed level-0 steps of each combination with CUDA events (two untimed
-    steps first capture the graphs); returns (ctas_per_sm, streams).  The pool's
-    state advances: tune on a pool that is rebuilt afterwards."""
+def autotune(pool, candidates=(2, 3, 4, 6, 8), streams=(1, 2), staging=(0, 1, 2), steps=4):
+    """Pick the CTAs per SM of the interior collide-stream kernel, the class-stream layout
+    (every launch on one stream, or the per-level dependency graph over two) and how the
+    collide kernels read a brick's own populations (fl_pool_set_staging: 128-bit loads into
+    registers, or bulk copies into shared memory one brick ahead, with or without the
+    general bricks' descriptor values) by timing graph-replayed level-0 steps with CUDA
+    events (two untimed steps first capture the graphs): every CTA count and stream layout
+    with register loads, then each staging mode at the best of those; returns
+    (ctas_per_sm, streams, staging).  The pool's state advances: tune on a pool that is
+    rebuilt afterwards."""
     import ctypes
     ctx = pool.ctx
+
+    def timed(g, st, sg):
+        pool.set_options(graphs=1, grid_mult=g, streams=st, staging=sg)
+        pool.step(2)
+        ctx.call("fl_ctx_timer_start")
+        pool.step(steps)
+        ms = ctypes.c_float()
+        ctx.call("fl_ctx_timer_stop", ctypes.byref(ms))
+        return ms.value
+
     best, best_ms = None, None
     for st in streams:
         for g in candidates:
-            pool.set_options(graphs=1, grid_mult=g, streams=st)
-            pool.step(2)
-            ctx.call("fl_ctx_timer_start")
-            pool.step(steps)
-            ms = ctypes.c_float()
-            ctx.call("fl_ctx_timer_stop", ctypes.byref(ms))
-            if best_ms is None or ms.value < best_ms:
-                best, best_ms = (g, st), ms.value
-    pool.set_options(graphs=1, grid_mult=best[0], streams=best[1])
+            ms = timed(g, st, 0)
+            if best_ms is None or ms < best_ms:
+                best, best_ms = (g, st, 0), ms
+    for sg in staging:
+        if sg == 0:
+            continue
+        ms = timed(best[0], best[1], sg)
+        if ms < best_ms:
+            best, best_ms = (best[0], best[1], sg), ms
+    pool.set_options(graphs=1, grid_mult=best[0], streams=best[1], staging=best[2])
     return best
 
 
@@ -72,10 +87,10 @@ def benchmark(ctx, cases, steps=500, regrid_every=20, check=-1):
     """The batched pool against the same cases one at a time (both with the autotuned options);
     returns throughput, speed-up and the cases whose batched populations differ from their solo run."""
     pool = Pool(ctx, cases)
-    tuned, tuned_streams = autotune(pool)
+    tuned, tuned_streams, tuned_staging = autotune(pool)
     pool.close()
     pool = Pool(ctx, cases)
-    pool.set_options(graphs=1, grid_mult=tuned, streams=tuned_streams)
+    pool.set_options(graphs=1, grid_mult=tuned, streams=tuned_streams, staging=tuned_staging)
     ctx.sync()
     t0 = time.perf_counter()
     lups_b = run(pool, steps, regrid_every)
@@ -91,7 +106,7 @@ def benchmark(ctx, cases, steps=500, regrid_every=20, check=-1):
     mismatched = []
     for i, c in enumerate(cases):
         p = Pool(ctx, [c])
-        p.set_options(graphs=1, grid_mult=tuned, streams=tuned_streams)
+        p.set_options(graphs=1, grid_mult=tuned, streams=tuned_streams, staging=tuned_staging)
         ctx.sync()
         t0 = time.perf_counter()
         lups_p += run(p, steps, regrid_every)
@@ -106,7 +121,7 @@ def benchmark(ctx, cases, steps=500, regrid_every=20, check=-1):
             "batched_mlups": round(lups_b / tb / 1e6, 1), "plain_mlups": round(lups_p / tp / 1e6, 1),
             "speedup": round((lups_b / tb) / (lups_p / tp), 3), "batched_s": round(tb, 3), "plain_s": round(tp, 3),
             "lups_batched": int(lups_b), "lups_plain": int(lups_p), "autotuned_ctas_per_sm": tuned,
-            "autotuned_class_streams": tuned_streams, "cases_checked": nchk, "cases_mismatched": mismatched}
+            "autotuned_class_streams": tuned_streams, "autotuned_staging": tuned_staging, "cases_checked": nchk, "cases_mismatched": mismatched}
 
 
 def main(argv=None):
