@@ -484,9 +484,17 @@ def run_gpu(args):
     vel = np.ctypeslib.as_array(ctypes.cast(vp, ctypes.POINTER(ctypes.c_float)), shape=(2, 3))
     vel[:] = 0.0
     vel[1, 0] = 0.04
-    cons = np.empty((1, 4), np.float64)
+    # each step's conservation sums (mass, momentum; FP64) land in pinned host memory, one row per
+    # step, copied asynchronously so the steps stay queued back to back
+    cp = ctypes.c_void_p()
+    ctx.call("fl_host_alloc_pinned", ctypes.c_size_t(max(args.steps, 1) * 32), ctypes.byref(cp))
+    cons = np.ctypeslib.as_array(ctypes.cast(cp, ctypes.POINTER(ctypes.c_double)), shape=(max(args.steps, 1), 4))
+    cons[:] = np.nan
     e2e_lups = 0
-    pool.step(1)  # graph capture for the uploaded state happens in the loop below
+    # the steps after an upload replay graphs that also rewrite the all-solid bricks, the
+    # steps after those the plain ones: capture all four (two level-0 parities each) first
+    ctx.call("fl_pool_upload", pool.h, hp)
+    pool.step(4)
     ctx.sync()
     rep.barrier()
     t0 = time.perf_counter()
@@ -498,7 +506,8 @@ def run_gpu(args):
         ctx.call("fl_pool_set_velocities", pool.h, vp, ctypes.c_void_p(vp.value + 12))
         e2e_lups += inf.fluid_lups_per_step
         pool.step(1)
-        ctx.call("fl_pool_conservation", pool.h, cons.ctypes.data_as(ctypes.c_void_p))
+        ctx.call("fl_pool_conservation_async", pool.h, ctypes.c_void_p(cp.value + 32 * k))
+    ctx.sync()
     t_steps = time.perf_counter()
     ctx.call("fl_pool_download", pool.h, None, None, None, None, None, hp)
     e2e_ms = stop()
@@ -510,8 +519,12 @@ def run_gpu(args):
     e2e_value = rep.sum(float(e2e_lups)) / (e2e_ms * 1e-3) / 1e6
     h2d = (fbytes + args.steps * 24) / args.steps
     d2h = (fbytes + args.steps * 32) / args.steps
+    # every step's sums arrived and are physical (mass positive and finite)
+    if not (np.isfinite(cons[:args.steps]).all() and (cons[:args.steps, 0] > 0).all()):
+        raise RuntimeError("e2e: a step's conservation read is missing or not finite")
     ctx.call("fl_host_free_pinned", hp)
     ctx.call("fl_host_free_pinned", vp)
+    ctx.call("fl_host_free_pinned", cp)
     pool.close()
     full = None
     if rank == 0 and not args.no_full_run:

@@ -1593,6 +1593,11 @@ struct fl_pool {
     cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one level-0 step, per level-0 parity
     uint64_t graph_kernels[2] = {0, 0};             // kernel nodes of each
     bool graph_ok[2] = {false, false};              // graph[k] matches the current pool
+    // the same with every level's all-solid bricks written in every sub-step, replayed
+    // while some level still owes such writes (after its populations were replaced)
+    cudaGraphExec_t graph_solid[2] = {nullptr, nullptr};
+    uint64_t graph_solid_kernels[2] = {0, 0};
+    bool graph_solid_ok[2] = {false, false};
     uint64_t version = 0;                           // bumped whenever the emitted launches change
     void* adapt_scratch = nullptr;
     size_t adapt_scratch_bytes = 0;
@@ -1741,10 +1746,15 @@ int alloc_brick_arrays_beside(fl_ctx* ctx, fl_pool* P, size_t cap, BrickArrays* 
 // (cudaGraphExecUpdate) instead of instantiating anew.  Every change of the
 // bricks or populations passes here, so it also makes each level write its
 // all-solid bricks for its next two sub-steps (both buffers).
-void drop_graph(fl_pool* P) {
+void populations_replaced(fl_pool* P) {
     ++P->version;
-    P->graph_ok[0] = P->graph_ok[1] = false;
     for (int l = 0; l < kMaxPoolLevels; ++l) P->solid_due[l] = 2;
+}
+
+void drop_graph(fl_pool* P) {
+    populations_replaced(P);
+    P->graph_ok[0] = P->graph_ok[1] = false;
+    P->graph_solid_ok[0] = P->graph_solid_ok[1] = false;
 }
 
 void free_graphs(fl_pool* P) {
@@ -1752,6 +1762,9 @@ void free_graphs(fl_pool* P) {
         if (P->graph[k]) cudaGraphExecDestroy(P->graph[k]);
         P->graph[k] = nullptr;
         P->graph_ok[k] = false;
+        if (P->graph_solid[k]) cudaGraphExecDestroy(P->graph_solid[k]);
+        P->graph_solid[k] = nullptr;
+        P->graph_solid_ok[k] = false;
     }
 }
 
@@ -2435,49 +2448,62 @@ int fl_pool_step(fl_ctx* ctx, fl_pool* P, int nsteps) {
     FL_TRY_CUDA(ctx, cudaStreamIsCapturing(ctx->stream, &capturing), "capture status");
     P->emit_solid = capturing != cudaStreamCaptureStatusNone;
     for (int i = 0; i < nsteps; ++i) {
-        // inside a caller's stream capture the launches join that capture
-        // directly; the steps that still write all-solid bricks run uncaptured
-        bool settled = true;
-        for (int l = 0; l <= P->maxL; ++l) settled = settled && P->solid_due[l] == 0;
-        if (!P->graphs || capturing != cudaStreamCaptureStatusNone || !settled) {
+        // inside a caller's stream capture the launches join that capture directly
+        if (!P->graphs || capturing != cudaStreamCaptureStatusNone) {
             level0_step(ctx, P);
             FL_CHECK_ERRORS(ctx, "k_collide_stream");
             continue;
         }
         // One level-0 step changes only level 0's parity (level l >= 1 runs an
         // even number of sub-steps), so two captured graphs, one per level-0
-        // parity, replay every step until the topology changes.
-        int p0 = P->parity[0];
-        if (!P->graph_ok[p0]) {
+        // parity, replay every step until the topology changes.  While some
+        // level still owes all-solid writes (both buffers must hold the rest
+        // state), a second pair, captured with those bricks written in every
+        // sub-step, replays instead: writing the rest state once more changes
+        // nothing, so the populations are those of the uncaptured steps.
+        bool settled = true;
+        for (int l = 0; l <= P->maxL; ++l) settled = settled && P->solid_due[l] == 0;
+        const int p0 = P->parity[0];
+        cudaGraphExec_t* exec = settled ? &P->graph[p0] : &P->graph_solid[p0];
+        bool* ok = settled ? &P->graph_ok[p0] : &P->graph_solid_ok[p0];
+        uint64_t* kernels = settled ? &P->graph_kernels[p0] : &P->graph_solid_kernels[p0];
+        if (!*ok) {
             int saved[16];
             std::memcpy(saved, P->parity, sizeof(saved));
+            int saved_due[kMaxPoolLevels];
+            std::memcpy(saved_due, P->solid_due, sizeof(saved_due));
             cudaGraph_t g;
             const uint64_t c0 = ctx->launches;
+            P->emit_solid = !settled;
             FL_TRY_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "capture begin");
             level0_step(ctx, P);
             cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
-            P->graph_kernels[p0] = ctx->launches - c0;  // recorded, not launched: counted per replay
+            P->emit_solid = false;
+            *kernels = ctx->launches - c0;  // recorded, not launched: counted per replay
             ctx->launches = c0;
             std::memcpy(P->parity, saved, sizeof(saved));
+            std::memcpy(P->solid_due, saved_due, sizeof(saved_due));
             FL_TRY_CUDA(ctx, e, "capture end");
             bool updated = false;
-            if (P->graph[p0]) {
+            if (*exec) {
                 cudaGraphExecUpdateResultInfo info;
-                updated = cudaGraphExecUpdate(P->graph[p0], g, &info) == cudaSuccess;
+                updated = cudaGraphExecUpdate(*exec, g, &info) == cudaSuccess;
                 if (!updated) {
                     cudaGetLastError();  // a failed update leaves no sticky error; clear the last one
-                    cudaGraphExecDestroy(P->graph[p0]);
-                    P->graph[p0] = nullptr;
+                    cudaGraphExecDestroy(*exec);
+                    *exec = nullptr;
                 }
             }
-            if (!updated) e = cudaGraphInstantiate(&P->graph[p0], g, 0);
+            if (!updated) e = cudaGraphInstantiate(exec, g, 0);
             cudaGraphDestroy(g);
             FL_TRY_CUDA(ctx, e, "graph instantiate");
-            P->graph_ok[p0] = true;
+            *ok = true;
         }
-        FL_TRY_CUDA(ctx, cudaGraphLaunch(P->graph[p0], ctx->stream), "graph launch");
-        ctx->launches += P->graph_kernels[p0];
+        FL_TRY_CUDA(ctx, cudaGraphLaunch(*exec, ctx->stream), "graph launch");
+        ctx->launches += *kernels;
         P->parity[0] ^= 1;
+        if (!settled)  // level l ran 2^l sub-steps, each of which pays one owed write
+            for (int l = 0; l <= P->maxL; ++l) P->solid_due[l] = std::max(0, P->solid_due[l] - (1 << l));
     }
     return FL_OK;
 }
@@ -2567,6 +2593,13 @@ int fl_pool_flags(fl_ctx* ctx, fl_pool* P, int32_t* flags, float* wmax) {
 }
 
 int fl_pool_conservation(fl_ctx* ctx, fl_pool* P, double* out) {
+    int rc = fl_pool_conservation_async(ctx, P, out);
+    if (rc) return rc;
+    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "conservation");
+    return fl_collect_device_status(ctx, "fl_pool_conservation");
+}
+
+int fl_pool_conservation_async(fl_ctx* ctx, fl_pool* P, double* out) {
     if (!ctx || !P || !out) return FL_E_INVALID_ARG;
     FL_POOL_USABLE(ctx, P);
     size_t n = P->mesh.num_cells;
@@ -2580,9 +2613,8 @@ int fl_pool_conservation(fl_ctx* ctx, fl_pool* P, double* out) {
     }
     k_case_sums<<<(nc * 4 + 255) / 256, 256, 0, ctx->stream>>>(P->chunk_part, P->d_case_chunk, nc, P->cons);
     FL_CHECK_LAUNCH(ctx, "k_case_sums");
-    FL_TRY_CUDA(ctx, cudaMemcpyAsync(out, P->cons, nc * 32, cudaMemcpyDeviceToHost, ctx->stream), "conservation");
-    FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "conservation");
-    return fl_collect_device_status(ctx, "fl_pool_conservation");
+    FL_TRY_CUDA(ctx, cudaMemcpyAsync(out, P->cons, nc * 32, cudaMemcpyDefault, ctx->stream), "conservation");
+    return FL_OK;
 }
 
 // Per-launch timing pass shared by the two profile entry points: totals per
@@ -2603,8 +2635,7 @@ int profile_levels(fl_ctx* ctx, fl_pool* P, int nsteps, double* ms, uint32_t* cn
         cudaEventDestroy(tm.ev[k]);
         cudaEventDestroy(tm.ev[k + 1]);
     }
-    drop_graph(P);
-    return FL_OK;
+    return FL_OK;  // the topology and buffers are unchanged: the captured steps stay valid
 }
 
 int fl_pool_profile_steps(fl_ctx* ctx, fl_pool* P, int nsteps, double* kernel_ms, uint32_t* launches,
@@ -2644,8 +2675,10 @@ int fl_pool_upload(fl_ctx* ctx, fl_pool* P, const float* f) {
     for (int q = 0; q < Q; ++q)
         FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->f[0] + (size_t)q * P->cap * 512, f + (size_t)q * n * 512, n * 512 * 4,
                                          cudaMemcpyHostToDevice, ctx->stream), "upload");
+    // level l >= 1 is back to parity 0 at every level-0 step boundary, so the captured
+    // steps stay valid; only the all-solid bricks must be written again
     for (int l = 0; l < 16; ++l) P->parity[l] = 0;
-    drop_graph(P);
+    populations_replaced(P);
     return FL_OK;
 }
 

@@ -344,6 +344,11 @@ int fl_pool_nbr(fl_ctx* ctx, fl_pool* pool, uint32_t* nbr);
 int fl_pool_flags(fl_ctx* ctx, fl_pool* pool, int32_t* flags, float* wmax);
 /* Per case: fluid mass and momentum (FP64, sites weighted by 8^-level) -> out[ncases][4] (host). */
 int fl_pool_conservation(fl_ctx* ctx, fl_pool* pool, double* out);
+/* The same sums enqueued on the context stream without waiting: out (ncases x 4 doubles, pinned
+ * host memory or device memory for the call not to block) holds them once the stream has reached
+ * this point (fl_ctx_synchronize, or any later call that synchronises).  Device-side status is
+ * collected by the next call that synchronises. */
+int fl_pool_conservation_async(fl_ctx* ctx, fl_pool* pool, double* out);
 /* Advance nsteps with a CUDA event pair around every collide-stream launch (no graphs); returns,
  * per kernel ([0] interior bricks, [1] interface/boundary/near-sphere bricks, [2] all-solid bricks),
  * the summed kernel time, the launch count and the fluid sites those launches updated (each output

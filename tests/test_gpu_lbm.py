@@ -101,6 +101,52 @@ def test_bulk_staged_kernels_match_register_kernels(ctx, staging, graphs):
     np.testing.assert_array_equal(a.populations(), b.populations())
 
 
+def test_graphs_after_upload_match_direct_launches(ctx):
+    """After an upload the captured steps stay valid: the first steps replay graphs that also
+    rewrite the all-solid bricks (the uploaded state is perturbed everywhere, inside the sphere
+    too), then the plain ones, and every step equals uncaptured launches bit for bit."""
+    from fluidloom_gb300.lbm import Pool
+    c = cases_small()[1]
+    a, b = Pool(ctx, [c]), Pool(ctx, [c])
+    a.set_options(graphs=1)
+    b.set_options(graphs=0)
+    a.step(3)
+    b.step(3)
+    f = a.populations()
+    f = (f * (1.0 + 1e-3 * np.random.default_rng(7).standard_normal(f.shape))).astype(np.float32)
+    for rnd in range(2):
+        a.upload(f)
+        b.upload(f)
+        for k in range(5):
+            a.step(1)
+            b.step(1)
+            np.testing.assert_array_equal(a.populations(), b.populations())
+
+
+def test_conservation_async_equals_sync(ctx):
+    """fl_pool_conservation_async queues the sums and their copy into pinned host memory
+    without waiting; after a synchronise they equal the synchronous call's, step by step."""
+    import ctypes
+    from fluidloom_gb300.lbm import Pool
+    p = Pool(ctx, [cases_small()[1]])
+    cp = ctypes.c_void_p()
+    ctx.call("fl_host_alloc_pinned", ctypes.c_size_t(3 * 32), ctypes.byref(cp))
+    got = np.ctypeslib.as_array(ctypes.cast(cp, ctypes.POINTER(ctypes.c_double)), shape=(3, 4))
+    got[:] = np.nan
+    want = []
+    q = Pool(ctx, [cases_small()[1]])
+    for k in range(3):
+        p.step(1)
+        ctx.call("fl_pool_conservation_async", p.h, ctypes.c_void_p(cp.value + 32 * k))
+        q.step(1)
+        want.append(q.conservation()[0])
+    ctx.sync()
+    np.testing.assert_array_equal(got, np.array(want))
+    ctx.call("fl_host_free_pinned", cp)
+    p.close()
+    q.close()
+
+
 def test_batch_equals_solo(ctx):
     """Two cases in one pool reproduce their solo runs bit for bit."""
     from fluidloom_gb300.lbm import Pool
