@@ -358,6 +358,50 @@ def full_run(ctx, steps=1000):
             "mlups": round(lups / dt / 1e6, 1), "peak_fluid_sites": peak_sites, "mesh": trace}
 
 
+def config1_run(ctx, cpu=True):
+    """Configuration 1 as it is specified: the lid-driven cavity, 32^3 sites, max level 2,
+    lid 0.05 in +x on the top z face, tau 0.56, 200 steps with a vorticity regrid every 20, from
+    a fresh pool.  GPU: wall time from the first step to the last (synchronised), regrids
+    included, and each regrid's CUDA-event time; CPU: the oracle (OpenMP over all host
+    threads) on the same 200 steps and regrids."""
+    from fluidloom_gb300.lbm import Pool, cavity
+    case = cavity(32, 2, u_lid=0.05, tau=0.56)
+    pool = Pool(ctx, [case])
+    ctx.sync()
+    lups, regrid_ms = 0, []
+    t0 = time.perf_counter()
+    for s in range(1, 201):
+        lups += pool.info().fluid_lups_per_step
+        pool.step(1)
+        if s % 20 == 0:
+            stop = timer(ctx)
+            pool.regrid()
+            regrid_ms.append(stop())
+    ctx.sync()
+    dt = time.perf_counter() - t0
+    inf = pool.info()
+    out = {"workload": "lid-driven cavity 32^3, max level 2, lid 0.05, tau 0.56, 200 steps, regrid every 20",
+           "gpu_mlups": round(lups / dt / 1e6, 1), "gpu_wall_s": round(dt, 4),
+           "regrid_ms_per_cycle_median": round(float(np.median(regrid_ms)), 3),
+           "regrid_ms_per_cycle_max": round(float(max(regrid_ms)), 3), "fluid_lups": int(lups),
+           "final_bricks_per_level": [int(inf.bricks_per_level[l]) for l in range(3)]}
+    pool.close()
+    if cpu:
+        from tests import _oracle as O
+        threads = os.cpu_count() or 1
+        op = O.OraclePool([case])
+        cl = 0
+        t0 = time.perf_counter()
+        for s in range(1, 201):
+            cl += op.lups()
+            op.step(1, threads)
+            if s % 20 == 0:
+                op.regrid()
+        out["cpu_mlups"] = round(cl / (time.perf_counter() - t0) / 1e6, 2)
+        out["cpu"] = "oracle port, %d host threads, the same 200 steps and regrids" % threads
+    return out
+
+
 def cpu_sample(steps, threads=None):
     """The oracle (CPU port) on the workload itself (128x64x64 base, 3 levels, r=8): `steps` level-0 steps."""
     from tests import _oracle as O
@@ -529,6 +573,9 @@ def run_gpu(args):
     full = None
     if rank == 0 and not args.no_full_run:
         full = full_run(ctx)
+    cfg1 = None
+    if rank == 0 and not args.no_config1:
+        cfg1 = config1_run(ctx, cpu=not args.no_cpu)
     micro = None
     if rank == 0 and not args.no_microbench:
         micro = regrid_microbench(ctx)
@@ -569,7 +616,7 @@ def run_gpu(args):
                         "d2h_bytes_per_step": int(d2h), "phases_wall": e2e_phases},
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
                 "regrid_ms_per_cycle": round(statistics.mean(regrid_ms), 3), "regrids_in_timed_region": regrids,
-                "config2_full_run": full, "regrid_microbench": micro, "batching": batch, "serving": serve,
+                "config1_cavity": cfg1, "config2_full_run": full, "regrid_microbench": micro, "batching": batch, "serving": serve,
                 "fp32_vs_fp64": fp64}
         print(json.dumps(line))
     rep.close()
@@ -633,6 +680,7 @@ def main():
                     help="untimed level-0 steps (with regrids) before the warm-up; default: so that the timed "
                          "steps end at step 1000, the end of the configuration's run, where its mesh peaks")
     ap.add_argument("--no-full-run", action="store_true")
+    ap.add_argument("--no-config1", action="store_true", help="skip the 32^3 cavity run of configuration 1")
     ap.add_argument("--scale", type=int, default=1, choices=[1, 2],
                     help="2 runs the sphere at half resolution per axis (profiling captures only; the "
                          "reported workload is scale 1)")
