@@ -182,8 +182,11 @@ def regrid_microbench(ctx, L=8):
     mb = microbench_mesh(L)
     m = Mesh(ctx, mb["start"], capacity=1 << (3 * L))
     out = {}
+    st = None
     for r, (blobs, lo, hi, ml) in enumerate(mb["rounds"]):
-        cfg = AdaptConfig.make(max_level=ml, min_level=0, balance_mode=1)
+        # round 2's input is round 1's output: stated balanced when round 1's balance converged
+        cfg = AdaptConfig.make(max_level=ml, min_level=0, balance_mode=1,
+                               input_balanced=st is not None and st.balance.converged == 1)
         leaves_in = m.n
         stop = timer(ctx)
         ctx.call("fl_flags_from_blobs", ctypes.byref(m.m), blobs.ctypes.data_as(ctypes.c_void_p), len(blobs),

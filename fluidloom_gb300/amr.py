@@ -21,11 +21,12 @@ class AdaptConfig(ctypes.Structure):
                 ("max_balance_iterations", ctypes.c_uint32), ("enforce_2_1_balance", ctypes.c_int32),
                 ("balance_mode", ctypes.c_int32), ("averaging_rule", ctypes.c_int32),
                 ("buffer_growth_factor", ctypes.c_double), ("key_depth", ctypes.c_int32),
-                ("anchor_level", ctypes.c_int32), ("ext", ctypes.c_int32 * 3), ("periodic", ctypes.c_int32 * 3)]
+                ("anchor_level", ctypes.c_int32), ("ext", ctypes.c_int32 * 3), ("periodic", ctypes.c_int32 * 3),
+                ("input_balanced", ctypes.c_int32)]
 
     @classmethod
     def make(cls, max_level=8, min_level=0, balance_mode=0, enforce=True, iters=10, rule=0, depth=21, anchor=None,
-             ext=(1, 1, 1), periodic=(0, 0, 0), growth=1.5):
+             ext=(1, 1, 1), periodic=(0, 0, 0), growth=1.5, input_balanced=False):
         if anchor is None:  # deepest anchor level with ext << anchor inside the depth-bit key space
             e = max(ext)
             anchor = depth - (int(e - 1).bit_length() if e > 1 else 0)
@@ -41,6 +42,7 @@ class AdaptConfig(ctypes.Structure):
         c.anchor_level = anchor
         c.ext[:] = list(ext)
         c.periodic[:] = list(periodic)
+        c.input_balanced = int(input_balanced)
         return c
 
 

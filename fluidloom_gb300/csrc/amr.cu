@@ -71,14 +71,16 @@ __device__ __forceinline__ uint8_t shadow_of(const fl_mesh_dev& m, size_t i, int
     return (uint8_t)(m.level[i] + (up ? 1 : 0));
 }
 
-// Shadow levels; lowest[0] / lowest[1] (when given) receive their minimum and maximum.
+// Shadow levels; lowest[0] / lowest[1] (when given) receive their minimum and
+// maximum; refining (when given) a byte per leaf, set where the leaf will split.
 __global__ void k_shadow(fl_mesh_dev m, int mode, int max_level, uint8_t* __restrict__ shadow,
-                         uint32_t* __restrict__ lowest) {
+                         uint32_t* __restrict__ lowest, uint8_t* __restrict__ refining) {
     size_t stride = (size_t)gridDim.x * blockDim.x;
     unsigned lo = 255u, hi = 0u;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
         const uint8_t v = mode == 0 ? m.level[i] : shadow_of(m, i, mode, max_level);
         shadow[i] = v;
+        if (refining) refining[i] = v > m.level[i] ? 1 : 0;
         lo = min(lo, (unsigned)v);
         hi = max(hi, (unsigned)v);
     }
@@ -696,9 +698,15 @@ size_t fl_adapt_scratch_bytes(size_t n, uint64_t cap) {
 // nullptr to probe from every leaf each round) holds one byte per leaf, set
 // for the next round's probing leaves, then at offset fl_align256(n) the list
 // they are gathered into before that round.
+// balanced_input: the caller states that no two touching leaves differ by more
+// than one level.  A violation needs shadow[i] >= shadow[r] + 2 with shadow[i]
+// <= level[i] + 1 and shadow[r] >= level[r] >= level[i] - 1, so in the first
+// round only a leaf that will split can find one: only those probe (through the
+// list, like the later rounds).
 int fl_balance_run(fl_ctx* ctx, fl_mesh_dev md, int32_t* flags, const fl_domain_dev& dom, const uint64_t* tk,
                    const uint32_t* tv, uint64_t cap, const fl_locator* L, int mode, int max_level, int max_iters,
-                   uint8_t* shadow, uint8_t* viol, uint8_t* act, uint32_t* counters, fl_balance_result* res) {
+                   uint8_t* shadow, uint8_t* viol, uint8_t* act, uint32_t* counters, fl_balance_result* res,
+                   bool balanced_input) {
     fl_balance_result r{};
     if (md.n == 0) { r.converged = 1; if (res) *res = r; return FL_OK; }
     unsigned nb = fl_blocks(md.n, kT, ctx->num_sms * 8);
@@ -706,7 +714,9 @@ int fl_balance_run(fl_ctx* ctx, fl_mesh_dev md, int32_t* flags, const fl_domain_
     uint32_t* lowest = counters + 2;  // lowest and highest shadow level, for FULL26's early outs
     const uint32_t extremes[2] = {0xFFFFFFFFu, 0u};
     FL_TRY_CUDA(ctx, cudaMemcpyAsync(lowest, extremes, 8, cudaMemcpyHostToDevice, ctx->stream), "balance extremes");
-    k_shadow<<<nb, kT, 0, ctx->stream>>>(md, mode, max_level, shadow, lowest);
+    // a balanced input: the first round probes only from the leaves that will split
+    const bool first_listed = act && mode == 1 && balanced_input;
+    k_shadow<<<nb, kT, 0, ctx->stream>>>(md, mode, max_level, shadow, lowest, first_listed ? act : nullptr);
     FL_CHECK_LAUNCH(ctx, "k_shadow");
     int cap_it = mode == 0 ? max_iters : 4096;
     uint32_t it = 0;
@@ -715,14 +725,15 @@ int fl_balance_run(fl_ctx* ctx, fl_mesh_dev md, int32_t* flags, const fl_domain_
         FL_TRY_CUDA(ctx, cudaMemsetAsync(counters, 0, 8, ctx->stream), "balance counters");
         // this round's probing leaves (all of them in the first round) and the next round's
         uint8_t* nxt = (act && mode == 1) ? act : nullptr;
-        uint32_t* list = (act && mode == 1 && it > 0) ? (uint32_t*)(act + fl_align256(md.n)) : nullptr;
+        uint32_t* list = (act && mode == 1 && (it > 0 || first_listed)) ? (uint32_t*)(act + fl_align256(md.n)) : nullptr;
         uint32_t* list_n = counters + 4;  // free until the merge grouping after balance
         if (mode == 0) {
             k_detect_face6<<<nb, kT, 0, ctx->stream>>>(md, dom, tk, tv, lg, shadow, viol, counters);
         } else {
             k_clear_u8<<<nb, kT, 0, ctx->stream>>>(viol, md.n);
             if (list) {
-                // this round's probing leaves: those flagged in the last round (the flags are cleared)
+                // this round's probing leaves: those flagged in the last round, or (first round of a
+                // balanced input) those that will split; the flags are cleared
                 FL_TRY_CUDA(ctx, cudaMemsetAsync(list_n, 0, 4, ctx->stream), "balance list");
                 k_compact_active<<<nb, kT, 0, ctx->stream>>>(nxt, md.n, list, list_n);
             } else if (nxt) {
@@ -823,7 +834,7 @@ int fl_adapt_prepare(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cf
     if (run_balance) {
         rc = fl_balance_run(ctx, md, mesh->flags, dom, w.tk, w.tv, w.cap, &L, cfg->balance_mode,
                             cfg->max_refinement_level, (int)cfg->max_balance_iterations, w.shadow, w.viol, w.act,
-                            w.counters + 8, &s.balance);
+                            w.counters + 8, &s.balance, cfg->input_balanced != 0);
         if (rc) return rc;
     }
     unsigned nb = fl_blocks(n, kT, ctx->num_sms * 8);
@@ -951,7 +962,7 @@ int fl_balance_enforce(fl_ctx* ctx, fl_mesh* mesh, const fl_adapt_config* cfg, f
     if (rc) return rc;
     fl_balance_result r;
     rc = fl_balance_run(ctx, md, mesh->flags, dom, tk, tv, cap, &L, cfg->balance_mode, cfg->max_refinement_level,
-                        (int)cfg->max_balance_iterations, shadow, viol, act, counters, &r);
+                        (int)cfg->max_balance_iterations, shadow, viol, act, counters, &r, cfg->input_balanced != 0);
     if (rc) return rc;
     rc = fl_collect_device_status(ctx, "fl_balance_enforce");
     if (rc) return rc;

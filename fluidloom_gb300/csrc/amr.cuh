@@ -14,7 +14,8 @@ size_t fl_adapt_scratch_bytes(size_t n, uint64_t cap);
 // through the sorted locator L.
 int fl_balance_run(fl_ctx* ctx, fl_mesh_dev md, int32_t* flags, const fl_domain_dev& dom, const uint64_t* tk,
                    const uint32_t* tv, uint64_t cap, const fl_locator* L, int mode, int max_level, int max_iters,
-                   uint8_t* shadow, uint8_t* viol, uint8_t* act, uint32_t* counters, fl_balance_result* res);
+                   uint8_t* shadow, uint8_t* viol, uint8_t* act, uint32_t* counters, fl_balance_result* res,
+                   bool balanced_input = false);
 // level_bound >= 0: no cell of the mesh is deeper (the point locator then skips a host read).
 int fl_adapt_prepare(fl_ctx* ctx, const fl_mesh* mesh, const fl_adapt_config* cfg, const fl_domain_dev& dom,
                      bool run_balance, void* scratch, size_t* M_out, fl_adapt_stats* st, int level_bound = -1);

@@ -1602,6 +1602,9 @@ struct fl_pool {
     void* adapt_scratch = nullptr;
     size_t adapt_scratch_bytes = 0;
     int grid_mult = 4;
+    // the bricks are the output of an adapt whose FULL26 balance converged (no two
+    // touching bricks more than one level apart): the next regrid's adapt may say so
+    bool mesh_balanced = false;
     // 0: collide kernels load straight into registers; 1: the brick's own
     // population planes bulk-copied into shared memory one brick ahead
     // (k_collide_staged); 2: as 1, with the general bricks' quad masks and
@@ -1981,6 +1984,8 @@ int pool_regrid(fl_ctx* ctx, fl_pool* P, int use_vorticity, fl_adapt_stats* st, 
     cfg.enforce_2_1_balance = 1;
     cfg.balance_mode = 1;
     cfg.averaging_rule = 0;
+    cfg.input_balanced = P->mesh_balanced ? 1 : 0;
+    P->mesh_balanced = false;  // until this regrid has succeeded
     fl_domain_dev dom = pool_domain(P);
     size_t sb = fl_adapt_scratch_bytes(n, fl_table_capacity(n));
     if (sb > P->adapt_scratch_bytes) {
@@ -2001,6 +2006,7 @@ int pool_regrid(fl_ctx* ctx, fl_pool* P, int use_vorticity, fl_adapt_stats* st, 
     // cases were appended (use_vorticity < 0) must still reorder.
     if (use_vorticity >= 0 && s.num_split == 0 && s.num_groups == 0) {
         FL_TRY_CUDA(ctx, cudaMemsetAsync(P->mesh.flags, 0, n * 4, ctx->stream), "flags reset");
+        P->mesh_balanced = s.balance.converged != 0;
         if (st) *st = s;
         return FL_OK;
     }
@@ -2069,6 +2075,7 @@ int pool_regrid(fl_ctx* ctx, fl_pool* P, int use_vorticity, fl_adapt_stats* st, 
     }
     for (int l = 0; l < 16; ++l) P->parity[l] = 0;
     rc = pool_topology(ctx, P);
+    if (rc == FL_OK) P->mesh_balanced = s.balance.converged != 0;
     if (st) *st = s;
     return rc;
 }
@@ -2729,6 +2736,7 @@ int fl_pool_load(fl_ctx* ctx, fl_pool* P, size_t n, const int32_t* x, const int3
     FL_TRY_CUDA(ctx, cudaMemsetAsync(P->mesh.flags, 0, n * 4, ctx->stream), "load");
     FL_TRY_CUDA(ctx, cudaMemsetAsync(P->mesh.material, 0, n * 4, ctx->stream), "load");
     P->mesh.num_cells = n;
+    P->mesh_balanced = false;  // bricks from outside
     for (int q = 0; q < Q; ++q)
         FL_TRY_CUDA(ctx, cudaMemcpyAsync(P->f[0] + (size_t)q * P->cap * 512, f + (size_t)q * n * 512, n * 512 * 4,
                                          cudaMemcpyHostToDevice, ctx->stream), "load populations");
@@ -2889,6 +2897,7 @@ int fl_pool_add_cases(fl_ctx* ctx, fl_pool* P, const fl_lbm_case* cases, int nca
     }
     fl_pool_destroy(ctx, T);
     P->mesh.num_cells = n + nt;
+    P->mesh_balanced = false;  // new cases' bricks
     // one regrid with every flag 0 only re-sorts by (case, key) and rebuilds the topology
     rc = pool_regrid(ctx, P, -1, nullptr);
     if (rc) return rc;

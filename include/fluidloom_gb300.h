@@ -175,6 +175,12 @@ typedef struct fl_adapt_config {
     int32_t anchor_level;           /* 0 -> 21: anchor = native << (anchor_level - level) */
     int32_t ext[3];                 /* level-0 extent in cells (0 -> 1) */
     int32_t periodic[3];
+    int32_t input_balanced;         /* no reference counterpart; 1: the caller states that no two touching
+                                       leaves of the input differ by more than one level (faces, edges,
+                                       corners), as after an adapt whose FULL26 balance converged.  The
+                                       first FULL26 round then probes only from the leaves that will split,
+                                       the only ones that can find a violation in such a mesh; results
+                                       equal those with 0 (every leaf probes) whenever the statement holds */
 } fl_adapt_config;
 
 /* BalanceResult (AdaptationTypes.h:94-109). */

@@ -82,6 +82,7 @@ struct AdaptationConfig {
     int anchor_level = 21;
     int32_t ext[3] = {1, 1, 1};
     int32_t periodic[3] = {0, 0, 0};
+    bool input_balanced = false;  // the input has no FULL26 violation (fl_adapt_config.input_balanced)
 
     void validate() const {
         if (max_refinement_level > 21) throw std::invalid_argument("max_refinement_level cannot exceed 21");
@@ -100,6 +101,7 @@ struct AdaptationConfig {
         k.key_depth = key_depth;
         k.anchor_level = anchor_level;
         for (int a = 0; a < 3; ++a) { k.ext[a] = ext[a]; k.periodic[a] = periodic[a]; }
+        k.input_balanced = input_balanced ? 1 : 0;
         return k;
     }
 };

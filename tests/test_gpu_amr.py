@@ -94,6 +94,46 @@ def test_adapt_vs_oracle(ctx, seed, mode, shuffled):
     assert st.balance.total_cells_marked_for_balance == wst.balance.marked
 
 
+@pytest.mark.parametrize("seed,shuffled", [(21, False), (22, False), (23, True)])
+def test_input_balanced_hint_equals_full_probing(ctx, seed, shuffled):
+    """An adapt whose FULL26 balance converged leaves no two touching leaves more than one
+    level apart.  A second adapt of its output with input_balanced set (the first round
+    probes only from the leaves that will split) equals the same adapt without it -- leaves,
+    flags and every statistic -- and both equal the oracle."""
+    cols = O.random_octree(seed, ext=(2, 2, 1), rounds=4, max_level=6, frac=0.3, balanced=True)
+    rng = np.random.default_rng(seed)
+    cols["flags"] = rng.choice([-1, 0, 1], len(cols["x"]), p=[0.3, 0.4, 0.3]).astype(np.int32)
+    # a balanced start below the maximum level: every violator can split, the balance converges
+    rc, out, st, _ = run_adapt(ctx, cols, cfg(max_level=8, balance_mode=1, ext=(2, 2, 1)))
+    assert rc == 0 and st.balance.converged == 1
+    n = len(out["x"])
+    out["flags"] = rng.choice([-1, 0, 1], n, p=[0.45, 0.35, 0.2]).astype(np.int32)
+    if shuffled:
+        perm = rng.permutation(n)
+        out = {k: np.ascontiguousarray(v[perm]) for k, v in out.items()}
+    runs = []
+    for hint in (False, True):
+        rc, got, gst, _ = run_adapt(ctx, {k: v.copy() for k, v in out.items()},
+                                    cfg(max_level=8, balance_mode=1, ext=(2, 2, 1), input_balanced=hint))
+        assert rc == 0
+        runs.append((got, gst))
+    (a, sa), (b, sb) = runs
+    for k in ("x", "y", "z", "level", "state", "flags", "material"):
+        np.testing.assert_array_equal(b[k], a[k], err_msg=k)
+    assert (sb.num_split, sb.num_groups, sb.num_survivors) == (sa.num_split, sa.num_groups, sa.num_survivors)
+    assert (sb.balance.converged, sb.balance.iterations, sb.balance.total_violations_detected,
+            sb.balance.total_cells_marked_for_balance) == (sa.balance.converged, sa.balance.iterations,
+                                                           sa.balance.total_violations_detected,
+                                                           sa.balance.total_cells_marked_for_balance)
+    assert sa.balance.total_cells_marked_for_balance > 0  # the balance has work to do
+    kw = dict(max_level=8, min_level=0, balance_mode=1, max_balance_iterations=10, enforce_balance=1,
+              averaging_rule=0)
+    want, wst, *_ = O.adapt(out, kw, O.domain(ext=(2, 2, 1), max_level=8))
+    for k in ("x", "y", "z", "level", "state", "flags", "material"):
+        np.testing.assert_array_equal(b[k], want[k], err_msg=k)
+    assert sb.balance.total_cells_marked_for_balance == wst.balance.marked
+
+
 @pytest.mark.parametrize("mode,shuffled", [(0, False), (1, False), (1, True)])
 def test_balance_vs_oracle(ctx, mode, shuffled):
     from fluidloom_gb300.amr import BalanceResult

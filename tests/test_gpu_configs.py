@@ -106,9 +106,10 @@ def _adapt_gpu(ctx, m, cfg):
     return st
 
 
-def _gpu_two_rounds(ctx, L):
+def _gpu_two_rounds(ctx, L, hint=True):
     """The microbenchmark's octree on the GPU: round 1 from the uniform level-L mesh,
-    round 2 (the timed regrid of the benchmark) from its output."""
+    round 2 (the timed regrid of the benchmark) from its output -- stated balanced when
+    hint is set and round 1's balance converged, as the benchmark does."""
     from bench import microbench_mesh
     from fluidloom_gb300.amr import AdaptConfig, Mesh
     rounds = microbench_mesh(L)
@@ -117,13 +118,16 @@ def _gpu_two_rounds(ctx, L):
     for blobs, lo, hi, ml in rounds["rounds"]:
         ctx.call("fl_flags_from_blobs", ctypes.byref(m.m), blobs.ctypes.data_as(ctypes.c_void_p), len(blobs),
                  ctypes.c_float(lo), ctypes.c_float(hi), ml)
-        stats.append(_adapt_gpu(ctx, m, AdaptConfig.make(max_level=ml, min_level=0, balance_mode=1)))
+        balanced = hint and bool(stats) and stats[-1].balance.converged == 1
+        stats.append(_adapt_gpu(ctx, m, AdaptConfig.make(max_level=ml, min_level=0, balance_mode=1,
+                                                         input_balanced=balanced)))
     return m, stats, rounds
 
 
-def test_config3_microbench_octree_exact_at_2_18(ctx):
+@pytest.mark.parametrize("hint", [False, True])
+def test_config3_microbench_octree_exact_at_2_18(ctx, hint):
     L = 6
-    m, stats, rounds = _gpu_two_rounds(ctx, L)
+    m, stats, rounds = _gpu_two_rounds(ctx, L, hint)
     g = m.download()
     c = {k: v.copy() for k, v in rounds["start"].items()}
     dom = O.domain(max_level=L + 2)
