@@ -538,6 +538,8 @@ def run_gpu(args):
     cons = np.ctypeslib.as_array(ctypes.cast(cp, ctypes.POINTER(ctypes.c_double)), shape=(max(args.steps, 1), 4))
     cons[:] = np.nan
     e2e_lups = 0
+    # the caller reads the conservation sums every step: the steps write them as they go
+    ctx.call("fl_pool_set_step_sums", pool.h, 1)
     # the steps after an upload replay graphs that also rewrite the all-solid bricks, the
     # steps after those the plain ones: capture all four (two level-0 parities each) first
     ctx.call("fl_pool_upload", pool.h, hp)

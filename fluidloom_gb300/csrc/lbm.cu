@@ -126,6 +126,21 @@ __device__ __forceinline__ void moments(const float* f, float& rho, float& jx, f
     rho = r; jx = a; jy = b; jz = c;
 }
 
+// Double-single (hi, lo) FP32 pairs for the per-brick sums: Knuth's TwoSum
+// (exact rounding error of one addition; needs no FMA contraction) and the
+// pair addition with one renormalisation -- about 2^-44 relative per add.
+struct DS {
+    float hi, lo;
+};
+__device__ __forceinline__ DS ds_add(DS a, DS b) {
+    float s = a.hi + b.hi;
+    float bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (b.hi - bb);
+    e = e + (a.lo + b.lo);
+    float h = s + e;
+    return DS{h, e - (h - s)};
+}
+
 // Voxel of the case's solid mask under the centre of level-l site (sx, sy, sz):
 // a coarser site samples the voxel at its centre (the upper of the two middle
 // ones), a finer site the voxel that holds it; sites outside the case grid are
@@ -179,6 +194,8 @@ struct StepArgs {
     const uint32_t* smask;     // [n][16]: own sites inside the sphere
     const uint4* qmask;        // [n][128]: per x-quad descriptor bits (4q + i) and first descriptor
     const float* pv;           // descriptor values of this sub-step (k_interface)
+    float* part;               // non-null in each level's last sub-step of a level-0 step: the
+                               // bricks' conservation sums are written there (brick_sums_store)
 };
 
 __device__ __forceinline__ size_t fidx(size_t cap, int q, size_t b, int s) { return ((size_t)q * cap + b) * 512 + s; }
@@ -263,10 +280,48 @@ __device__ __forceinline__ void relax_site(float (&g)[Q], float omega, bool soli
     }
 }
 
+// The conservation sums of brick b from the values its 128 threads have just
+// stored (thread t: the x-quad of k_brick_sums' thread t; bit i of solid4 marks
+// site i of the quad solid), in k_brick_sums' arithmetic and order: each
+// thread's fluid sites' moments in double-single, a warp xor-reduction, and
+// per warp its (hi, lo) pairs of the four sums at part[((b * 4 + warp) * 4 + k)
+// * 2] -- FP32 work only; k_chunk_sums combines the warps in FP64.  So part[b]
+// holds what k_brick_sums would compute from the stored state.
+__device__ __forceinline__ void brick_sums_store(const float (&f)[Q][4], uint32_t solid4, size_t b,
+                                                 float* __restrict__ part) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    DS acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        if ((solid4 >> i) & 1u) continue;
+        float g[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) g[q] = f[q][i];
+        float m[4];
+        moments(g, m[0], m[1], m[2], m[3]);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc[k] = ds_add(acc[k], DS{m[k], 0.f});
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            DS other{__shfl_xor_sync(0xFFFFFFFFu, acc[k].hi, o), __shfl_xor_sync(0xFFFFFFFFu, acc[k].lo, o)};
+            acc[k] = ds_add(acc[k], other);
+        }
+    }
+    if (lane == 0) {
+        float4* w = (float4*)(part + (b * 4 + wid) * 8);
+        w[0] = make_float4(acc[0].hi, acc[0].lo, acc[1].hi, acc[1].lo);
+        w[1] = make_float4(acc[2].hi, acc[2].lo, acc[3].hi, acc[3].lo);
+    }
+}
+
 // Interior bricks: all 18 face/edge neighbours at this level, no sphere in
 // reach.  One CTA per brick (persistent over the level's list), 128 threads;
 // thread t owns the x-quad x0 = 4(t & 1), y = (t >> 1) & 7, z = t >> 4.  The
 // 27-entry neighbour row comes precomputed (k_brick_table).
+template <bool kSums>
 __global__ void __launch_bounds__(128, 4) k_collide_fast(StepArgs a, const uint32_t* __restrict__ nb27) {
     __shared__ uint32_t s_nb[27];
     const int l = a.level;
@@ -299,6 +354,7 @@ __global__ void __launch_bounds__(128, 4) k_collide_fast(StepArgs a, const uint3
 #pragma unroll
         for (int q = 0; q < Q; ++q)
             *(float4*)(a.W + fidx(a.cap, q, b, own)) = make_float4(f[q][0], f[q][1], f[q][2], f[q][3]);
+        if (kSums) brick_sums_store(f, 0u, b, a.part);
         __syncthreads();
         b = bn;
     }
@@ -526,6 +582,7 @@ __global__ void __launch_bounds__(256) k_interface(StepArgs a, uint32_t d0, uint
 // descriptors, from the quad's first descriptor on -- by the descriptor
 // values k_interface computed for this sub-step, and relaxes the quad.  Sites
 // inside the sphere take the rest equilibrium.
+template <bool kSums>
 __global__ void __launch_bounds__(128, 4) k_collide_general(StepArgs a, const uint32_t* __restrict__ nb27) {
     __shared__ uint32_t s_nb[27];
     const int l = a.level;
@@ -581,6 +638,7 @@ __global__ void __launch_bounds__(128, 4) k_collide_general(StepArgs a, const ui
 #pragma unroll
         for (int q = 0; q < Q; ++q)
             *(float4*)(a.W + fidx(a.cap, q, b, own)) = make_float4(f[q][0], f[q][1], f[q][2], f[q][3]);
+        if (kSums) brick_sums_store(f, (sw >> (own & 31)) & 0xFu, b, a.part);
         __syncthreads();
         b = bn;
     }
@@ -718,7 +776,7 @@ __device__ __forceinline__ void stage_issue(const StepArgs& a, uint32_t w, uint3
     }
 }
 
-template <bool kGeneral, bool kDesc>
+template <bool kGeneral, bool kDesc, bool kSums>
 __global__ void __launch_bounds__(128, 4) k_collide_staged(StepArgs a, const uint32_t* __restrict__ nb27) {
     extern __shared__ __align__(128) unsigned char s_dyn[];
     __shared__ uint32_t s_nb[27];
@@ -784,6 +842,7 @@ __global__ void __launch_bounds__(128, 4) k_collide_staged(StepArgs a, const uin
 #pragma unroll
         for (int q = 0; q < Q; ++q)
             *(float4*)(a.W + fidx(a.cap, q, b, own)) = make_float4(f[q][0], f[q][1], f[q][2], f[q][3]);
+        if (kSums) brick_sums_store(f, kGeneral ? (sw >> (own & 31)) & 0xFu : 0u, b, a.part);
         b = bn;
     }
 }
@@ -1269,75 +1328,31 @@ __global__ void k_remap(PoolView p, size_t M, const uint32_t* __restrict__ osrc,
     }
 }
 
-// Double-single (hi, lo) FP32 pairs for the per-brick sums: Knuth's TwoSum
-// (exact rounding error of one addition; needs no FMA contraction) and the
-// pair addition with one renormalisation -- about 2^-44 relative per add.
-struct DS {
-    float hi, lo;
-};
-__device__ __forceinline__ DS ds_add(DS a, DS b) {
-    float s = a.hi + b.hi;
-    float bb = s - a.hi;
-    float e = (a.hi - (s - bb)) + (b.hi - bb);
-    e = e + (a.lo + b.lo);
-    float h = s + e;
-    return DS{h, e - (h - s)};
-}
-
 // One CTA of 128 threads per brick (persistent), thread = x-quad: per brick
-// the sums of rho and j over its fluid sites, weighted by the site volume
-// 2^-3l, and the fluid-site count.  Quads accumulate in double-single, warps
-// reduce in double-single by shuffles, the four warp totals in FP64.
-__global__ void __launch_bounds__(128) k_brick_sums(PoolView p, size_t n, double* __restrict__ part,
-                                                    uint32_t* __restrict__ fluid) {
-    __shared__ double red[4][4];
-    __shared__ uint32_t redc[4];
-    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+// the sums of rho and j over its fluid sites.  Quads accumulate in
+// double-single, warps reduce in double-single by shuffles, and each warp
+// stores its (hi, lo) pairs (layout of brick_sums_store); k_chunk_sums
+// combines the four warps in FP64 and weights the brick by its site volume.
+__global__ void __launch_bounds__(128) k_brick_sums(PoolView p, size_t n, float* __restrict__ part) {
+    const int t = threadIdx.x;
     const int x0 = (t & 1) * 4, y = (t >> 1) & 7, z = t >> 4;
     const int own = x0 + 8 * y + 64 * z;
     for (size_t b = blockIdx.x; b < n; b += gridDim.x) {
         const int l = p.blevel[b];
         const LbmCaseDev& c = p.cases[p.bcase[b]];
         const float* F = cur_buf(p, l);
-        float4 v4[Q];
+        float f[Q][4];
 #pragma unroll
-        for (int q = 0; q < Q; ++q) v4[q] = __ldg((const float4*)(F + fidx(p.cap, q, b, own)));
-        DS acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-        uint32_t cnt = 0;
+        for (int q = 0; q < Q; ++q) {
+            const float4 v = __ldg((const float4*)(F + fidx(p.cap, q, b, own)));
+            f[q][0] = v.x; f[q][1] = v.y; f[q][2] = v.z; f[q][3] = v.w;
+        }
+        uint32_t solid4 = 0;
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < 4; ++i)
             if (solid_at(c, (int64_t)p.bx[b] * 8 + x0 + i, (int64_t)p.by[b] * 8 + y, (int64_t)p.bz[b] * 8 + z, l))
-                continue;
-            float f[Q];
-#pragma unroll
-            for (int q = 0; q < Q; ++q) f[q] = i == 0 ? v4[q].x : (i == 1 ? v4[q].y : (i == 2 ? v4[q].z : v4[q].w));
-            float m[4];
-            moments(f, m[0], m[1], m[2], m[3]);
-#pragma unroll
-            for (int k = 0; k < 4; ++k) acc[k] = ds_add(acc[k], DS{m[k], 0.f});
-            ++cnt;
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                DS other{__shfl_xor_sync(0xFFFFFFFFu, acc[k].hi, o), __shfl_xor_sync(0xFFFFFFFFu, acc[k].lo, o)};
-                acc[k] = ds_add(acc[k], other);
-            }
-        }
-        cnt = __reduce_add_sync(0xFFFFFFFFu, cnt);
-        if (lane == 0) {
-#pragma unroll
-            for (int k = 0; k < 4; ++k) red[k][wid] = (double)acc[k].hi + (double)acc[k].lo;
-            redc[wid] = cnt;
-        }
-        __syncthreads();
-        if (t < 4) {
-            double s4 = ((red[t][0] + red[t][1]) + red[t][2]) + red[t][3];
-            part[b * 4 + t] = s4 / (double)(1ull << (3 * l));
-        }
-        if (t == 4) fluid[b] = (redc[0] + redc[1]) + (redc[2] + redc[3]);
-        __syncthreads();
+                solid4 |= 1u << i;
+        brick_sums_store(f, solid4, b, part);
     }
 }
 
@@ -1386,14 +1401,23 @@ __global__ void __launch_bounds__(128) k_macroscopic(PoolView p, size_t n, float
 // brick, so a case's sums do not depend on the other cases of the pool.
 constexpr uint32_t kChunkBricks = 1024;
 
-__global__ void __launch_bounds__(256) k_chunk_sums(const double* __restrict__ part, const uint2* __restrict__ chunks,
-                                                    uint32_t nchunks, double* __restrict__ chunk_part) {
+__global__ void __launch_bounds__(256) k_chunk_sums(const float* __restrict__ part, const uint8_t* __restrict__ level,
+                                                    const uint2* __restrict__ chunks, uint32_t nchunks,
+                                                    double* __restrict__ chunk_part) {
     __shared__ double red[4][256];
     for (uint32_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
         const uint2 r = chunks[c];
         double acc[4] = {0, 0, 0, 0};
-        for (uint32_t b = r.x + threadIdx.x; b < r.y; b += 256)
-            for (int k = 0; k < 4; ++k) acc[k] += part[(size_t)b * 4 + k];
+        for (uint32_t b = r.x + threadIdx.x; b < r.y; b += 256) {
+            // the brick's four warp totals in order, times its site volume 8^-level (exact)
+            const double vol = __longlong_as_double((long long)(1023 - 3 * (int)level[b]) << 52);
+            const float* w = part + (size_t)b * 32;
+            for (int k = 0; k < 4; ++k) {
+                double s4 = (double)w[2 * k] + (double)w[2 * k + 1];
+                for (int v = 1; v < 4; ++v) s4 = s4 + ((double)w[v * 8 + 2 * k] + (double)w[v * 8 + 2 * k + 1]);
+                acc[k] += s4 * vol;
+            }
+        }
         for (int k = 0; k < 4; ++k) red[k][threadIdx.x] = acc[k];
         __syncthreads();
         for (int o = 128; o > 0; o >>= 1) {
@@ -1584,7 +1608,7 @@ struct fl_pool {
     uint32_t nchunks = 0;
     float* wmax = nullptr;
     unsigned* case_max = nullptr;
-    double* part = nullptr;
+    float* part = nullptr;            // per brick and warp: (hi, lo) of the four conservation sums
     double* cons = nullptr;
     uint32_t* fluid = nullptr;
     uint64_t lups = 0;
@@ -1605,6 +1629,12 @@ struct fl_pool {
     // the bricks are the output of an adapt whose FULL26 balance converged (no two
     // touching bricks more than one level apart): the next regrid's adapt may say so
     bool mesh_balanced = false;
+    // fl_pool_set_step_sums: each level's last sub-step of a level-0 step writes its
+    // bricks' conservation sums into `part` (never once the populations were exported
+    // as a writable field); sums_fresh: `part` holds the sums of the current state
+    bool sums_enabled = false;
+    bool field_exported = false;
+    bool sums_fresh = false;
     // 0: collide kernels load straight into registers; 1: the brick's own
     // population planes bulk-copied into shared memory one brick ahead
     // (k_collide_staged); 2: as 1, with the general bricks' quad masks and
@@ -1676,7 +1706,7 @@ int alloc_brick_arrays(fl_ctx* ctx, fl_pool* P, size_t cap) {
     FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->nbr, cap * 26 * 4 * 4, ctx->stream), "pool nbr");
     FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->list, cap * 8, ctx->stream), "pool list");  // list + general positions
     FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->wmax, cap * 4, ctx->stream), "pool wmax");
-    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->part, cap * 32, ctx->stream), "pool partials");
+    FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->part, cap * 128, ctx->stream), "pool partials");
     FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->fluid, cap * 4, ctx->stream), "pool fluid");
     FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->nb27, cap * 28 * 4, ctx->stream), "pool nb27");
     FL_TRY_CUDA(ctx, fl_dev_malloc_async(ctx, (void**)&P->bclass, cap, ctx->stream), "pool classes");
@@ -1751,6 +1781,7 @@ int alloc_brick_arrays_beside(fl_ctx* ctx, fl_pool* P, size_t cap, BrickArrays* 
 // all-solid bricks for its next two sub-steps (both buffers).
 void populations_replaced(fl_pool* P) {
     ++P->version;
+    P->sums_fresh = false;
     for (int l = 0; l < kMaxPoolLevels; ++l) P->solid_due[l] = 2;
 }
 
@@ -1779,6 +1810,12 @@ int pool_topology_build(fl_ctx* ctx, fl_pool* P);
 int pool_topology(fl_ctx* ctx, fl_pool* P) {
     P->unusable = true;
     int rc = pool_topology_build(ctx, P);
+    if (rc == FL_OK) {
+        // all-solid bricks hold no fluid: their sums stay 0 (the fused sums never write them)
+        P->sums_fresh = false;
+        if (cudaMemsetAsync(P->part, 0, P->cap * 128, ctx->stream) != cudaSuccess)
+            rc = fl_set_error(ctx, FL_E_CUDA, "conservation partials clear");
+    }
     if (rc == FL_OK) P->unusable = false;
     return rc;
 }
@@ -2174,23 +2211,31 @@ void launch_class(fl_ctx* ctx, fl_pool* P, StepArgs a, int l, int kind, cudaStre
     a.list = P->list + off;
     a.count = cnt;
     ctx->launches += (kind == 1 && P->lvl_desc[l + 1] > P->lvl_desc[l]) ? 2 : 1;
+    const bool sums = a.part != nullptr;
     if (kind == 0) {
         unsigned grid = std::min<unsigned>(cnt, (unsigned)ctx->num_sms * P->grid_mult);
-        if (P->staging)
-            k_collide_staged<false, false><<<grid, 128, stage_bytes(false, false), st>>>(a, P->nb27);
-        else
-            k_collide_fast<<<grid, 128, 0, st>>>(a, P->nb27);
+        if (P->staging) {
+            if (sums) k_collide_staged<false, false, true><<<grid, 128, stage_bytes(false, false), st>>>(a, P->nb27);
+            else k_collide_staged<false, false, false><<<grid, 128, stage_bytes(false, false), st>>>(a, P->nb27);
+        } else {
+            if (sums) k_collide_fast<true><<<grid, 128, 0, st>>>(a, P->nb27);
+            else k_collide_fast<false><<<grid, 128, 0, st>>>(a, P->nb27);
+        }
     } else if (kind == 1) {
         a.desc_off = P->slow_off + off;
         const uint32_t dd0 = P->lvl_desc[l], dd1 = P->lvl_desc[l + 1];
         if (dd1 > dd0) k_interface<<<fl_blocks(dd1 - dd0, 256, ctx->num_sms * 8), 256, 0, st>>>(a, dd0, dd1, P->pv);
         const unsigned grid = std::min<unsigned>(cnt, (unsigned)ctx->num_sms * 4);
-        if (P->staging == 2)
-            k_collide_staged<true, true><<<grid, 128, stage_bytes(true, true), st>>>(a, P->nb27);
-        else if (P->staging == 1)
-            k_collide_staged<true, false><<<grid, 128, stage_bytes(true, false), st>>>(a, P->nb27);
-        else
-            k_collide_general<<<grid, 128, 0, st>>>(a, P->nb27);
+        if (P->staging == 2) {
+            if (sums) k_collide_staged<true, true, true><<<grid, 128, stage_bytes(true, true), st>>>(a, P->nb27);
+            else k_collide_staged<true, true, false><<<grid, 128, stage_bytes(true, true), st>>>(a, P->nb27);
+        } else if (P->staging == 1) {
+            if (sums) k_collide_staged<true, false, true><<<grid, 128, stage_bytes(true, false), st>>>(a, P->nb27);
+            else k_collide_staged<true, false, false><<<grid, 128, stage_bytes(true, false), st>>>(a, P->nb27);
+        } else {
+            if (sums) k_collide_general<true><<<grid, 128, 0, st>>>(a, P->nb27);
+            else k_collide_general<false><<<grid, 128, 0, st>>>(a, P->nb27);
+        }
     } else {
         k_collide_solid<<<fl_blocks((size_t)cnt * 512, 256, ctx->num_sms * 8), 256, 0, st>>>(a);
     }
@@ -2217,8 +2262,9 @@ struct Dag {
 // and l + 1; its interior bricks run on P->sf[l], after level l's previous
 // general sub-step.  Same-stream order covers the rest, including the
 // write-after-read of each level's two population buffers.
-void launch_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm, Dag* dag) {
-    const StepArgs a = level_args(ctx, P, l, sub);
+void launch_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm, Dag* dag, bool last) {
+    StepArgs a = level_args(ctx, P, l, sub);
+    if (last && P->sums_enabled) a.part = P->part;  // the level's state after this level-0 step
     const bool solid = P->emit_solid || P->solid_due[l] > 0;
     if (!P->emit_solid && P->solid_due[l] > 0) --P->solid_due[l];
     if (!dag) {
@@ -2239,11 +2285,13 @@ void launch_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm, Dag*
     P->parity[l] ^= 1;
 }
 
-void step_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm, Dag* dag) {
-    launch_level(ctx, P, l, sub, tm, dag);
+// last: this is level l's last sub-step of the level-0 step (every coarser
+// level is in its last sub-step too).
+void step_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm, Dag* dag, bool last) {
+    launch_level(ctx, P, l, sub, tm, dag, last);
     if (l < P->maxL) {
-        step_level(ctx, P, l + 1, 0, tm, dag);
-        step_level(ctx, P, l + 1, 1, tm, dag);
+        step_level(ctx, P, l + 1, 0, tm, dag, false);
+        step_level(ctx, P, l + 1, 1, tm, dag, last);
     }
 }
 
@@ -2251,7 +2299,7 @@ void step_level(fl_ctx* ctx, fl_pool* P, int l, int sub, LaunchTimer* tm, Dag* d
 // forked from and joined back into the context stream.
 void level0_step(fl_ctx* ctx, fl_pool* P, LaunchTimer* tm = nullptr) {
     if (tm || P->streams < 2) {
-        step_level(ctx, P, 0, 0, tm, nullptr);
+        step_level(ctx, P, 0, 0, tm, nullptr, true);
         return;
     }
     Dag dag;
@@ -2260,7 +2308,7 @@ void level0_step(fl_ctx* ctx, fl_pool* P, LaunchTimer* tm = nullptr) {
         cudaStreamWaitEvent(P->sg[l], P->ev_root, 0);
         cudaStreamWaitEvent(P->sf[l], P->ev_root, 0);
     }
-    step_level(ctx, P, 0, 0, nullptr, &dag);
+    step_level(ctx, P, 0, 0, nullptr, &dag, true);
     for (int l = 0; l <= P->maxL; ++l) {
         cudaStreamWaitEvent(ctx->stream, P->evg[l][(dag.k[l] - 1) & 1], 0);
         cudaStreamWaitEvent(ctx->stream, P->evf[l][(dag.k[l] - 1) & 1], 0);
@@ -2512,6 +2560,8 @@ int fl_pool_step(fl_ctx* ctx, fl_pool* P, int nsteps) {
         if (!settled)  // level l ran 2^l sub-steps, each of which pays one owed write
             for (int l = 0; l <= P->maxL; ++l) P->solid_due[l] = std::max(0, P->solid_due[l] - (1 << l));
     }
+    // the steps wrote the sums of the state they leave (a caller's capture only recorded them)
+    if (nsteps > 0) P->sums_fresh = P->sums_enabled && capturing == cudaStreamCaptureStatusNone;
     return FL_OK;
 }
 
@@ -2610,12 +2660,15 @@ int fl_pool_conservation_async(fl_ctx* ctx, fl_pool* P, double* out) {
     if (!ctx || !P || !out) return FL_E_INVALID_ARG;
     FL_POOL_USABLE(ctx, P);
     size_t n = P->mesh.num_cells;
-    k_brick_sums<<<fl_blocks(n, 1, ctx->num_sms * 16), 128, 0, ctx->stream>>>(view(P), n, P->part, P->fluid);
-    FL_CHECK_LAUNCH(ctx, "k_brick_sums");
+    if (!P->sums_fresh) {  // else the last step's collide kernels wrote them (brick_sums_store)
+        k_brick_sums<<<fl_blocks(n, 1, ctx->num_sms * 16), 128, 0, ctx->stream>>>(view(P), n, P->part);
+        FL_CHECK_LAUNCH(ctx, "k_brick_sums");
+        P->sums_fresh = P->sums_enabled;
+    }
     int nc = (int)P->cases.size();
     if (P->nchunks) {
         k_chunk_sums<<<std::min<uint32_t>(P->nchunks, (uint32_t)ctx->num_sms * 8), 256, 0, ctx->stream>>>(
-            P->part, P->d_chunks, P->nchunks, P->chunk_part);
+            P->part, P->mesh.level, P->d_chunks, P->nchunks, P->chunk_part);
         FL_CHECK_LAUNCH(ctx, "k_chunk_sums");
     }
     k_case_sums<<<(nc * 4 + 255) / 256, 256, 0, ctx->stream>>>(P->chunk_part, P->d_case_chunk, nc, P->cons);
@@ -3015,6 +3068,14 @@ int fl_pool_populations_field(fl_ctx* ctx, fl_pool* P, const char* name, uint64_
         }
         P->parity[l] = 0;
     }
+    // writes through the view are invisible to the pool: from here on the conservation sums are
+    // always recomputed from the stored state (k_brick_sums)
+    P->field_exported = true;
+    if (P->sums_enabled) {
+        P->sums_enabled = false;
+        drop_graph(P);
+    }
+    P->sums_fresh = false;
     fl_field_desc d;
     if (fl_field_make(name, 0, Q, 1, 0, 0, &d) != FL_OK)
         return fl_set_error(ctx, FL_E_INVALID_ARG, "fl_pool_populations_field: bad field name");
@@ -3038,13 +3099,27 @@ int fl_pool_set_staging(fl_ctx* ctx, fl_pool* P, int mode) {
     FL_POOL_USABLE(ctx, P);
     if (mode) {
         // above the default 48 KB of dynamic shared memory per block
-        FL_TRY_CUDA(ctx, cudaFuncSetAttribute(k_collide_staged<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)stage_bytes(true, true)),
+        FL_TRY_CUDA(ctx, cudaFuncSetAttribute(k_collide_staged<true, true, false>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stage_bytes(true, true)),
+                    "staged kernel shared memory");
+        FL_TRY_CUDA(ctx, cudaFuncSetAttribute(k_collide_staged<true, true, true>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stage_bytes(true, true)),
                     "staged kernel shared memory");
     }
     FL_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "fl_pool_set_staging");
     P->staging = mode;
     drop_graph(P);
+    return FL_OK;
+}
+
+int fl_pool_set_step_sums(fl_ctx* ctx, fl_pool* P, int on) {
+    if (!ctx || !P) return FL_E_INVALID_ARG;
+    FL_POOL_USABLE(ctx, P);
+    const bool want = on != 0 && !P->field_exported;
+    if (want != P->sums_enabled) {
+        P->sums_enabled = want;
+        drop_graph(P);  // the captured steps launch other kernels
+    }
     return FL_OK;
 }
 

@@ -162,8 +162,10 @@ class Pool:
         self.ctx.call("fl_pool_info_get", self.h, ctypes.byref(i))
         return i
 
-    def set_options(self, graphs=1, grid_mult=0, streams=None, staging=None):
+    def set_options(self, graphs=1, grid_mult=0, streams=None, staging=None, step_sums=None):
         self.ctx.call("fl_pool_set_options", self.h, graphs, grid_mult)
+        if step_sums is not None:
+            self.ctx.call("fl_pool_set_step_sums", self.h, int(step_sums))
         if streams is not None:
             self.ctx.call("fl_pool_set_class_streams", self.h, streams)
         if staging is not None:

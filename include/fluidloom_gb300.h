@@ -355,6 +355,13 @@ int fl_pool_conservation(fl_ctx* ctx, fl_pool* pool, double* out);
  * this point (fl_ctx_synchronize, or any later call that synchronises).  Device-side status is
  * collected by the next call that synchronises. */
 int fl_pool_conservation_async(fl_ctx* ctx, fl_pool* pool, double* out);
+/* on != 0: every level-0 step also writes the conservation sums of the state it leaves (each
+ * level's last sub-step sums the values it stores, in the arithmetic of the separate pass), so a
+ * conservation call after a step reads no populations; for callers that read the sums every step.
+ * Off (the default) the steps carry no extra work and a conservation call reads the populations.
+ * Results are identical either way.  Ignored (stays off) once the populations were exported as a
+ * field (fl_pool_populations_field), whose writes the pool cannot see. */
+int fl_pool_set_step_sums(fl_ctx* ctx, fl_pool* pool, int on);
 /* Advance nsteps with a CUDA event pair around every collide-stream launch (no graphs); returns,
  * per kernel ([0] interior bricks, [1] interface/boundary/near-sphere bricks, [2] all-solid bricks),
  * the summed kernel time, the launch count and the fluid sites those launches updated (each output

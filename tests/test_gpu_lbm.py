@@ -123,12 +123,32 @@ def test_graphs_after_upload_match_direct_launches(ctx):
             np.testing.assert_array_equal(a.populations(), b.populations())
 
 
+@pytest.mark.parametrize("staging", [0, 1, 2])
+def test_fused_conservation_sums_equal_recomputed(ctx, staging):
+    """Each level's last sub-step writes its bricks' conservation sums from the values it
+    stores; they equal k_brick_sums' recomputation from the stored state bit for bit (both
+    cases in one pool: walls, a moving lid, the sphere's solid sites, three levels), after
+    steps and after a regrid, in every staging mode."""
+    from fluidloom_gb300.lbm import Pool
+    p = Pool(ctx, list(cases_small()))
+    p.set_options(staging=staging, step_sums=True)
+    for rnd in range(2):
+        p.step(3)
+        fused = p.conservation()           # from the step's own sums
+        p.upload(p.populations())          # the same state, marked replaced: sums recomputed
+        again = p.conservation()
+        np.testing.assert_array_equal(fused, again)
+        p.regrid()
+    p.close()
+
+
 def test_conservation_async_equals_sync(ctx):
     """fl_pool_conservation_async queues the sums and their copy into pinned host memory
     without waiting; after a synchronise they equal the synchronous call's, step by step."""
     import ctypes
     from fluidloom_gb300.lbm import Pool
     p = Pool(ctx, [cases_small()[1]])
+    p.set_options(step_sums=True)  # the sums of each step from the step itself
     cp = ctypes.c_void_p()
     ctx.call("fl_host_alloc_pinned", ctypes.c_size_t(3 * 32), ctypes.byref(cp))
     got = np.ctypeslib.as_array(ctypes.cast(cp, ctypes.POINTER(ctypes.c_double)), shape=(3, 4))
