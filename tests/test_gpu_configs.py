@@ -78,6 +78,30 @@ def test_config2_sphere_full_size(ctx):
     gp.close()
 
 
+def test_config2_half_resolution_developing_mesh(ctx):
+    """The sphere case with the benchmark's vorticity thresholds at half resolution (64x32x32
+    base, 3 levels, r=4) for 100 steps, a regrid every 25: the wake starts to refine (the mesh
+    grows past its band refinement) and the GPU pool -- whose regrids after the first state
+    their input balanced -- equals the oracle, which probes every leaf, bit for bit at every
+    regrid: bricks, neighbour rows, populations."""
+    from bench import sphere_case
+    case = sphere_case(2)
+    gp, op = Pool(ctx, [case]), O.OraclePool([case])
+    n0 = gp.info().num_bricks
+    for s in range(1, 101):
+        gp.step(1)
+        op.step(1)
+        if s % 25 == 0:
+            gp.regrid()
+            op.regrid()
+            _same_bricks(gp, op)
+            assert np.array_equal(gp.nbr(), op.nbr()), s
+            assert np.array_equal(gp.populations(), op.populations()), s
+    assert gp.info().num_bricks > n0  # the vorticity-driven refinement happened
+    np.testing.assert_allclose(gp.conservation(), op.conservation(), rtol=1e-12, atol=1e-9)
+    gp.close()
+
+
 def test_config2_sphere_bulk_staged_equals_register_kernels(ctx):
     """Full-size sphere: the bulk-staged collide kernels (both staging modes) equal the
     register kernels bit for bit over 6 level-0 steps (48 level-3 sub-steps)."""
