@@ -207,16 +207,18 @@ __global__ void k_locator_dir(const uint64_t* __restrict__ keys, size_t n, int l
 // the first pass (k < 13) finds a leaf j of cell i's own level, i is j's
 // neighbour in direction 25 - k on every sub-slot, so it writes that entry of
 // j's row too and marks it (bit 12 - k of marks[j]); the second pass probes
-// only the unmarked directions 13..25.  Blocks of kNbrThreads: 48 / S cells
+// only the unmarked directions 13..25.  Blocks of kNbrThreads: kNbrCells / S cells
 // x 13 directions x S sub-slots, a cell's probes in consecutive threads; three
 // blocks per SM (32 registers a thread).
-constexpr int kNbrThreads = 624;
+constexpr int kNbrCells = 48;        // cells per block at one sub-slot
+constexpr int kNbrBlocksPerSM = 3;
+constexpr int kNbrThreads = kNbrCells * 13;
 
 template <int S, bool kFirst>
-__global__ void __launch_bounds__(kNbrThreads, 3) k_neighbours_sorted(fl_mesh_dev m, fl_domain_dev dom,
+__global__ void __launch_bounds__(kNbrThreads, kNbrBlocksPerSM) k_neighbours_sorted(fl_mesh_dev m, fl_domain_dev dom,
                                                                         fl_locator L, uint32_t* __restrict__ nbr,
                                                                         uint32_t* __restrict__ marks) {
-    constexpr int kCells = 48 / S;
+    constexpr int kCells = kNbrCells / S;
     __shared__ uint8_t t1[96];
     __shared__ uint16_t t3c[12 * 512];
     fl_keys_fill_tables_cat(t1, t3c);
@@ -317,8 +319,9 @@ int fl_neighbours_sorted(fl_ctx* ctx, const fl_mesh_dev& m, const fl_domain_dev&
                          int subslots, uint32_t* nbr, uint32_t* marks) {
     if (m.n == 0) return FL_OK;
     FL_TRY_CUDA(ctx, cudaMemsetAsync(marks, 0, m.n * 4, ctx->stream), "neighbour marks");
-    const size_t cells = (size_t)(48 / subslots);
-    const unsigned grid = (unsigned)std::min<size_t>((m.n + cells - 1) / cells, (size_t)ctx->num_sms * 3);
+    const size_t cells = (size_t)(kNbrCells / subslots);
+    const unsigned grid =
+        (unsigned)std::min<size_t>((m.n + cells - 1) / cells, (size_t)ctx->num_sms * kNbrBlocksPerSM);
     if (subslots == 4) {
         k_neighbours_sorted<4, true><<<grid, kNbrThreads, 0, ctx->stream>>>(m, dom, L, nbr, marks);
         FL_CHECK_LAUNCH(ctx, "k_neighbours_sorted");
