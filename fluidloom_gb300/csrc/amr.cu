@@ -274,6 +274,29 @@ __device__ __forceinline__ uint32_t sibling_of(const fl_probe& P, const fl_mesh_
     return j;
 }
 
+// The same without a search, for a mesh in key order (the locator's run order
+// is the mesh order, L.ids == nullptr): the parent's run holds its children's
+// runs, so a complete octet of leaves is 8 consecutive cells, starting h cells
+// before the candidate, h = the candidate's Hilbert digit at its level (read
+// from its run key).  Lane c takes the c-th of them, in key order; it is a
+// member when it is a leaf of the candidate's level under the same parent
+// (case, x >> 1, y >> 1, z >> 1).  Eight members <=> the eight children are
+// leaves of that level <=> sibling_of finds all eight; `ok` as there.  The
+// members come in key order, not by child position (their child bits say
+// which is which).
+__device__ __forceinline__ uint32_t sibling_in_run(const fl_probe& P, const fl_mesh_dev& m, size_t i, int c, bool* ok) {
+    const int l = m.level[i];
+    const int h = (int)((__ldg((const unsigned long long*)(P.L.keys + i)) >> (3 * (P.top - l))) & 7u);
+    *ok = false;
+    if (i < (size_t)h) return FL_INVALID_INDEX;
+    const size_t j = i - h + c;
+    if (j >= m.n || m.level[j] != l || (m.x[j] >> 1) != (m.x[i] >> 1) || (m.y[j] >> 1) != (m.y[i] >> 1) ||
+        (m.z[j] >> 1) != (m.z[i] >> 1) || (m.case_id && m.case_id[j] != m.case_id[i]))
+        return FL_INVALID_INDEX;
+    *ok = m.flags[j] == -1 && m.state[j] == 0;
+    return (uint32_t)j;
+}
+
 // Leaders: a warp screens 32 cells, a lane each, then checks the chunk's
 // candidates four at a time -- lanes 8s .. 8s + 7 locate the eight siblings of
 // the s-th (all must be mergeable leaves of its level) -- and, for the FULL26
@@ -324,7 +347,7 @@ __global__ void __launch_bounds__(kT) k_leaders(fl_mesh_dev m, fl_domain_dev dom
             const size_t i = have ? base + (__ffs(pick) - 1) : 0;
             bool ok = true;
             uint32_t j = FL_INVALID_INDEX;
-            if (have) j = sibling_of(P, m, dom, i, lane & 7, &ok);
+            if (have) j = P.L.ids ? sibling_of(P, m, dom, i, lane & 7, &ok) : sibling_in_run(P, m, i, lane & 7, &ok);
             const unsigned okm = __ballot_sync(0xFFFFFFFFu, ok);
             unsigned lead4 = 0;  // bit s: candidate s has eight mergeable siblings
             for (int s = 0; s < n4; ++s)
@@ -421,9 +444,15 @@ __global__ void __launch_bounds__(kT) k_members(fl_mesh_dev m, fl_domain_dev dom
             for (int s = 0; s < 4 && cm; ++s) cm &= cm - 1;
             if (pick) {
                 const size_t i = base + (__ffs(pick) - 1);
-                const int c = lane & 7;
                 bool ok;
-                const uint32_t j = sibling_of(P, m, dom, i, c, &ok);
+                uint32_t j;
+                int c = lane & 7;
+                if (P.L.ids) {
+                    j = sibling_of(P, m, dom, i, c, &ok);
+                } else {  // the octet's c-th cell in key order: file it under its child position
+                    j = sibling_in_run(P, m, i, c, &ok);
+                    c = (m.x[j] & 1) | ((m.y[j] & 1) << 1) | ((m.z[j] & 1) << 2);
+                }
                 const uint32_t g = gid[i];
                 members[(size_t)g * 8 + c] = j;
                 group_of[j] = g;
