@@ -162,18 +162,18 @@ def microbench_mesh(L=8):
     regridded once by thresholding blob field 1 (refine above 0.7 to level L+1, coarsen
     below 0.4) -- about 0.98 x 8^L leaves over three levels -- then the benchmark's
     regrid by an independent blob field 2 (same thresholds, up to level L+2), whose
-    refinement crosses the first round's level boundaries so FULL26 balance iterates."""
+    refinement crosses the first regrid's level boundaries so FULL26 balance iterates."""
     n1 = 1 << L
     idx = np.arange(n1 ** 3, dtype=np.int64)
     N = len(idx)
     start = {"x": (idx % n1).astype(np.int32), "y": ((idx // n1) % n1).astype(np.int32),
              "z": (idx // (n1 * n1)).astype(np.int32), "level": np.full(N, L, np.uint8),
              "state": np.zeros(N, np.uint8), "flags": np.zeros(N, np.int32), "material": np.zeros(N, np.uint32)}
-    return {"start": start, "rounds": [(blob_table(1), 0.4, 0.7, L + 1), (blob_table(2), 0.4, 0.7, L + 2)]}
+    return {"start": start, "regrids": [(blob_table(1), 0.4, 0.7, L + 1), (blob_table(2), 0.4, 0.7, L + 2)]}
 
 
 def regrid_microbench(ctx, L=8):
-    """The regrid of the microbenchmark octree (microbench_mesh; round 1 untimed):
+    """The regrid of the microbenchmark octree (microbench_mesh; the first regrid untimed):
     blob flags, FULL26 balance to a fixed point, split/merge, key-order rebuild, the
     neighbour table; then a 63-bit key sort of the result alone and the primitives."""
     import ctypes
@@ -183,8 +183,8 @@ def regrid_microbench(ctx, L=8):
     m = Mesh(ctx, mb["start"], capacity=1 << (3 * L))
     out = {}
     st = None
-    for r, (blobs, lo, hi, ml) in enumerate(mb["rounds"]):
-        # round 2's input is round 1's output: stated balanced when round 1's balance converged
+    for r, (blobs, lo, hi, ml) in enumerate(mb["regrids"]):
+        # the second regrid's input is the first's output: stated balanced when its balance converged
         cfg = AdaptConfig.make(max_level=ml, min_level=0, balance_mode=1,
                                input_balanced=st is not None and st.balance.converged == 1)
         leaves_in = m.n

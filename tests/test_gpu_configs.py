@@ -7,7 +7,7 @@ Config 1: the lid-driven cavity (32^3 sites, max level 2, lid 0.05 +x on the top
 Config 2: the flow past a sphere at full size (128x64x64 base, 3 levels, r = 8
   at (32,32,32), inlet 0.04, tau 0.56): 25 steps, a regrid, one more step, all
   equal.
-Config 3: the regrid microbenchmark's two-round blob octree (microbench_mesh):
+Config 3: the regrid microbenchmark's two-regrid blob octree (microbench_mesh):
   exact against the oracle at 2^18 leaves (the oracle's single-threaded
   balance takes seconds there, hours at 2^24), and at the full 2^24 leaves
   the size-independent properties: the output tiles the domain in strictly
@@ -130,32 +130,32 @@ def _adapt_gpu(ctx, m, cfg):
     return st
 
 
-def _gpu_two_rounds(ctx, L, hint=True):
-    """The microbenchmark's octree on the GPU: round 1 from the uniform level-L mesh,
-    round 2 (the timed regrid of the benchmark) from its output -- stated balanced when
-    hint is set and round 1's balance converged, as the benchmark does."""
+def _gpu_two_regrids(ctx, L, hint=True):
+    """The microbenchmark's octree on the GPU: the first regrid from the uniform level-L
+    mesh, the second (the timed regrid of the benchmark) from its output -- stated balanced
+    when hint is set and the first regrid's balance converged, as the benchmark does."""
     from bench import microbench_mesh
     from fluidloom_gb300.amr import AdaptConfig, Mesh
-    rounds = microbench_mesh(L)
-    m = Mesh(ctx, rounds["start"], capacity=1 << (3 * L))
+    mb = microbench_mesh(L)
+    m = Mesh(ctx, mb["start"], capacity=1 << (3 * L))
     stats = []
-    for blobs, lo, hi, ml in rounds["rounds"]:
+    for blobs, lo, hi, ml in mb["regrids"]:
         ctx.call("fl_flags_from_blobs", ctypes.byref(m.m), blobs.ctypes.data_as(ctypes.c_void_p), len(blobs),
                  ctypes.c_float(lo), ctypes.c_float(hi), ml)
         balanced = hint and bool(stats) and stats[-1].balance.converged == 1
         stats.append(_adapt_gpu(ctx, m, AdaptConfig.make(max_level=ml, min_level=0, balance_mode=1,
                                                          input_balanced=balanced)))
-    return m, stats, rounds
+    return m, stats, mb
 
 
 @pytest.mark.parametrize("hint", [False, True])
 def test_config3_microbench_octree_exact_at_2_18(ctx, hint):
     L = 6
-    m, stats, rounds = _gpu_two_rounds(ctx, L, hint)
+    m, stats, mb = _gpu_two_regrids(ctx, L, hint)
     g = m.download()
-    c = {k: v.copy() for k, v in rounds["start"].items()}
+    c = {k: v.copy() for k, v in mb["start"].items()}
     dom = O.domain(max_level=L + 2)
-    for (blobs, lo, hi, ml), gst in zip(rounds["rounds"], stats):
+    for (blobs, lo, hi, ml), gst in zip(mb["regrids"], stats):
         c["flags"] = O.blob_flags(c, blobs, lo, hi, ml)
         c, st, *_ = O.adapt(c, dict(max_level=ml, min_level=0, balance_mode=1, max_balance_iterations=10,
                                     enforce_balance=1, averaging_rule=0), dom)
@@ -178,7 +178,7 @@ def test_config3_microbench_octree_properties_at_2_24(ctx):
     from fluidloom_gb300 import DeviceArray
     from fluidloom_gb300.amr import AdaptConfig
     L = 8
-    m, stats, _ = _gpu_two_rounds(ctx, L)
+    m, stats, _ = _gpu_two_regrids(ctx, L)
     n = m.n
     assert stats[1].balance.iterations > 1 and stats[1].balance.total_cells_marked_for_balance > 0
     cols = m.download()
@@ -212,7 +212,7 @@ def test_config3_microbench_octree_properties_at_2_24(ctx):
     assert r.converged == 1 and r.total_cells_marked_for_balance == 0
     m2.free()
     # run twice: bitwise the same leaves
-    m3, stats3, _ = _gpu_two_rounds(ctx, L)
+    m3, stats3, _ = _gpu_two_regrids(ctx, L)
     c3 = m3.download()
     for key in ("x", "y", "z", "level"):
         assert np.array_equal(c3[key], cols[key]), key
