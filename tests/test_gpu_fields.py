@@ -52,3 +52,35 @@ def test_populations_field_view(ctx, steps):
     ctx.call("fl_memcpy_h2d", p5, v.ctypes.data_as(ctypes.c_void_p), ctypes.c_size_t(4))
     assert gp.populations()[5, 0, 0] == np.float32(0.125)
     gp.close()
+
+
+def test_step_sums_stop_after_field_export(ctx):
+    """With step sums on, a conservation read after a step uses the step's own sums.  Once
+    the populations are exported as a writable field the pool cannot see writes through it,
+    so it recomputes the sums from the stored state: a write through the field shows up in
+    the next conservation read, which equals that of a pool uploaded with the same state."""
+    from fluidloom_gb300.lbm import Pool
+    from tests.test_gpu_lbm import cases_small
+    gp = Pool(ctx, [cases_small()[1]])
+    gp.set_options(step_sums=True)
+    gp.step(3)
+    before = gp.conservation()
+    h = ctypes.c_uint64()
+    ctx.call("fl_pool_populations_field", gp.h, b"populations", ctypes.byref(h))
+    n = gp.info().num_bricks
+    _, p0 = _component(ctx, h.value, 0, n)
+    f0 = np.empty(1, np.float32)
+    ctx.call("fl_memcpy_d2h", f0.ctypes.data_as(ctypes.c_void_p), p0, ctypes.c_size_t(4))
+    v = np.array([f0[0] + 0.5], np.float32)  # add mass at the first site of the first brick
+    ctx.call("fl_memcpy_h2d", p0, v.ctypes.data_as(ctypes.c_void_p), ctypes.c_size_t(4))
+    after = gp.conservation()
+    assert after[0, 0] != before[0, 0]
+    ref = Pool(ctx, [cases_small()[1]])
+    ref.upload(gp.populations())
+    np.testing.assert_array_equal(after, ref.conservation())
+    gp.step(1)
+    ref.step(1)
+    np.testing.assert_array_equal(gp.conservation(), ref.conservation())
+    ref.close()
+    gp.close()
+
