@@ -1442,9 +1442,12 @@ __global__ void k_case_sums(const double* __restrict__ chunk_part, const uint32_
 }
 
 // exp(x) for x <= 0 from the mathematics: x = n ln2 + r with |r| <= ln2/2
-// (Cody & Waite 1980 two-constant reduction), e^r by its Taylor series to r^7,
-// then an exact scaling by 2^n.  Written operation by operation (this unit has
-// no FMA contraction) so the CPU restatement gives the same bits.
+// (Cody & Waite 1980 two-constant reduction; the split ln2 = 0.693145752 +
+// 1.42860677e-6 is the one published with fdlibm's single-precision expf,
+// e_expf.c, whose high part has a short mantissa so n * ln2_hi is exact),
+// e^r by its Taylor series to r^7, then an exact scaling by 2^n.  Written
+// operation by operation (this unit has no FMA contraction) so the CPU
+// restatement gives the same bits.
 __device__ __forceinline__ float fl_exp_neg(float x) {
     if (x < -87.0f) return 0.0f;
     float t = x * 1.44269504f;

@@ -517,9 +517,10 @@ void init_populations(Pool& P) {
 }  // namespace
 
 // exp(x) for x <= 0: Cody & Waite (1980) reduction x = n ln2 + r with ln2
-// split into a 16-bit head (0.693145751953125, so n*head is exact) and a tail,
-// Taylor series of e^r to r^7, exact scaling by 2^n.  Operation by operation,
-// as the CUDA flag kernel computes it.
+// split into a 16-bit head (0.693145751953125, so n*head is exact) and a tail
+// (the split published with fdlibm's single-precision expf, e_expf.c), Taylor
+// series of e^r to r^7, exact scaling by 2^n.  Operation by operation, as the
+// CUDA flag kernel computes it.
 static float exp_neg(float x) {
     if (x < -87.0f) return 0.0f;
     float t = x * 1.44269504f;
