@@ -211,11 +211,12 @@ def regrid_microbench(ctx, L=8):
     perm = np.random.default_rng(5).permutation(n).astype(np.uint32)
     hk = keys.to_host()[perm]
     keys.free()
-    # warm-up sort of a copy (the library's scratch then has its size), then the timed sort
-    wk, wi = DeviceArray.from_host(ctx, hk), DeviceArray.from_host(ctx, perm)
-    ctx.call("fl_sort_pairs_u64_u32", wk.ptr, wi.ptr, n, 0, 63)
-    wk.free()
-    wi.free()
+    # the sort's shape (digit width, tile threads) tuned on copies of these keys (each shape's
+    # first call untimed, so the library's scratch already has its size), then the timed sort
+    from fluidloom_gb300.batching import autotune_sort
+    shape, shape_ms = autotune_sort(ctx, hk, perm, 0, 63)
+    out["sort_shape"] = {"digit_bits": shape[0], "tile_threads": shape[1], "passes": -(-63 // shape[0]),
+                         "tuned_ms": {"%dx%d" % s: round(t, 4) for s, t in shape_ms.items()}}
     keys = DeviceArray.from_host(ctx, hk)
     ids = DeviceArray.from_host(ctx, perm)
     del hk
@@ -239,7 +240,7 @@ def regrid_microbench(ctx, L=8):
 def primitives_on(ctx, m, keys, ids, n, out):
     """The regrid's primitives alone on the n-leaf result mesh, each against the algorithmic
     bytes of its unit: encode 24 B per key (12 B coordinates in, 8 B key + 4 B id out); radix
-    sort 8 + 24 B per key and pass (8 passes of 8-bit digits over 63 bits); scan 8 B per
+    sort 8 + 24 B per key and pass (ceil(63 / d) passes of the tuned d-bit digits); scan 8 B per
     element; hash build 24 B per key + 12 B per slot cleared; hash query 12 B per query + one
     32-byte sector per probe; neighbour rebuild 104 B of table written + 23 B read per leaf
     (coordinates, level, locator key, directory share); halo pack / unpack of a 19-component field 4 + 2 x 76 B per cell
@@ -265,7 +266,7 @@ def primitives_on(ctx, m, keys, ids, n, out):
     put("hilbert_encode", stop(), 24.0 * n, n, "keys")
     ek.free()
     ei.free()
-    put("radix_sort", out["sort_ms"], (8.0 + 24.0 * 8) * n, n, "keys")
+    put("radix_sort", out["sort_ms"], (8.0 + 24.0 * out["sort_shape"]["passes"]) * n, n, "keys")
     a = DeviceArray(ctx, (n,), np.uint32).zero()
     b = DeviceArray(ctx, (n,), np.uint32)
     tot = DeviceArray(ctx, (1,), np.uint32)

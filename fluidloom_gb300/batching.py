@@ -72,6 +72,42 @@ def autotune(pool, candidates=(2, 3, 4, 6, 8), streams=(1, 2), staging=(0, 1, 2)
     return best
 
 
+SORT_SHAPES = ((8, 256), (8, 512), (9, 512))
+
+
+def autotune_sort(ctx, hkeys, hids, begin_bit=0, end_bit=64, shapes=SORT_SHAPES, reps=3):
+    """Pick the radix sort's shape -- digit width and tile threads (fl_sort_set_config) -- for
+    keys like these: per shape, a device copy of (hkeys, hids) is sorted once untimed and then
+    `reps` times timed with CUDA events (the copy refreshed before each call); the fastest
+    shape is set on the context.  Every shape gives the same sorted output.  Returns
+    ((digit_bits, tile_threads), {(digit_bits, tile_threads): best ms})."""
+    import ctypes
+    from . import DeviceArray
+    hkeys = np.ascontiguousarray(hkeys, np.uint64)
+    hids = np.ascontiguousarray(hids, np.uint32)
+    n = len(hkeys)
+    k, v = DeviceArray.from_host(ctx, hkeys), DeviceArray.from_host(ctx, hids)
+    times = {}
+    for bits, threads in shapes:
+        ctx.call("fl_sort_set_config", bits, threads)
+        best = None
+        for r in range(reps + 1):
+            ctx.call("fl_memcpy_h2d", k.ptr, hkeys.ctypes.data_as(ctypes.c_void_p), ctypes.c_size_t(hkeys.nbytes))
+            ctx.call("fl_memcpy_h2d", v.ptr, hids.ctypes.data_as(ctypes.c_void_p), ctypes.c_size_t(hids.nbytes))
+            ctx.call("fl_ctx_timer_start")
+            ctx.call("fl_sort_pairs_u64_u32", k.ptr, v.ptr, ctypes.c_size_t(n), begin_bit, end_bit)
+            ms = ctypes.c_float()
+            ctx.call("fl_ctx_timer_stop", ctypes.byref(ms))
+            if r > 0 and (best is None or ms.value < best):
+                best = ms.value
+        times[(bits, threads)] = best
+    choice = min(times, key=times.get)
+    ctx.call("fl_sort_set_config", *choice)
+    k.free()
+    v.free()
+    return choice, times
+
+
 def run(pool, steps, regrid_every):
     """Advance `steps` level-0 steps with a regrid every `regrid_every`; returns fluid LUPs done."""
     lups = 0

@@ -29,6 +29,8 @@ struct fl_ctx {
     void* soa = nullptr;                       // structure-of-arrays field manager (fields.cu)
     uint64_t launches = 0;                     // kernels launched on behalf of this context
     int64_t alloc_fail_countdown = -1;         // fault injection: allocations left before they fail (-1 off)
+    int sort_digit_bits = 8;                   // radix sort shape (fl_sort_set_config)
+    int sort_tile_threads = 256;
 };
 
 // Every device allocation the library makes goes through these two: cudaMalloc

@@ -118,6 +118,91 @@ def test_sort_hilbert_keys_16m_sorted_and_permutation(ctx):
     assert np.bincount(i, minlength=n).max() == 1
 
 
+SORT_SHAPES = [(8, 256), (8, 512), (9, 512)]
+
+
+@pytest.fixture
+def sort_shape(ctx, request):
+    """Set the context's radix sort shape for one test; the default shape afterwards."""
+    ctx.call("fl_sort_set_config", *request.param)
+    yield request.param
+    ctx.call("fl_sort_set_config", 8, 256)
+
+
+@pytest.mark.parametrize("sort_shape", SORT_SHAPES, indirect=True)
+@pytest.mark.parametrize("n,b0,b1", [(0, 0, 64), (1, 0, 64), (6143, 0, 64), (6144, 0, 63), (6145, 5, 29),
+                                      (300_001, 0, 64), (300_001, 0, 63), (70_000, 0, 3), (70_000, 55, 64)])
+def test_sort_shapes_equal_stable_sort(ctx, sort_shape, n, b0, b1):
+    """Every sort shape (digit width x tile threads) gives the stable order of the key bits
+    [b0, b1): ragged tiles, one-digit and odd-width ranges, the top bits."""
+    rng = np.random.default_rng(n + b0 + 7 * b1)
+    k = rng.integers(0, 2**63, n, dtype=np.uint64) * 2 + rng.integers(0, 2, n).astype(np.uint64)
+    v = np.arange(n, dtype=np.uint32)
+    gk, gv = _sort(ctx, k, v, b0, b1)
+    mask = np.uint64(((1 << (b1 - b0)) - 1) << b0) if b1 - b0 < 64 else np.uint64(0xFFFFFFFFFFFFFFFF)
+    order = np.argsort(k & mask, kind="stable")
+    np.testing.assert_array_equal(gv, v[order])
+    np.testing.assert_array_equal(gk, k[order])
+
+
+@pytest.mark.parametrize("sort_shape", SORT_SHAPES[1:], indirect=True)
+def test_sort_shapes_ties_and_full_size(ctx, sort_shape):
+    """Ties keep input order in every shape; 2^24 Hilbert keys equal the oracle's stable sort."""
+    rng = np.random.default_rng(19)
+    n = 400_000
+    k = rng.integers(0, 700, n).astype(np.uint64) << np.uint64(30)
+    v = rng.integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32)
+    gk, gv = _sort(ctx, k, v)
+    wk, wv = k.copy(), v.copy()
+    O.load().or_sort_pairs_u64_u32(O.ptr(wk), O.ptr(wv), n)
+    np.testing.assert_array_equal(gk, wk)
+    np.testing.assert_array_equal(gv, wv)
+    from fluidloom_gb300 import DeviceArray
+    n = 1 << 24
+    x, y, z = (rng.integers(0, 1 << 21, n).astype(np.int32) for _ in range(3))
+    d = [DeviceArray.from_host(ctx, a) for a in (x, y, z)]
+    dk, di = E(ctx, (n,), np.uint64), E(ctx, (n,), np.uint32)
+    ctx.call("fl_hilbert_encode", d[0].ptr, d[1].ptr, d[2].ptr, 21, dk.ptr, di.ptr, n)
+    wk, wv = dk.to_host(), di.to_host()
+    ctx.call("fl_sort_pairs_u64_u32", dk.ptr, di.ptr, n, 0, 63)
+    O.load().or_sort_pairs_u64_u32(O.ptr(wk), O.ptr(wv), n)
+    np.testing.assert_array_equal(dk.to_host(), wk)
+    np.testing.assert_array_equal(di.to_host(), wv)
+
+
+def test_sort_shape_validation(ctx):
+    from fluidloom_gb300.runtime import FluidLoomError
+    for bad in [(7, 256), (9, 256), (10, 512), (8, 384), (8, 0)]:
+        with pytest.raises(FluidLoomError):
+            ctx.call("fl_sort_set_config", *bad)
+    b, t = ctypes.c_int(), ctypes.c_int()
+    ctx.call("fl_sort_get_config", ctypes.byref(b), ctypes.byref(t))
+    assert (b.value, t.value) == (8, 256)
+
+
+@pytest.mark.parametrize("sort_shape", SORT_SHAPES[1:], indirect=True)
+def test_sort_shapes_inside_compaction(ctx, sort_shape):
+    """The compaction's sort runs in the context's shape: same survivors, order and permutation."""
+    rng = np.random.default_rng(23)
+    n = 250_000
+    keys = rng.integers(0, 2**62, n, dtype=np.uint64)
+    keys[rng.integers(0, n, 1000)] = np.uint64(0xFFFFFFFFFFFFFFFF)
+    state = rng.integers(0, 2, n).astype(np.uint32)
+    dk, ds = D(ctx, keys), D(ctx, state)
+    perm, sk, si = E(ctx, (n,), np.uint32), E(ctx, (n,), np.uint64), E(ctx, (n,), np.uint32)
+    nv = ctypes.c_size_t()
+    ctx.call("fl_compact_and_permute", dk.ptr, ds.ptr, n, perm.ptr, sk.ptr, si.ptr, ctypes.byref(nv))
+    keep = np.nonzero((state != 0) & (keys != np.uint64(0xFFFFFFFFFFFFFFFF)))[0]
+    order = keep[np.argsort(keys[keep], kind="stable")]
+    m = nv.value
+    assert m == len(order)
+    np.testing.assert_array_equal(sk.to_host()[:m], keys[order])
+    np.testing.assert_array_equal(si.to_host()[:m], order.astype(np.uint32))
+    want = np.full(n, 0xFFFFFFFF, np.uint32)
+    want[order] = np.arange(m, dtype=np.uint32)
+    np.testing.assert_array_equal(perm.to_host(), want)
+
+
 def test_compact_and_permute(ctx):
     # test_hash_table.cpp:54-116 cases plus a random one
     cases = [(np.arange(10, dtype=np.uint64) * 100, (np.arange(10) % 2).astype(np.uint32)),
