@@ -72,7 +72,7 @@ def autotune(pool, candidates=(2, 3, 4, 6, 8), streams=(1, 2), staging=(0, 1, 2)
     return best
 
 
-SORT_SHAPES = ((8, 256), (8, 512), (9, 512))
+SORT_SHAPES = ((8, 256), (8, 512), (9, 256), (9, 512))
 
 
 def autotune_sort(ctx, hkeys, hids, begin_bit=0, end_bit=64, shapes=SORT_SHAPES, reps=3):

@@ -13,10 +13,11 @@
 //     per-digit base by decoupled look-back over earlier tiles (one thread per
 //     digit, bounded spin), stages the tile in shared memory in rank order and
 //     writes it out with coalesced runs.
-// Three shapes, chosen per context (fl_sort_set_config): 8-bit digits on tiles
-// of 256 threads x 12 keys (4 CTAs per SM), 8-bit digits on tiles of 512 x 12
-// (2 per SM: half the tiles, twice the keys per digit run written), 9-bit
-// digits on tiles of 512 x 12 (7 passes over 63-bit keys instead of 8).
+// Four shapes, chosen per context (fl_sort_set_config): 8- or 9-bit digits (9:
+// 7 passes over 63-bit keys instead of 8) on tiles of 256 or 512 threads x 12
+// keys (512: half the tiles and twice the keys per digit run written, at 2
+// CTAs per SM; 256: 4 CTAs per SM with 8-bit digits, 3 with 9-bit, whose
+// threads then take two digits each).
 // Stable: ties keep input order, so (key, payload) pairs match std::stable_sort.
 #include "common.cuh"
 #include "scan.cuh"
@@ -89,14 +90,16 @@ __host__ __device__ constexpr size_t onesweep_smem() {
 }
 
 template <int kThreads, int kBits>
-__global__ void __launch_bounds__(kThreads, kThreads == 256 ? 4 : 2)
+__global__ void __launch_bounds__(kThreads, kThreads == 512 ? 2 : (kBits == 8 ? 4 : 3))
     k_onesweep(const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
                uint32_t* __restrict__ vout, size_t n, int shift, uint32_t dmask,
                const uint32_t* __restrict__ bin_off, uint32_t* status, unsigned* ticket, uint32_t* dev_status) {
     constexpr int R = 1 << kBits;
     constexpr int kWarps = kThreads / 32;
     constexpr int kTile = kThreads * kItems;
-    static_assert(R <= kThreads && R % 32 == 0, "one thread per digit, whole warps");
+    // digit scan: each of the first R / D threads takes D consecutive digits
+    constexpr int D = R > kThreads ? R / kThreads : 1;
+    static_assert(R % 32 == 0 && (R <= kThreads || R % kThreads == 0), "whole warps of digits");
     extern __shared__ __align__(16) unsigned char s_dyn[];
     uint64_t* s_keys = (uint64_t*)s_dyn;
     uint32_t* s_vals = (uint32_t*)(s_keys + kTile);
@@ -136,9 +139,9 @@ __global__ void __launch_bounds__(kThreads, kThreads == 256 ? 4 : 2)
         rank[i] = base + __popc(peers & lt);
     }
     __syncthreads();
-    // per-digit: tile count, cross-warp exclusive offsets (thread = digit)
-    if (threadIdx.x < R) {
-        const int d = threadIdx.x;
+    // per-digit: tile count, cross-warp exclusive offsets (a thread per digit, or
+    // R / kThreads digits per thread one after another)
+    for (int d = threadIdx.x; d < R; d += kThreads) {
         uint32_t run = 0;
         for (int w = 0; w < kWarps; ++w) {
             uint32_t c = s_warp_hist[w * R + d];
@@ -176,13 +179,18 @@ __global__ void __launch_bounds__(kThreads, kThreads == 256 ? 4 : 2)
         s_tile_excl[d] = run;
     }
     __syncthreads();
-    // block exclusive scan of s_tile_excl (R entries, one per thread of the first R)
+    // block exclusive scan of s_tile_excl (R entries; thread t < R / D holds digits
+    // tD .. tD + D - 1)
     {
-        const int d = threadIdx.x;
-        uint32_t c = 0, incl = 0;
-        if (d < R) {
-            c = s_tile_excl[d];
-            incl = c;
+        const int t0 = threadIdx.x * D;
+        uint32_t c[D], sum = 0, incl = 0;
+        if (t0 < R) {
+#pragma unroll
+            for (int j = 0; j < D; ++j) {
+                c[j] = s_tile_excl[t0 + j];
+                sum += c[j];
+            }
+            incl = sum;
             for (int o = 1; o < 32; o <<= 1) {
                 uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
                 if (lane >= o) incl += t;
@@ -190,10 +198,14 @@ __global__ void __launch_bounds__(kThreads, kThreads == 256 ? 4 : 2)
             if (lane == 31) s_wsum[warp] = incl;
         }
         __syncthreads();
-        if (d < R) {
-            uint32_t wofs = 0;
-            for (int w = 0; w < warp; ++w) wofs += s_wsum[w];
-            s_tile_excl[d] = wofs + incl - c;
+        if (t0 < R) {
+            uint32_t ex = incl - sum;
+            for (int w = 0; w < warp; ++w) ex += s_wsum[w];
+#pragma unroll
+            for (int j = 0; j < D; ++j) {
+                s_tile_excl[t0 + j] = ex;
+                ex += c[j];
+            }
         }
     }
     __syncthreads();
@@ -221,7 +233,12 @@ __global__ void __launch_bounds__(kThreads, kThreads == 256 ? 4 : 2)
     }
 }
 
-size_t status_stride_min(size_t n) { return fl_align256(((n + kTileMin - 1) / kTileMin) * 256 * 4 + 4) + 4096; }
+// Bytes of one pass's tile status words and ticket, for every shape: at most
+// ceil(n / kTileMin) tiles of at most kMaxRadix digits (9-bit digits on the
+// smallest tile reach both bounds at once).
+size_t status_stride_min(size_t n) {
+    return fl_align256(((n + kTileMin - 1) / kTileMin) * kMaxRadix * 4 + 4) + 4096;
+}
 
 // All passes of one shape.  The scratch layout (fl_sort_scratch_bytes): the
 // alternate key and value buffers, the pass histograms (kMaxPasses x
@@ -282,6 +299,8 @@ size_t fl_sort_scratch_bytes(size_t n, int passes) {
 int fl_sort_pairs_with(fl_ctx* ctx, uint64_t* keys, uint32_t* vals, size_t n, int begin_bit, int end_bit,
                        void* scratch) {
     if (n <= 1 || end_bit <= begin_bit) return FL_OK;
+    if (ctx->sort_digit_bits == 9 && ctx->sort_tile_threads == 256)
+        return sort_passes<256, 9>(ctx, keys, vals, n, begin_bit, end_bit, scratch);
     if (ctx->sort_digit_bits == 9) return sort_passes<512, 9>(ctx, keys, vals, n, begin_bit, end_bit, scratch);
     if (ctx->sort_tile_threads == 512) return sort_passes<512, 8>(ctx, keys, vals, n, begin_bit, end_bit, scratch);
     return sort_passes<256, 8>(ctx, keys, vals, n, begin_bit, end_bit, scratch);
@@ -289,11 +308,10 @@ int fl_sort_pairs_with(fl_ctx* ctx, uint64_t* keys, uint32_t* vals, size_t n, in
 
 extern "C" int fl_sort_set_config(fl_ctx* ctx, int digit_bits, int tile_threads) {
     if (!ctx) return FL_E_INVALID_ARG;
-    const bool ok = (digit_bits == 8 && (tile_threads == 256 || tile_threads == 512)) ||
-                    (digit_bits == 9 && tile_threads == 512);
+    const bool ok = (digit_bits == 8 || digit_bits == 9) && (tile_threads == 256 || tile_threads == 512);
     if (!ok)
         return fl_set_error(ctx, FL_E_INVALID_ARG,
-                            "fl_sort_set_config: shapes are 8-bit digits on 256 or 512 threads, 9-bit on 512");
+                            "fl_sort_set_config: digit_bits 8 or 9, tile_threads 256 or 512");
     ctx->sort_digit_bits = digit_bits;
     ctx->sort_tile_threads = tile_threads;
     return FL_OK;

@@ -126,8 +126,8 @@ int fl_lookback_timeout_probe(fl_ctx* ctx, uint32_t spin_limit);
 int fl_sort_pairs_u64_u32(fl_ctx* ctx, uint64_t* keys, uint32_t* vals, size_t n, int begin_bit, int end_bit);
 /* The radix sort's shape for every later sort on this context (the reference fixes 8-bit digits,
  * kernels/hashmap/radix_sort.cl:5-6 BITS_PER_PASS; the tile shape has no reference counterpart):
- * digit_bits 8 on tiles of tile_threads 256 (default) or 512 threads x 12 keys, or digit_bits 9 on
- * 512 (ceil(bits / 9) passes instead of ceil(bits / 8)).  Every shape gives the same sorted output;
+ * digit_bits 8 (default) or 9 (ceil(bits / 9) passes instead of ceil(bits / 8)) on tiles of
+ * tile_threads 256 (default) or 512 threads x 12 keys.  Every shape gives the same sorted output;
  * any other pair returns FL_E_INVALID_ARG and keeps the current shape. */
 int fl_sort_set_config(fl_ctx* ctx, int digit_bits, int tile_threads);
 int fl_sort_get_config(fl_ctx* ctx, int* digit_bits, int* tile_threads);

@@ -118,7 +118,7 @@ def test_sort_hilbert_keys_16m_sorted_and_permutation(ctx):
     assert np.bincount(i, minlength=n).max() == 1
 
 
-SORT_SHAPES = [(8, 256), (8, 512), (9, 512)]
+SORT_SHAPES = [(8, 256), (8, 512), (9, 256), (9, 512)]
 
 
 @pytest.fixture
@@ -172,7 +172,7 @@ def test_sort_shapes_ties_and_full_size(ctx, sort_shape):
 
 def test_sort_shape_validation(ctx):
     from fluidloom_gb300.runtime import FluidLoomError
-    for bad in [(7, 256), (9, 256), (10, 512), (8, 384), (8, 0)]:
+    for bad in [(7, 256), (10, 512), (9, 384), (8, 384), (8, 0)]:
         with pytest.raises(FluidLoomError):
             ctx.call("fl_sort_set_config", *bad)
     b, t = ctypes.c_int(), ctypes.c_int()
