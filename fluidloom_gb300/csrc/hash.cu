@@ -172,9 +172,11 @@ __global__ void k_check_sorted(const uint64_t* __restrict__ keys, size_t n, uint
 }
 
 // dir[b] = first run whose bucket is >= b, b in [0, nb]: run i fills the
-// buckets after its predecessor's up to its own (run n stands for bucket nb).
-// A wide range (a gap in the keys, between cases say) is filled by the whole
-// warp, so it costs 1/32 of its length.
+// buckets after its predecessor's up to its own.  A wide range (a gap in the
+// keys, between cases say) is filled by the whole warp, so it costs 1/32 of
+// its length; the buckets after the last run's (n: none starts there), up to
+// a directory's worth when the keys span less than the directory (a uniform
+// mesh), by the whole grid.
 __global__ void k_locator_dir(const uint64_t* __restrict__ keys, size_t n, int log2nb, uint32_t* __restrict__ dir) {
     const uint64_t nb = 1ull << log2nb;
     const uint64_t k0 = keys[0], span = keys[n - 1] - k0;
@@ -182,11 +184,13 @@ __global__ void k_locator_dir(const uint64_t* __restrict__ keys, size_t n, int l
     const int shift = bits > log2nb ? bits - log2nb : 0;
     const int lane = threadIdx.x & 31;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t base = (size_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base <= n; base += stride) {
+    for (uint64_t b = (span >> shift) + 1 + (size_t)blockIdx.x * blockDim.x + threadIdx.x; b <= nb; b += stride)
+        dir[b] = (uint32_t)n;
+    for (size_t base = (size_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
         const size_t i = base + lane;
-        uint64_t bl = 1, bh = 0;  // empty unless i <= n
-        if (i <= n) {
-            bh = i < n ? (keys[i] - k0) >> shift : nb;
+        uint64_t bl = 1, bh = 0;  // empty unless i < n
+        if (i < n) {
+            bh = (keys[i] - k0) >> shift;
             bl = i > 0 ? ((keys[i - 1] - k0) >> shift) + 1 : 0;
         }
         // short ranges (the common case: one or two buckets) by their own lane,
