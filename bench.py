@@ -82,10 +82,17 @@ class ClockSampler:
              "clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return
+        # the sampler is up once it has written its first sample (at most 3 s)
+        t0 = time.time()
+        while time.time() - t0 < 3.0 and self.proc.poll() is None:
+            if os.path.getsize(self.path) > 0:
+                break
+            time.sleep(0.01)
 
     def stop(self):
         if self.proc is None:
@@ -451,7 +458,6 @@ def run_gpu(args):
         torch.cuda.profiler.start()
     clocks = ClockSampler(local)
     clocks.start()
-    time.sleep(0.3)
     total_lups = 0
     regrids = 0
     regrid_ms = []
