@@ -229,6 +229,11 @@ public:
     void sortByKey(uint64_t* keys, uint32_t* vals, size_t n, int begin_bit = 0, int end_bit = 64) {
         check(dev_.get(), fl_sort_pairs_u64_u32(dev_.get(), keys, vals, n, begin_bit, end_bit), "sortByKey");
     }
+    // The sort's shape for the device context (fl_sort_set_config): 8- or 9-bit digits on
+    // tiles of 256 or 512 threads; every shape gives the same order.
+    void setShape(int digit_bits, int tile_threads) {
+        check(dev_.get(), fl_sort_set_config(dev_.get(), digit_bits, tile_threads), "setShape");
+    }
 
 private:
     Device& dev_;

@@ -89,6 +89,48 @@ int main() {
         EXPECT_EQ(m.size(), (size_t)1);
         EXPECT_EQ((int)m.read(m.raw().level)[0], 0);
     }
+    // RadixSort::sortByKey in every shape: the same stable order (ties keep input order)
+    {
+        const size_t n = 100003;
+        std::vector<uint64_t> k(n);
+        std::vector<uint32_t> v(n);
+        uint64_t s = 88172645463325252ull;
+        for (size_t i = 0; i < n; ++i) {
+            s ^= s << 13; s ^= s >> 7; s ^= s << 17;
+            k[i] = s % 5000;  // many ties
+            v[i] = (uint32_t)i;
+        }
+        uint64_t* dk = nullptr;
+        uint32_t* dv = nullptr;
+        check(dev.get(), fl_device_alloc(dev.get(), n * 8, (void**)&dk), "alloc");
+        check(dev.get(), fl_device_alloc(dev.get(), n * 4, (void**)&dv), "alloc");
+        hashmap::RadixSort rs(dev);
+        std::vector<uint64_t> k0(n);
+        std::vector<uint32_t> v0(n);
+        const int shapes[4][2] = {{8, 256}, {8, 512}, {9, 256}, {9, 512}};
+        for (int t = 0; t < 4; ++t) {
+            rs.setShape(shapes[t][0], shapes[t][1]);
+            check(dev.get(), fl_memcpy_h2d(dev.get(), dk, k.data(), n * 8), "h2d");
+            check(dev.get(), fl_memcpy_h2d(dev.get(), dv, v.data(), n * 4), "h2d");
+            rs.sortByKey(dk, dv, n, 0, 13);
+            std::vector<uint64_t> kk(n);
+            std::vector<uint32_t> vv(n);
+            check(dev.get(), fl_memcpy_d2h(dev.get(), kk.data(), dk, n * 8), "d2h");
+            check(dev.get(), fl_memcpy_d2h(dev.get(), vv.data(), dv, n * 4), "d2h");
+            bool stable = true;
+            for (size_t i = 1; i < n; ++i)
+                stable = stable && (kk[i - 1] < kk[i] || (kk[i - 1] == kk[i] && vv[i - 1] < vv[i]));
+            EXPECT_TRUE(stable);
+            if (t == 0) { k0 = kk; v0 = vv; }
+            EXPECT_TRUE(kk == k0 && vv == v0);
+        }
+        rs.setShape(8, 256);
+        bool refused = false;
+        try { rs.setShape(10, 256); } catch (const FluidLoomError&) { refused = true; }
+        EXPECT_TRUE(refused);
+        fl_device_free(dev.get(), dk);
+        fl_device_free(dev.get(), dv);
+    }
     // a pool step through the runtime nodes
     {
         fl_lbm_case c{};
