@@ -4,7 +4,7 @@ every case resident on the device until it finishes, and reports aggregate
 MLUPS with p50/p99 time-to-completion against plain sequential GPU runs of the
 same jobs (one job at a time, arrival order).
 
-  python -m fluidloom_gb300.serving [--rate 50] [--duration 60] [--steps 200 2000] [--budget-gb 150]
+  python -m fluidloom_gb300.serving [--rate 50] [--duration 60] [--steps 200 2000] [--budget-gb 150] [--trace t.json]
 
 Jobs (synthetic, seeded): Poisson arrivals; 70 % lid-driven cavities, 30 %
 sphere-in-channel; base size log-uniform between 16^3 and 128x64x64 sites;
@@ -32,7 +32,7 @@ BRICK_BYTES = 3 * 19 * 512 * 4  # three population buffers per brick
 
 class Job:
     __slots__ = ("jid", "arrival", "case", "steps", "regrid_every", "done", "cid", "start", "end", "result",
-                 "refused")
+                 "refused", "deferred")
 
     def __init__(self, jid, arrival, case, steps, regrid_every=20):
         self.jid, self.arrival, self.case, self.steps, self.regrid_every = jid, arrival, case, steps, regrid_every
@@ -41,6 +41,7 @@ class Job:
         self.start = self.end = None
         self.result = None
         self.refused = None  # the reason, when admission refused the job for good
+        self.deferred = 0  # times it was added and taken out again over the budget
 
     def start_bytes(self):
         """Population bytes of the job's level-0 bricks: the least it holds from its first step,
@@ -135,6 +136,7 @@ def run_served(ctx, jobs, budget_bytes, check_ids=(), regrid_every=20, resident_
                 if active and (now_used > cap or reserved_bytes(pool) > budget_bytes):
                     pool.remove_cases([cid])  # over the budget: back to the queue until jobs finish
                     deferrals += 1
+                    j.deferred += 1
                     break
                 used = now_used
                 queue.popleft()
@@ -176,6 +178,34 @@ def run_served(ctx, jobs, budget_bytes, check_ids=(), regrid_every=20, resident_
     return lups, makespan, steps_run
 
 
+def trace_events(jobs):
+    """The served timeline as Chrome trace events, in the reference profiler's event format
+    (src/profiling/Profiler.cpp:53-96: name, cat, ph, ts and dur in microseconds, pid, tid):
+    per job, on a track of its own, a "queued" span from arrival to admission and a
+    "resident" span from admission to completion (its steps, case slot and deferrals as
+    args); a refused job is an instant event at its arrival with the reason."""
+    ev = []
+    for j in sorted(jobs, key=lambda j: j.jid):
+        base = {"pid": 0, "tid": int(j.jid)}
+        if j.refused:
+            ev.append(dict(base, name="job %d refused" % j.jid, cat="admission", ph="i", s="t",
+                           ts=int(round(j.arrival * 1e6)), args={"reason": j.refused}))
+            continue
+        if j.start is None or j.end is None:
+            continue
+        a, st, en = (int(round(t * 1e6)) for t in (j.arrival, j.start, j.end))
+        ev.append(dict(base, name="job %d queued" % j.jid, cat="queue", ph="X", ts=a, dur=max(0, st - a)))
+        ev.append(dict(base, name="job %d" % j.jid, cat="resident", ph="X", ts=st, dur=max(0, en - st),
+                       args={"steps": int(j.steps), "case_slot": j.cid, "deferred": int(j.deferred)}))
+    return ev
+
+
+def write_trace(jobs, path):
+    """trace_events(jobs) as a JSON array (chrome://tracing, Perfetto)."""
+    with open(path, "w") as f:
+        json.dump(trace_events(jobs), f)
+
+
 def run_solo(ctx, job):
     """The same job alone on the GPU; returns (seconds, LUPs, final state)."""
     p = Pool(ctx, [job.case])
@@ -199,13 +229,16 @@ def percentile(v, q):
 
 
 def benchmark(ctx, rate=50.0, duration=60.0, steps_range=(200, 2000), budget_gb=150.0, resident_gb=6.0, check=8,
-              seed=5):
+              seed=5, trace=None):
     """Serve the arrival stream, then run the same jobs one at a time in arrival order;
     returns throughput and p50/p99 time to completion of both, and the checked jobs whose
-    served result differs from their solo run."""
+    served result differs from their solo run.  trace: a path for the served timeline
+    (write_trace)."""
     jobs = make_jobs(rate, duration, list(steps_range), seed)
     check_ids = set(range(min(check, len(jobs))))
     lups, makespan, steps_run = run_served(ctx, jobs, budget_gb * 1e9, check_ids, resident_bytes=resident_gb * 1e9)
+    if trace:
+        write_trace(jobs, trace)
     refused = [j for j in jobs if j.refused]
     jobs = [j for j in jobs if not j.refused]
     lat = [j.end - j.arrival for j in jobs]
@@ -245,10 +278,11 @@ def main(argv=None):
                     help="admission stops while the resident population footprint exceeds this")
     ap.add_argument("--check", type=int, default=8, help="jobs whose result is compared with their solo run")
     ap.add_argument("--seed", type=int, default=5)
+    ap.add_argument("--trace", default=None, help="write the served timeline as a Chrome trace JSON file")
     args = ap.parse_args(argv)
     ctx = Context(0)
     res = benchmark(ctx, args.rate, args.duration, args.steps, args.budget_gb, args.resident_gb, args.check,
-                    args.seed)
+                    args.seed, trace=args.trace)
     print(json.dumps(res))
     return res
 

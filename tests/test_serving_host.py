@@ -108,3 +108,22 @@ def test_job_above_the_budget_is_refused(fake_pool):
     assert jobs[0].refused is None and jobs[0].done == 20
     assert jobs[1].refused and "budget" in jobs[1].refused and jobs[1].done == 0
     assert ("add", 1) not in fake_pool.log
+
+
+def test_trace_of_the_served_timeline(fake_pool, tmp_path):
+    import json
+    jobs = _jobs([(16, 20), (16, 20), (64, 20)])
+    serving.run_served(FakeCtx(), jobs, budget_bytes=jobs[2].start_bytes() - 1,
+                       resident_bytes=12 * serving.BRICK_BYTES)
+    path = tmp_path / "t.json"
+    serving.write_trace(jobs, str(path))
+    ev = json.load(open(path))
+    for j in jobs[:2]:
+        mine = [e for e in ev if e["tid"] == j.jid]
+        queued, resident = mine
+        assert queued["ph"] == resident["ph"] == "X" and queued["cat"] == "queue"
+        assert queued["ts"] + queued["dur"] == resident["ts"]  # admitted when the queue span ends
+        assert resident["args"]["steps"] == 20 and resident["dur"] >= 0
+    assert sum(e["args"]["deferred"] for e in ev if e["cat"] == "resident") >= 1
+    refused = [e for e in ev if e["tid"] == 2]
+    assert len(refused) == 1 and refused[0]["ph"] == "i" and "budget" in refused[0]["args"]["reason"]
