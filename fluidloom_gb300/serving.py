@@ -32,10 +32,12 @@ BRICK_BYTES = 3 * 19 * 512 * 4  # three population buffers per brick
 
 class Job:
     __slots__ = ("jid", "arrival", "case", "steps", "regrid_every", "done", "cid", "start", "end", "result",
-                 "refused", "deferred")
+                 "refused", "deferred", "deadline", "cancelled")
 
-    def __init__(self, jid, arrival, case, steps, regrid_every=20):
+    def __init__(self, jid, arrival, case, steps, regrid_every=20, deadline=None):
         self.jid, self.arrival, self.case, self.steps, self.regrid_every = jid, arrival, case, steps, regrid_every
+        self.deadline = deadline  # seconds from arrival to completion; past it the job is cancelled
+        self.cancelled = None  # the reason, when the job was cancelled before it finished
         self.done = 0
         self.cid = None
         self.start = self.end = None
@@ -84,7 +86,18 @@ def reserved_bytes(pool):
     return 0 if pool is None else int(pool.info().population_bytes)
 
 
-def run_served(ctx, jobs, budget_bytes, check_ids=(), regrid_every=20, resident_bytes=None, admit_every=None):
+def _cancel_reason(j, now, cancel):
+    if cancel is not None:
+        why = cancel(j, now)
+        if why:
+            return str(why)
+    if j.deadline is not None and now - j.arrival > j.deadline:
+        return "deadline of %.3f s passed" % j.deadline
+    return None
+
+
+def run_served(ctx, jobs, budget_bytes, check_ids=(), regrid_every=20, resident_bytes=None, admit_every=None,
+               cancel=None):
     """Continuous batching; returns the LUPs done, the makespan and the pool steps run.
 
     Jobs are admitted in arrival order at pool steps that are multiples of
@@ -96,7 +109,12 @@ def run_served(ctx, jobs, budget_bytes, check_ids=(), regrid_every=20, resident_
     again once that fits.  A job whose level-0 bricks alone exceed the whole
     budget (start_bytes) is refused.  resident_bytes is the throughput knob:
     enough resident bricks to keep HBM busy, and no more, so queued jobs start in
-    order instead of all sharing the GPU."""
+    order instead of all sharing the GPU.
+
+    Cancellation, at step boundaries (no kernel of the pool in flight): a queued or
+    resident job is cancelled when cancel(job, now) returns a reason, or when its
+    deadline (seconds from arrival) has passed; a resident job's case leaves the pool
+    like a finished one, and the other jobs go on unaffected."""
     cap = budget_bytes if resident_bytes is None else min(budget_bytes, resident_bytes)
     admit_every = admit_every or regrid_every
     pending = collections.deque(sorted(jobs, key=lambda j: j.arrival))
@@ -118,6 +136,15 @@ def run_served(ctx, jobs, budget_bytes, check_ids=(), regrid_every=20, resident_
                 j.start = j.end = now
                 continue
             queue.append(j)
+        for j in [j for j in queue if _cancel_reason(j, now, cancel)]:
+            queue.remove(j)
+            j.cancelled, j.end = _cancel_reason(j, now, cancel), now
+        gone = [cid for cid, j in active.items() if _cancel_reason(j, now, cancel)]
+        if gone:
+            for cid in gone:
+                j = active.pop(cid)
+                j.cancelled, j.end = _cancel_reason(j, now, cancel), now
+            pool.remove_cases(gone)
         if not active:
             phase = 0
         if phase % admit_every == 0 and queue:
@@ -183,7 +210,8 @@ def trace_events(jobs):
     (src/profiling/Profiler.cpp:53-96: name, cat, ph, ts and dur in microseconds, pid, tid):
     per job, on a track of its own, a "queued" span from arrival to admission and a
     "resident" span from admission to completion (its steps, case slot and deferrals as
-    args); a refused job is an instant event at its arrival with the reason."""
+    args); a refused job is an instant event at its arrival with the reason, a cancelled
+    one an instant event when it was cancelled."""
     ev = []
     for j in sorted(jobs, key=lambda j: j.jid):
         base = {"pid": 0, "tid": int(j.jid)}
@@ -191,12 +219,18 @@ def trace_events(jobs):
             ev.append(dict(base, name="job %d refused" % j.jid, cat="admission", ph="i", s="t",
                            ts=int(round(j.arrival * 1e6)), args={"reason": j.refused}))
             continue
-        if j.start is None or j.end is None:
+        if j.end is None:
             continue
-        a, st, en = (int(round(t * 1e6)) for t in (j.arrival, j.start, j.end))
+        a, en = int(round(j.arrival * 1e6)), int(round(j.end * 1e6))
+        st = en if j.start is None else int(round(j.start * 1e6))  # a job cancelled in the queue
         ev.append(dict(base, name="job %d queued" % j.jid, cat="queue", ph="X", ts=a, dur=max(0, st - a)))
-        ev.append(dict(base, name="job %d" % j.jid, cat="resident", ph="X", ts=st, dur=max(0, en - st),
-                       args={"steps": int(j.steps), "case_slot": j.cid, "deferred": int(j.deferred)}))
+        if j.start is not None:
+            ev.append(dict(base, name="job %d" % j.jid, cat="resident", ph="X", ts=st, dur=max(0, en - st),
+                           args={"steps": int(j.steps), "steps_done": int(j.done), "case_slot": j.cid,
+                                 "deferred": int(j.deferred)}))
+        if j.cancelled:
+            ev.append(dict(base, name="job %d cancelled" % j.jid, cat="admission", ph="i", s="t", ts=en,
+                           args={"reason": j.cancelled}))
     return ev
 
 
@@ -240,7 +274,7 @@ def benchmark(ctx, rate=50.0, duration=60.0, steps_range=(200, 2000), budget_gb=
     if trace:
         write_trace(jobs, trace)
     refused = [j for j in jobs if j.refused]
-    jobs = [j for j in jobs if not j.refused]
+    jobs = [j for j in jobs if not j.refused and not j.cancelled]
     lat = [j.end - j.arrival for j in jobs]
     # plain sequential: each job alone, one after another in arrival order
     end_prev, lat_plain, solo_s, solo_lups, mismatched = 0.0, [], 0.0, 0, []

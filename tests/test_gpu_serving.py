@@ -147,3 +147,22 @@ def test_admission_defers_and_refuses_under_a_small_budget(ctx):
 def run_deferrals():
     from fluidloom_gb300 import serving
     return serving.run_served.deferrals
+
+
+def test_cancelled_job_leaves_the_others_unchanged(ctx):
+    """A job cancelled after 12 of its steps leaves the pool at that step boundary; the
+    jobs that stay still end in their solo states."""
+    from fluidloom_gb300 import serving
+    a, b, c = _cases()
+    jobs = [serving.Job(0, 0.0, a, 45), serving.Job(1, 0.0, b, 40), serving.Job(2, 0.0, c, 33)]
+    cancel = lambda j, now: "cancelled by the test" if j.jid == 1 and j.done >= 12 else None
+    serving.run_served(ctx, jobs, budget_bytes=1e12, check_ids={0, 2}, cancel=cancel)
+    assert jobs[1].cancelled == "cancelled by the test" and jobs[1].done == 12
+    for j in (jobs[0], jobs[2]):
+        assert j.cancelled is None and j.done == j.steps
+        _, _, solo = serving.run_solo(ctx, j)
+        g1, f1 = j.result
+        g2, f2 = solo
+        for k in ("x", "y", "z", "level"):
+            np.testing.assert_array_equal(g1[k], g2[k])
+        np.testing.assert_array_equal(f1, f2)

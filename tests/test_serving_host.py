@@ -127,3 +127,32 @@ def test_trace_of_the_served_timeline(fake_pool, tmp_path):
     assert sum(e["args"]["deferred"] for e in ev if e["cat"] == "resident") >= 1
     refused = [e for e in ev if e["tid"] == 2]
     assert len(refused) == 1 and refused[0]["ph"] == "i" and "budget" in refused[0]["args"]["reason"]
+
+
+def test_cancelled_jobs_leave_at_a_step_boundary(fake_pool):
+    # job 1 is cancelled after 10 of its steps (resident), job 2 while it waits in the queue
+    jobs = _jobs([(16, 40), (16, 40), (16, 40)])
+
+    def cancel(j, now):
+        if j.jid == 1 and j.done >= 10:
+            return "client cancelled"
+        if j.jid == 2 and jobs[0].done >= 5 and j.start is None:
+            return "client cancelled"
+        return None
+
+    serving.run_served(FakeCtx(), jobs, budget_bytes=10 ** 12, resident_bytes=20 * serving.BRICK_BYTES,
+                       cancel=cancel)
+    assert jobs[0].done == 40 and jobs[0].cancelled is None
+    assert jobs[1].cancelled == "client cancelled" and jobs[1].done == 10 and jobs[1].end is not None
+    assert ("remove", jobs[1].cid) in fake_pool.log  # its case left the pool
+    assert jobs[2].cancelled and jobs[2].start is None and jobs[2].done == 0
+    assert jobs[2].deferred >= 1 and jobs[2].cid is None  # tried once (over the cap), never resident
+    ev = serving.trace_events(jobs)
+    assert [e["name"] for e in ev if e["ph"] == "i"] == ["job 1 cancelled", "job 2 cancelled"]
+
+
+def test_deadline_cancels(fake_pool):
+    jobs = [serving.Job(0, 0.0, cavity(16, 1), 30), serving.Job(1, 0.0, cavity(16, 1), 30, deadline=0.0)]
+    serving.run_served(FakeCtx(), jobs, budget_bytes=10 ** 12)
+    assert jobs[0].done == 30 and jobs[0].cancelled is None
+    assert jobs[1].cancelled.startswith("deadline") and jobs[1].done < 30
