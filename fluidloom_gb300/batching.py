@@ -3,7 +3,7 @@ launch per level sub-step across all cases, each level-0 step replayed as a
 CUDA graph) against the same cases run one at a time, and the check that every
 batched case equals its solo run bit for bit.
 
-  python -m fluidloom_gb300.batching [--cases 256] [--steps 500] [--regrid-every 20]
+  python -m fluidloom_gb300.batching [--cases 256] [--steps 500] [--regrid-every 20] [--tune-cache t.json]
 
 Workload (synthetic, seeded): lid-driven cavities with base edge log-uniform in
 [16, 64] sites rounded to a multiple of 8, max level uniform in {1, 2, 3}, lid
@@ -34,7 +34,32 @@ def cavity_batch(n=256, seed=4):
     return out
 
 
-def autotune(pool, candidates=(2, 3, 4, 6, 8), streams=(1, 2), staging=(0, 1, 2), steps=4):
+def _cache_load(path):
+    import os
+    if not path or not os.path.exists(path):
+        return {}
+    with open(path) as f:
+        return json.load(f)
+
+
+def _cache_store(path, section, key, value):
+    """Record a tuned choice under cache[section][key] (read, update, write back whole)."""
+    if not path:
+        return
+    data = _cache_load(path)
+    data.setdefault(section, {})[key] = list(value)
+    with open(path, "w") as f:
+        json.dump(data, f, indent=1, sort_keys=True)
+
+
+def pool_signature(pool):
+    """The autotuner cache key of a pool's workload: its cases and bricks per level."""
+    inf = pool.info()
+    return "cases=%d bricks=%s" % (inf.num_cases, ",".join(str(int(inf.bricks_per_level[l]))
+                                                           for l in range(inf.max_level + 1)))
+
+
+def autotune(pool, candidates=(2, 3, 4, 6, 8), streams=(1, 2), staging=(0, 1, 2), steps=4, cache=None, key=None):
     """Pick the CTAs per SM of the interior collide-stream kernel, the class-stream layout
     (every launch on one stream, or the per-level dependency graph over two) and how the
     collide kernels read a brick's own populations (fl_pool_set_staging: 128-bit loads into
@@ -43,9 +68,18 @@ def autotune(pool, candidates=(2, 3, 4, 6, 8), streams=(1, 2), staging=(0, 1, 2)
     events (two untimed steps first capture the graphs): every CTA count and stream layout
     with register loads, then each staging mode at the best of those; returns
     (ctas_per_sm, streams, staging).  The pool's state advances: tune on a pool that is
-    rebuilt afterwards."""
+    rebuilt afterwards.  cache: a JSON file of earlier choices; with it, a workload already
+    tuned (key, default pool_signature(pool)) takes its recorded choice without timing, and a
+    new one is recorded."""
     import ctypes
     ctx = pool.ctx
+    if cache:
+        key = key or pool_signature(pool)
+        hit = _cache_load(cache).get("pool", {}).get(key)
+        if hit:
+            best = tuple(hit)
+            pool.set_options(graphs=1, grid_mult=best[0], streams=best[1], staging=best[2])
+            return best
 
     def timed(g, st, sg):
         pool.set_options(graphs=1, grid_mult=g, streams=st, staging=sg)
@@ -69,23 +103,33 @@ def autotune(pool, candidates=(2, 3, 4, 6, 8), streams=(1, 2), staging=(0, 1, 2)
         if ms < best_ms:
             best, best_ms = (best[0], best[1], sg), ms
     pool.set_options(graphs=1, grid_mult=best[0], streams=best[1], staging=best[2])
+    if cache:
+        _cache_store(cache, "pool", key, best)
     return best
 
 
 SORT_SHAPES = ((8, 256), (8, 512), (9, 256), (9, 512))
 
 
-def autotune_sort(ctx, hkeys, hids, begin_bit=0, end_bit=64, shapes=SORT_SHAPES, reps=3):
+def autotune_sort(ctx, hkeys, hids, begin_bit=0, end_bit=64, shapes=SORT_SHAPES, reps=3, cache=None, key=None):
     """Pick the radix sort's shape -- digit width and tile threads (fl_sort_set_config) -- for
     keys like these: per shape, a device copy of (hkeys, hids) is sorted once untimed and then
     `reps` times timed with CUDA events (the copy refreshed before each call); the fastest
     shape is set on the context.  Every shape gives the same sorted output.  Returns
-    ((digit_bits, tile_threads), {(digit_bits, tile_threads): best ms})."""
+    ((digit_bits, tile_threads), {(digit_bits, tile_threads): best ms}).  cache: as for
+    autotune (key, default: the key count rounded to a power of two and the bit range); a
+    cached choice is set without timing and returned with no times."""
     import ctypes
     from . import DeviceArray
     hkeys = np.ascontiguousarray(hkeys, np.uint64)
     hids = np.ascontiguousarray(hids, np.uint32)
     n = len(hkeys)
+    if cache:
+        key = key or "n=2^%d bits=%d-%d" % (max(0, int(n - 1).bit_length()), begin_bit, end_bit)
+        hit = _cache_load(cache).get("sort", {}).get(key)
+        if hit:
+            ctx.call("fl_sort_set_config", hit[0], hit[1])
+            return tuple(hit), {}
     k, v = DeviceArray.from_host(ctx, hkeys), DeviceArray.from_host(ctx, hids)
     times = {}
     for bits, threads in shapes:
@@ -105,6 +149,8 @@ def autotune_sort(ctx, hkeys, hids, begin_bit=0, end_bit=64, shapes=SORT_SHAPES,
     ctx.call("fl_sort_set_config", *choice)
     k.free()
     v.free()
+    if cache:
+        _cache_store(cache, "sort", key, choice)
     return choice, times
 
 
@@ -119,11 +165,12 @@ def run(pool, steps, regrid_every):
     return lups
 
 
-def benchmark(ctx, cases, steps=500, regrid_every=20, check=-1):
+def benchmark(ctx, cases, steps=500, regrid_every=20, check=-1, tune_cache=None):
     """The batched pool against the same cases one at a time (both with the autotuned options);
-    returns throughput, speed-up and the cases whose batched populations differ from their solo run."""
+    returns throughput, speed-up and the cases whose batched populations differ from their solo run.
+    tune_cache: the autotuner's cache file (autotune)."""
     pool = Pool(ctx, cases)
-    tuned, tuned_streams, tuned_staging = autotune(pool)
+    tuned, tuned_streams, tuned_staging = autotune(pool, cache=tune_cache)
     pool.close()
     pool = Pool(ctx, cases)
     pool.set_options(graphs=1, grid_mult=tuned, streams=tuned_streams, staging=tuned_staging)
@@ -166,9 +213,10 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--regrid-every", type=int, default=20)
     ap.add_argument("--check", type=int, default=-1, help="cases compared bitwise with their solo run (-1 = all)")
+    ap.add_argument("--tune-cache", default=None, help="JSON file of autotuned choices, read and extended")
     args = ap.parse_args(argv)
     ctx = Context(0)
-    res = benchmark(ctx, cavity_batch(args.cases), args.steps, args.regrid_every, args.check)
+    res = benchmark(ctx, cavity_batch(args.cases), args.steps, args.regrid_every, args.check, args.tune_cache)
     print(json.dumps(res))
     return res
 

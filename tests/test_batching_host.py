@@ -99,3 +99,30 @@ def test_autotune_pool_picks_staging_when_faster():
     pool = FakePool(lambda g, st, sg: {0: 2.0, 1: 1.5, 2: 1.7}[sg] + 0.01 * g + (0.1 if st == 2 else 0))
     best = batching.autotune(pool, candidates=(2, 4), streams=(1, 2), staging=(0, 1, 2))
     assert best == (2, 1, 1) and pool.opts == (2, 1, 1)
+
+
+def test_autotune_cache_skips_tuned_workloads(tmp_path):
+    cache = str(tmp_path / "tune.json")
+    first = FakePool(lambda g, st, sg: abs(g - 4) + (0.5 if st == 1 else 0.0) + 0.3 * sg + 1.0)
+    assert batching.autotune(first, candidates=(2, 4, 8), cache=cache, key="wl") == (4, 2, 0)
+    # the same workload again, on a GPU that would now prefer 8 CTAs per SM: the recorded
+    # choice is set without timing anything
+    second = FakePool(lambda g, st, sg: abs(g - 8) + 1.0)
+    assert batching.autotune(second, candidates=(2, 4, 8), cache=cache, key="wl") == (4, 2, 0)
+    assert second.tried == [(4, 2, 0)]
+    # another workload is tuned and recorded beside it
+    third = FakePool(lambda g, st, sg: abs(g - 8) + 1.0)
+    assert batching.autotune(third, candidates=(2, 4, 8), staging=(0,), cache=cache, key="other")[0] == 8
+    import json
+    assert set(json.load(open(cache))["pool"]) == {"wl", "other"}
+
+
+def test_autotune_sort_cache(tmp_path):
+    cache = str(tmp_path / "tune.json")
+    keys, ids = np.arange(5000, dtype=np.uint64), np.arange(5000, dtype=np.uint32)
+    ctx = FakeCtx({(8, 256): 1.0, (8, 512): 1.2, (9, 256): 1.5, (9, 512): 0.9})
+    assert batching.autotune_sort(ctx, keys, ids, 0, 63, cache=cache)[0] == (9, 512)
+    ctx2 = FakeCtx({(8, 256): 0.5, (8, 512): 1.2, (9, 256): 1.5, (9, 512): 0.9})
+    choice, times = batching.autotune_sort(ctx2, keys, ids, 0, 63, cache=cache)
+    assert choice == (9, 512) and times == {} and ctx2.shape == (9, 512)
+    assert "fl_sort_pairs_u64_u32" not in ctx2.calls
