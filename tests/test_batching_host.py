@@ -126,3 +126,14 @@ def test_autotune_sort_cache(tmp_path):
     choice, times = batching.autotune_sort(ctx2, keys, ids, 0, 63, cache=cache)
     assert choice == (9, 512) and times == {} and ctx2.shape == (9, 512)
     assert "fl_sort_pairs_u64_u32" not in ctx2.calls
+
+
+def test_pool_signature():
+    import types
+    from fluidloom_gb300.lbm import PoolInfo
+    inf = PoolInfo()
+    inf.num_cases, inf.max_level = 3, 2
+    for l, n in enumerate((48, 100, 224)):
+        inf.bricks_per_level[l] = n
+    pool = types.SimpleNamespace(info=lambda: inf)
+    assert batching.pool_signature(pool) == "cases=3 bricks=48,100,224"
