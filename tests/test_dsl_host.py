@@ -111,3 +111,28 @@ def test_placed_solids_map_to_mask_geometry(tmp_path):
     assert none is None and stl.type == G.STL and tris.shape == (4, 9) and list(stl.scale) == [16.0] * 3
     with pytest.raises(dsl.ParseError, match="not placed"):
         dsl.Scenario(dsl.parse("initial_condition: { place_geometry(type = \"implicit\") }"))
+
+
+def test_expression_parser_agrees_with_python_on_random_arithmetic():
+    """Random integer expressions over + - * % and ( ): left-associative binary operators
+    with * and % above + and -, as FluidLoomExpressionParser.g4 orders them (and Python)."""
+    pytest.importorskip("hypothesis")
+    from hypothesis import given, settings, strategies as st
+
+    atoms = st.integers(0, 9).map(str) | st.integers(1, 9).map(lambda v: "(-%d)" % v)
+
+    def extend(children):
+        return (st.tuples(children, st.sampled_from(["+", "-", "*", "%"]), children)
+                .filter(lambda t: t[1] != "%" or t[2] not in ("0", "(0)"))
+                .map(lambda t: "%s %s %s" % t) | children.map(lambda c: "(%s)" % c))
+
+    @settings(max_examples=300, deadline=None)
+    @given(st.recursive(atoms, extend, max_leaves=12))
+    def check(src):
+        try:
+            want = eval(src)
+        except ZeroDivisionError:
+            return
+        assert ev(src) == want, src
+
+    check()
